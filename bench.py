@@ -1,0 +1,415 @@
+#!/usr/bin/env python
+"""Benchmark: one training step of the batched wave RNN on a GB300.
+
+Workload (the reference's batched training configuration): batch 32 of
+vowel-like waveforms (3 formants, 10 kHz, Hann envelope, peak 1), T = 3500
+steps, 120 x 120 grid with a 20-cell PML (order 2, max 3.0), dt = 0.707,
+c0 = 1, c1 = 0.5, free-form rho ~ U(0,1) with 1-cell blur and projection
+(beta 100, eta 0.5), one point source at (20, 60), intensity probes at
+(80, {35, 50, 65}), loss CE(normalize_power(sum_t I), label).
+
+A step is rho -> c, the forward time loop, the loss, the hand-written adjoint
+back to dL/drho.  Metric: cell-steps/s = batch * 120^2 * 3500 / step time
+(the adjoint is not counted again).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Prints ONE JSON line (rank 0).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+
+METRIC = "cell-steps/s fwd+adjoint, fused vs plain per-step on GB300, grad rel err <=1e-5"
+WORKLOAD = dict(workload="batched training step: B=32, 120x120 (PML 20), T=3500, linear, "
+                         "fwd + hand-written adjoint to dL/drho",
+                batch=32, nx=120, ny=120, steps=3500, abs_N=20)
+BYTES_FWD = 12     # algorithmic bytes per forward cell-step (read y_t, y_{t-1}; write y_{t+1})
+BYTES_ADJ = 20     # per adjoint cell-step (read lam_{t+1}, lam_{t+2}, h_{t-1}; write lam_t; + y)
+L2_FLUSH_BYTES = 512 << 20
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=5)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    p.add_argument("--form", choices=["fused", "plain"], default="fused")
+    p.add_argument("--no-plain", action="store_true", help="skip the plain-form comparison")
+    p.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
+    p.add_argument("--batch", type=int, default=WORKLOAD["batch"])
+    p.add_argument("--T", type=int, default=WORKLOAD["steps"])
+    return p.parse_args()
+
+
+# ---------------------------------------------------------------------------
+def dist_env():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def max_over_ranks(v: float, world: int, device=None) -> float:
+    """Largest value of v over all ranks (identity for one process)."""
+    if world <= 1:
+        return v
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([v], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(world: int, device=None):
+    if world > 1:
+        import torch.distributed as dist
+        if device is not None and device.type == "cuda":
+            dist.barrier(device_ids=[device.index])
+        else:
+            dist.barrier()
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle samples taken while the timed region runs."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            threading.Thread(target=self._read, daemon=True).start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.lines:
+            return None
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peaks():
+    p = os.path.join(HERE, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as fh:
+            d = json.load(fh)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def committed_traffic(kernel: str):
+    """Per-launch DRAM bytes of `kernel` from the committed ncu summary."""
+    p = os.path.join(HERE, "profiles", "traffic.json")
+    if not os.path.exists(p):
+        return None
+    with open(p) as fh:
+        d = json.load(fh)
+    return d.get(kernel)
+
+
+# ---------------------------------------------------------------------------
+def build_model(dev, B, T, seed, form):
+    import numpy as np
+    import torch
+    import wavetorch_gb300 as wt
+    from wavetorch_gb300.data import vowel_like
+    N = WORKLOAD["nx"]
+    rho = torch.rand(N, N, generator=torch.Generator().manual_seed(seed))
+    geom = wt.WaveGeometryFreeForm((N, N), 1.0, c0=1.0, c1=0.5, abs_N=WORKLOAD["abs_N"],
+                                   abs_sig=3.0, abs_p=2, eta=0.5, beta=100.0, rho=rho)
+    cell = wt.WaveCell(0.707, geom)
+    model = wt.WaveRNN(cell, wt.WaveSource(20, 60),
+                       [wt.WaveIntensityProbe(80, y) for y in (35, 50, 65)], form=form).to(dev)
+    x, labels = vowel_like(B, T, seed=seed)
+    return model, np.ascontiguousarray(x), labels
+
+
+def train_step(model, x, labels):
+    import torch
+    import wavetorch_gb300 as wt
+    model.cell.geom.rho.grad = None
+    y = model(x)
+    loss = torch.nn.CrossEntropyLoss()(wt.utils.normalize_power(y.sum(dim=1)), labels)
+    loss.backward()
+    return loss
+
+
+def run_ours(args):
+    import numpy as np
+    import torch
+    import torch.distributed as dist
+    from wavetorch_gb300 import _lib
+    from wavetorch_gb300.functional import SeqSpec, lap_order, scalars, seq_backward, seq_forward
+
+    world, rank, local = dist_env()
+    if world > 1:
+        dist.init_process_group("nccl", init_method="env://")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    B, T, N = args.batch, args.T, WORKLOAD["nx"]
+    cell_steps = B * N * N * T
+
+    model, x_np, lab_np = build_model(dev, B, T, seed=1234 + rank, form=args.form)
+    x = torch.from_numpy(x_np).to(dev)
+    labels = torch.from_numpy(lab_np).to(dev)
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
+    stream = torch.cuda.current_stream(dev)
+
+    for _ in range(args.warmup):
+        train_step(model, x, labels)
+    torch.cuda.synchronize(dev)
+
+    # ---- device-resident timed region: K steps, L2 flushed before each ----
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+           for _ in range(args.steps)]
+    launches0 = _lib.kernel_launches()
+    barrier(world, dev)
+    torch.cuda.synchronize(dev)
+    with ClockSampler(local) as clk:
+        for k in range(args.steps):
+            flush.zero_()
+            evs[k][0].record(stream)
+            train_step(model, x, labels)
+            evs[k][1].record(stream)
+        torch.cuda.synchronize(dev)
+    barrier(world, dev)
+    launches = (_lib.kernel_launches() - launches0) // max(1, args.steps)
+    t_step = sum(a.elapsed_time(b) for a, b in evs) / 1e3 / args.steps
+    t_step = max_over_ranks(t_step, world, dev)
+    value = world * cell_steps / t_step
+    grad_fused = model.cell.geom.rho.grad.detach().clone()
+
+    # ---- end to end through the public API with host buffers ----
+    x_host = torch.from_numpy(x_np).pin_memory()
+    l_host = torch.from_numpy(lab_np).pin_memory()
+    g_host = torch.empty((N, N), dtype=torch.float32).pin_memory()
+    loss_host = torch.empty((), dtype=torch.float32).pin_memory()
+    for _ in range(2):
+        xd = x_host.to(dev, non_blocking=True)
+        ld = l_host.to(dev, non_blocking=True)
+        loss = train_step(model, xd, ld)
+        g_host.copy_(model.cell.geom.rho.grad, non_blocking=True)
+        loss_host.copy_(loss.detach(), non_blocking=True)
+    barrier(world, dev)
+    torch.cuda.synchronize(dev)
+    e0 = time.perf_counter()
+    for k in range(args.steps):
+        xd = x_host.to(dev, non_blocking=True)
+        ld = l_host.to(dev, non_blocking=True)
+        loss = train_step(model, xd, ld)
+        g_host.copy_(model.cell.geom.rho.grad, non_blocking=True)
+        loss_host.copy_(loss.detach(), non_blocking=True)
+        torch.cuda.synchronize(dev)
+    t_e2e = (time.perf_counter() - e0) / args.steps
+    t_e2e = max_over_ranks(t_e2e, world, dev)
+    h2d = x_host.numel() * 4 + l_host.numel() * 8
+    d2h = g_host.numel() * 4 + 4
+
+    # ---- the kernels alone (roofline of the dominant kernel) ----
+    geom = model.cell.geom
+    with torch.no_grad():
+        c = geom.c.contiguous()
+    b = geom.b.contiguous()
+    sc = scalars(0.707, 1.0, lap_order(B, N, N, 1.0))
+    src = model.source_table(B)
+    prb, _ = model.probe_table()
+    form_id = _lib.WT_FORM_FUSED if args.form == "fused" else _lib.WT_FORM_PLAIN
+    spec = SeqSpec(B, N, N, T, src, prb, form=form_id)
+    gout = torch.randn(B, T, len(prb), generator=torch.Generator().manual_seed(3)).to(dev)
+    kf, kb = [], []
+    for k in range(args.warmup + args.steps):
+        flush.zero_()
+        e = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+        e[0].record(stream)
+        out, _, _, ws = seq_forward(spec, sc, b, c, x)
+        e[1].record(stream)
+        seq_backward(spec, sc, b, c, x, gout, ws, False)
+        e[2].record(stream)
+        torch.cuda.synchronize(dev)
+        if k >= args.warmup:
+            kf.append(e[0].elapsed_time(e[1]) / 1e3)
+            kb.append(e[1].elapsed_time(e[2]) / 1e3)
+        del ws
+    t_f, t_b = statistics.mean(kf), statistics.mean(kb)
+    dom, t_dom, bpc = ("seq_bwd_fused_kernel", t_b, BYTES_ADJ) if t_b >= t_f else \
+        ("seq_fwd_fused_kernel", t_f, BYTES_FWD)
+    if args.form == "plain":
+        dom = "seq_adj_step_kernel" if t_b >= t_f else "step_fwd_kernel"
+    peak, peak_src = measured_peaks()
+    achieved = bpc * cell_steps / t_dom / 1e9
+    traffic = committed_traffic(dom)
+
+    # ---- plain per-step form: the metric's comparison arm ----
+    plain = None
+    if not args.no_plain and args.form == "fused":
+        pm = model
+        pm.form = "plain"
+        train_step(pm, x, labels)
+        torch.cuda.synchronize(dev)
+        pe = []
+        for k in range(max(2, min(args.steps, 3))):
+            flush.zero_()
+            a, z = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            train_step(pm, x, labels)
+            z.record(stream)
+            torch.cuda.synchronize(dev)
+            pe.append(a.elapsed_time(z) / 1e3)
+        grad_plain = pm.cell.geom.rho.grad.detach().clone()
+        pm.form = "fused"
+        t_plain = max_over_ranks(statistics.mean(pe), world, dev)
+        g_rel = float(torch.linalg.norm((grad_fused - grad_plain).double()) /
+                      torch.linalg.norm(grad_plain.double()))
+        plain = {"value": world * cell_steps / t_plain, "ms_per_step": t_plain * 1e3,
+                 "fused_over_plain": t_plain / t_step,
+                 "grad_rel_err_fused_vs_plain": g_rel,
+                 "note": "plain = one kernel per step, every field kept; bit-exact with the "
+                         "reference's float32 CPU path"}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        cpu = cpu_baseline(sample_T=1000)
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "cell-steps/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_step * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "fp32",
+            "data": "synthetic (seeded vowel-like waveforms, random-init rho)",
+            "config": {**WORKLOAD, "batch": B, "steps": T, "form": args.form,
+                       "l2": "flushed (512 MiB write) before every timed step",
+                       "parallelism": "replicas" if world > 1 else "single GPU"},
+            "e2e": {"value": world * cell_steps / t_e2e, "unit": "cell-steps/s",
+                    "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                    "ms_per_step": t_e2e * 1e3},
+            "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak,
+                         "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
+                         "peak_source": f"hbm_gbs of {peak_src}",
+                         "algorithmic_bytes_per_cell_step": bpc,
+                         "ms_fwd_kernel": t_f * 1e3, "ms_bwd_kernels": t_b * 1e3},
+            "cpu_baseline": cpu,
+            "plain_form": plain,
+            "clocks": clk.summary(),
+            "gpu_launches": int(launches),
+        }
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+
+
+# ---------------------------------------------------------------------------
+def cpu_baseline(sample_T: int, batch: int = WORKLOAD["batch"]):
+    """The oracle port (plain C, OpenMP over all host threads) on a bounded
+    sample of the workload: the full batch and grid, the first sample_T steps."""
+    import numpy as np
+    import oracle.oracle as o
+    import torch
+    from wavetorch_gb300.data import vowel_like
+    from wavetorch_gb300.geom import pml_profile
+    N, T = WORKLOAD["nx"], sample_T
+    b = pml_profile((N, N), WORKLOAD["abs_N"], 3.0, 2).numpy()
+    rho = torch.rand(N, N, generator=torch.Generator().manual_seed(1234)).numpy()
+    rho[b > 0] = 0
+    kern = np.full((3, 3), np.float32(1.0) / np.float32(9.0), np.float32)
+    c, _ = o.rho_to_c(rho, kern, 1, 0.5, 100.0, 1.0, 0.5)
+    x, _ = vowel_like(batch, T, seed=1234)
+    S = o.Seq(batch, N, N, T, 0.707, 1.0, [(20 * N + 60, -1)],
+              [(80 * N + y, 1, i) for i, y in enumerate((35, 50, 65))])
+    g = np.ones((batch, T, 3), np.float32) * 1e-3
+    t0 = time.perf_counter()
+    out, hist = S.forward(b, c, x)
+    S.backward(b, c, hist, g)
+    dt = time.perf_counter() - t0
+    return {"value": batch * N * N * T / dt, "unit": "cell-steps/s", "cores": o.num_threads(),
+            "kind": "port",
+            "sample": f"batch {batch}, {N}x{N}, first {T} of {WORKLOAD['steps']} steps, "
+                      f"fwd + adjoint, {dt:.2f} s"}
+
+
+def run_reference(args):
+    world, rank, _ = dist_env()
+    if rank != 0:
+        return
+    import oracle.oracle as o
+    o.build()
+    B = args.batch
+    sample_T = 350
+    for _ in range(args.warmup):
+        cpu_baseline(sample_T, B)
+    vals = [cpu_baseline(sample_T, B) for _ in range(args.steps)]
+    v = statistics.mean(r["value"] for r in vals)
+    N = WORKLOAD["nx"]
+    ms = B * N * N * args.T / v * 1e3
+    line = {"metric": METRIC, "value": v, "unit": "cell-steps/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "fp32",
+            "data": "synthetic (seeded vowel-like waveforms, random-init rho)",
+            "config": {**WORKLOAD, "batch": B, "form": "reference CPU path (oracle port)"},
+            "impl": "reference",
+            "cpu_baseline": {"value": v, "unit": "cell-steps/s", "kind": "port",
+                             "cores": vals[0]["cores"], "sample": vals[0]["sample"]},
+            "e2e": {"value": v, "unit": "cell-steps/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,193 @@
+/*
+ * wavetorch_gb300 -- C ABI of the GB300 (sm_103a) time-stepping kernels for the
+ * damped 2-D scalar wave equation of fancompute/wavetorch v0.2.1.
+ *
+ * Conventions
+ *   - Every pointer argument is a DEVICE pointer (float32, C-contiguous) unless
+ *     the parameter name ends in "_host".  The caller owns all memory; the only
+ *     device memory the library uses beyond the caller's buffers is the
+ *     workspace the caller passes in (size from the *_workspace_bytes queries).
+ *   - Fields are row-major [batch][nx][ny]: x is the row index, y the column
+ *     index, exactly the reference's tensor layout (wavetorch/rnn.py:39-41).
+ *   - Every call is asynchronous on the given stream and returns a status code
+ *     (WT_OK on success).  No exception crosses this boundary.
+ *   - Arithmetic is IEEE float32 in the reference's own association order, so
+ *     the per-step entry points reproduce the reference's CPU results bit for
+ *     bit (see each entry point for the remaining differences).
+ */
+#ifndef WAVETORCH_GB300_H
+#define WAVETORCH_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct CUstream_st* wt_stream_t; /* == cudaStream_t */
+
+/* ---- status codes ------------------------------------------------------- */
+#define WT_OK               0
+#define WT_ERR_INVALID      1  /* bad argument (shape, index, null pointer)  */
+#define WT_ERR_CUDA         2  /* a CUDA runtime call failed                 */
+#define WT_ERR_TIMEOUT      3  /* a bounded device-side wait gave up         */
+#define WT_ERR_UNSUPPORTED  4  /* valid request this build cannot serve      */
+
+/* ---- Laplacian association order ---------------------------------------
+ * The reference computes the 5-point Laplacian with torch conv2d
+ * (wavetorch/operators.py:5-11).  On CPU torch picks oneDNN when the batch is
+ * above 1 or the grid has more than 20480 cells, else an im2col+GEMM path; the
+ * two sum the five taps in different orders:
+ *   WT_LAP_SEQ    : ((((w*u + w*l) - 4w*c) + w*r) + w*d)   (fused multiply-adds)
+ *   WT_LAP_PAIRED : (u + l) + (-4c + (r + d))              (h == 1 only)
+ * u/d are the x-1/x+1 neighbours, l/r the y-1/y+1 neighbours; taps outside the
+ * grid are zero (Dirichlet, conv2d padding=1).                              */
+#define WT_LAP_SEQ     0
+#define WT_LAP_PAIRED  1
+
+/* Physics scalars shared by every entry point.  dt and h are the float32
+ * values of the reference's `dt` buffer (wavetorch/cell.py:60) and the
+ * geometry's `h` buffer (wavetorch/geom.py:20).                             */
+typedef struct wt_scalars {
+    float dt;
+    float h;
+    int32_t lap_order;   /* WT_LAP_SEQ or WT_LAP_PAIRED */
+} wt_scalars;
+
+/* Library version / build identification ("wavetorch_gb300 <ver> sm_103a"). */
+const char* wt_version(void);
+/* Human-readable text for a status code. */
+const char* wt_status_string(int status);
+/* Text of the last CUDA error seen by this library in the calling thread. */
+const char* wt_last_error(void);
+/* Number of kernels this library has launched since it was loaded (all
+ * threads); a diagnostic for counting the launches of a timed region.  No
+ * counterpart in the reference, which has no kernels of its own.          */
+uint64_t wt_kernel_launches(void);
+
+/* ======================================================================== *
+ * 1. One leapfrog step: drop-in for TimeStep (wavetorch/cell.py:20-44).     *
+ * ======================================================================== */
+
+/* Forward, wavetorch/cell.py:12-17:
+ *   y = (dt^-2 + b dt^-1)^-1 * ((2/dt^2) y1 - (dt^-2 - b dt^-1) y2 + c^2 Lap(y1))
+ * b, c: [nx,ny] (coef_batched == 0) or [batch,nx,ny] (coef_batched == 1).
+ * y1, y2, y: [batch,nx,ny].  Bit-exact with the reference's float32 CPU path. */
+int wt_step_fwd(const wt_scalars* s, int32_t batch, int32_t nx, int32_t ny,
+                int32_t coef_batched, const float* b, const float* c,
+                const float* y1, const float* y2, float* y, wt_stream_t stream);
+
+/* Backward, wavetorch/cell.py:26-44.  Each output pointer may be NULL (that
+ * input needs no gradient).  When coef_batched == 0, grad_b and grad_c are
+ * [nx,ny]: the [batch,nx,ny] per-instance terms are summed over the batch in
+ * torch's CPU order (sequential within blocks of 16, blocks added in order),
+ * which is what autograd's sum-to-shape does in the reference.  When
+ * coef_batched == 1 they are [batch,nx,ny].                                 */
+int wt_step_bwd(const wt_scalars* s, int32_t batch, int32_t nx, int32_t ny,
+                int32_t coef_batched, const float* b, const float* c,
+                const float* y1, const float* y2, const float* grad_y,
+                float* grad_b, float* grad_c, float* grad_y1, float* grad_y2,
+                wt_stream_t stream);
+
+/* ======================================================================== *
+ * 2. A whole sequence: drop-in for the time loop of WaveRNN.forward         *
+ *    (wavetorch/rnn.py:50-70) and its backward through T TimeStep nodes.    *
+ * ======================================================================== */
+
+/* One injection: field[b, cell] += x[in_row(b), t] every step, applied after
+ * the update in table order (wavetorch/source.py:15-22, rnn.py:56-57).
+ * in_row == -1 means "the instance's own row b"; in_row >= 0 means that fixed
+ * row of x for every instance (the reference's broadcast of a [batch] input
+ * over a line of `batch` cells, source.py:19-20).                           */
+typedef struct wt_source_entry {
+    int32_t cell;      /* x*ny + y */
+    int32_t in_row;
+} wt_source_entry;
+
+/* One probe output column q: out[b, t, q] = field[b, cell] (kind 0, WaveProbe,
+ * probe.py:14-15) or its square (kind 1, WaveIntensityProbe, probe.py:26-27),
+ * read after the injection.  `order` is the reference's probe index, which
+ * fixes the order in which backward seeds are added (descending order).     */
+typedef struct wt_probe_entry {
+    int32_t cell;
+    int32_t kind;
+    int32_t order;
+} wt_probe_entry;
+
+#define WT_FORM_PLAIN  0   /* per-step kernels, every field kept (exact)     */
+#define WT_FORM_FUSED  1   /* persistent cluster kernels, checkpointed       */
+
+typedef struct wt_seq_desc {
+    int32_t batch, nx, ny, steps;
+    int32_t n_sources;
+    const wt_source_entry* sources_host;   /* host array, n_sources entries  */
+    int32_t n_probes;
+    const wt_probe_entry* probes_host;     /* host array, n_probes entries   */
+    int32_t form;                          /* WT_FORM_PLAIN / WT_FORM_FUSED  */
+    int32_t segment;                       /* checkpoint interval, 0 = auto  */
+    int32_t cluster;                       /* CTAs per instance, 0 = auto    */
+    int32_t output_fields;                 /* 1: also write every field      */
+} wt_seq_desc;
+
+/* Bytes of workspace that wt_seq_fwd must be given and that must be handed,
+ * unchanged, to wt_seq_bwd (checkpoints or the full field history, plus the
+ * per-step probe amplitudes).                                               */
+int wt_seq_workspace_bytes(const wt_seq_desc* d, size_t* bytes);
+
+/* Forward.  b, c: [nx,ny]; x: [batch,steps]; out: [batch,steps,n_probes];
+ * fields (only if output_fields): [batch,steps,nx,ny]; probe_sum (nullable):
+ * [batch,n_probes] Kahan-compensated time sums of out.                      */
+int wt_seq_fwd(const wt_scalars* s, const wt_seq_desc* d,
+               const float* b, const float* c, const float* x,
+               float* out, float* fields, float* probe_sum,
+               void* workspace, size_t workspace_bytes, wt_stream_t stream);
+
+/* Backward.  grad_out: [batch,steps,n_probes] (dLoss/d out).  grad_c: [nx,ny],
+ * overwritten with dLoss/dc.  grad_x (nullable): [batch,steps], overwritten
+ * with dLoss/dx.  The plain form is bit-exact with the reference; the fused
+ * form sums the per-instance terms over time first and then over the batch. */
+int wt_seq_bwd(const wt_scalars* s, const wt_seq_desc* d,
+               const float* b, const float* c, const float* x,
+               const float* grad_out, float* grad_c, float* grad_x,
+               void* workspace, size_t workspace_bytes, wt_stream_t stream);
+
+/* Waits for `stream`, then reads the device-side status word that the last
+ * wt_seq_fwd / wt_seq_bwd on this workspace left (bounds checks inside the
+ * kernels record instead of trapping).  Returns WT_OK, WT_ERR_INVALID
+ * (a device-side bounds check fired) or WT_ERR_TIMEOUT.                      */
+int wt_seq_device_status(const wt_seq_desc* d, const void* workspace, size_t workspace_bytes,
+                         wt_stream_t stream);
+
+/* ======================================================================== *
+ * 3. Free-form geometry: rho -> c (wavetorch/geom.py:207-233).              *
+ * ======================================================================== */
+
+typedef struct wt_geom_desc {
+    int32_t nx, ny;
+    int32_t blur_radius;      /* kernel is (2r+1)^2, weights from blur_kernel */
+    int32_t blur_n;           /* blur passes                                  */
+    float eta, beta;          /* projection parameters                        */
+    float c0, c1;             /* float32 values of the c0/c1 buffers          */
+} wt_geom_desc;
+
+/* c = c0 + (c1-c0) * P(blur^n(rho)),  P(r) = (tanh(beta eta) + tanh(beta (r-eta)))
+ *                                           / (tanh(beta eta) + tanh(beta (1-eta))).
+ * blur_kernel: [(2r+1),(2r+1)] device weights.  work: 2*nx*ny floats scratch
+ * (caller-owned) that wt_rho_to_c_bwd reads back: it holds the last blurred
+ * density and the tanh values.                                              */
+int wt_rho_to_c_fwd(const wt_geom_desc* g, const float* rho, const float* blur_kernel,
+                    float* c, float* work, wt_stream_t stream);
+
+/* grad_rho = (d c / d rho)^T grad_c, using `work` from the matching forward
+ * (it reads the stored tanh values and reuses the rest as scratch).         */
+int wt_rho_to_c_bwd(const wt_geom_desc* g, const float* rho, const float* blur_kernel,
+                    const float* grad_c, float* grad_rho, float* work, wt_stream_t stream);
+
+/* Bytes of `work` the two calls above need (2 * nx * ny floats). */
+int wt_rho_to_c_work_bytes(const wt_geom_desc* g, size_t* bytes);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* WAVETORCH_GB300_H */

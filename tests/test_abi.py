@@ -1,0 +1,114 @@
+"""The C-ABI library builds, loads and exports every symbol the header
+declares; host-side argument validation (no GPU needed for any of this)."""
+import ctypes as C
+import os
+import re
+import shutil
+
+import pytest
+
+from conftest import ROOT
+
+HEADER = os.path.join(ROOT, "include", "wavetorch_gb300.h")
+
+
+def declared_functions():
+    text = open(HEADER).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(wt_[a-z0-9_]+)\s*\(", text)))
+
+
+@pytest.fixture(scope="module")
+def lib():
+    if not (shutil.which("nvcc") or os.path.exists("/usr/local/cuda/bin/nvcc")):
+        pytest.skip("nvcc not available")
+    from wavetorch_gb300 import _lib
+    return _lib.load()
+
+
+def test_header_declares_the_api():
+    names = declared_functions()
+    for n in ["wt_step_fwd", "wt_step_bwd", "wt_seq_fwd", "wt_seq_bwd", "wt_seq_workspace_bytes",
+              "wt_rho_to_c_fwd", "wt_rho_to_c_bwd"]:
+        assert n in names
+
+
+def test_every_declared_symbol_is_exported(lib):
+    from wavetorch_gb300 import _lib
+    names = declared_functions()
+    assert set(names) == set(_lib.EXPORTED)
+    for n in names:
+        assert hasattr(lib, n), n
+
+
+def test_version_and_status_strings(lib):
+    assert b"sm_103a" in lib.wt_version()
+    assert lib.wt_status_string(1) == b"invalid argument"
+
+
+def _desc(B=2, N=32, T=10, sources=((5 * 32 + 16, -1),), probes=((20 * 32 + 16, 1, 0),),
+          form=1, cluster=0):
+    from wavetorch_gb300 import _lib
+    src = (_lib.SourceEntry * max(1, len(sources)))(*[_lib.SourceEntry(*s) for s in sources])
+    prb = (_lib.ProbeEntry * max(1, len(probes)))(*[_lib.ProbeEntry(*p) for p in probes])
+    d = _lib.SeqDesc(B, N, N, T, len(sources), C.cast(src, C.POINTER(_lib.SourceEntry)),
+                     len(probes), C.cast(prb, C.POINTER(_lib.ProbeEntry)), form, 0, cluster, 0)
+    return d, (src, prb)
+
+
+def test_workspace_query(lib):
+    from wavetorch_gb300 import _lib
+    for form in (0, 1):
+        d, keep = _desc(form=form)
+        n = C.c_size_t(0)
+        assert lib.wt_seq_workspace_bytes(C.byref(d), C.byref(n)) == _lib.WT_OK
+        assert n.value > 0
+    # the plain form keeps every field: at least T * B * N * N floats
+    d, keep = _desc(form=0, B=2, N=32, T=10)
+    n = C.c_size_t(0)
+    lib.wt_seq_workspace_bytes(C.byref(d), C.byref(n))
+    assert n.value >= 10 * 2 * 32 * 32 * 4
+
+
+@pytest.mark.parametrize("bad", [
+    dict(sources=((32 * 32, -1),)),          # cell out of range
+    dict(sources=((5, 2),)),                  # input row >= batch
+    dict(probes=((5, 2, 0),)),                # unknown probe kind
+    dict(probes=((-1, 1, 0),)),
+    dict(B=0), dict(T=0), dict(form=7),
+])
+def test_invalid_descriptors_rejected(lib, bad):
+    from wavetorch_gb300 import _lib
+    d, keep = _desc(**bad)
+    n = C.c_size_t(0)
+    assert lib.wt_seq_workspace_bytes(C.byref(d), C.byref(n)) == _lib.WT_ERR_INVALID
+
+
+def test_fused_tap_capacity(lib):
+    """More than 4 source entries on one thread's cells is refused (the plain
+    form serves it)."""
+    from wavetorch_gb300 import _lib
+    srcs = tuple((r * 32 + 16, -1) for r in range(1, 6))   # one column, 5 rows of one strip
+    d, keep = _desc(sources=srcs, form=1)
+    n = C.c_size_t(0)
+    assert lib.wt_seq_workspace_bytes(C.byref(d), C.byref(n)) == _lib.WT_ERR_UNSUPPORTED
+    d, keep = _desc(sources=srcs, form=0)
+    assert lib.wt_seq_workspace_bytes(C.byref(d), C.byref(n)) == _lib.WT_OK
+
+
+def test_step_entry_points_validate_before_touching_the_device(lib):
+    from wavetorch_gb300 import _lib
+    sc = _lib.Scalars(0.707, 1.0, 0)
+    assert lib.wt_step_fwd(C.byref(sc), 1, 8, 8, 0, None, None, None, None, None, None) == _lib.WT_ERR_INVALID
+    bad = _lib.Scalars(-1.0, 1.0, 0)
+    p = C.c_void_p(16)
+    assert lib.wt_step_fwd(C.byref(bad), 1, 8, 8, 0, p, p, p, p, C.c_void_p(32), None) == _lib.WT_ERR_INVALID
+    assert lib.wt_step_fwd(C.byref(sc), 1, 8, 8, 0, p, p, p, p, p, None) == _lib.WT_ERR_INVALID  # y aliases y1
+
+
+def test_geom_work_bytes(lib):
+    from wavetorch_gb300 import _lib
+    g = _lib.GeomDesc(10, 12, 1, 1, 0.5, 100.0, 1.0, 0.5)
+    n = C.c_size_t(0)
+    assert lib.wt_rho_to_c_work_bytes(C.byref(g), C.byref(n)) == 0
+    assert n.value == 2 * 10 * 12 * 4

@@ -1,0 +1,142 @@
+"""GPU checks at the benchmark's full sizes, where the oracle is too slow or
+too large to run whole: agreement with the oracle on a truncated horizon,
+plain/fused agreement at full length, and size-independent properties
+(exact linearity under power-of-two input scaling, silence for zero input)."""
+import numpy as np
+import pytest
+import torch
+
+import oracle.oracle as o
+from wavetorch_gb300 import _lib
+from wavetorch_gb300.data import vowel_like
+from wavetorch_gb300.functional import (SeqSpec, lap_order, scalars, seq_backward,
+                                        seq_device_status, seq_forward)
+import wavetorch_gb300 as wt
+
+pytestmark = pytest.mark.gpu
+
+
+def rel(a, b):
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    return np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300)
+
+
+def cfg1_problem(dev, B=32, N=120, steps=3500, seed=11):
+    geom = wt.WaveGeometryFreeForm((N, N), 1.0, c0=1.0, c1=0.5, abs_N=20, abs_sig=3.0, abs_p=2,
+                                   rho=torch.rand(N, N, generator=torch.Generator().manual_seed(seed)))
+    geom = geom.to(dev)
+    with torch.no_grad():
+        c = geom.c.detach().contiguous()
+    b = geom.b.contiguous()
+    x, labels = vowel_like(B, steps, seed=seed)
+    src = [(20 * N + 60, -1)]
+    prb = [(80 * N + y, 1, i) for i, y in enumerate((35, 50, 65))]
+    return b, c, torch.from_numpy(x).to(dev), labels, src, prb
+
+
+def run(spec, sc, b, c, x, g=None):
+    out, _, _, ws = seq_forward(spec, sc, b, c, x)
+    gc = None
+    if g is not None:
+        gc, _ = seq_backward(spec, sc, b, c, x, g, ws, False)
+    torch.cuda.synchronize()
+    assert seq_device_status(spec, ws) == _lib.WT_OK
+    return out, gc
+
+
+def test_cfg1_batch_against_oracle_truncated(cuda):
+    """B=32, 120x120, first 600 steps: plain form bit-exact with the oracle,
+    fused form forward bit-exact and dL/dc within 1e-6."""
+    B, N, steps = 32, 120, 600
+    b, c, x, _, src, prb = cfg1_problem(cuda, B, N, 3500)
+    x = x[:, :steps].contiguous()
+    g = torch.randn(B, steps, 3, generator=torch.Generator().manual_seed(5)).to(cuda)
+    sc = scalars(0.707, 1.0, lap_order(B, N, N, 1.0))
+    S = o.Seq(B, N, N, steps, 0.707, 1.0, src, prb)
+    oout, hist = S.forward(b.cpu().numpy(), c.cpu().numpy(), x.cpu().numpy())
+    ogc, _ = S.backward(b.cpu().numpy(), c.cpu().numpy(), hist, g.cpu().numpy())
+    for form in (_lib.WT_FORM_PLAIN, _lib.WT_FORM_FUSED):
+        spec = SeqSpec(B, N, N, steps, src, prb, form=form)
+        out, gc = run(spec, sc, b, c, x, g)
+        assert np.array_equal(out.cpu().numpy(), oout), form
+        if form == _lib.WT_FORM_PLAIN:
+            assert np.array_equal(gc.cpu().numpy(), ogc)
+        else:
+            assert rel(gc.cpu().numpy(), ogc) <= 1e-6
+
+
+def test_cfg1_full_plain_vs_fused(cuda):
+    """The benchmark workload (B=32, 120x120, T=3500): both forms agree."""
+    b, c, x, _, src, prb = cfg1_problem(cuda)
+    B, steps = x.shape
+    N = 120
+    g = torch.randn(B, steps, 3, generator=torch.Generator().manual_seed(6)).to(cuda)
+    sc = scalars(0.707, 1.0, lap_order(B, N, N, 1.0))
+    outs, gcs = {}, {}
+    for form in (_lib.WT_FORM_PLAIN, _lib.WT_FORM_FUSED):
+        spec = SeqSpec(B, N, N, steps, src, prb, form=form)
+        outs[form], gcs[form] = run(spec, sc, b, c, x, g)
+    assert torch.equal(outs[0], outs[1])
+    assert rel(gcs[1].cpu().numpy(), gcs[0].cpu().numpy()) <= 1e-6
+    assert torch.isfinite(gcs[1]).all()
+
+
+@pytest.mark.parametrize("form", [_lib.WT_FORM_PLAIN, _lib.WT_FORM_FUSED])
+def test_power_of_two_scaling_is_exact(cuda, form):
+    """Scaling the input by 2 scales every field by 2 exactly (every operation
+    is a float32 multiply/add, which commutes exactly with powers of two), so
+    intensities scale by exactly 4 and dL/dc by exactly 2 for a linear seed."""
+    b, c, x, _, src, prb = cfg1_problem(cuda, B=32, N=120, steps=3500)
+    B, steps = x.shape
+    sc = scalars(0.707, 1.0, lap_order(B, 120, 120, 1.0))
+    spec = SeqSpec(B, 120, 120, steps, src, prb, form=form)
+    g = torch.randn(B, steps, 3, generator=torch.Generator().manual_seed(7)).to(cuda)
+    o1, g1 = run(spec, sc, b, c, x, g)
+    o2, g2 = run(spec, sc, b, c, 2 * x, g)
+    assert torch.equal(o2, 4 * o1)
+    # intensity seeds g * 2y double with y, so the adjoint doubles
+    assert torch.equal(g2, 2 * g1) or rel(g2.cpu().numpy(), 2 * g1.cpu().numpy()) <= 1e-6
+
+
+def test_zero_input_is_silent(cuda):
+    b, c, x, _, src, prb = cfg1_problem(cuda, B=4, N=120, steps=500)
+    sc = scalars(0.707, 1.0, lap_order(4, 120, 120, 1.0))
+    for form in (_lib.WT_FORM_PLAIN, _lib.WT_FORM_FUSED):
+        spec = SeqSpec(4, 120, 120, 500, src, prb, form=form)
+        out, _ = run(spec, sc, b, c, torch.zeros_like(x))
+        assert torch.count_nonzero(out) == 0
+
+
+def test_ragged_segments(cuda):
+    """Checkpoint intervals that do not divide T give the same adjoint."""
+    b, c, x, _, src, prb = cfg1_problem(cuda, B=3, N=120, steps=301)
+    B, steps = x.shape
+    sc = scalars(0.707, 1.0, lap_order(B, 120, 120, 1.0))
+    g = torch.randn(B, steps, 3, generator=torch.Generator().manual_seed(8)).to(cuda)
+    ref_spec = SeqSpec(B, 120, 120, steps, src, prb, form=_lib.WT_FORM_PLAIN)
+    _, gref = run(ref_spec, sc, b, c, x, g)
+    for seg in (1, 7, 64, 301, 1000):
+        spec = SeqSpec(B, 120, 120, steps, src, prb, form=_lib.WT_FORM_FUSED, segment=seg)
+        _, gf = run(spec, sc, b, c, x, g)
+        assert rel(gf.cpu().numpy(), gref.cpu().numpy()) <= 1e-6, seg
+
+
+@pytest.mark.parametrize("cluster", [1, 2, 4, 8])
+def test_cluster_sizes_agree(cuda, cluster):
+    N = 64
+    geom = wt.WaveGeometryFreeForm((N, N), 1.0, c0=1.0, c1=0.5, abs_N=10, abs_sig=3.0, abs_p=2,
+                                   rho=torch.rand(N, N, generator=torch.Generator().manual_seed(9))).to(cuda)
+    with torch.no_grad():
+        c = geom.c.contiguous()
+    b = geom.b.contiguous()
+    x = torch.from_numpy(vowel_like(2, 200, seed=9)[0]).to(cuda)
+    src = [(10 * N + 32, -1)]
+    prb = [(50 * N + 32, 1, 0), (50 * N + 20, 0, 1)]
+    sc = scalars(0.707, 1.0, lap_order(2, N, N, 1.0))
+    g = torch.randn(2, 200, 2, generator=torch.Generator().manual_seed(10)).to(cuda)
+    p_out, p_gc = run(SeqSpec(2, N, N, 200, src, prb, form=_lib.WT_FORM_PLAIN), sc, b, c, x, g)
+    f_out, f_gc = run(SeqSpec(2, N, N, 200, src, prb, form=_lib.WT_FORM_FUSED, cluster=cluster),
+                      sc, b, c, x, g)
+    assert torch.equal(p_out, f_out)
+    assert rel(f_gc.cpu().numpy(), p_gc.cpu().numpy()) <= 1e-6

@@ -1,0 +1,178 @@
+"""GPU parity: the CUDA kernels against the reference's golden vectors and the
+oracle.  Tolerances (relative L2):
+  * forward outputs and fields: bit-exact (0) for both sequence forms;
+  * dL/dc, plain form: bit-exact; fused form: <= 1e-6 (it sums each
+    instance over time before summing over the batch);
+  * end to end through rho -> c (tanh differs from the reference by ulps):
+    <= 1e-5, the parity bar for this path.
+"""
+import numpy as np
+import pytest
+import torch
+
+from conftest import golden
+import oracle.oracle as o
+import wavetorch_gb300 as wt
+from wavetorch_gb300 import _lib
+from wavetorch_gb300.functional import (SeqSpec, WaveStepFn, lap_order, scalars, seq_backward,
+                                        seq_device_status, seq_forward)
+
+pytestmark = pytest.mark.gpu
+
+SEQ_CASES = ["cfg0_small", "cfg1_small", "multi", "line"]
+FORMS = {"plain": _lib.WT_FORM_PLAIN, "fused": _lib.WT_FORM_FUSED}
+
+
+def rel(a, b):
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    return np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300)
+
+
+def T(a, dev):
+    return torch.from_numpy(np.ascontiguousarray(a)).to(dev)
+
+
+def spec_of(d, form, output_fields=False):
+    B, N, Tn = int(d["B"]), int(d["N"]), int(d["T"])
+    return SeqSpec(B, N, N, Tn, [tuple(map(int, s)) for s in d["sources"]],
+                   [] if output_fields else [tuple(map(int, p)) for p in d["probes"]],
+                   form=FORMS[form], output_fields=output_fields)
+
+
+def sc_of(d):
+    B, N = int(d["B"]), int(d["N"])
+    return scalars(float(d["dt"]), float(d["h"]), lap_order(B, N, N, float(d["h"])))
+
+
+@pytest.mark.parametrize("form", ["plain", "fused"])
+@pytest.mark.parametrize("name", SEQ_CASES)
+def test_seq_forward_bit_exact(cuda, name, form):
+    d = golden(name)
+    spec = spec_of(d, form)
+    b, c, x = T(d["b"], cuda), T(d["c"], cuda), T(d["x"], cuda)
+    out, _, _, ws = seq_forward(spec, sc_of(d), b, c, x)
+    torch.cuda.synchronize()
+    assert seq_device_status(spec, ws) == _lib.WT_OK
+    assert np.array_equal(out.cpu().numpy(), d["out"])
+
+
+@pytest.mark.parametrize("form", ["plain", "fused"])
+@pytest.mark.parametrize("name", SEQ_CASES)
+def test_seq_fields_bit_exact(cuda, name, form):
+    d = golden(name)
+    spec = spec_of(d, form, output_fields=True)
+    b, c, x = T(d["b"], cuda), T(d["c"], cuda), T(d["x"], cuda)
+    _, fields, _, _ = seq_forward(spec, sc_of(d), b, c, x)
+    f = fields.cpu().numpy()
+    for k in d.files:
+        if k.startswith("field_"):
+            t = int(k.split("_")[1])
+            assert np.array_equal(f[:, t], d[k]), k
+
+
+@pytest.mark.parametrize("form", ["plain", "fused"])
+@pytest.mark.parametrize("name", SEQ_CASES)
+def test_seq_backward(cuda, name, form):
+    d = golden(name)
+    spec = spec_of(d, form)
+    b, c, x = T(d["b"], cuda), T(d["c"], cuda), T(d["x"], cuda)
+    sc = sc_of(d)
+    _, _, _, ws = seq_forward(spec, sc, b, c, x)
+    gc, _ = seq_backward(spec, sc, b, c, x, T(d["grad_out"], cuda), ws, False)
+    torch.cuda.synchronize()
+    assert seq_device_status(spec, ws) == _lib.WT_OK
+    got = gc.cpu().numpy()
+    if form == "plain":
+        assert np.array_equal(got, d["grad_c"])
+    else:
+        assert rel(got, d["grad_c"]) <= 1e-6
+
+
+@pytest.mark.parametrize("name", ["step_b2_h025", "step_b1_h1", "step_b20_h1"])
+def test_timestep_drop_in(cuda, name):
+    d = golden(name)
+    dt, h = float(d["dt"]), float(d["h"])
+    b = T(d["b"], cuda).requires_grad_()
+    c = T(d["c"], cuda).requires_grad_()
+    y1 = T(d["y1"], cuda).requires_grad_()
+    y2 = T(d["y2"], cuda).requires_grad_()
+    y = WaveStepFn.apply(b, c, y1, y2, dt, h)
+    assert np.array_equal(y.detach().cpu().numpy(), d["y"])
+    gb, gc, gy1, gy2 = torch.autograd.grad(y, [b, c, y1, y2], T(d["grad_y"], cuda))
+    assert np.array_equal(gy1.cpu().numpy(), d["grad_y1"])
+    assert np.array_equal(gy2.cpu().numpy(), d["grad_y2"])
+    ob, oc, _, _ = o.step_bwd(d["b"], d["c"], d["y1"], d["y2"], d["grad_y"], dt, h)
+    assert np.array_equal(gb.cpu().numpy(), ob)
+    assert np.array_equal(gc.cpu().numpy(), oc)
+    assert rel(gb.cpu().numpy(), d["grad_b"]) < 1e-7
+    assert rel(gc.cpu().numpy(), d["grad_c"]) < 1e-7
+
+
+@pytest.mark.parametrize("name", ["geom_n100", "geom_n160", "cfg0_small"])
+def test_rho_to_c(cuda, name):
+    d = golden(name)
+    N = d["rho"].shape[0]
+    g = wt.WaveGeometryFreeForm((N, N), 1.0, c0=1.0, c1=0.5, abs_N=20, abs_sig=3.0, abs_p=2,
+                                rho=torch.from_numpy(d["rho"])).to(cuda)
+    with torch.no_grad():
+        g.rho.copy_(T(d["rho"], cuda))   # keep the stored (constrained) density
+    c = g.c
+    assert rel(c.detach().cpu().numpy(), d["c"]) < 3e-7
+    oc, th = o.rho_to_c(d["rho"], d["blur_kernel"], 1, 0.5, 100.0, 1.0, 0.5)
+    assert rel(c.detach().cpu().numpy(), oc) < 3e-7
+    (gr,) = torch.autograd.grad(c, [g.rho], T(d["grad_c"], cuda))
+    assert rel(gr.cpu().numpy(), d["grad_rho"]) < 5e-6
+
+
+def build_model(d, dev, form, cnl=0.0, b0=0.0, uth=0.0):
+    N = int(d["N"])
+    geom = wt.WaveGeometryFreeForm((N, N), 1.0, c0=1.0, c1=0.5, abs_N=int(d["abs_N"]),
+                                   abs_sig=3.0, abs_p=2, rho=torch.from_numpy(d["rho"]))
+    cell = wt.WaveCell(0.707, geom, satdamp_b0=b0, satdamp_uth=uth, c_nl=cnl)
+    srcs = [wt.WaveSource(int(cc) // N, int(cc) % N) for cc, _ in d["sources"]]
+    prbs = [(wt.WaveIntensityProbe if k else wt.WaveProbe)(int(cc) // N, int(cc) % N)
+            for cc, k, _ in d["probes"]]
+    m = wt.WaveRNN(cell, srcs, prbs, form=form).to(dev)
+    with torch.no_grad():
+        m.cell.geom.rho.copy_(T(d["rho"], dev))
+    return m
+
+
+@pytest.mark.parametrize("form", ["plain", "fused", "step"])
+@pytest.mark.parametrize("name", ["cfg0_small", "cfg1_small", "multi"])
+def test_end_to_end_training_step(cuda, name, form):
+    """rho -> c -> T steps -> CE(normalize_power(sum_t I)) -> rho.grad."""
+    d = golden(name)
+    m = build_model(d, cuda, form)
+    x = T(d["x"], cuda)
+    y = m(x)
+    loss = torch.nn.CrossEntropyLoss()(wt.utils.normalize_power(y.sum(dim=1)),
+                                       T(d["labels"], cuda))
+    loss.backward()
+    assert rel(y.detach().cpu().numpy(), d["out"]) <= 1e-5
+    assert abs(loss.item() - float(d["loss"])) <= 1e-5 * abs(float(d["loss"]))
+    assert rel(m.cell.geom.rho.grad.cpu().numpy(), d["grad_rho"]) <= 1e-5
+
+
+def test_nonlinear_step_form(cuda):
+    d = golden("nonlinear")
+    m = build_model(d, cuda, "step", cnl=float(d["c_nl"]), b0=float(d["satdamp_b0"]),
+                    uth=float(d["satdamp_uth"]))
+    y = m(T(d["x"], cuda))
+    loss = torch.nn.CrossEntropyLoss()(wt.utils.normalize_power(y.sum(dim=1)),
+                                       T(d["labels"], cuda))
+    loss.backward()
+    assert rel(y.detach().cpu().numpy(), d["out"]) <= 1e-5
+    assert rel(m.cell.geom.rho.grad.cpu().numpy(), d["grad_rho"]) <= 1e-5
+
+
+def test_cfg0_error_vs_fp64_is_at_the_reference_floor(cuda):
+    """Our float32 result against the reference run in float64, next to the
+    reference's own float32 result against float64."""
+    d = golden("cfg0_small")
+    m = build_model(d, cuda, "fused")
+    y = m(T(d["x"], cuda))
+    ours = rel(y.detach().cpu().numpy(), d["out64"])
+    theirs = rel(d["out"], d["out64"])
+    assert ours <= 2 * theirs + 1e-6

@@ -1,0 +1,137 @@
+"""Host-side behaviour of the drop-in modules (CPU only: no kernels run)."""
+import json
+import os
+
+import numpy as np
+import pytest
+import torch
+
+from conftest import GOLDEN, golden
+import wavetorch_gb300 as wt
+from wavetorch_gb300.functional import lap_order
+from wavetorch_gb300 import _lib
+
+
+def model_cfg0(N=100):
+    geom = wt.WaveGeometryFreeForm((N, N), 1.0, c0=1.0, c1=0.5, abs_N=20, abs_sig=3.0, abs_p=2,
+                                   rho=torch.rand(N, N, generator=torch.Generator().manual_seed(0)))
+    cell = wt.WaveCell(0.707, geom)
+    return wt.WaveRNN(cell, wt.WaveSource(20, 50), [wt.WaveIntensityProbe(80, y) for y in (35, 50, 65)])
+
+
+def test_pml_profile_matches_reference_bit_exact():
+    for name in ["cfg0_small", "cfg1_small", "geom_n160"]:
+        d = golden(name)
+        N = d["b"].shape[0]
+        abs_N = 20 if name != "multi" else 10
+        g = wt.WaveGeometryFreeForm((N, N), 1.0, c0=1.0, c1=0.5, abs_N=abs_N, abs_sig=3.0, abs_p=2)
+        assert np.array_equal(g.b.numpy(), d["b"]), name
+
+
+def test_blur_kernel_matches_reference():
+    d = golden("cfg0_small")
+    g = wt.WaveGeometryFreeForm((50, 50), 1.0, c0=1.0, c1=0.5, abs_N=10)
+    assert np.array_equal(g.blur_kernel[0, 0].numpy(), d["blur_kernel"])
+
+
+def test_state_dict_keys_match_reference():
+    ref = json.load(open(os.path.join(GOLDEN, "state_keys.json")))
+    geom = wt.WaveGeometryFreeForm((50, 50), 1.0, c0=1.0, c1=0.5, abs_N=10, abs_sig=3.0, abs_p=2,
+                                   rho='half')
+    model = wt.WaveRNN(wt.WaveCell(0.707, geom), [wt.WaveSource(10, 25)],
+                       [wt.WaveIntensityProbe(40, y) for y in (15, 25, 35)])
+    ours = {k: [list(v.shape), str(v.dtype)] for k, v in model.state_dict().items()}
+    assert ours == ref
+
+
+def test_cfl_violation_raises_value_error():
+    geom = wt.WaveGeometryFreeForm((50, 50), 1.0, c0=1.0, c1=0.5, abs_N=10)
+    with pytest.raises(ValueError, match="CFL"):
+        wt.WaveCell(0.8, geom)
+    wt.WaveCell(0.707, geom)   # 0.707 <= 1/sqrt(2)
+
+
+def test_pml_must_fit():
+    with pytest.raises(AssertionError):
+        wt.WaveGeometryFreeForm((40, 40), 1.0, c0=1.0, c1=0.5, abs_N=20)
+
+
+def test_rho_init_modes():
+    for mode in ("half", "blank", "rand"):
+        wt.WaveGeometryFreeForm((30, 30), 1.0, c0=1.0, c1=0.5, abs_N=5, rho=mode)
+    with pytest.raises(ValueError):
+        wt.WaveGeometryFreeForm((30, 30), 1.0, c0=1.0, c1=0.5, abs_N=5, rho='bogus')
+
+
+def test_constrain_to_design_region_zeroes_pml():
+    g = wt.WaveGeometryFreeForm((40, 40), 1.0, c0=1.0, c1=0.5, abs_N=8, rho='half')
+    assert torch.all(g.rho[g.b > 0] == 0)
+    assert torch.all(g.rho[g.b == 0] == 0.5)
+
+
+def test_parameters_are_only_rho():
+    m = model_cfg0(60)
+    names = [p.shape for p in m.parameters()]
+    assert names == [torch.Size([60, 60])]
+
+
+def test_no_cpu_fallback():
+    m = model_cfg0(60)
+    with pytest.raises((RuntimeError, _lib.WaveKernelError), match="CUDA|cuda"):
+        m(torch.zeros(1, 5))
+
+
+def test_lap_order_rule():
+    assert lap_order(1, 100, 100, 1.0) == _lib.WT_LAP_PAIRED
+    assert lap_order(32, 120, 120, 1.0) == _lib.WT_LAP_SEQ
+    assert lap_order(1, 1024, 1024, 1.0) == _lib.WT_LAP_SEQ
+    assert lap_order(1, 100, 100, 1.43) == _lib.WT_LAP_SEQ
+
+
+def test_source_table_broadcast_rules():
+    geom = wt.WaveGeometryFreeForm((64, 64), 1.0, c0=1.0, c1=0.5, abs_N=10)
+    line = wt.WaveLineSource(14, 12, 14, 50)
+    m = wt.WaveRNN(wt.WaveCell(0.707, geom), [wt.WaveSource(20, 30), line],
+                   [wt.WaveIntensityProbe(50, 20)])
+    t1 = m.source_table(1)
+    assert t1[0] == (20 * 64 + 30, -1)
+    assert len(t1) == 1 + 39 and all(r == -1 for _, r in t1)
+    with pytest.raises(RuntimeError, match="shape mismatch"):
+        m.source_table(3)
+    # batch == number of line cells: cell l takes instance l's input
+    t39 = m.source_table(39)
+    assert [r for _, r in t39[1:]] == list(range(39))
+
+
+def test_line_cells_match_golden():
+    d = golden("line")
+    N = int(d["N"])
+    cells = [cc for cc, _ in d["sources"]]
+    a = wt.WaveLineSource(14, 12, 14, 50).cells()
+    b = wt.WaveLineSource(20, 15, 31, 40).cells()
+    assert [x * N + y for x, y in a + b] == cells
+
+
+def test_probe_table_order():
+    geom = wt.WaveGeometryFreeForm((48, 48), 1.0, c0=1.0, c1=0.5, abs_N=10)
+    probes = [wt.WaveIntensityProbe(30, 20), wt.WaveProbe(30, 24), wt.WaveProbe(30, 20)]
+    m = wt.WaveRNN(wt.WaveCell(0.707, geom), wt.WaveSource(12, 24), probes)
+    table, L = m.probe_table()
+    assert L == 1
+    assert table == [(30 * 48 + 20, 1, 0), (30 * 48 + 24, 0, 1), (30 * 48 + 20, 0, 2)]
+
+
+def test_save_load_roundtrip(tmp_path):
+    m = model_cfg0(60)
+    wt.io.save_model(m, "m", savedir=str(tmp_path) + "/", cfg={"dtype": "float32"}, verbose=False)
+    m2, hist, geo_hist, cfg = wt.io.load_model(str(tmp_path / "m.pt"))
+    for (k, v), (k2, v2) in zip(m.state_dict().items(), m2.state_dict().items()):
+        assert k == k2 and torch.equal(v, v2)
+
+
+def test_synthetic_vowels_shape_and_norm():
+    from wavetorch_gb300.data import vowel_like
+    x, y = vowel_like(8, 3500, seed=3)
+    assert x.shape == (8, 3500) and x.dtype == np.float32
+    assert np.allclose(np.abs(x).max(axis=1), 1.0)
+    assert set(np.unique(y)) <= {0, 1, 2}

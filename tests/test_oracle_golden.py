@@ -1,0 +1,88 @@
+"""Pin the CPU oracle against golden vectors produced by the reference itself.
+
+Expected agreement (see oracle/wave_oracle.c):
+  * sequence forward outputs and fields, and dL/dc: bit-exact;
+  * one-step backward: bit-exact except a few cells where torch's own
+    kernels take a tail path (the last plane%16 cells of a batch sum over
+    more than 16 instances; im2col+GEMM tail cells of single-instance grids);
+  * rho -> c: the blur of small grids and tanh differ by ulps.
+"""
+import numpy as np
+import pytest
+
+from conftest import golden
+import oracle.oracle as o
+
+SEQ_CASES = ["cfg0_small", "cfg1_small", "multi", "line"]
+
+
+def rel(a, b):
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    return np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300)
+
+
+def seq_of(d):
+    B, N, T = int(d["B"]), int(d["N"]), int(d["T"])
+    return o.Seq(B, N, N, T, float(d["dt"]), float(d["h"]), [tuple(s) for s in d["sources"]],
+                 [tuple(p) for p in d["probes"]])
+
+
+@pytest.mark.parametrize("name", SEQ_CASES)
+def test_seq_forward_bit_exact(name):
+    d = golden(name)
+    S = seq_of(d)
+    out, hist = S.forward(d["b"], d["c"], d["x"])
+    assert np.array_equal(out, d["out"])
+    for k in d.files:
+        if k.startswith("field_"):
+            t = int(k.split("_")[1])
+            assert np.array_equal(hist[:, t], d[k]), k
+
+
+@pytest.mark.parametrize("name", SEQ_CASES)
+def test_seq_backward_bit_exact(name):
+    d = golden(name)
+    S = seq_of(d)
+    _, hist = S.forward(d["b"], d["c"], d["x"])
+    gc, _ = S.backward(d["b"], d["c"], hist, d["grad_out"])
+    assert np.array_equal(gc, d["grad_c"])
+
+
+def test_lap_order_rule():
+    # oneDNN for batch > 1 or > 20480 cells, else im2col+GEMM
+    assert o.lap_order(1, 100, 100) == o.ORD_PAIRED
+    assert o.lap_order(1, 143, 143) == o.ORD_PAIRED
+    assert o.lap_order(1, 144, 144) == o.ORD_SEQ
+    assert o.lap_order(2, 16, 16) == o.ORD_SEQ
+
+
+@pytest.mark.parametrize("name", ["step_b2_h025", "step_b1_h1", "step_b20_h1"])
+def test_timestep(name):
+    d = golden(name)
+    dt, h = float(d["dt"]), float(d["h"])
+    y = o.step_fwd(d["b"], d["c"], d["y1"], d["y2"], dt, h)
+    assert np.array_equal(y, d["y"])
+    gb, gc, gy1, gy2 = o.step_bwd(d["b"], d["c"], d["y1"], d["y2"], d["grad_y"], dt, h)
+    assert np.array_equal(gy1, d["grad_y1"])
+    assert np.array_equal(gy2, d["grad_y2"])
+    for got, ref in ((gb, d["grad_b"]), (gc, d["grad_c"])):
+        assert np.count_nonzero(got != ref) <= 4
+        assert rel(got, ref) < 1e-7
+
+
+@pytest.mark.parametrize("name", ["cfg0_small", "geom_n100", "geom_n160"])
+def test_rho_to_c(name):
+    d = golden(name)
+    c, th = o.rho_to_c(d["rho"], d["blur_kernel"], 1, 0.5, 100.0, 1.0, 0.5)
+    assert rel(c, d["c"]) < 3e-7
+    gr = o.rho_to_c_bwd(th, d["blur_kernel"], 1, 0.5, 100.0, 1.0, 0.5, d["grad_c"])
+    assert rel(gr, d["grad_rho"]) < 5e-6
+
+
+def test_fp32_vs_fp64_floor():
+    """The reference's own float32 error against its float64 run (the noise
+    floor every float32 implementation sits on)."""
+    d = golden("cfg0_small")
+    assert rel(d["out"], d["out64"]) < 1e-4
+    assert rel(d["grad_rho"], d["grad_rho64"]) < 1e-4

@@ -1,0 +1,399 @@
+// extern "C" entry points declared in include/wavetorch_gb300.h: argument
+// validation, workspace layout, host-side tables and kernel launches.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <vector>
+
+#include "internal.cuh"
+
+// ---------------------------------------------------------------------------
+static thread_local char g_last_err[256] = "";
+
+int wt_cuda_status(cudaError_t e) {
+    if (e == cudaSuccess) return WT_OK;
+    std::snprintf(g_last_err, sizeof(g_last_err), "%s: %s", cudaGetErrorName(e), cudaGetErrorString(e));
+    return WT_ERR_CUDA;
+}
+
+StepScalars wt_make_scalars(const wt_scalars* s) {
+    // float32 arithmetic in the reference's order (torch pow(-2) on a float
+    // tensor is 1/(x*x), pow(-1) is 1/x, `2 / t` is reciprocal(t) * 2)
+    StepScalars k;
+    const float dt = s->dt, h = s->h;
+    const float dtdt = dt * dt;
+    k.inv_dt2 = 1.0f / dtdt;
+    k.inv_dt = 1.0f / dt;
+    k.two_over = (1.0f / dtdt) * 2.0f;
+    k.dt = dt;
+    k.dt2 = dtdt;
+    const float hh = h * h;
+    k.lap_w = 1.0f / hh;
+    k.lap_w4 = k.lap_w * -4.0f;
+    k.lap_order = s->lap_order;
+    return k;
+}
+
+static bool scalars_ok(const wt_scalars* s) {
+    return s && std::isfinite(s->dt) && s->dt > 0.f && std::isfinite(s->h) && s->h > 0.f &&
+           (s->lap_order == WT_LAP_SEQ || s->lap_order == WT_LAP_PAIRED);
+}
+
+extern "C" const char* wt_version(void) { return "wavetorch_gb300 0.1.0 sm_103a"; }
+
+extern "C" const char* wt_status_string(int status) {
+    switch (status) {
+        case WT_OK: return "ok";
+        case WT_ERR_INVALID: return "invalid argument";
+        case WT_ERR_CUDA: return "CUDA runtime error";
+        case WT_ERR_TIMEOUT: return "device-side wait timed out";
+        case WT_ERR_UNSUPPORTED: return "unsupported configuration";
+        default: return "unknown status";
+    }
+}
+
+extern "C" const char* wt_last_error(void) { return g_last_err; }
+
+#include <atomic>
+static std::atomic<uint64_t> g_launches{0};
+void wt_count_launches(unsigned n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+extern "C" uint64_t wt_kernel_launches(void) { return g_launches.load(std::memory_order_relaxed); }
+
+// ---------------------------------------------------------------------------
+// 1. single step
+extern "C" int wt_step_fwd(const wt_scalars* s, int32_t batch, int32_t nx, int32_t ny,
+                           int32_t coef_batched, const float* b, const float* c,
+                           const float* y1, const float* y2, float* y, wt_stream_t stream) {
+    if (!scalars_ok(s) || batch <= 0 || nx <= 0 || ny <= 0 || !b || !c || !y1 || !y2 || !y)
+        return WT_ERR_INVALID;
+    if (y == y1 || y == y2) return WT_ERR_INVALID;   // the stencil reads y1 halos
+    const size_t plane = (size_t)nx * ny;
+    return wt_launch_step_fwd(wt_make_scalars(s), batch, nx, ny, coef_batched ? 1 : 0, b, c, y1,
+                              plane, y2, plane, y, plane, nullptr, (cudaStream_t)stream);
+}
+
+extern "C" int wt_step_bwd(const wt_scalars* s, int32_t batch, int32_t nx, int32_t ny,
+                           int32_t coef_batched, const float* b, const float* c,
+                           const float* y1, const float* y2, const float* grad_y,
+                           float* grad_b, float* grad_c, float* grad_y1, float* grad_y2,
+                           wt_stream_t stream) {
+    if (!scalars_ok(s) || batch <= 0 || nx <= 0 || ny <= 0 || !b || !c || !y1 || !y2 || !grad_y)
+        return WT_ERR_INVALID;
+    if (!grad_b && !grad_c && !grad_y1 && !grad_y2) return WT_OK;
+    return wt_launch_step_bwd(wt_make_scalars(s), batch, nx, ny, coef_batched ? 1 : 0, b, c, y1,
+                              y2, grad_y, grad_b, grad_c, grad_y1, grad_y2, (cudaStream_t)stream);
+}
+
+// ---------------------------------------------------------------------------
+// 2. sequences: workspace plan
+namespace {
+
+constexpr size_t ALIGN = 256;
+size_t up(size_t v) { return (v + ALIGN - 1) / ALIGN * ALIGN; }
+
+struct SeqPlan {
+    int B, nx, ny, T, ns, np, form;
+    size_t plane;
+    // int tables
+    size_t o_srcmap, o_srcnext, o_srcrow, o_srccell;
+    size_t o_prbmap, o_prbnext, o_prbkind;          // entry index == output column
+    size_t o_fcell, o_fkind, o_fcol;                // probes, descending reference order
+    size_t o_err;
+    size_t tables_end;
+    // float areas
+    size_t o_amp;
+    size_t o_hist, o_zero, o_lam, o_gc;             // plain
+    size_t o_ckpt, o_stash, o_gcpart;               // fused
+    size_t total;
+    int seg, nseg;
+    WtFusedLaunch L;
+};
+
+int make_plan(const wt_seq_desc* d, SeqPlan* p) {
+    if (!d || d->batch <= 0 || d->nx <= 0 || d->ny <= 0 || d->steps <= 0) return WT_ERR_INVALID;
+    if (d->n_sources < 0 || d->n_probes < 0) return WT_ERR_INVALID;
+    if ((d->n_sources > 0 && !d->sources_host) || (d->n_probes > 0 && !d->probes_host))
+        return WT_ERR_INVALID;
+    if (d->form != WT_FORM_PLAIN && d->form != WT_FORM_FUSED) return WT_ERR_INVALID;
+    const long long cells = (long long)d->nx * d->ny;
+    if (cells > (1LL << 30)) return WT_ERR_INVALID;
+    for (int i = 0; i < d->n_sources; ++i) {
+        const wt_source_entry& e = d->sources_host[i];
+        if (e.cell < 0 || e.cell >= cells || e.in_row < -1 || e.in_row >= d->batch) return WT_ERR_INVALID;
+    }
+    for (int i = 0; i < d->n_probes; ++i) {
+        const wt_probe_entry& e = d->probes_host[i];
+        if (e.cell < 0 || e.cell >= cells || (e.kind != 0 && e.kind != 1)) return WT_ERR_INVALID;
+    }
+    SeqPlan& P = *p;
+    std::memset(&P, 0, sizeof(P));
+    P.B = d->batch; P.nx = d->nx; P.ny = d->ny; P.T = d->steps;
+    P.ns = d->n_sources; P.np = d->n_probes; P.form = d->form;
+    P.plane = (size_t)cells;
+    const size_t I = sizeof(int), F = sizeof(float);
+    size_t o = 0;
+    P.o_srcmap = o; o = up(o + P.plane * I);
+    P.o_srcnext = o; o = up(o + (P.ns + 1) * I);
+    P.o_srcrow = o; o = up(o + (P.ns + 1) * I);
+    P.o_srccell = o; o = up(o + (P.ns + 1) * I);
+    P.o_prbmap = o; o = up(o + P.plane * I);
+    P.o_prbnext = o; o = up(o + (P.np + 1) * I);
+    P.o_prbkind = o; o = up(o + (P.np + 1) * I);
+    P.o_fcell = o; o = up(o + (P.np + 1) * I);
+    P.o_fkind = o; o = up(o + (P.np + 1) * I);
+    P.o_fcol = o; o = up(o + (P.np + 1) * I);
+    P.o_err = o; o = up(o + I);
+    P.tables_end = o;
+    const size_t bp = (size_t)P.B * P.plane;
+    P.o_amp = o; o = up(o + (size_t)P.B * P.T * (P.np + 1) * F);
+    if (P.form == WT_FORM_PLAIN) {
+        P.o_hist = o; o = up(o + (size_t)P.T * bp * F);
+        P.o_zero = o; o = up(o + P.plane * F);
+        P.o_lam = o; o = up(o + 3 * bp * F);
+        P.o_gc = o; o = up(o + bp * F);
+    } else {
+        int st = wt_fused_plan(P.nx, P.ny, d->cluster, &P.L);
+        if (st) return st;
+        // segment length: sqrt(T) by default, capped so the stash stays
+        // L2-resident (<= 48 MiB)
+        const size_t per_step = (size_t)P.B * P.L.C * P.L.M * P.L.threads * F;
+        int seg = d->segment > 0 ? d->segment : (int)std::ceil(std::sqrt((double)P.T));
+        if (d->segment <= 0) {
+            size_t cap = (48u << 20) / per_step;
+            seg = std::max(1, std::min<int>(seg, (int)std::max<size_t>(1, cap)));
+        }
+        seg = std::min(seg, P.T);
+        P.seg = seg;
+        P.nseg = (P.T + seg - 1) / seg;
+        P.o_ckpt = o; o = up(o + (size_t)P.nseg * 2 * bp * F);
+        P.o_stash = o; o = up(o + (size_t)seg * per_step);
+        P.o_gcpart = o; o = up(o + bp * F);
+        // per-thread tap capacity of the fused kernels
+        std::vector<int> cnt;
+        auto key = [&](int cell) {
+            int gx = cell / P.ny, gy = cell % P.ny;
+            int cta = gx / P.L.R, strip = (gx % P.L.R) / P.L.M;
+            return ((size_t)cta * P.L.S + strip) * P.L.NCP + gy;
+        };
+        size_t nkeys = (size_t)P.L.C * P.L.S * P.L.NCP;
+        cnt.assign(nkeys, 0);
+        for (int i = 0; i < P.ns; ++i)
+            if (++cnt[key(d->sources_host[i].cell)] > 4) return WT_ERR_UNSUPPORTED;
+        cnt.assign(nkeys, 0);
+        for (int i = 0; i < P.np; ++i)
+            if (++cnt[key(d->probes_host[i].cell)] > 4) return WT_ERR_UNSUPPORTED;
+    }
+    P.total = o;
+    return WT_OK;
+}
+
+template <class T>
+T* at(void* ws, size_t off) { return reinterpret_cast<T*>(static_cast<char*>(ws) + off); }
+
+// Build and upload the lookup tables (sources in table order; probes linked
+// per cell in descending reference order).
+int upload_tables(const wt_seq_desc* d, const SeqPlan& P, void* ws, cudaStream_t st) {
+    std::vector<int> h(P.tables_end / sizeof(int), 0);
+    auto H = [&](size_t off) { return h.data() + off / sizeof(int); };
+    std::fill(H(P.o_srcmap), H(P.o_srcmap) + P.plane, -1);
+    std::fill(H(P.o_prbmap), H(P.o_prbmap) + P.plane, -1);
+    // sources: per-cell chains in table order
+    std::vector<int> tail(P.plane, -1);
+    for (int i = 0; i < P.ns; ++i) {
+        const wt_source_entry& e = d->sources_host[i];
+        H(P.o_srcnext)[i] = -1;
+        H(P.o_srcrow)[i] = e.in_row;
+        H(P.o_srccell)[i] = e.cell;
+        if (tail[e.cell] < 0) H(P.o_srcmap)[e.cell] = i;
+        else H(P.o_srcnext)[tail[e.cell]] = i;
+        tail[e.cell] = i;
+    }
+    // probes: descending `order` (stable), chains per cell in that order
+    std::vector<int> idx(P.np);
+    for (int i = 0; i < P.np; ++i) idx[i] = i;
+    std::stable_sort(idx.begin(), idx.end(), [&](int a, int b) {
+        return d->probes_host[a].order > d->probes_host[b].order;
+    });
+    std::fill(tail.begin(), tail.end(), -1);
+    for (int j = 0; j < P.np; ++j) {
+        int i = idx[j];
+        const wt_probe_entry& e = d->probes_host[i];
+        H(P.o_prbnext)[i] = -1;
+        H(P.o_prbkind)[i] = e.kind;
+        if (tail[e.cell] < 0) H(P.o_prbmap)[e.cell] = i;
+        else H(P.o_prbnext)[tail[e.cell]] = i;
+        tail[e.cell] = i;
+        H(P.o_fcell)[j] = e.cell;
+        H(P.o_fkind)[j] = e.kind;
+        H(P.o_fcol)[j] = i;
+    }
+    H(P.o_err)[0] = 0;
+    cudaError_t e = cudaMemcpyAsync(ws, h.data(), P.tables_end, cudaMemcpyHostToDevice, st);
+    if (e != cudaSuccess) return wt_cuda_status(e);
+    // pageable source: make sure the staging copy has consumed `h`
+    return wt_cuda_status(cudaStreamSynchronize(st));
+}
+
+wt::FusedParams fused_params(const wt_scalars* s, const SeqPlan& P, const float* b, const float* c,
+                             const float* x, void* ws) {
+    wt::FusedParams F;
+    std::memset(&F, 0, sizeof(F));
+    F.k = wt_make_scalars(s);
+    F.batch = P.B; F.nx = P.nx; F.ny = P.ny; F.steps = P.T;
+    F.C = P.L.C; F.R = P.L.R; F.NCP = P.L.NCP; F.LD = P.L.LD; F.seg = P.seg;
+    F.b = b; F.c = c; F.x = x;
+    F.n_src = P.ns;
+    F.src_cell = at<int>(ws, P.o_srccell);
+    F.src_row = at<int>(ws, P.o_srcrow);
+    F.n_prb = P.np;
+    F.prb_cell = at<int>(ws, P.o_fcell);
+    F.prb_kind = at<int>(ws, P.o_fkind);
+    F.prb_col = at<int>(ws, P.o_fcol);
+    F.amp = at<float>(ws, P.o_amp);
+    F.ckpt = at<float>(ws, P.o_ckpt);
+    F.stash = at<float>(ws, P.o_stash);
+    F.gc_part = at<float>(ws, P.o_gcpart);
+    F.err = at<int>(ws, P.o_err);
+    return F;
+}
+
+}  // namespace
+
+extern "C" int wt_seq_workspace_bytes(const wt_seq_desc* d, size_t* bytes) {
+    if (!bytes) return WT_ERR_INVALID;
+    SeqPlan P;
+    int st = make_plan(d, &P);
+    if (st) return st;
+    *bytes = P.total;
+    return WT_OK;
+}
+
+extern "C" int wt_seq_fwd(const wt_scalars* s, const wt_seq_desc* d, const float* b,
+                          const float* c, const float* x, float* out, float* fields,
+                          float* probe_sum, void* workspace, size_t workspace_bytes,
+                          wt_stream_t stream) {
+    if (!scalars_ok(s)) return WT_ERR_INVALID;
+    SeqPlan P;
+    int st = make_plan(d, &P);
+    if (st) return st;
+    if (!b || !c || !workspace || workspace_bytes < P.total) return WT_ERR_INVALID;
+    if (P.ns > 0 && !x) return WT_ERR_INVALID;
+    if (P.np > 0 && !out) return WT_ERR_INVALID;
+    if (d->output_fields && !fields) return WT_ERR_INVALID;
+    cudaStream_t cs = (cudaStream_t)stream;
+    if ((st = upload_tables(d, P, workspace, cs))) return st;
+    const StepScalars k = wt_make_scalars(s);
+    const size_t plane = P.plane;
+    if (P.form == WT_FORM_PLAIN) {
+        float* hist = at<float>(workspace, P.o_hist);
+        float* zero = at<float>(workspace, P.o_zero);
+        if ((st = wt_launch_fill_zero(zero, plane, cs))) return st;
+        wt::SeqEpilogue e;
+        e.srcmap = at<int>(workspace, P.o_srcmap);
+        e.src_next = at<int>(workspace, P.o_srcnext);
+        e.src_row = at<int>(workspace, P.o_srcrow);
+        e.x = x;
+        e.steps = P.T;
+        e.probemap = at<int>(workspace, P.o_prbmap);
+        e.probe_next = at<int>(workspace, P.o_prbnext);
+        e.probe_kind = at<int>(workspace, P.o_prbkind);
+        e.out = out;
+        e.amp = at<float>(workspace, P.o_amp);
+        e.n_probe = P.np;
+        const size_t hbs = (size_t)P.T * plane;   // history is [B][T][nx][ny]
+        for (int t = 0; t < P.T; ++t) {
+            e.t = t;
+            const float* y1 = t >= 1 ? hist + (size_t)(t - 1) * plane : zero;
+            const float* y2 = t >= 2 ? hist + (size_t)(t - 2) * plane : zero;
+            st = wt_launch_step_fwd(k, P.B, P.nx, P.ny, 0, b, c, y1, t >= 1 ? hbs : 0, y2,
+                                    t >= 2 ? hbs : 0, hist + (size_t)t * plane, hbs, &e, cs);
+            if (st) return st;
+        }
+        if (d->output_fields) {
+            cudaError_t ce = cudaMemcpyAsync(fields, hist, (size_t)P.B * hbs * sizeof(float),
+                                             cudaMemcpyDeviceToDevice, cs);
+            if (ce != cudaSuccess) return wt_cuda_status(ce);
+        }
+        if (probe_sum) return WT_ERR_UNSUPPORTED;   // the fused form computes it
+        return WT_OK;
+    }
+    wt::FusedParams F = fused_params(s, P, b, c, x, workspace);
+    F.out = out;
+    F.fields = d->output_fields ? fields : nullptr;
+    F.probe_sum = probe_sum;
+    return wt_launch_fused(true, F, P.L, cs);
+}
+
+extern "C" int wt_seq_bwd(const wt_scalars* s, const wt_seq_desc* d, const float* b,
+                          const float* c, const float* x, const float* grad_out, float* grad_c,
+                          float* grad_x, void* workspace, size_t workspace_bytes,
+                          wt_stream_t stream) {
+    if (!scalars_ok(s)) return WT_ERR_INVALID;
+    SeqPlan P;
+    int st = make_plan(d, &P);
+    if (st) return st;
+    if (!b || !c || !grad_c || !workspace || workspace_bytes < P.total) return WT_ERR_INVALID;
+    if (P.np > 0 && !grad_out) return WT_ERR_INVALID;
+    if (grad_x) {
+        // dL/dx is served for a single own-row source entry (a point source)
+        int own = 0;
+        for (int i = 0; i < P.ns; ++i) own += d->sources_host[i].in_row < 0;
+        if (own != 1 || P.ns != 1) return WT_ERR_UNSUPPORTED;
+    }
+    cudaStream_t cs = (cudaStream_t)stream;
+    const StepScalars k = wt_make_scalars(s);
+    const size_t plane = P.plane;
+    const size_t bp = (size_t)P.B * plane;
+    if (P.form == WT_FORM_PLAIN) {
+        float* hist = at<float>(workspace, P.o_hist);
+        float* lam = at<float>(workspace, P.o_lam);
+        float* gc = at<float>(workspace, P.o_gc);
+        wt::AdjEpilogue e;
+        e.probemap = at<int>(workspace, P.o_prbmap);
+        e.probe_next = at<int>(workspace, P.o_prbnext);
+        e.probe_kind = at<int>(workspace, P.o_prbkind);
+        e.grad_out = grad_out;
+        e.amp = at<float>(workspace, P.o_amp);
+        e.n_probe = P.np;
+        e.steps = P.T;
+        e.srcmap = at<int>(workspace, P.o_srcmap);
+        e.src_next = at<int>(workspace, P.o_srcnext);
+        e.src_row = at<int>(workspace, P.o_srcrow);
+        e.grad_x = grad_x;
+        const size_t hbs = (size_t)P.T * plane;
+        for (int t = P.T - 1; t >= 0; --t) {
+            e.t = t;
+            const float* l1 = t + 1 < P.T ? lam + (size_t)((t + 1) % 3) * bp : nullptr;
+            const float* l2 = t + 2 < P.T ? lam + (size_t)((t + 2) % 3) * bp : nullptr;
+            const float* hp = t >= 1 ? hist + (size_t)(t - 1) * plane : nullptr;
+            st = wt_launch_seq_adj_step(k, P.B, P.nx, P.ny, b, c, l1, l2, hp, hbs,
+                                        lam + (size_t)(t % 3) * bp, gc, e, cs);
+            if (st) return st;
+            st = wt_launch_seq_adj_reduce(P.B, plane, gc, grad_c, t == P.T - 1, cs);
+            if (st) return st;
+        }
+        return WT_OK;
+    }
+    wt::FusedParams F = fused_params(s, P, b, c, x, workspace);
+    F.grad_out = grad_out;
+    F.grad_x = grad_x;
+    if ((st = wt_launch_fused(false, F, P.L, cs))) return st;
+    return wt_launch_seq_adj_reduce(P.B, plane, F.gc_part, grad_c, 1, cs);
+}
+
+extern "C" int wt_seq_device_status(const wt_seq_desc* d, const void* workspace,
+                                    size_t workspace_bytes, wt_stream_t stream) {
+    SeqPlan P;
+    int st = make_plan(d, &P);
+    if (st) return st;
+    if (!workspace || workspace_bytes < P.total) return WT_ERR_INVALID;
+    int h = 0;
+    cudaError_t e = cudaMemcpyAsync(&h, static_cast<const char*>(workspace) + P.o_err, sizeof(int),
+                                    cudaMemcpyDeviceToHost, (cudaStream_t)stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize((cudaStream_t)stream);
+    if (e != cudaSuccess) return wt_cuda_status(e);
+    if (h == WT_DEVERR_BOUNDS) return WT_ERR_INVALID;
+    if (h == WT_DEVERR_TIMEOUT) return WT_ERR_TIMEOUT;
+    return WT_OK;
+}

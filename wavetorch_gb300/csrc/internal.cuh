@@ -1,0 +1,96 @@
+// Structures and launchers shared between the translation units.
+#pragma once
+#include "common.cuh"
+
+namespace wt {
+
+// Per-step epilogue of the plain sequence forward: sources and probes.
+// srcmap/probemap are per-cell heads of singly linked entry lists (-1: none).
+struct SeqEpilogue {
+    const int* srcmap;        // [nx*ny] first source entry index or -1
+    const int* src_next;      // [n_src] next entry at the same cell or -1
+    const int* src_row;       // [n_src] input row (-1 = own instance)
+    const float* x;           // [batch][steps]
+    int steps;
+    int t;
+    const int* probemap;      // [nx*ny] first probe entry or -1
+    const int* probe_next;    // [n_probe]
+    const int* probe_kind;    // [n_probe]
+    float* out;               // [batch][steps][n_probe]
+    float* amp;               // [batch][steps][n_probe] raw amplitudes (adjoint seeds)
+    int n_probe;
+};
+
+// Per-step epilogue of the plain sequence adjoint.
+struct AdjEpilogue {
+    const int* probemap;
+    const int* probe_next;         // per-cell chain in descending reference order
+    const int* probe_kind;
+    const float* grad_out;         // [batch][steps][n_probe]
+    const float* amp;              // [batch][steps][n_probe]
+    int n_probe, steps, t;
+    const int* srcmap;
+    const int* src_next;
+    const int* src_row;
+    float* grad_x;                 // [batch][steps] or null
+};
+
+// Parameters of the fused persistent kernels.
+struct FusedParams {
+    StepScalars k;
+    int batch, nx, ny, steps;
+    int C;          // CTAs per instance (cluster size)
+    int R;          // rows per CTA (multiple of M)
+    int NCP;        // threads per strip row (ny rounded up to 32)
+    int LD;         // tile column stride (floats)
+    int seg;        // checkpoint interval
+    const float* b;         // [nx,ny]
+    const float* c;         // [nx,ny]
+    const float* x;         // [batch][steps]
+    // sources in table order, probes in descending reference order
+    int n_src;
+    const int* src_cell;
+    const int* src_row;
+    int n_prb;
+    const int* prb_cell;
+    const int* prb_kind;
+    const int* prb_col;
+    // forward outputs
+    float* out;             // [batch][steps][n_prb]
+    float* amp;             // [batch][steps][n_prb]
+    float* fields;          // [batch][steps][nx][ny] or null
+    float* probe_sum;       // [batch][n_prb] or null
+    float* ckpt;            // [nseg][2][batch][nx][ny]
+    // adjoint
+    const float* grad_out;  // [batch][steps][n_prb]
+    float* gc_part;         // [batch][nx][ny] per-instance dL/dc
+    float* grad_x;          // [batch][steps] or null
+    float* stash;           // global stash: [batch][C][seg][M][nthreads]
+    int* err;
+};
+
+}  // namespace wt
+
+// Launch shape of the fused kernels for one grid size.
+struct WtFusedLaunch {
+    int C, M, R, S, NCP, LD, threads;
+    size_t smem_fwd, smem_bwd;
+};
+
+int wt_launch_step_fwd(const StepScalars& k, int batch, int nx, int ny, int coef_batched,
+                       const float* b, const float* c, const float* y1, size_t bs1,
+                       const float* y2, size_t bs2, float* y, size_t bs,
+                       const wt::SeqEpilogue* epi, cudaStream_t st);
+int wt_launch_step_bwd(const StepScalars& k, int batch, int nx, int ny, int coef_batched,
+                       const float* b, const float* c, const float* y1, const float* y2,
+                       const float* g, float* gb, float* gcp, float* gy1, float* gy2,
+                       cudaStream_t st);
+int wt_launch_seq_adj_step(const StepScalars& k, int batch, int nx, int ny, const float* b,
+                           const float* c, const float* lam1, const float* lam2,
+                           const float* hprev, size_t hbs, float* lam_out, float* gc,
+                           const wt::AdjEpilogue& epi, cudaStream_t st);
+int wt_launch_seq_adj_reduce(int batch, size_t plane, const float* gc, float* G, int first,
+                             cudaStream_t st);
+int wt_launch_fill_zero(float* p, size_t n, cudaStream_t st);
+int wt_fused_plan(int nx, int ny, int cluster_req, WtFusedLaunch* L);
+int wt_launch_fused(bool fwd, const wt::FusedParams& P, const WtFusedLaunch& L, cudaStream_t st);

@@ -1,0 +1,342 @@
+// Per-step ("plain") kernels: one launch advances every instance of the batch
+// by one leapfrog step, or runs one step of the adjoint.  These are the
+// drop-in for TimeStep (wavetorch/cell.py:20-44) and, with the fused source
+// and probe epilogues, the plain per-step form of the sequence.
+//
+// Layout: fields [batch][nx][ny] float32.  A CTA of 32x8 threads covers an
+// 8-row x 32-column tile; the tile plus a one-cell halo is staged in shared
+// memory with coalesced loads, so each input cell is read from L2/HBM once.
+#include "internal.cuh"
+
+namespace wt {
+
+constexpr int TX = 8;    // tile rows    (x)
+constexpr int TY = 32;   // tile columns (y)
+
+// Stage rows [x0-1, x0+TX] x cols [y0-1, y0+TY] of field f (one instance) into
+// s[TX+2][TY+2], zero outside the grid.
+WT_DEV void stage_tile(float (*s)[TY + 2], const float* __restrict__ f, int nx, int ny,
+                       int x0, int y0) {
+    const int tid = threadIdx.y * TY + threadIdx.x;
+    constexpr int NT = TX * TY;
+    constexpr int NS = (TX + 2) * (TY + 2);
+    for (int i = tid; i < NS; i += NT) {
+        int r = i / (TY + 2), q = i % (TY + 2);
+        int gx = x0 - 1 + r, gy = y0 - 1 + q;
+        float v = 0.0f;
+        if (gx >= 0 && gx < nx && gy >= 0 && gy < ny) v = __ldg(f + (size_t)gx * ny + gy);
+        s[r][q] = v;
+    }
+}
+
+template <int ORDER>
+WT_DEV float tile_lap(float (*s)[TY + 2], int r, int q, const StepScalars& k) {
+    return lap5<ORDER>(s[r - 1][q], s[r][q - 1], s[r][q], s[r][q + 1], s[r + 1][q], k.lap_w,
+                       k.lap_w4);
+}
+
+// ---------------------------------------------------------------------------
+// Forward step, optionally with the sequence epilogue:
+//   y = leapfrog(b, c, y1, y2); y[src] += x[.., t]; out[b, t, q] = probe(y)
+template <int ORDER, bool EPI>
+__global__ void __launch_bounds__(TX* TY)
+step_fwd_kernel(StepScalars k, int nx, int ny, int coef_batched, const float* __restrict__ b,
+                const float* __restrict__ c, const float* __restrict__ y1, size_t bs1,
+                const float* __restrict__ y2, size_t bs2, float* __restrict__ y, size_t bs,
+                SeqEpilogue e) {
+    __shared__ float s[TX + 2][TY + 2];
+    const int inst = blockIdx.z;
+    const int x0 = blockIdx.y * TX, y0 = blockIdx.x * TY;
+    const size_t plane = (size_t)nx * ny;
+    stage_tile(s, y1 + inst * bs1, nx, ny, x0, y0);
+    __syncthreads();
+    const int gx = x0 + threadIdx.y, gy = y0 + threadIdx.x;
+    if (gx >= nx || gy >= ny) return;
+    const size_t cell = (size_t)gx * ny + gy;
+    const size_t ci = coef_batched ? inst * plane + cell : cell;
+    FwdCoef f = fwd_coef(__ldg(b + ci), __ldg(c + ci), k);
+    const int r = threadIdx.y + 1, q = threadIdx.x + 1;
+    float L = tile_lap<ORDER>(s, r, q, k);
+    float v = leapfrog(f.A, f.Bc, f.c2, k.two_over, s[r][q], __ldg(y2 + inst * bs2 + cell), L);
+    if (EPI) {
+        // Sources, in table order (wavetorch/rnn.py:56-57, source.py:15-22).
+        for (int en = __ldg(e.srcmap + cell); en >= 0; en = __ldg(e.src_next + en)) {
+            int row = __ldg(e.src_row + en);
+            row = row < 0 ? inst : row;
+            v = fadd(v, __ldg(e.x + (size_t)row * e.steps + e.t));
+        }
+        // Probes (wavetorch/probe.py:14-15, :26-27).
+        for (int en = __ldg(e.probemap + cell); en >= 0; en = __ldg(e.probe_next + en)) {
+            size_t o = ((size_t)inst * e.steps + e.t) * e.n_probe + en;
+            e.out[o] = __ldg(e.probe_kind + en) ? fmul(v, v) : v;
+            if (e.amp) e.amp[o] = v;
+        }
+    }
+    y[inst * bs + cell] = v;
+}
+
+// ---------------------------------------------------------------------------
+// TimeStep.backward drop-in (wavetorch/cell.py:26-44).  One thread per cell;
+// the batch is walked in order so that the [nx,ny] reductions of grad_b and
+// grad_c use torch's CPU summation order (blocks of 16 summed sequentially,
+// block sums added in order).
+template <int ORDER>
+__global__ void __launch_bounds__(TX* TY)
+step_bwd_kernel(StepScalars k, int batch, int nx, int ny, int coef_batched,
+                const float* __restrict__ b, const float* __restrict__ c,
+                const float* __restrict__ y1, const float* __restrict__ y2,
+                const float* __restrict__ g, float* __restrict__ grad_b,
+                float* __restrict__ grad_c, float* __restrict__ grad_y1,
+                float* __restrict__ grad_y2) {
+    __shared__ float sy[TX + 2][TY + 2];
+    __shared__ float sg[TX + 2][TY + 2];
+    const int x0 = blockIdx.y * TX, y0 = blockIdx.x * TY;
+    const size_t plane = (size_t)nx * ny;
+    const int gx = x0 + threadIdx.y, gy = y0 + threadIdx.x;
+    const bool live = gx < nx && gy < ny;
+    const size_t cell = live ? (size_t)gx * ny + gy : 0;
+    const int r = threadIdx.y + 1, q = threadIdx.x + 1;
+    const bool need_lap_y = grad_b || grad_c;
+    float acc_b = 0.f, blk_b = 0.f, acc_c = 0.f, blk_c = 0.f;
+    // With [nx,ny] coefficients the per-cell constants are loop invariant.
+    float bb = 0.f, cc = 0.f;
+    if (live && !coef_batched) { bb = __ldg(b + cell); cc = __ldg(c + cell); }
+    for (int inst = 0; inst < batch; ++inst) {
+        __syncthreads();
+        if (need_lap_y) stage_tile(sy, y1 + inst * plane, nx, ny, x0, y0);
+        if (grad_y1) {
+            // c2_grad = (X1 * c^2) * g must be staged with its halo: it is the
+            // field the Laplacian of grad_y1 acts on.
+            const int tid = threadIdx.y * TY + threadIdx.x;
+            for (int i = tid; i < (TX + 2) * (TY + 2); i += TX * TY) {
+                int rr = i / (TY + 2), qq = i % (TY + 2);
+                int hx = x0 - 1 + rr, hy = y0 - 1 + qq;
+                float v = 0.f;
+                if (hx >= 0 && hx < nx && hy >= 0 && hy < ny) {
+                    size_t hc = (size_t)hx * ny + hy;
+                    size_t hi = coef_batched ? inst * plane + hc : hc;
+                    BwdCoef kb = bwd_coef(__ldg(b + hi), __ldg(c + hi), k);
+                    v = fmul(kb.Kg, __ldg(g + inst * plane + hc));
+                }
+                sg[rr][qq] = v;
+            }
+        }
+        __syncthreads();
+        if (!live) continue;
+        const size_t ic = inst * plane + cell;
+        if (coef_batched) { bb = __ldg(b + ic); cc = __ldg(c + ic); }
+        BwdCoef kb = bwd_coef(bb, cc, k);
+        const float gv = __ldg(g + ic);
+        float L = 0.f;
+        if (need_lap_y) L = tile_lap<ORDER>(sy, r, q, k);
+        if (grad_c) {
+            float t = fmul(fmul(kb.X1, fmul(kb.Kc, L)), gv);
+            if (coef_batched) grad_c[ic] = t;
+            else {
+                blk_c = fadd(blk_c, t);
+                if ((inst & 15) == 15 || inst == batch - 1) {
+                    acc_c = inst < 16 ? blk_c : fadd(acc_c, blk_c);
+                    blk_c = 0.f;
+                }
+            }
+        }
+        if (grad_b) {
+            // -(dt*b+1).pow(-2) * dt * (c^2 dt^2 Lap + 2 y1 - 2 y2) * g
+            float v = fadd(fmul(bb, k.dt), 1.0f);
+            float kb1 = fmul(-fdiv(1.0f, fmul(v, v)), k.dt);
+            float inner = fadd(fmul(fmul(fmul(cc, cc), k.dt2), L), fmul(2.0f, sy[r][q]));
+            inner = fsub(inner, fmul(2.0f, __ldg(y2 + ic)));
+            float t = fmul(fmul(kb1, inner), gv);
+            if (coef_batched) grad_b[ic] = t;
+            else {
+                blk_b = fadd(blk_b, t);
+                if ((inst & 15) == 15 || inst == batch - 1) {
+                    acc_b = inst < 16 ? blk_b : fadd(acc_b, blk_b);
+                    blk_b = 0.f;
+                }
+            }
+        }
+        if (grad_y1) {
+            float lg = lap5<ORDER>(sg[r - 1][q], sg[r][q - 1], sg[r][q], sg[r][q + 1], sg[r + 1][q],
+                                   k.lap_w, k.lap_w4);
+            grad_y1[ic] = fadd(fmul(k.dt2, lg), fmul(fmul(2.0f, gv), kb.X1));
+        }
+        if (grad_y2) grad_y2[ic] = fmul(kb.Ky2, gv);
+    }
+    if (live && !coef_batched) {
+        if (grad_c) grad_c[cell] = acc_c;
+        if (grad_b) grad_b[cell] = acc_b;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Plain sequence adjoint, phase 1 (one launch per step t, t = T-1 .. 0):
+//   lam_t = (gy2_{t+2} + gy1_{t+1}) then probe seeds in descending probe order
+// with gy1_{t+1} = dt^2 Lap(Kg lam_{t+1}) + (2 lam_{t+1}) X1 and
+// gy2_{t+2} = Ky2 lam_{t+2}.  Also writes the per-instance grad_c term
+//   gc[b] = (X1 * (Kc * Lap(h_{t-1}))) * lam_t
+// and, at source cells, dL/dx.  lam_{t+1}, lam_{t+2} may be null (t >= T-1,
+// t >= T-2), h_{t-1} is null at t == 0.
+template <int ORDER>
+__global__ void __launch_bounds__(TX* TY)
+seq_adj_step_kernel(StepScalars k, int nx, int ny, const float* __restrict__ b,
+                    const float* __restrict__ c, const float* __restrict__ lam1,
+                    const float* __restrict__ lam2, const float* __restrict__ hprev, size_t hbs,
+                    float* __restrict__ lam_out, float* __restrict__ gc, AdjEpilogue e) {
+    __shared__ float sg[TX + 2][TY + 2];
+    __shared__ float sy[TX + 2][TY + 2];
+    const int inst = blockIdx.z;
+    const int x0 = blockIdx.y * TX, y0 = blockIdx.x * TY;
+    const size_t plane = (size_t)nx * ny;
+    const int tid = threadIdx.y * TY + threadIdx.x;
+    for (int i = tid; i < (TX + 2) * (TY + 2); i += TX * TY) {
+        int rr = i / (TY + 2), qq = i % (TY + 2);
+        int hx = x0 - 1 + rr, hy = y0 - 1 + qq;
+        float v = 0.f, w = 0.f;
+        if (hx >= 0 && hx < nx && hy >= 0 && hy < ny) {
+            size_t hc = (size_t)hx * ny + hy;
+            if (lam1) {
+                BwdCoef kb = bwd_coef(__ldg(b + hc), __ldg(c + hc), k);
+                v = fmul(kb.Kg, __ldg(lam1 + inst * plane + hc));
+            }
+            if (hprev) w = __ldg(hprev + inst * hbs + hc);
+        }
+        sg[rr][qq] = v;
+        sy[rr][qq] = w;
+    }
+    __syncthreads();
+    const int gx = x0 + threadIdx.y, gy = y0 + threadIdx.x;
+    if (gx >= nx || gy >= ny) return;
+    const size_t cell = (size_t)gx * ny + gy;
+    const size_t ic = inst * plane + cell;
+    const int r = threadIdx.y + 1, q = threadIdx.x + 1;
+    BwdCoef kb = bwd_coef(__ldg(b + cell), __ldg(c + cell), k);
+    // gradient arriving at h_t: first gy2 from step t+2, then gy1 from t+1
+    float lam = 0.f;
+    if (lam2) lam = fmul(kb.Ky2, __ldg(lam2 + ic));
+    if (lam1) {
+        float l1 = __ldg(lam1 + ic);
+        float lg = lap5<ORDER>(sg[r - 1][q], sg[r][q - 1], sg[r][q], sg[r][q + 1], sg[r + 1][q],
+                               k.lap_w, k.lap_w4);
+        float gy1 = fadd(fmul(k.dt2, lg), fmul(fmul(2.0f, l1), kb.X1));
+        lam = lam2 ? fadd(lam, gy1) : gy1;
+    }
+    // probe seeds, highest probe index first (autograd runs the later-created
+    // IndexBackward nodes first); intensity: g * (2 y), amplitude: g.
+    int head = __ldg(e.probemap + cell);
+    if (head >= 0) {
+        // entries of one cell are linked in descending probe order on the host
+        for (int en = head; en >= 0; en = __ldg(e.probe_next + en)) {
+            size_t o = ((size_t)inst * e.steps + e.t) * e.n_probe + en;
+            float gv = __ldg(e.grad_out + o);
+            float s = __ldg(e.probe_kind + en) ? fmul(gv, fmul(2.0f, __ldg(e.amp + o))) : gv;
+            lam = fadd(lam, s);
+        }
+    }
+    lam_out[ic] = lam;
+    if (gc) {
+        float L = hprev ? tile_lap<ORDER>(sy, r, q, k) : 0.0f;
+        gc[ic] = fmul(fmul(kb.X1, fmul(kb.Kc, L)), lam);
+    }
+    if (e.grad_x) {
+        for (int en = __ldg(e.srcmap + cell); en >= 0; en = __ldg(e.src_next + en)) {
+            int row = __ldg(e.src_row + en);
+            // per-instance rows only (own-row injections); broadcast rows are
+            // reduced on the host side of the API.
+            if (row < 0) e.grad_x[(size_t)inst * e.steps + e.t] = lam;
+        }
+    }
+}
+
+// Phase 2: G_c += chunked batch sum of gc (wavetorch autograd: sum-to-shape of
+// each step's [batch,nx,ny] grad_c, then accumulation over steps).
+__global__ void seq_adj_reduce_kernel(int batch, size_t plane, const float* __restrict__ gc,
+                                      float* __restrict__ G, int first) {
+    size_t cell = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (cell >= plane) return;
+    float acc = 0.f, blk = 0.f;
+    for (int i = 0; i < batch; ++i) {
+        blk = fadd(blk, __ldg(gc + (size_t)i * plane + cell));
+        if ((i & 15) == 15 || i == batch - 1) {
+            acc = i < 16 ? blk : fadd(acc, blk);
+            blk = 0.f;
+        }
+    }
+    G[cell] = first ? acc : fadd(G[cell], acc);
+}
+
+__global__ void fill_zero_kernel(float* p, size_t n) {
+    size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) p[i] = 0.f;
+}
+
+}  // namespace wt
+
+// ---------------------------------------------------------------------------
+// Launch helpers used by api.cu
+int wt_launch_step_fwd(const StepScalars& k, int batch, int nx, int ny, int coef_batched,
+                       const float* b, const float* c, const float* y1, size_t bs1,
+                       const float* y2, size_t bs2, float* y, size_t bs,
+                       const wt::SeqEpilogue* epi, cudaStream_t st) {
+    dim3 blk(wt::TY, wt::TX);
+    dim3 grd((ny + wt::TY - 1) / wt::TY, (nx + wt::TX - 1) / wt::TX, batch);
+    if (epi) {
+        const wt::SeqEpilogue& e = *epi;
+        if (k.lap_order == WT_LAP_SEQ)
+            wt::step_fwd_kernel<WT_LAP_SEQ, true><<<grd, blk, 0, st>>>(k, nx, ny, coef_batched, b, c, y1, bs1, y2, bs2, y, bs, e);
+        else
+            wt::step_fwd_kernel<WT_LAP_PAIRED, true><<<grd, blk, 0, st>>>(k, nx, ny, coef_batched, b, c, y1, bs1, y2, bs2, y, bs, e);
+    } else {
+        wt::SeqEpilogue e{};
+        if (k.lap_order == WT_LAP_SEQ)
+            wt::step_fwd_kernel<WT_LAP_SEQ, false><<<grd, blk, 0, st>>>(k, nx, ny, coef_batched, b, c, y1, bs1, y2, bs2, y, bs, e);
+        else
+            wt::step_fwd_kernel<WT_LAP_PAIRED, false><<<grd, blk, 0, st>>>(k, nx, ny, coef_batched, b, c, y1, bs1, y2, bs2, y, bs, e);
+    }
+    wt_count_launches(1);
+    return wt_cuda_status(cudaGetLastError());
+}
+
+int wt_launch_step_bwd(const StepScalars& k, int batch, int nx, int ny, int coef_batched,
+                       const float* b, const float* c, const float* y1, const float* y2,
+                       const float* g, float* gb, float* gcp, float* gy1, float* gy2,
+                       cudaStream_t st) {
+    dim3 blk(wt::TY, wt::TX);
+    dim3 grd((ny + wt::TY - 1) / wt::TY, (nx + wt::TX - 1) / wt::TX, 1);
+    if (k.lap_order == WT_LAP_SEQ)
+        wt::step_bwd_kernel<WT_LAP_SEQ><<<grd, blk, 0, st>>>(k, batch, nx, ny, coef_batched, b, c, y1, y2, g, gb, gcp, gy1, gy2);
+    else
+        wt::step_bwd_kernel<WT_LAP_PAIRED><<<grd, blk, 0, st>>>(k, batch, nx, ny, coef_batched, b, c, y1, y2, g, gb, gcp, gy1, gy2);
+    wt_count_launches(1);
+    return wt_cuda_status(cudaGetLastError());
+}
+
+int wt_launch_seq_adj_step(const StepScalars& k, int batch, int nx, int ny, const float* b,
+                           const float* c, const float* lam1, const float* lam2,
+                           const float* hprev, size_t hbs, float* lam_out, float* gc,
+                           const wt::AdjEpilogue& e, cudaStream_t st) {
+    dim3 blk(wt::TY, wt::TX);
+    dim3 grd((ny + wt::TY - 1) / wt::TY, (nx + wt::TX - 1) / wt::TX, batch);
+    if (k.lap_order == WT_LAP_SEQ)
+        wt::seq_adj_step_kernel<WT_LAP_SEQ><<<grd, blk, 0, st>>>(k, nx, ny, b, c, lam1, lam2, hprev, hbs, lam_out, gc, e);
+    else
+        wt::seq_adj_step_kernel<WT_LAP_PAIRED><<<grd, blk, 0, st>>>(k, nx, ny, b, c, lam1, lam2, hprev, hbs, lam_out, gc, e);
+    wt_count_launches(1);
+    return wt_cuda_status(cudaGetLastError());
+}
+
+int wt_launch_seq_adj_reduce(int batch, size_t plane, const float* gc, float* G, int first,
+                             cudaStream_t st) {
+    int thr = 256;
+    wt::seq_adj_reduce_kernel<<<(unsigned)((plane + thr - 1) / thr), thr, 0, st>>>(batch, plane, gc, G, first);
+    wt_count_launches(1);
+    return wt_cuda_status(cudaGetLastError());
+}
+
+int wt_launch_fill_zero(float* p, size_t n, cudaStream_t st) {
+    if (n == 0) return WT_OK;
+    int thr = 256;
+    wt::fill_zero_kernel<<<(unsigned)((n + thr - 1) / thr), thr, 0, st>>>(p, n);
+    wt_count_launches(1);
+    return wt_cuda_status(cudaGetLastError());
+}
