@@ -383,7 +383,7 @@ void or_rho_to_c(int nx, int ny, int rad, int blur_n, float eta, float beta, flo
     float dc = (float)((double)c1 - (double)c0);
     for (size_t q = 0; q < n; ++q) {
         float z = beta * (a[q] - eta);
-        float tz = tanhf(z);
+        float tz = (float)tanh((double)z);   /* rounded once, like the GPU path */
         if (th) th[q] = tz;
         float P = (tz + tbe) / den;
         c[q] = c0 + dc * P;

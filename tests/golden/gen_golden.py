@@ -163,6 +163,7 @@ def case_nonlinear(wt):
     g = torch.Generator().manual_seed(4)
     rho0 = torch.rand(N, N, generator=g)
     x, labels = vowel_like(B, T, seed=4)
+    x = (x * np.float32(0.2)).astype(np.float32)   # keeps the Kerr term inside the CFL limit
     r = run_model(wt, N=N, abs_N=8, B=B, T=T, x=x, labels=labels,
                   sources=[lambda: wt.WaveSource(10, 20)],
                   probes=[lambda y=y: wt.WaveIntensityProbe(30, y) for y in (12, 20, 28)],
