@@ -50,6 +50,8 @@ def parse():
     p.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
     p.add_argument("--batch", type=int, default=WORKLOAD["batch"])
     p.add_argument("--T", type=int, default=WORKLOAD["steps"])
+    p.add_argument("--kernels-only", action="store_true",
+                   help="run only the sequence kernels (forward + adjoint) -- the profiling case")
     return p.parse_args()
 
 
@@ -403,9 +405,47 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def run_kernels_only(args):
+    """seq forward + adjoint on the workload shape, no training glue: the
+    command the ncu captures run (small T keeps a capture short)."""
+    import torch
+    from wavetorch_gb300 import _lib
+    from wavetorch_gb300.functional import SeqSpec, lap_order, scalars, seq_backward, seq_forward
+    dev = torch.device("cuda", 0)
+    B, T, N = args.batch, args.T, WORKLOAD["nx"]
+    model, x_np, _ = build_model(dev, B, T, seed=1234, form=args.form)
+    x = torch.from_numpy(x_np).to(dev)
+    with torch.no_grad():
+        c = model.cell.geom.c.contiguous()
+    b = model.cell.geom.b.contiguous()
+    prb, _ = model.probe_table()
+    spec = SeqSpec(B, N, N, T, model.source_table(B), prb,
+                   form=_lib.WT_FORM_FUSED if args.form == "fused" else _lib.WT_FORM_PLAIN)
+    sc = scalars(0.707, 1.0, lap_order(B, N, N, 1.0))
+    g = torch.randn(B, T, len(prb), generator=torch.Generator().manual_seed(3)).to(dev)
+    t = []
+    for k in range(args.warmup + args.steps):
+        e = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+        e[0].record()
+        out, _, _, ws = seq_forward(spec, sc, b, c, x)
+        e[1].record()
+        seq_backward(spec, sc, b, c, x, g, ws, False)
+        e[2].record()
+        torch.cuda.synchronize()
+        if k >= args.warmup:
+            t.append((e[0].elapsed_time(e[1]), e[1].elapsed_time(e[2])))
+    f = sum(a for a, _ in t) / len(t)
+    bw = sum(b_ for _, b_ in t) / len(t)
+    print(json.dumps({"kernels_only": True, "batch": B, "T": T, "form": args.form,
+                      "ms_fwd": f, "ms_bwd": bw,
+                      "cell_steps_per_s": B * N * N * T / ((f + bw) / 1e3)}))
+
+
 def main():
     args = parse()
-    if args.impl == "reference":
+    if args.kernels_only:
+        run_kernels_only(args)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_ours(args)
