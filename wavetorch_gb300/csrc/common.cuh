@@ -135,6 +135,46 @@ WT_DEV void cluster_sync_all() {
     cluster_wait_acquire();
 }
 
+// ---- mbarrier / asynchronous DSMEM store helpers (inline PTX, sm_90+) ------
+WT_DEV uint32_t smem_addr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+WT_DEV void mbar_init(uint32_t addr, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(addr), "r"(count) : "memory");
+}
+WT_DEV void fence_mbarrier_init_cluster() {
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+// One local arrival that also raises the phase's expected transaction bytes.
+WT_DEV void mbar_arrive_expect_tx(uint32_t addr, uint32_t bytes) {
+    asm volatile("{\n\t.reg .b64 st;\n\t"
+                 "mbarrier.arrive.expect_tx.shared::cta.b64 st, [%0], %1;\n\t}" ::"r"(addr),
+                 "r"(bytes)
+                 : "memory");
+}
+// Non-blocking probe of phase completion (acquire at cluster scope, so data
+// delivered by remote st.async before the phase completed is visible).
+WT_DEV bool mbar_try_wait_parity(uint32_t addr, uint32_t parity) {
+    uint32_t ok;
+    asm volatile("{\n\t.reg .pred p;\n\t"
+                 "mbarrier.try_wait.parity.acquire.cluster.shared::cta.b64 p, [%1], %2;\n\t"
+                 "selp.u32 %0, 1, 0, p;\n\t}"
+                 : "=r"(ok)
+                 : "r"(addr), "r"(parity)
+                 : "memory");
+    return ok != 0;
+}
+// Asynchronous 4-byte store into another CTA's shared memory that completes
+// `4` transaction bytes on that CTA's mbarrier (both shared::cluster addresses).
+WT_DEV void st_async_f32(uint32_t remote, float v, uint32_t remote_mbar) {
+    asm volatile("st.async.shared::cluster.mbarrier::complete_tx::bytes.b32 [%0], %1, [%2];" ::"r"(remote),
+                 "r"(__float_as_uint(v)), "r"(remote_mbar)
+                 : "memory");
+}
+WT_DEV uint64_t global_ns() {
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
 // Host-side helpers shared by the translation units (defined in api.cu).
 StepScalars wt_make_scalars(const wt_scalars* s);
 int wt_cuda_status(cudaError_t e);

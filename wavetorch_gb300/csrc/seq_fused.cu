@@ -9,22 +9,32 @@
 // (strip*M .. strip*M+M-1, col) of its CTA and keeps their state (fields,
 // coefficients, adjoint accumulators) in registers.
 //
-// Exchange.  Every step each thread writes its new values into a column-major
-// shared-memory tile  F[col+1][OFF + row]  (the tile carries zero columns at
-// y = -1 and y = ny, and one halo row above and below); the first and last
-// rows of the CTA are also pushed into the neighbouring CTAs' halo rows with
-// st.shared::cluster (DSMEM).  One barrier.cluster (release/acquire) per step
-// publishes both; the tile is double buffered, so one barrier suffices.
-// Up/down neighbours inside a strip come from registers, left/right columns
-// and the strip ends from the tile (float4 loads, conflict-free because the
-// column stride LD is 4 mod 8 floats).
+// Exchange.  Each step every thread writes its M new values into a
+// column-major shared-memory tile  F[col+1][OFF + row]  (zero columns at
+// y = -1 and y = ny, one halo row above and below the CTA's rows).  The CTA's
+// first and last rows are pushed into the neighbouring CTAs' halo rows with
+// st.async (DSMEM), which completes transaction bytes on the receiver's
+// mbarrier for that tile.  Per step: one __syncthreads for the CTA's own
+// tile, and an mbarrier wait (acquire.cluster) by the warps that read halos.
+// Tiles rotate over three slots, so a neighbour can never overwrite a halo
+// row that is still being read: it writes slot s only after consuming this
+// CTA's data of the next slot, which this CTA sent after finishing its reads
+// of slot s.  No cluster-wide barrier or release fence runs in the step loop,
+// so global stores (outputs, checkpoints) never stall the exchange.
+//
+// Waits are bounded (~2 s).  A wait that gives up records WT_DEVERR_TIMEOUT
+// in the status word, every CTA leaves its loop at the next step, and the
+// cluster meets at one final barrier before exiting.
 //
 // Adjoint.  The forward stores the pair (h_{t-1}, h_{t-2}) every `seg` steps.
 // The adjoint walks the segments backwards: it reloads the checkpoint,
 // recomputes the segment's forward steps to rebuild Lap(h_{t-1}) for each of
 // its steps (the "stash"), then runs the segment's adjoint steps from the
 // stash.  Adjoint state per cell (pending grad_y1/grad_y2 terms and the
-// running dL/dc sum of this instance) stays in registers across segments.
+// running dL/dc sum of this instance) stays in registers across segments;
+// the coefficients of each phase are re-formed from b and c when the phase
+// starts (once per segment), so only one phase's coefficients occupy
+// registers at a time.
 #include "internal.cuh"
 
 namespace wt {
@@ -32,6 +42,7 @@ namespace wt {
 constexpr int OFF = 4;       // first own row in a tile column (16-byte aligned)
 constexpr int SRCMAX = 4;    // source entries one thread may own
 constexpr int PRBMAX = 4;    // probe entries one thread may own
+constexpr uint64_t WAIT_LIMIT_NS = 2000000000ull;   // bounded mbarrier waits (2 s)
 
 // load M consecutive floats from a 16-byte aligned (M%4==0) shared address
 template <int M>
@@ -70,9 +81,8 @@ WT_DEV void sts_col(float* p, const float (&s)[M]) {
 
 // Thread geometry shared by both kernels.
 struct Geo {
-    int inst, cta, col, strip, xl0, gx0;
+    int inst, cta, col, strip, xl0, gx0, S;
     bool colv;          // column inside the grid
-    uint32_t up_rank, dn_rank;
     bool has_up, has_dn;
 };
 
@@ -84,39 +94,97 @@ WT_DEV Geo make_geo(const FusedParams& P, int M) {
     g.strip = threadIdx.x / P.NCP;
     g.xl0 = g.strip * M;
     g.gx0 = g.cta * P.R + g.xl0;
+    g.S = P.R / M;
     g.colv = g.col < P.ny;
     g.has_up = g.cta > 0;
     g.has_dn = g.cta + 1 < P.C;
-    g.up_rank = g.cta - 1;
-    g.dn_rank = g.cta + 1;
     return g;
 }
 
-// Write the thread's M new values into tile `buf` and push the CTA boundary
-// rows into the neighbours' halo rows.
+// ---- neighbour exchange ----------------------------------------------------
+struct Xchg {
+    float* tiles;           // slot 0 (slots are `tile` floats apart)
+    int tile;               // floats per slot
+    uint32_t mbar;          // shared address of 3 consecutive mbarriers
+    uint32_t up_tile, dn_tile;   // slot-0 shared::cluster addresses in the neighbours
+    uint32_t up_mbar, dn_mbar;
+    uint32_t expect;        // halo bytes per phase
+    uint32_t par;           // bit p: parity of the next wait on slot p
+    bool waiter;            // reads a halo row (or arms the barriers)
+    bool armer;
+    int* abort;             // CTA-wide abort flag (shared)
+};
+
+WT_DEV void xchg_setup(Xchg& X, const FusedParams& P, const Geo& g, float* tiles, int tile,
+                       uint64_t* mbar, int* abort) {
+    X.tiles = tiles;
+    X.tile = tile;
+    X.mbar = smem_addr(mbar);
+    X.par = 0;
+    X.abort = abort;
+    X.expect = (uint32_t)((g.has_up + g.has_dn) * P.ny * 4);
+    const bool remote = P.C > 1;
+    X.armer = remote && threadIdx.x == 0;
+    X.waiter = remote && ((g.strip == 0 && g.has_up) || (g.strip == g.S - 1 && g.has_dn) || X.armer);
+    X.up_tile = X.dn_tile = X.up_mbar = X.dn_mbar = 0;
+    if (g.has_up) {
+        X.up_tile = map_shared_rank(tiles, g.cta - 1);
+        X.up_mbar = map_shared_rank(mbar, g.cta - 1);
+    }
+    if (g.has_dn) {
+        X.dn_tile = map_shared_rank(tiles, g.cta + 1);
+        X.dn_mbar = map_shared_rank(mbar, g.cta + 1);
+    }
+    if (X.armer) {
+        for (int p = 0; p < 3; ++p) mbar_init(X.mbar + 8 * p, 1);
+        fence_mbarrier_init_cluster();
+        for (int p = 0; p < 3; ++p) mbar_arrive_expect_tx(X.mbar + 8 * p, X.expect);
+    }
+    if (threadIdx.x == 0) *abort = 0;
+}
+
+// Publish the thread's M new values into slot `s`: the neighbours' halo rows
+// first (st.async, for the CTA's first/last row), then the own tile column.
 template <int M>
-WT_DEV void publish(const FusedParams& P, const Geo& g, float* buf, const float (&v)[M],
-                    int S) {
+WT_DEV void publish(const FusedParams& P, const Geo& g, const Xchg& X, int s, const float (&v)[M],
+                    bool remote) {
     if (!g.colv) return;
-    float* colp = buf + (size_t)(g.col + 1) * P.LD + OFF;
-    sts_col<M>(colp + g.xl0, v);
-    if (g.strip == 0 && g.has_up) {
-        // my row 0 is the up-neighbour CTA's halo row R
-        uint32_t a = map_shared_rank(colp + P.R, g.up_rank);
-        st_cluster_f32(a, v[0]);
+    const int colo = (g.col + 1) * P.LD + OFF;
+    if (remote) {
+        if (g.strip == 0 && g.has_up)      // my row 0 -> up neighbour's halo row R
+            st_async_f32(X.up_tile + 4u * (uint32_t)(s * X.tile + colo + P.R), v[0],
+                         X.up_mbar + 8u * s);
+        if (g.strip == g.S - 1 && g.has_dn)   // my row R-1 -> down neighbour's halo row -1
+            st_async_f32(X.dn_tile + 4u * (uint32_t)(s * X.tile + colo - 1), v[M - 1],
+                         X.dn_mbar + 8u * s);
     }
-    if (g.strip == S - 1 && g.has_dn) {
-        // my row R-1 is the down-neighbour CTA's halo row -1
-        uint32_t a = map_shared_rank(colp - 1, g.dn_rank);
-        st_cluster_f32(a, v[M - 1]);
+    sts_col<M>(X.tiles + s * X.tile + colo + g.xl0, v);
+}
+
+// Wait until slot s holds the neighbours' halo rows, then re-arm its barrier.
+WT_DEV void xchg_wait(const FusedParams& P, Xchg& X, int s) {
+    if (!X.waiter) return;
+    const uint32_t parity = (X.par >> s) & 1u;
+    const uint32_t a = X.mbar + 8u * s;
+    if (!mbar_try_wait_parity(a, parity)) {
+        const uint64_t t0 = global_ns();
+        while (!mbar_try_wait_parity(a, parity)) {
+            if (global_ns() - t0 > WAIT_LIMIT_NS) {
+                atomicExch(P.err, WT_DEVERR_TIMEOUT);
+                *(volatile int*)X.abort = 1;
+                break;
+            }
+        }
     }
+    X.par ^= 1u << s;
+    if (X.armer) mbar_arrive_expect_tx(a, X.expect);
 }
 
 // Laplacian of the thread's M cells from registers (center) + tile (rest).
 template <int M, int ORDER>
-WT_DEV void strip_lap(const FusedParams& P, const Geo& g, const float* buf, const float (&ctr)[M],
+WT_DEV void strip_lap(const FusedParams& P, const Geo& g, const float* slot, const float (&ctr)[M],
                       float (&L)[M]) {
-    const float* colp = buf + (size_t)(g.col + 1) * P.LD + OFF + g.xl0;
+    const float* colp = slot + (g.col + 1) * P.LD + OFF + g.xl0;
     float lf[M], rt[M];
     lds_col<M>(lf, colp - P.LD);
     lds_col<M>(rt, colp + P.LD);
@@ -134,52 +202,49 @@ WT_DEV void zero_smem(float* s, int n) {
     for (int i = threadIdx.x; i < n; i += blockDim.x) s[i] = 0.f;
 }
 
-// Per-thread source list (table order) and probe list (descending order).
-template <int M>
+// Per-thread source list (table order) and probe list (descending order),
+// packed into scalar words so they stay in registers:
+//   source e: (input row << 4) | cell index i      probe e: (column << 5) | (kind << 4) | i
 struct Taps {
     int ns, np;
-    int s_i[SRCMAX], s_row[SRCMAX];
-    int p_i[PRBMAX], p_kind[PRBMAX], p_col[PRBMAX];
+    int s0, s1, s2, s3;
+    int p0, p1, p2, p3;
+    WT_DEV int s(int e) const { return e == 0 ? s0 : e == 1 ? s1 : e == 2 ? s2 : s3; }
+    WT_DEV int p(int e) const { return e == 0 ? p0 : e == 1 ? p1 : e == 2 ? p2 : p3; }
 };
 
 template <int M>
-WT_DEV void build_taps(const FusedParams& P, const Geo& g, Taps<M>& tp) {
-    tp.ns = 0;
-    tp.np = 0;
-#pragma unroll
-    for (int j = 0; j < SRCMAX; ++j) tp.s_i[j] = tp.s_row[j] = 0;
-#pragma unroll
-    for (int j = 0; j < PRBMAX; ++j) tp.p_i[j] = tp.p_kind[j] = tp.p_col[j] = 0;
-    if (!g.colv) return;
-    // (writes go through unrolled predicated stores so the lists stay in
-    // registers instead of local memory)
-    for (int e = 0; e < P.n_src; ++e) {
-        int cell = __ldg(P.src_cell + e);
-        int cx = cell / P.ny, cy = cell - cx * P.ny;
-        int i = cx - g.gx0;
-        if (cy == g.col && i >= 0 && i < M) {
-            int row = __ldg(P.src_row + e);
-            row = row < 0 ? g.inst : row;
-            if (tp.ns >= SRCMAX) { atomicExch(P.err, WT_DEVERR_BOUNDS); continue; }
-#pragma unroll
-            for (int j = 0; j < SRCMAX; ++j)
-                if (j == tp.ns) { tp.s_i[j] = i; tp.s_row[j] = row; }
-            ++tp.ns;
+WT_DEV void build_taps(const FusedParams& P, const Geo& g, Taps& tp) {
+    int ns = 0, np = 0;
+    int s0 = 0, s1 = 0, s2 = 0, s3 = 0, p0 = 0, p1 = 0, p2 = 0, p3 = 0;
+    if (g.colv) {
+        for (int e = 0; e < P.n_src; ++e) {
+            int cell = __ldg(P.src_cell + e);
+            int cx = cell / P.ny, cy = cell - cx * P.ny;
+            int i = cx - g.gx0;
+            if (cy == g.col && i >= 0 && i < M) {
+                int row = __ldg(P.src_row + e);
+                int v = ((row < 0 ? g.inst : row) << 4) | i;
+                if (ns == 0) s0 = v; else if (ns == 1) s1 = v; else if (ns == 2) s2 = v;
+                else if (ns == 3) s3 = v; else atomicExch(P.err, WT_DEVERR_BOUNDS);
+                ++ns;
+            }
+        }
+        for (int e = 0; e < P.n_prb; ++e) {
+            int cell = __ldg(P.prb_cell + e);
+            int cx = cell / P.ny, cy = cell - cx * P.ny;
+            int i = cx - g.gx0;
+            if (cy == g.col && i >= 0 && i < M) {
+                int v = (__ldg(P.prb_col + e) << 5) | (__ldg(P.prb_kind + e) << 4) | i;
+                if (np == 0) p0 = v; else if (np == 1) p1 = v; else if (np == 2) p2 = v;
+                else if (np == 3) p3 = v; else atomicExch(P.err, WT_DEVERR_BOUNDS);
+                ++np;
+            }
         }
     }
-    for (int e = 0; e < P.n_prb; ++e) {
-        int cell = __ldg(P.prb_cell + e);
-        int cx = cell / P.ny, cy = cell - cx * P.ny;
-        int i = cx - g.gx0;
-        if (cy == g.col && i >= 0 && i < M) {
-            int kind = __ldg(P.prb_kind + e), col = __ldg(P.prb_col + e);
-            if (tp.np >= PRBMAX) { atomicExch(P.err, WT_DEVERR_BOUNDS); continue; }
-#pragma unroll
-            for (int j = 0; j < PRBMAX; ++j)
-                if (j == tp.np) { tp.p_i[j] = i; tp.p_kind[j] = kind; tp.p_col[j] = col; }
-            ++tp.np;
-        }
-    }
+    tp.ns = min(ns, SRCMAX); tp.np = min(np, PRBMAX);
+    tp.s0 = s0; tp.s1 = s1; tp.s2 = s2; tp.s3 = s3;
+    tp.p0 = p0; tp.p1 = p1; tp.p2 = p2; tp.p3 = p3;
 }
 
 // select v[i] for a runtime i without dynamic register indexing
@@ -197,37 +262,13 @@ WT_DEV void add_at(float (&v)[M], int i, float a) {
         if (j == i) v[j] = fadd(v[j], a);
 }
 
-// One forward step for the thread's cells: Laplacian, update, sources.
-template <int M, int ORDER>
-WT_DEV void fwd_cells(const FusedParams& P, const Geo& g, const float* buf, const float (&A)[M],
-                      const float (&Bc)[M], const float (&C2)[M], float (&y1)[M],
-                      float (&y2)[M], float (&yn)[M], float (&L)[M], const Taps<M>& tp,
-                      const float (&xv)[SRCMAX]) {
-    strip_lap<M, ORDER>(P, g, buf, y1, L);
-#pragma unroll
-    for (int i = 0; i < M; ++i) yn[i] = leapfrog(A[i], Bc[i], C2[i], P.k.two_over, y1[i], y2[i], L[i]);
-#pragma unroll
-    for (int e = 0; e < SRCMAX; ++e)
-        if (e < tp.ns) add_at<M>(yn, tp.s_i[e], xv[e]);
-}
-
-// ============================================================================
-// Forward
-template <int M, int ORDER>
-__global__ void __launch_bounds__(512, 1) seq_fwd_fused_kernel(FusedParams P) {
-    extern __shared__ __align__(16) float smem[];
-    const Geo g = make_geo(P, M);
-    const int S = P.R / M;
-    const int tile = (P.ny + 2) * P.LD;
-    float* F0 = smem;
-    float* F1 = smem + tile;
-    zero_smem(smem, 2 * tile);
-
-    float A[M], Bc[M], C2[M], y1[M], y2[M];
+// Per-cell coefficients of one phase, re-formed from b and c.
+template <int M>
+WT_DEV void load_fwd_coef(const FusedParams& P, const Geo& g, float (&A)[M], float (&Bc)[M],
+                          float (&C2)[M]) {
 #pragma unroll
     for (int i = 0; i < M; ++i) {
         A[i] = Bc[i] = C2[i] = 0.f;
-        y1[i] = y2[i] = 0.f;
         int gx = g.gx0 + i;
         if (g.colv && gx < P.nx) {
             size_t cell = (size_t)gx * P.ny + g.col;
@@ -235,56 +276,109 @@ __global__ void __launch_bounds__(512, 1) seq_fwd_fused_kernel(FusedParams P) {
             A[i] = f.A; Bc[i] = f.Bc; C2[i] = f.c2;
         }
     }
-    Taps<M> tp;
-    build_taps<M>(P, g, tp);
-    float psum[PRBMAX], pcmp[PRBMAX];
+}
+template <int M>
+WT_DEV void load_bwd_coef(const FusedParams& P, const Geo& g, float (&X1)[M], float (&Kc)[M],
+                          float (&Kg)[M], float (&Ky2)[M]) {
 #pragma unroll
-    for (int e = 0; e < PRBMAX; ++e) psum[e] = pcmp[e] = 0.f;
-    float xv[SRCMAX];
+    for (int i = 0; i < M; ++i) {
+        X1[i] = Kc[i] = Kg[i] = Ky2[i] = 0.f;
+        int gx = g.gx0 + i;
+        if (g.colv && gx < P.nx) {
+            size_t cell = (size_t)gx * P.ny + g.col;
+            BwdCoef k = bwd_coef(__ldg(P.b + cell), __ldg(P.c + cell), P.k);
+            X1[i] = k.X1; Kc[i] = k.Kc; Kg[i] = k.Kg; Ky2[i] = k.Ky2;
+        }
+    }
+}
+
+// One forward step for the thread's cells: Laplacian, update, sources.
+template <int M, int ORDER>
+WT_DEV void fwd_cells(const FusedParams& P, const Geo& g, const float* slot, const float (&A)[M],
+                      const float (&Bc)[M], const float (&C2)[M], const float (&y1)[M],
+                      const float (&y2)[M], float (&yn)[M], float (&L)[M], const Taps& tp,
+                      const float (&xv)[SRCMAX]) {
+    strip_lap<M, ORDER>(P, g, slot, y1, L);
 #pragma unroll
-    for (int e = 0; e < SRCMAX; ++e) xv[e] = 0.f;
+    for (int i = 0; i < M; ++i) yn[i] = leapfrog(A[i], Bc[i], C2[i], P.k.two_over, y1[i], y2[i], L[i]);
 #pragma unroll
     for (int e = 0; e < SRCMAX; ++e)
-        if (e < tp.ns) xv[e] = __ldg(P.x + (size_t)tp.s_row[e] * P.steps);
+        if (e < tp.ns) add_at<M>(yn, tp.s(e) & 15, xv[e]);
+}
+
+WT_DEV int next3(int s) { return s == 2 ? 0 : s + 1; }
+
+// ============================================================================
+// Forward
+template <int M, int ORDER>
+__global__ void __launch_bounds__(512, 1) seq_fwd_fused_kernel(FusedParams P) {
+    extern __shared__ __align__(16) float smem[];
+    __shared__ __align__(8) uint64_t mbar[3];
+    __shared__ int abort_flag;
+    const Geo g = make_geo(P, M);
+    const int tile = (P.ny + 2) * P.LD;
+    zero_smem(smem, 3 * tile);
+    Xchg X;
+    xchg_setup(X, P, g, smem, tile, mbar, &abort_flag);
+
+    float A[M], Bc[M], C2[M], y1[M], y2[M];
+    load_fwd_coef<M>(P, g, A, Bc, C2);
+#pragma unroll
+    for (int i = 0; i < M; ++i) y1[i] = y2[i] = 0.f;
+    Taps tp;
+    build_taps<M>(P, g, tp);
+    float psum[PRBMAX], pcmp[PRBMAX], xv[SRCMAX];
+#pragma unroll
+    for (int e = 0; e < PRBMAX; ++e) psum[e] = pcmp[e] = 0.f;
+#pragma unroll
+    for (int e = 0; e < SRCMAX; ++e)
+        xv[e] = e < tp.ns ? __ldg(P.x + (size_t)(tp.s(e) >> 4) * P.steps) : 0.f;
 
     const size_t plane = (size_t)P.nx * P.ny;
     const size_t bplane = (size_t)P.batch * plane;
-    cluster_sync_all();
+    cluster_sync_all();   // zeroed tiles and initialised barriers, cluster-wide
 
+    int rs = 0;           // slot holding h_{t-1} (h_{-1} = 0 is slot 0)
+    int ck = P.seg;       // steps until the next checkpoint boundary
     for (int t = 0; t < P.steps; ++t) {
-        const float* buf = (t & 1) ? F1 : F0;
-        float* nbuf = (t & 1) ? F0 : F1;
-        if (t > 0 && t % P.seg == 0 && g.colv) {
-            // checkpoint (h_{t-1}, h_{t-2}) for the adjoint's segment t/seg
-            float* ck = P.ckpt + (size_t)(t / P.seg) * 2 * bplane + (size_t)g.inst * plane;
+        const int ws = next3(rs);
+        const bool remote = t + 1 < P.steps;   // the last step's halos have no reader
+        if (ck == 0) {
+            ck = P.seg;
+            // state before step t: (h_{t-1}, h_{t-2}) -> checkpoint of segment t/seg
+            if (g.colv) {
+                float* cp = P.ckpt + (size_t)(t / P.seg) * 2 * bplane + (size_t)g.inst * plane;
 #pragma unroll
-            for (int i = 0; i < M; ++i) {
-                int gx = g.gx0 + i;
-                if (gx < P.nx) {
-                    size_t cell = (size_t)gx * P.ny + g.col;
-                    ck[cell] = y1[i];
-                    ck[bplane + cell] = y2[i];
+                for (int i = 0; i < M; ++i) {
+                    int gx = g.gx0 + i;
+                    if (gx < P.nx) {
+                        size_t cell = (size_t)gx * P.ny + g.col;
+                        __stcg(cp + cell, y1[i]);
+                        __stcg(cp + bplane + cell, y2[i]);
+                    }
                 }
             }
         }
-        float yn[M], L[M];
+        --ck;
         if (g.colv) {
             float xc[SRCMAX];
 #pragma unroll
             for (int e = 0; e < SRCMAX; ++e) xc[e] = xv[e];
-            // prefetch next step's inputs
             if (t + 1 < P.steps) {
 #pragma unroll
                 for (int e = 0; e < SRCMAX; ++e)
-                    if (e < tp.ns) xv[e] = __ldg(P.x + (size_t)tp.s_row[e] * P.steps + t + 1);
+                    if (e < tp.ns) xv[e] = __ldg(P.x + (size_t)(tp.s(e) >> 4) * P.steps + t + 1);
             }
-            fwd_cells<M, ORDER>(P, g, buf, A, Bc, C2, y1, y2, yn, L, tp, xc);
+            float yn[M], L[M];
+            fwd_cells<M, ORDER>(P, g, smem + rs * tile, A, Bc, C2, y1, y2, yn, L, tp, xc);
+            publish<M>(P, g, X, ws, yn, remote);
 #pragma unroll
             for (int e = 0; e < PRBMAX; ++e) {
-                if (e >= tp.np) break;
-                float v = pick<M>(yn, tp.p_i[e]);
-                float o = tp.p_kind[e] ? fmul(v, v) : v;
-                size_t oi = ((size_t)g.inst * P.steps + t) * P.n_prb + tp.p_col[e];
+                if (e >= tp.np) continue;
+                const int pe = tp.p(e);
+                float v = pick<M>(yn, pe & 15);
+                float o = (pe & 16) ? fmul(v, v) : v;
+                size_t oi = ((size_t)g.inst * P.steps + t) * P.n_prb + (pe >> 5);
                 P.out[oi] = o;
                 P.amp[oi] = v;
                 // Kahan-compensated running time sum
@@ -301,17 +395,20 @@ __global__ void __launch_bounds__(512, 1) seq_fwd_fused_kernel(FusedParams P) {
                     if (gx < P.nx) fo[(size_t)gx * P.ny + g.col] = yn[i];
                 }
             }
-            publish<M>(P, g, nbuf, yn, S);
 #pragma unroll
             for (int i = 0; i < M; ++i) { y2[i] = y1[i]; y1[i] = yn[i]; }
         }
-        cluster_sync_all();
+        __syncthreads();
+        if (*(volatile int*)&abort_flag) break;
+        if (remote) xchg_wait(P, X, ws);
+        rs = ws;
     }
     if (P.probe_sum && g.colv) {
 #pragma unroll
         for (int e = 0; e < PRBMAX; ++e)
-            if (e < tp.np) P.probe_sum[(size_t)g.inst * P.n_prb + tp.p_col[e]] = psum[e];
+            if (e < tp.np) P.probe_sum[(size_t)g.inst * P.n_prb + (tp.p(e) >> 5)] = psum[e];
     }
+    cluster_sync_all();
 }
 
 // ============================================================================
@@ -319,38 +416,15 @@ __global__ void __launch_bounds__(512, 1) seq_fwd_fused_kernel(FusedParams P) {
 template <int M, int ORDER>
 __global__ void __launch_bounds__(512, 1) seq_bwd_fused_kernel(FusedParams P) {
     extern __shared__ __align__(16) float smem[];
+    __shared__ __align__(8) uint64_t mbar[3];
+    __shared__ int abort_flag;
     const Geo g = make_geo(P, M);
-    const int S = P.R / M;
     const int NT = blockDim.x;
     const int tile = (P.ny + 2) * P.LD;
-    float* F0 = smem;
-    float* F1 = smem + tile;
-    // forward coefficients for the recompute live in shared memory,
-    // layout [3][M][NT] (a warp reads 32 consecutive floats)
-    float* KA = smem + 2 * tile;
-    float* KB = KA + M * NT;
-    float* KC2 = KB + M * NT;
-    zero_smem(smem, 2 * tile);
-
-    float X1[M], Kc[M], Kg[M], Ky2[M];
-#pragma unroll
-    for (int i = 0; i < M; ++i) {
-        X1[i] = Kc[i] = Kg[i] = Ky2[i] = 0.f;
-        float a = 0.f, bc = 0.f, c2 = 0.f;
-        int gx = g.gx0 + i;
-        if (g.colv && gx < P.nx) {
-            size_t cell = (size_t)gx * P.ny + g.col;
-            float bb = __ldg(P.b + cell), cc = __ldg(P.c + cell);
-            FwdCoef f = fwd_coef(bb, cc, P.k);
-            BwdCoef k = bwd_coef(bb, cc, P.k);
-            a = f.A; bc = f.Bc; c2 = f.c2;
-            X1[i] = k.X1; Kc[i] = k.Kc; Kg[i] = k.Kg; Ky2[i] = k.Ky2;
-        }
-        KA[i * NT + threadIdx.x] = a;
-        KB[i * NT + threadIdx.x] = bc;
-        KC2[i * NT + threadIdx.x] = c2;
-    }
-    Taps<M> tp;
+    zero_smem(smem, 3 * tile);
+    Xchg X;
+    xchg_setup(X, P, g, smem, tile, mbar, &abort_flag);
+    Taps tp;
     build_taps<M>(P, g, tp);
 
     const size_t plane = (size_t)P.nx * P.ny;
@@ -358,108 +432,112 @@ __global__ void __launch_bounds__(512, 1) seq_bwd_fused_kernel(FusedParams P) {
     // stash of this thread: [seg][M] strided by NT
     float* stash = P.stash + ((size_t)(g.inst * P.C + g.cta) * P.seg) * M * NT + threadIdx.x;
 
-    // adjoint state: gy1 pending from t+1, gy2 pending from t+1 and t+2
+    // adjoint state: gy1 pending from t+1, gy2 pending from t+1 (a) and t+2 (b)
     float gy1[M], gy2a[M], gy2b[M], acc[M];
 #pragma unroll
     for (int i = 0; i < M; ++i) gy1[i] = gy2a[i] = gy2b[i] = acc[i] = 0.f;
-    bool have_gy1 = false, have_gy2b = false;   // gy2b: from t+2
+    bool have_gy1 = false, have_gy2b = false;
 
     cluster_sync_all();
     const int nseg = (P.steps + P.seg - 1) / P.seg;
-    // wsel: the tile to write next.  Invariant: its last reader finished
-    // before the most recent cluster barrier, so writing it is race free.
-    int wsel = 0;
-    for (int sgi = nseg - 1; sgi >= 0; --sgi) {
+    int xs = 0;           // next slot to publish into
+    bool aborted = false;
+    for (int sgi = nseg - 1; sgi >= 0 && !aborted; --sgi) {
         const int t0 = sgi * P.seg;
         const int t1 = min(P.steps, t0 + P.seg);
         // ---- recompute the segment's forward, stashing Lap(h_{t-1}) ----
-        float y1[M], y2[M];
+        {
+            float y1[M], y2[M];
 #pragma unroll
-        for (int i = 0; i < M; ++i) y1[i] = y2[i] = 0.f;
-        if (sgi > 0 && g.colv) {
-            const float* ck = P.ckpt + (size_t)sgi * 2 * bplane + (size_t)g.inst * plane;
-#pragma unroll
-            for (int i = 0; i < M; ++i) {
-                int gx = g.gx0 + i;
-                if (gx < P.nx) {
-                    size_t cell = (size_t)gx * P.ny + g.col;
-                    y1[i] = __ldcg(ck + cell);
-                    y2[i] = __ldcg(ck + bplane + cell);
-                }
-            }
-        }
-        publish<M>(P, g, wsel ? F1 : F0, y1, S);
-        cluster_sync_all();
-        int rsel = wsel;
-        wsel ^= 1;
-        float A[M], Bc[M], C2[M];
-#pragma unroll
-        for (int i = 0; i < M; ++i) {
-            A[i] = KA[i * NT + threadIdx.x];
-            Bc[i] = KB[i * NT + threadIdx.x];
-            C2[i] = KC2[i * NT + threadIdx.x];
-        }
-        for (int t = t0; t < t1; ++t) {
-            if (g.colv) {
-                float xc[SRCMAX];
-#pragma unroll
-                for (int e = 0; e < SRCMAX; ++e)
-                    xc[e] = e < tp.ns ? __ldg(P.x + (size_t)tp.s_row[e] * P.steps + t) : 0.f;
-                float yn[M], L[M];
-                fwd_cells<M, ORDER>(P, g, rsel ? F1 : F0, A, Bc, C2, y1, y2, yn, L, tp, xc);
-                float* sp = stash + (size_t)(t - t0) * M * NT;
-#pragma unroll
-                for (int i = 0; i < M; ++i) sp[(size_t)i * NT] = L[i];
-                if (t + 1 < t1) publish<M>(P, g, wsel ? F1 : F0, yn, S);
-#pragma unroll
-                for (int i = 0; i < M; ++i) { y2[i] = y1[i]; y1[i] = yn[i]; }
-            }
-            if (t + 1 < t1) {
-                cluster_sync_all();
-                rsel = wsel;
-                wsel ^= 1;
-            }
-        }
-        // ---- adjoint sweep over the segment ----
-        for (int t = t1 - 1; t >= t0; --t) {
-            float* buf = wsel ? F1 : F0;
-            float lam[M];
-#pragma unroll
-            for (int i = 0; i < M; ++i) lam[i] = 0.f;
-            if (g.colv) {
+            for (int i = 0; i < M; ++i) y1[i] = y2[i] = 0.f;
+            if (sgi > 0 && g.colv) {
+                const float* cp = P.ckpt + (size_t)sgi * 2 * bplane + (size_t)g.inst * plane;
 #pragma unroll
                 for (int i = 0; i < M; ++i) {
-                    float v = 0.f;
-                    if (have_gy2b) v = gy2b[i];
-                    if (have_gy1) v = have_gy2b ? fadd(v, gy1[i]) : gy1[i];
-                    lam[i] = v;
+                    int gx = g.gx0 + i;
+                    if (gx < P.nx) {
+                        size_t cell = (size_t)gx * P.ny + g.col;
+                        y1[i] = __ldcg(cp + cell);
+                        y2[i] = __ldcg(cp + bplane + cell);
+                    }
                 }
+            }
+            publish<M>(P, g, X, xs, y1, true);
+            __syncthreads();
+            if (*(volatile int*)&abort_flag) { aborted = true; break; }
+            xchg_wait(P, X, xs);
+            int rs = xs;
+            xs = next3(xs);
+            float A[M], Bc[M], C2[M];
+            load_fwd_coef<M>(P, g, A, Bc, C2);
+            for (int t = t0; t < t1; ++t) {
+                const bool more = t + 1 < t1;
+                if (g.colv) {
+                    float xc[SRCMAX];
+#pragma unroll
+                    for (int e = 0; e < SRCMAX; ++e)
+                        xc[e] = e < tp.ns ? __ldg(P.x + (size_t)(tp.s(e) >> 4) * P.steps + t) : 0.f;
+                    float yn[M], L[M];
+                    fwd_cells<M, ORDER>(P, g, smem + rs * tile, A, Bc, C2, y1, y2, yn, L, tp, xc);
+                    if (more) publish<M>(P, g, X, xs, yn, true);
+                    float* sp = stash + (size_t)(t - t0) * M * NT;
+#pragma unroll
+                    for (int i = 0; i < M; ++i) sp[(size_t)i * NT] = L[i];
+#pragma unroll
+                    for (int i = 0; i < M; ++i) { y2[i] = y1[i]; y1[i] = yn[i]; }
+                }
+                if (more) {
+                    __syncthreads();
+                    if (*(volatile int*)&abort_flag) { aborted = true; break; }
+                    xchg_wait(P, X, xs);
+                    rs = xs;
+                    xs = next3(xs);
+                }
+            }
+        }
+        if (aborted) break;
+        // ---- adjoint sweep over the segment ----
+        float X1[M], Kc[M], Kg[M], Ky2[M];
+        load_bwd_coef<M>(P, g, X1, Kc, Kg, Ky2);
+        for (int t = t1 - 1; t >= t0; --t) {
+            float lam[M];
+#pragma unroll
+            for (int i = 0; i < M; ++i) {
+                float v = 0.f;
+                if (have_gy2b) v = gy2b[i];
+                if (have_gy1) v = have_gy2b ? fadd(v, gy1[i]) : gy1[i];
+                lam[i] = v;
+            }
+            float c2g[M];
+#pragma unroll
+            for (int i = 0; i < M; ++i) c2g[i] = 0.f;
+            if (g.colv) {
                 // probe seeds, descending reference order (list order)
 #pragma unroll
                 for (int e = 0; e < PRBMAX; ++e) {
-                    if (e >= tp.np) break;
-                    size_t oi = ((size_t)g.inst * P.steps + t) * P.n_prb + tp.p_col[e];
+                    if (e >= tp.np) continue;
+                    const int pe = tp.p(e);
+                    size_t oi = ((size_t)g.inst * P.steps + t) * P.n_prb + (pe >> 5);
                     float gv = __ldg(P.grad_out + oi);
-                    float sd = tp.p_kind[e] ? fmul(gv, fmul(2.0f, __ldg(P.amp + oi))) : gv;
-                    add_at<M>(lam, tp.p_i[e], sd);
+                    float sd = (pe & 16) ? fmul(gv, fmul(2.0f, __ldg(P.amp + oi))) : gv;
+                    add_at<M>(lam, pe & 15, sd);
                 }
+#pragma unroll
+                for (int i = 0; i < M; ++i) c2g[i] = fmul(Kg[i], lam[i]);
+                publish<M>(P, g, X, xs, c2g, true);
                 if (P.grad_x) {
 #pragma unroll
                     for (int e = 0; e < SRCMAX; ++e)
-                        if (e < tp.ns && tp.s_row[e] == g.inst)
-                            P.grad_x[(size_t)g.inst * P.steps + t] = pick<M>(lam, tp.s_i[e]);
+                        if (e < tp.ns && (tp.s(e) >> 4) == g.inst)
+                            P.grad_x[(size_t)g.inst * P.steps + t] = pick<M>(lam, tp.s(e) & 15);
                 }
-                float c2g[M];
-#pragma unroll
-                for (int i = 0; i < M; ++i) c2g[i] = fmul(Kg[i], lam[i]);
-                publish<M>(P, g, buf, c2g, S);
             }
-            cluster_sync_all();
+            __syncthreads();
+            if (*(volatile int*)&abort_flag) { aborted = true; break; }
+            xchg_wait(P, X, xs);
             if (g.colv) {
-                float c2g[M], lg[M];
-#pragma unroll
-                for (int i = 0; i < M; ++i) c2g[i] = fmul(Kg[i], lam[i]);
-                strip_lap<M, ORDER>(P, g, buf, c2g, lg);
+                float lg[M];
+                strip_lap<M, ORDER>(P, g, smem + xs * tile, c2g, lg);
                 const float* sp = stash + (size_t)(t - t0) * M * NT;
 #pragma unroll
                 for (int i = 0; i < M; ++i) {
@@ -472,10 +550,10 @@ __global__ void __launch_bounds__(512, 1) seq_bwd_fused_kernel(FusedParams P) {
             }
             have_gy2b = have_gy1;   // gy2 from t+1 becomes "from t+2" at t-1
             have_gy1 = true;
-            wsel ^= 1;
+            xs = next3(xs);
         }
     }
-    if (g.colv) {
+    if (g.colv && !aborted) {
         float* o = P.gc_part + (size_t)g.inst * plane;
 #pragma unroll
         for (int i = 0; i < M; ++i) {
@@ -490,8 +568,6 @@ __global__ void __launch_bounds__(512, 1) seq_bwd_fused_kernel(FusedParams P) {
 
 // ---------------------------------------------------------------------------
 // Host side: configuration and launch
-#include <cstdio>
-
 static int tile_ld(int rows) {
     int ld = rows + wt::OFF + 1;
     while (ld % 8 != 4) ++ld;
@@ -518,11 +594,10 @@ int wt_fused_plan(int nx, int ny, int cluster_req, WtFusedLaunch* L) {
             if (threads > 512) continue;
             int LD = tile_ld(R);
             size_t tile = (size_t)(ny + 2) * LD * sizeof(float);
-            size_t fwd = 2 * tile;
-            size_t bwd = 2 * tile + 3 * (size_t)M * threads * sizeof(float);
-            if (bwd > 227 * 1024) continue;
+            size_t smem = 3 * tile;
+            if (smem > 220 * 1024) continue;
             L->C = C; L->M = M; L->R = R; L->S = S; L->NCP = NCP; L->LD = LD;
-            L->threads = threads; L->smem_fwd = fwd; L->smem_bwd = bwd;
+            L->threads = threads; L->smem_fwd = smem; L->smem_bwd = smem;
             return 0;
         }
     }
