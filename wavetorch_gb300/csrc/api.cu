@@ -153,21 +153,13 @@ int make_plan(const wt_seq_desc* d, SeqPlan* p) {
         P.o_lam = o; o = up(o + 3 * bp * F);
         P.o_gc = o; o = up(o + bp * F);
     } else {
-        int st = wt_fused_plan(P.nx, P.ny, d->cluster, &P.L);
+        int st = wt_fused_plan(P.nx, P.ny, P.T, d->cluster, d->segment, &P.L);
         if (st) return st;
-        // segment length: sqrt(T) by default, capped so the stash stays
-        // L2-resident (<= 48 MiB)
         const size_t per_step = (size_t)P.B * P.L.C * P.L.M * P.L.threads * F;
-        int seg = d->segment > 0 ? d->segment : (int)std::ceil(std::sqrt((double)P.T));
-        if (d->segment <= 0) {
-            size_t cap = (48u << 20) / per_step;
-            seg = std::max(1, std::min<int>(seg, (int)std::max<size_t>(1, cap)));
-        }
-        seg = std::min(seg, P.T);
-        P.seg = seg;
-        P.nseg = (P.T + seg - 1) / seg;
+        P.seg = P.L.seg;
+        P.nseg = (P.T + P.seg - 1) / P.seg;
         P.o_ckpt = o; o = up(o + (size_t)P.nseg * 2 * bp * F);
-        P.o_stash = o; o = up(o + (size_t)seg * per_step);
+        P.o_stash = o; o = up(o + (P.L.stash_smem ? 0 : (size_t)P.seg * per_step));
         P.o_gcpart = o; o = up(o + bp * F);
         // per-thread tap capacity of the fused kernels
         std::vector<int> cnt;
@@ -253,6 +245,7 @@ wt::FusedParams fused_params(const wt_scalars* s, const SeqPlan& P, const float*
     F.amp = at<float>(ws, P.o_amp);
     F.ckpt = at<float>(ws, P.o_ckpt);
     F.stash = at<float>(ws, P.o_stash);
+    F.stash_smem = P.L.stash_smem;
     F.gc_part = at<float>(ws, P.o_gcpart);
     F.err = at<int>(ws, P.o_err);
     return F;

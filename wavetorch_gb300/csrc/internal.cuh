@@ -65,7 +65,8 @@ struct FusedParams {
     const float* grad_out;  // [batch][steps][n_prb]
     float* gc_part;         // [batch][nx][ny] per-instance dL/dc
     float* grad_x;          // [batch][steps] or null
-    float* stash;           // global stash: [batch][C][seg][M][nthreads]
+    float* stash;           // global stash [batch][C][seg][M][nthreads] (unless in smem)
+    int stash_smem;         // 1: the stash lives in shared memory after the tiles
     int* err;
 };
 
@@ -74,7 +75,10 @@ struct FusedParams {
 // Launch shape of the fused kernels for one grid size.
 struct WtFusedLaunch {
     int C, M, R, S, NCP, LD, threads;
-    size_t smem_fwd, smem_bwd;
+    size_t smem_fwd;        // tiles
+    size_t smem_bwd;        // tiles (+ the stash when stash_smem)
+    int seg;                // checkpoint interval
+    int stash_smem;
 };
 
 int wt_launch_step_fwd(const StepScalars& k, int batch, int nx, int ny, int coef_batched,
@@ -92,5 +96,5 @@ int wt_launch_seq_adj_step(const StepScalars& k, int batch, int nx, int ny, cons
 int wt_launch_seq_adj_reduce(int batch, size_t plane, const float* gc, float* G, int first,
                              cudaStream_t st);
 int wt_launch_fill_zero(float* p, size_t n, cudaStream_t st);
-int wt_fused_plan(int nx, int ny, int cluster_req, WtFusedLaunch* L);
+int wt_fused_plan(int nx, int ny, int steps, int cluster_req, int seg_req, WtFusedLaunch* L);
 int wt_launch_fused(bool fwd, const wt::FusedParams& P, const WtFusedLaunch& L, cudaStream_t st);

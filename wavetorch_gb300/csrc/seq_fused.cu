@@ -35,6 +35,9 @@
 // the coefficients of each phase are re-formed from b and c when the phase
 // starts (once per segment), so only one phase's coefficients occupy
 // registers at a time.
+#include <algorithm>
+#include <cmath>
+
 #include "internal.cuh"
 
 namespace wt {
@@ -292,21 +295,104 @@ WT_DEV void load_bwd_coef(const FusedParams& P, const Geo& g, float (&X1)[M], fl
     }
 }
 
-// One forward step for the thread's cells: Laplacian, update, sources.
+// h_t for the thread's cells from cur = h_{t-1} (registers + tile slot) and
+// inout = h_{t-2}; the result overwrites inout (ping-pong register sets).
 template <int M, int ORDER>
-WT_DEV void fwd_cells(const FusedParams& P, const Geo& g, const float* slot, const float (&A)[M],
-                      const float (&Bc)[M], const float (&C2)[M], const float (&y1)[M],
-                      const float (&y2)[M], float (&yn)[M], float (&L)[M], const Taps& tp,
-                      const float (&xv)[SRCMAX]) {
-    strip_lap<M, ORDER>(P, g, slot, y1, L);
+WT_DEV void fwd_update(const FusedParams& P, const Geo& g, const float* slot, const float (&A)[M],
+                       const float (&Bc)[M], const float (&C2)[M], const float (&cur)[M],
+                       float (&inout)[M], float (&L)[M]) {
+    strip_lap<M, ORDER>(P, g, slot, cur, L);
 #pragma unroll
-    for (int i = 0; i < M; ++i) yn[i] = leapfrog(A[i], Bc[i], C2[i], P.k.two_over, y1[i], y2[i], L[i]);
+    for (int i = 0; i < M; ++i)
+        inout[i] = leapfrog(A[i], Bc[i], C2[i], P.k.two_over, cur[i], inout[i], L[i]);
+}
+
+// Sources (in table order) with the inputs prefetched one step ahead.
+template <int M>
+WT_DEV void apply_sources(const FusedParams& P, const Taps& tp, float (&y)[M], float (&xv)[SRCMAX],
+                          int tnext) {
 #pragma unroll
     for (int e = 0; e < SRCMAX; ++e)
-        if (e < tp.ns) add_at<M>(yn, tp.s(e) & 15, xv[e]);
+        if (e < tp.ns) add_at<M>(y, tp.s(e) & 15, xv[e]);
+    if (tnext >= 0 && tnext < P.steps) {
+#pragma unroll
+        for (int e = 0; e < SRCMAX; ++e)
+            if (e < tp.ns) xv[e] = __ldg(P.x + (size_t)(tp.s(e) >> 4) * P.steps + tnext);
+    }
 }
 
 WT_DEV int next3(int s) { return s == 2 ? 0 : s + 1; }
+
+struct FwdState {
+    int ck;                   // steps until the next checkpoint boundary
+    float xv[SRCMAX];         // this step's source inputs
+    float psum[PRBMAX], pcmp[PRBMAX];
+};
+
+// One step of the forward kernel (everything but the exchange wait).
+template <int M, int ORDER>
+WT_DEV void fwd_step(const FusedParams& P, const Geo& g, const Xchg& X, const Taps& tp,
+                     FwdState& st, int t, int rs, int ws, const float (&A)[M], const float (&Bc)[M],
+                     const float (&C2)[M], const float (&cur)[M], float (&inout)[M]) {
+    const size_t plane = (size_t)P.nx * P.ny;
+    const size_t bplane = (size_t)P.batch * plane;
+    if (st.ck == 0) {
+        st.ck = P.seg;
+        // state before step t: (h_{t-1}, h_{t-2}) -> checkpoint of segment t/seg
+        if (g.colv) {
+            float* cp = P.ckpt + (size_t)(t / P.seg) * 2 * bplane + (size_t)g.inst * plane;
+#pragma unroll
+            for (int i = 0; i < M; ++i) {
+                int gx = g.gx0 + i;
+                if (gx < P.nx) {
+                    size_t cell = (size_t)gx * P.ny + g.col;
+                    __stcg(cp + cell, cur[i]);
+                    __stcg(cp + bplane + cell, inout[i]);
+                }
+            }
+        }
+    }
+    --st.ck;
+    if (!g.colv) return;
+    float L[M];
+    fwd_update<M, ORDER>(P, g, X.tiles + rs * X.tile, A, Bc, C2, cur, inout, L);
+    if (tp.ns) apply_sources<M>(P, tp, inout, st.xv, t + 1);
+    publish<M>(P, g, X, ws, inout, t + 1 < P.steps);
+    if (tp.np) {
+#pragma unroll
+        for (int e = 0; e < PRBMAX; ++e) {
+            if (e >= tp.np) continue;
+            const int pe = tp.p(e);
+            float v = pick<M>(inout, pe & 15);
+            float o = (pe & 16) ? fmul(v, v) : v;
+            size_t oi = ((size_t)g.inst * P.steps + t) * P.n_prb + (pe >> 5);
+            P.out[oi] = o;
+            P.amp[oi] = v;
+            // Kahan-compensated running time sum
+            float yk = fsub(o, st.pcmp[e]);
+            float tk = fadd(st.psum[e], yk);
+            st.pcmp[e] = fsub(fsub(tk, st.psum[e]), yk);
+            st.psum[e] = tk;
+        }
+    }
+    if (P.fields) {
+        float* fo = P.fields + ((size_t)g.inst * P.steps + t) * plane;
+#pragma unroll
+        for (int i = 0; i < M; ++i) {
+            int gx = g.gx0 + i;
+            if (gx < P.nx) fo[(size_t)gx * P.ny + g.col] = inout[i];
+        }
+    }
+}
+
+// End of an exchange: CTA barrier, abort check, halo wait.  Returns false
+// when the CTA must leave its loop.
+WT_DEV bool exchange_end(const FusedParams& P, Xchg& X, int s, bool wait_remote) {
+    __syncthreads();
+    if (*(volatile int*)X.abort) return false;
+    if (wait_remote) xchg_wait(P, X, s);
+    return true;
+}
 
 // ============================================================================
 // Forward
@@ -321,98 +407,67 @@ __global__ void __launch_bounds__(512, 1) seq_fwd_fused_kernel(FusedParams P) {
     Xchg X;
     xchg_setup(X, P, g, smem, tile, mbar, &abort_flag);
 
-    float A[M], Bc[M], C2[M], y1[M], y2[M];
+    float A[M], Bc[M], C2[M], ya[M], yb[M];
     load_fwd_coef<M>(P, g, A, Bc, C2);
 #pragma unroll
-    for (int i = 0; i < M; ++i) y1[i] = y2[i] = 0.f;
+    for (int i = 0; i < M; ++i) ya[i] = yb[i] = 0.f;
     Taps tp;
     build_taps<M>(P, g, tp);
-    float psum[PRBMAX], pcmp[PRBMAX], xv[SRCMAX];
+    FwdState st;
+    st.ck = P.seg;
 #pragma unroll
-    for (int e = 0; e < PRBMAX; ++e) psum[e] = pcmp[e] = 0.f;
+    for (int e = 0; e < PRBMAX; ++e) st.psum[e] = st.pcmp[e] = 0.f;
 #pragma unroll
     for (int e = 0; e < SRCMAX; ++e)
-        xv[e] = e < tp.ns ? __ldg(P.x + (size_t)(tp.s(e) >> 4) * P.steps) : 0.f;
-
-    const size_t plane = (size_t)P.nx * P.ny;
-    const size_t bplane = (size_t)P.batch * plane;
+        st.xv[e] = e < tp.ns ? __ldg(P.x + (size_t)(tp.s(e) >> 4) * P.steps) : 0.f;
     cluster_sync_all();   // zeroed tiles and initialised barriers, cluster-wide
 
+    // ya holds h_{t-1} at even t, yb at odd t (the update overwrites h_{t-2})
     int rs = 0;           // slot holding h_{t-1} (h_{-1} = 0 is slot 0)
-    int ck = P.seg;       // steps until the next checkpoint boundary
-    for (int t = 0; t < P.steps; ++t) {
-        const int ws = next3(rs);
-        const bool remote = t + 1 < P.steps;   // the last step's halos have no reader
-        if (ck == 0) {
-            ck = P.seg;
-            // state before step t: (h_{t-1}, h_{t-2}) -> checkpoint of segment t/seg
-            if (g.colv) {
-                float* cp = P.ckpt + (size_t)(t / P.seg) * 2 * bplane + (size_t)g.inst * plane;
-#pragma unroll
-                for (int i = 0; i < M; ++i) {
-                    int gx = g.gx0 + i;
-                    if (gx < P.nx) {
-                        size_t cell = (size_t)gx * P.ny + g.col;
-                        __stcg(cp + cell, y1[i]);
-                        __stcg(cp + bplane + cell, y2[i]);
-                    }
-                }
-            }
-        }
-        --ck;
-        if (g.colv) {
-            float xc[SRCMAX];
-#pragma unroll
-            for (int e = 0; e < SRCMAX; ++e) xc[e] = xv[e];
-            if (t + 1 < P.steps) {
-#pragma unroll
-                for (int e = 0; e < SRCMAX; ++e)
-                    if (e < tp.ns) xv[e] = __ldg(P.x + (size_t)(tp.s(e) >> 4) * P.steps + t + 1);
-            }
-            float yn[M], L[M];
-            fwd_cells<M, ORDER>(P, g, smem + rs * tile, A, Bc, C2, y1, y2, yn, L, tp, xc);
-            publish<M>(P, g, X, ws, yn, remote);
-#pragma unroll
-            for (int e = 0; e < PRBMAX; ++e) {
-                if (e >= tp.np) continue;
-                const int pe = tp.p(e);
-                float v = pick<M>(yn, pe & 15);
-                float o = (pe & 16) ? fmul(v, v) : v;
-                size_t oi = ((size_t)g.inst * P.steps + t) * P.n_prb + (pe >> 5);
-                P.out[oi] = o;
-                P.amp[oi] = v;
-                // Kahan-compensated running time sum
-                float yk = fsub(o, pcmp[e]);
-                float tk = fadd(psum[e], yk);
-                pcmp[e] = fsub(fsub(tk, psum[e]), yk);
-                psum[e] = tk;
-            }
-            if (P.fields) {
-                float* fo = P.fields + ((size_t)g.inst * P.steps + t) * plane;
-#pragma unroll
-                for (int i = 0; i < M; ++i) {
-                    int gx = g.gx0 + i;
-                    if (gx < P.nx) fo[(size_t)gx * P.ny + g.col] = yn[i];
-                }
-            }
-#pragma unroll
-            for (int i = 0; i < M; ++i) { y2[i] = y1[i]; y1[i] = yn[i]; }
-        }
-        __syncthreads();
-        if (*(volatile int*)&abort_flag) break;
-        if (remote) xchg_wait(P, X, ws);
+    for (int t = 0; t < P.steps;) {
+        int ws = next3(rs);
+        fwd_step<M, ORDER>(P, g, X, tp, st, t, rs, ws, A, Bc, C2, ya, yb);
+        if (!exchange_end(P, X, ws, t + 1 < P.steps)) break;
         rs = ws;
+        if (++t >= P.steps) break;
+        ws = next3(rs);
+        fwd_step<M, ORDER>(P, g, X, tp, st, t, rs, ws, A, Bc, C2, yb, ya);
+        if (!exchange_end(P, X, ws, t + 1 < P.steps)) break;
+        rs = ws;
+        ++t;
     }
-    if (P.probe_sum && g.colv) {
+    if (P.probe_sum && g.colv && tp.np) {
 #pragma unroll
         for (int e = 0; e < PRBMAX; ++e)
-            if (e < tp.np) P.probe_sum[(size_t)g.inst * P.n_prb + (tp.p(e) >> 5)] = psum[e];
+            if (e < tp.np) P.probe_sum[(size_t)g.inst * P.n_prb + (tp.p(e) >> 5)] = st.psum[e];
     }
     cluster_sync_all();
 }
 
 // ============================================================================
 // Adjoint with segment recompute.
+template <int M>
+struct Stash {
+    float* p;       // this thread's element 0; cell i of step s at p[(s*M + i)*NT]
+    int NT;
+    WT_DEV float* at(int s, int i) const { return p + (size_t)(s * M + i) * NT; }
+};
+
+// Recompute step: like fwd_step, but stashes Lap(h_{t-1}) instead of writing outputs.
+template <int M, int ORDER>
+WT_DEV void rec_step(const FusedParams& P, const Geo& g, const Xchg& X, const Taps& tp,
+                     float (&xv)[SRCMAX], int t, int t0, int t1, int rs, int ws,
+                     const Stash<M>& sh, const float (&A)[M], const float (&Bc)[M],
+                     const float (&C2)[M], const float (&cur)[M], float (&inout)[M]) {
+    if (!g.colv) return;
+    float L[M];
+    fwd_update<M, ORDER>(P, g, X.tiles + rs * X.tile, A, Bc, C2, cur, inout, L);
+    if (tp.ns) apply_sources<M>(P, tp, inout, xv, t + 1 < t1 ? t + 1 : -1);
+    if (t + 1 < t1) publish<M>(P, g, X, ws, inout, true);
+#pragma unroll
+    for (int i = 0; i < M; ++i) *sh.at(t - t0, i) = L[i];
+}
+
 template <int M, int ORDER>
 __global__ void __launch_bounds__(512, 1) seq_bwd_fused_kernel(FusedParams P) {
     extern __shared__ __align__(16) float smem[];
@@ -429,27 +484,43 @@ __global__ void __launch_bounds__(512, 1) seq_bwd_fused_kernel(FusedParams P) {
 
     const size_t plane = (size_t)P.nx * P.ny;
     const size_t bplane = (size_t)P.batch * plane;
-    // stash of this thread: [seg][M] strided by NT
-    float* stash = P.stash + ((size_t)(g.inst * P.C + g.cta) * P.seg) * M * NT + threadIdx.x;
+    Stash<M> sh;
+    sh.NT = NT;
+    sh.p = P.stash_smem ? smem + 3 * tile + threadIdx.x
+                        : P.stash + ((size_t)(g.inst * P.C + g.cta) * P.seg) * M * NT + threadIdx.x;
 
-    // adjoint state: gy1 pending from t+1, gy2 pending from t+1 (a) and t+2 (b)
+    // adjoint state: gy1 pending from t+1, gy2 pending from t+1 (a) and t+2 (b).
+    // Zero-initialised, so the first arrivals reproduce autograd's "first
+    // gradient is stored" up to the sign of an exact zero.
     float gy1[M], gy2a[M], gy2b[M], acc[M];
 #pragma unroll
     for (int i = 0; i < M; ++i) gy1[i] = gy2a[i] = gy2b[i] = acc[i] = 0.f;
-    bool have_gy1 = false, have_gy2b = false;
+    // probe seeds prefetched one step ahead: grad_out and amplitude
+    float sg[PRBMAX], sa[PRBMAX];
+#pragma unroll
+    for (int e = 0; e < PRBMAX; ++e) sg[e] = sa[e] = 0.f;
+    if (tp.np && g.colv) {
+#pragma unroll
+        for (int e = 0; e < PRBMAX; ++e)
+            if (e < tp.np) {
+                size_t oi = ((size_t)g.inst * P.steps + (P.steps - 1)) * P.n_prb + (tp.p(e) >> 5);
+                sg[e] = __ldg(P.grad_out + oi);
+                sa[e] = __ldg(P.amp + oi);
+            }
+    }
 
     cluster_sync_all();
     const int nseg = (P.steps + P.seg - 1) / P.seg;
     int xs = 0;           // next slot to publish into
-    bool aborted = false;
-    for (int sgi = nseg - 1; sgi >= 0 && !aborted; --sgi) {
+    bool ok = true;
+    for (int sgi = nseg - 1; sgi >= 0 && ok; --sgi) {
         const int t0 = sgi * P.seg;
         const int t1 = min(P.steps, t0 + P.seg);
         // ---- recompute the segment's forward, stashing Lap(h_{t-1}) ----
         {
-            float y1[M], y2[M];
+            float ya[M], yb[M];   // h_{t0-1}, h_{t0-2}
 #pragma unroll
-            for (int i = 0; i < M; ++i) y1[i] = y2[i] = 0.f;
+            for (int i = 0; i < M; ++i) ya[i] = yb[i] = 0.f;
             if (sgi > 0 && g.colv) {
                 const float* cp = P.ckpt + (size_t)sgi * 2 * bplane + (size_t)g.inst * plane;
 #pragma unroll
@@ -457,103 +528,90 @@ __global__ void __launch_bounds__(512, 1) seq_bwd_fused_kernel(FusedParams P) {
                     int gx = g.gx0 + i;
                     if (gx < P.nx) {
                         size_t cell = (size_t)gx * P.ny + g.col;
-                        y1[i] = __ldcg(cp + cell);
-                        y2[i] = __ldcg(cp + bplane + cell);
+                        ya[i] = __ldcg(cp + cell);
+                        yb[i] = __ldcg(cp + bplane + cell);
                     }
                 }
             }
-            publish<M>(P, g, X, xs, y1, true);
-            __syncthreads();
-            if (*(volatile int*)&abort_flag) { aborted = true; break; }
-            xchg_wait(P, X, xs);
+            publish<M>(P, g, X, xs, ya, true);
+            if (!(ok = exchange_end(P, X, xs, true))) break;
             int rs = xs;
             xs = next3(xs);
             float A[M], Bc[M], C2[M];
             load_fwd_coef<M>(P, g, A, Bc, C2);
-            for (int t = t0; t < t1; ++t) {
-                const bool more = t + 1 < t1;
-                if (g.colv) {
-                    float xc[SRCMAX];
+            float xv[SRCMAX];
 #pragma unroll
-                    for (int e = 0; e < SRCMAX; ++e)
-                        xc[e] = e < tp.ns ? __ldg(P.x + (size_t)(tp.s(e) >> 4) * P.steps + t) : 0.f;
-                    float yn[M], L[M];
-                    fwd_cells<M, ORDER>(P, g, smem + rs * tile, A, Bc, C2, y1, y2, yn, L, tp, xc);
-                    if (more) publish<M>(P, g, X, xs, yn, true);
-                    float* sp = stash + (size_t)(t - t0) * M * NT;
-#pragma unroll
-                    for (int i = 0; i < M; ++i) sp[(size_t)i * NT] = L[i];
-#pragma unroll
-                    for (int i = 0; i < M; ++i) { y2[i] = y1[i]; y1[i] = yn[i]; }
-                }
-                if (more) {
-                    __syncthreads();
-                    if (*(volatile int*)&abort_flag) { aborted = true; break; }
-                    xchg_wait(P, X, xs);
-                    rs = xs;
-                    xs = next3(xs);
-                }
+            for (int e = 0; e < SRCMAX; ++e)
+                xv[e] = (e < tp.ns) ? __ldg(P.x + (size_t)(tp.s(e) >> 4) * P.steps + t0) : 0.f;
+            for (int t = t0; t < t1;) {
+                rec_step<M, ORDER>(P, g, X, tp, xv, t, t0, t1, rs, xs, sh, A, Bc, C2, ya, yb);
+                if (++t >= t1) break;
+                if (!(ok = exchange_end(P, X, xs, true))) break;
+                rs = xs;
+                xs = next3(xs);
+                rec_step<M, ORDER>(P, g, X, tp, xv, t, t0, t1, rs, xs, sh, A, Bc, C2, yb, ya);
+                if (++t >= t1) break;
+                if (!(ok = exchange_end(P, X, xs, true))) break;
+                rs = xs;
+                xs = next3(xs);
             }
+            if (!ok) break;
         }
-        if (aborted) break;
+        // the stash of the last recompute step was written by this thread
+        // only, so no barrier is needed before the adjoint reads it back
         // ---- adjoint sweep over the segment ----
         float X1[M], Kc[M], Kg[M], Ky2[M];
         load_bwd_coef<M>(P, g, X1, Kc, Kg, Ky2);
         for (int t = t1 - 1; t >= t0; --t) {
-            float lam[M];
+            float lam[M], c2g[M];
 #pragma unroll
             for (int i = 0; i < M; ++i) {
-                float v = 0.f;
-                if (have_gy2b) v = gy2b[i];
-                if (have_gy1) v = have_gy2b ? fadd(v, gy1[i]) : gy1[i];
-                lam[i] = v;
+                lam[i] = fadd(gy2b[i], gy1[i]);
+                c2g[i] = 0.f;
             }
-            float c2g[M];
-#pragma unroll
-            for (int i = 0; i < M; ++i) c2g[i] = 0.f;
             if (g.colv) {
-                // probe seeds, descending reference order (list order)
+                if (tp.np) {
+                    // probe seeds, descending reference order (list order)
 #pragma unroll
-                for (int e = 0; e < PRBMAX; ++e) {
-                    if (e >= tp.np) continue;
-                    const int pe = tp.p(e);
-                    size_t oi = ((size_t)g.inst * P.steps + t) * P.n_prb + (pe >> 5);
-                    float gv = __ldg(P.grad_out + oi);
-                    float sd = (pe & 16) ? fmul(gv, fmul(2.0f, __ldg(P.amp + oi))) : gv;
-                    add_at<M>(lam, pe & 15, sd);
+                    for (int e = 0; e < PRBMAX; ++e) {
+                        if (e >= tp.np) continue;
+                        const int pe = tp.p(e);
+                        float sd = (pe & 16) ? fmul(sg[e], fmul(2.0f, sa[e])) : sg[e];
+                        add_at<M>(lam, pe & 15, sd);
+                        if (t > 0) {
+                            size_t oi = ((size_t)g.inst * P.steps + (t - 1)) * P.n_prb + (pe >> 5);
+                            sg[e] = __ldg(P.grad_out + oi);
+                            sa[e] = __ldg(P.amp + oi);
+                        }
+                    }
                 }
 #pragma unroll
                 for (int i = 0; i < M; ++i) c2g[i] = fmul(Kg[i], lam[i]);
                 publish<M>(P, g, X, xs, c2g, true);
-                if (P.grad_x) {
+                if (P.grad_x && tp.ns) {
 #pragma unroll
                     for (int e = 0; e < SRCMAX; ++e)
                         if (e < tp.ns && (tp.s(e) >> 4) == g.inst)
                             P.grad_x[(size_t)g.inst * P.steps + t] = pick<M>(lam, tp.s(e) & 15);
                 }
             }
-            __syncthreads();
-            if (*(volatile int*)&abort_flag) { aborted = true; break; }
-            xchg_wait(P, X, xs);
+            if (!(ok = exchange_end(P, X, xs, true))) break;
             if (g.colv) {
                 float lg[M];
                 strip_lap<M, ORDER>(P, g, smem + xs * tile, c2g, lg);
-                const float* sp = stash + (size_t)(t - t0) * M * NT;
 #pragma unroll
                 for (int i = 0; i < M; ++i) {
-                    float Ly = sp[(size_t)i * NT];
+                    float Ly = *sh.at(t - t0, i);
                     acc[i] = fadd(acc[i], fmul(fmul(X1[i], fmul(Kc[i], Ly)), lam[i]));
                     gy1[i] = fadd(fmul(P.k.dt2, lg[i]), fmul(fmul(2.0f, lam[i]), X1[i]));
                     gy2b[i] = gy2a[i];
                     gy2a[i] = fmul(Ky2[i], lam[i]);
                 }
             }
-            have_gy2b = have_gy1;   // gy2 from t+1 becomes "from t+2" at t-1
-            have_gy1 = true;
             xs = next3(xs);
         }
     }
-    if (g.colv && !aborted) {
+    if (g.colv && ok) {
         float* o = P.gc_part + (size_t)g.inst * plane;
 #pragma unroll
         for (int i = 0; i < M; ++i) {
@@ -575,11 +633,14 @@ static int tile_ld(int rows) {
 }
 
 // Pick (C, M) for a grid: clusters of C CTAs, M cells per thread, at most
-// 512 threads per CTA.  Returns 0 on success.
-int wt_fused_plan(int nx, int ny, int cluster_req, WtFusedLaunch* L) {
+// 512 threads per CTA; then the checkpoint interval: the largest stash that
+// fits in shared memory next to the three tiles (at least 4 steps), else a
+// sqrt(T) interval with the stash in global memory.  Returns 0 on success.
+int wt_fused_plan(int nx, int ny, int steps, int cluster_req, int seg_req, WtFusedLaunch* L) {
     const int NCP = ((ny + 31) / 32) * 32;
     const int Ms[2] = {8, 4};
     const int Cs[5] = {4, 2, 8, 1, 16};
+    const size_t SMEM_MAX = 227 * 1024 - 64;   // dynamic smem per CTA (static: 28 B)
     for (int ci = 0; ci < 5; ++ci) {
         int C = Cs[ci];
         if (cluster_req > 0 && C != cluster_req) continue;
@@ -593,11 +654,17 @@ int wt_fused_plan(int nx, int ny, int cluster_req, WtFusedLaunch* L) {
             int threads = S * NCP;
             if (threads > 512) continue;
             int LD = tile_ld(R);
-            size_t tile = (size_t)(ny + 2) * LD * sizeof(float);
-            size_t smem = 3 * tile;
-            if (smem > 220 * 1024) continue;
+            size_t tiles = 3 * (size_t)(ny + 2) * LD * sizeof(float);
+            if (tiles > SMEM_MAX) continue;
             L->C = C; L->M = M; L->R = R; L->S = S; L->NCP = NCP; L->LD = LD;
-            L->threads = threads; L->smem_fwd = smem; L->smem_bwd = smem;
+            L->threads = threads; L->smem_fwd = tiles;
+            const size_t per_step = (size_t)M * threads * sizeof(float);
+            const int fit = (int)((SMEM_MAX - tiles) / per_step);
+            int seg = seg_req > 0 ? seg_req : (fit >= 4 ? fit : (int)std::ceil(std::sqrt((double)steps)));
+            seg = std::max(1, std::min(seg, steps));
+            L->seg = seg;
+            L->stash_smem = seg <= fit;
+            L->smem_bwd = tiles + (L->stash_smem ? (size_t)seg * per_step : 0);
             return 0;
         }
     }
