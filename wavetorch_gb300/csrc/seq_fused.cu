@@ -183,22 +183,26 @@ WT_DEV void xchg_wait(const FusedParams& P, Xchg& X, int s) {
     if (X.armer) mbar_arrive_expect_tx(a, X.expect);
 }
 
-// Laplacian of the thread's M cells from registers (center) + tile (rest).
-template <int M, int ORDER>
-WT_DEV void strip_lap(const FusedParams& P, const Geo& g, const float* slot, const float (&ctr)[M],
-                      float (&L)[M]) {
-    const float* colp = slot + (g.col + 1) * P.LD + OFF + g.xl0;
+// The thread's column of slot `slot`: left/right neighbour columns of its M
+// cells, and the two cells just above and below its strip.
+template <int M>
+struct Column {
     float lf[M], rt[M];
-    lds_col<M>(lf, colp - P.LD);
-    lds_col<M>(rt, colp + P.LD);
-    const float up = colp[-1];
-    const float dn = colp[M];
-#pragma unroll
-    for (int i = 0; i < M; ++i) {
-        float u = i == 0 ? up : ctr[i - 1];
-        float d = i == M - 1 ? dn : ctr[i + 1];
-        L[i] = lap5<ORDER>(u, lf[i], ctr[i], rt[i], d, P.k.lap_w, P.k.lap_w4);
-    }
+    const float* colp;     // own cell 0 in the slot
+};
+template <int M>
+WT_DEV void load_sides(Column<M>& c, const FusedParams& P, const Geo& g, const float* slot) {
+    c.colp = slot + (g.col + 1) * P.LD + OFF + g.xl0;
+    lds_col<M>(c.lf, c.colp - P.LD);
+    lds_col<M>(c.rt, c.colp + P.LD);
+}
+// Laplacian of cell i (0 < i < M-1 use registers for up/down; the ends read
+// the tile: a halo row for the CTA's boundary strips).
+template <int M, int ORDER>
+WT_DEV float lap_cell(const FusedParams& P, const Column<M>& c, const float (&ctr)[M], int i) {
+    float u = i == 0 ? c.colp[-1] : ctr[i - 1];
+    float d = i == M - 1 ? c.colp[M] : ctr[i + 1];
+    return lap5<ORDER>(u, c.lf[i], ctr[i], c.rt[i], d, P.k.lap_w, P.k.lap_w4);
 }
 
 WT_DEV void zero_smem(float* s, int n) {
@@ -295,16 +299,31 @@ WT_DEV void load_bwd_coef(const FusedParams& P, const Geo& g, float (&X1)[M], fl
     }
 }
 
-// h_t for the thread's cells from cur = h_{t-1} (registers + tile slot) and
+WT_DEV int next3(int s) { return s == 2 ? 0 : s + 1; }
+
+// h_t for the thread's cells from cur = h_{t-1} (registers + tile slot rs) and
 // inout = h_{t-2}; the result overwrites inout (ping-pong register sets).
+// Cells that need no halo row are updated first; then the warps that read a
+// halo wait for it (when `halo` says the slot carries remote rows), so the
+// DSMEM latency overlaps the interior work.  L receives Lap(h_{t-1}).
 template <int M, int ORDER>
-WT_DEV void fwd_update(const FusedParams& P, const Geo& g, const float* slot, const float (&A)[M],
-                       const float (&Bc)[M], const float (&C2)[M], const float (&cur)[M],
-                       float (&inout)[M], float (&L)[M]) {
-    strip_lap<M, ORDER>(P, g, slot, cur, L);
+WT_DEV void fwd_update(const FusedParams& P, const Geo& g, Xchg& X, int rs, bool halo,
+                       const float (&A)[M], const float (&Bc)[M], const float (&C2)[M],
+                       const float (&cur)[M], float (&inout)[M], float (&L)[M]) {
+    if (!g.colv) return;   // padding columns read nothing (their tile columns do not exist)
+    Column<M> c;
+    load_sides<M>(c, P, g, X.tiles + rs * X.tile);
 #pragma unroll
-    for (int i = 0; i < M; ++i)
+    for (int i = 1; i < M - 1; ++i) {
+        L[i] = lap_cell<M, ORDER>(P, c, cur, i);
         inout[i] = leapfrog(A[i], Bc[i], C2[i], P.k.two_over, cur[i], inout[i], L[i]);
+    }
+    if (halo) xchg_wait(P, X, rs);
+    L[0] = lap_cell<M, ORDER>(P, c, cur, 0);
+    inout[0] = leapfrog(A[0], Bc[0], C2[0], P.k.two_over, cur[0], inout[0], L[0]);
+    L[M - 1] = lap_cell<M, ORDER>(P, c, cur, M - 1);
+    inout[M - 1] = leapfrog(A[M - 1], Bc[M - 1], C2[M - 1], P.k.two_over, cur[M - 1],
+                            inout[M - 1], L[M - 1]);
 }
 
 // Sources (in table order) with the inputs prefetched one step ahead.
@@ -321,18 +340,16 @@ WT_DEV void apply_sources(const FusedParams& P, const Taps& tp, float (&y)[M], f
     }
 }
 
-WT_DEV int next3(int s) { return s == 2 ? 0 : s + 1; }
-
 struct FwdState {
     int ck;                   // steps until the next checkpoint boundary
     float xv[SRCMAX];         // this step's source inputs
     float psum[PRBMAX], pcmp[PRBMAX];
 };
 
-// One step of the forward kernel (everything but the exchange wait).
+// One step of the forward kernel (everything but the closing barrier).
 template <int M, int ORDER>
-WT_DEV void fwd_step(const FusedParams& P, const Geo& g, const Xchg& X, const Taps& tp,
-                     FwdState& st, int t, int rs, int ws, const float (&A)[M], const float (&Bc)[M],
+WT_DEV void fwd_step(const FusedParams& P, const Geo& g, Xchg& X, const Taps& tp, FwdState& st,
+                     int t, int rs, int ws, const float (&A)[M], const float (&Bc)[M],
                      const float (&C2)[M], const float (&cur)[M], float (&inout)[M]) {
     const size_t plane = (size_t)P.nx * P.ny;
     const size_t bplane = (size_t)P.batch * plane;
@@ -353,9 +370,10 @@ WT_DEV void fwd_step(const FusedParams& P, const Geo& g, const Xchg& X, const Ta
         }
     }
     --st.ck;
-    if (!g.colv) return;
     float L[M];
-    fwd_update<M, ORDER>(P, g, X.tiles + rs * X.tile, A, Bc, C2, cur, inout, L);
+    // h_{t-1} came with remote halo rows for every t >= 1 (h_{-1} = 0 is local)
+    fwd_update<M, ORDER>(P, g, X, rs, t >= 1, A, Bc, C2, cur, inout, L);
+    if (!g.colv) return;
     if (tp.ns) apply_sources<M>(P, tp, inout, st.xv, t + 1);
     publish<M>(P, g, X, ws, inout, t + 1 < P.steps);
     if (tp.np) {
@@ -385,19 +403,19 @@ WT_DEV void fwd_step(const FusedParams& P, const Geo& g, const Xchg& X, const Ta
     }
 }
 
-// End of an exchange: CTA barrier, abort check, halo wait.  Returns false
-// when the CTA must leave its loop.
-WT_DEV bool exchange_end(const FusedParams& P, Xchg& X, int s, bool wait_remote) {
+// CTA barrier closing an exchange; false when the CTA must leave its loop.
+WT_DEV bool exchange_end(const Xchg& X) {
     __syncthreads();
-    if (*(volatile int*)X.abort) return false;
-    if (wait_remote) xchg_wait(P, X, s);
-    return true;
+    return *(volatile int*)X.abort == 0;
 }
+
+template <int M>
+constexpr int max_threads() { return M >= 10 ? 384 : 512; }
 
 // ============================================================================
 // Forward
 template <int M, int ORDER>
-__global__ void __launch_bounds__(512, 1) seq_fwd_fused_kernel(FusedParams P) {
+__global__ void __launch_bounds__(max_threads<M>(), 1) seq_fwd_fused_kernel(FusedParams P) {
     extern __shared__ __align__(16) float smem[];
     __shared__ __align__(8) uint64_t mbar[3];
     __shared__ int abort_flag;
@@ -427,12 +445,12 @@ __global__ void __launch_bounds__(512, 1) seq_fwd_fused_kernel(FusedParams P) {
     for (int t = 0; t < P.steps;) {
         int ws = next3(rs);
         fwd_step<M, ORDER>(P, g, X, tp, st, t, rs, ws, A, Bc, C2, ya, yb);
-        if (!exchange_end(P, X, ws, t + 1 < P.steps)) break;
+        if (!exchange_end(X)) break;
         rs = ws;
         if (++t >= P.steps) break;
         ws = next3(rs);
         fwd_step<M, ORDER>(P, g, X, tp, st, t, rs, ws, A, Bc, C2, yb, ya);
-        if (!exchange_end(P, X, ws, t + 1 < P.steps)) break;
+        if (!exchange_end(X)) break;
         rs = ws;
         ++t;
     }
@@ -455,21 +473,31 @@ struct Stash {
 
 // Recompute step: like fwd_step, but stashes Lap(h_{t-1}) instead of writing outputs.
 template <int M, int ORDER>
-WT_DEV void rec_step(const FusedParams& P, const Geo& g, const Xchg& X, const Taps& tp,
+WT_DEV void rec_step(const FusedParams& P, const Geo& g, Xchg& X, const Taps& tp,
                      float (&xv)[SRCMAX], int t, int t0, int t1, int rs, int ws,
                      const Stash<M>& sh, const float (&A)[M], const float (&Bc)[M],
                      const float (&C2)[M], const float (&cur)[M], float (&inout)[M]) {
-    if (!g.colv) return;
     float L[M];
-    fwd_update<M, ORDER>(P, g, X.tiles + rs * X.tile, A, Bc, C2, cur, inout, L);
+    fwd_update<M, ORDER>(P, g, X, rs, true, A, Bc, C2, cur, inout, L);
+    if (!g.colv) return;
     if (tp.ns) apply_sources<M>(P, tp, inout, xv, t + 1 < t1 ? t + 1 : -1);
     if (t + 1 < t1) publish<M>(P, g, X, ws, inout, true);
 #pragma unroll
     for (int i = 0; i < M; ++i) *sh.at(t - t0, i) = L[i];
 }
 
+// Adjoint of one cell (wavetorch/cell.py:36-42 with autograd's accumulation):
+// dL/dc += (X1 * (Kc * Lap(h_{t-1}))) * lam; pending grad_y1 / grad_y2 terms.
+WT_DEV void adj_cell(float lg, float lam, float Ly, float X1, float Kc, float Ky2, float dt2,
+                     float& acc, float& gy1, float& gy2a, float& gy2b) {
+    acc = fadd(acc, fmul(fmul(X1, fmul(Kc, Ly)), lam));
+    gy1 = fadd(fmul(dt2, lg), fmul(fmul(2.0f, lam), X1));
+    gy2b = gy2a;
+    gy2a = fmul(Ky2, lam);
+}
+
 template <int M, int ORDER>
-__global__ void __launch_bounds__(512, 1) seq_bwd_fused_kernel(FusedParams P) {
+__global__ void __launch_bounds__(max_threads<M>(), 1) seq_bwd_fused_kernel(FusedParams P) {
     extern __shared__ __align__(16) float smem[];
     __shared__ __align__(8) uint64_t mbar[3];
     __shared__ int abort_flag;
@@ -534,7 +562,7 @@ __global__ void __launch_bounds__(512, 1) seq_bwd_fused_kernel(FusedParams P) {
                 }
             }
             publish<M>(P, g, X, xs, ya, true);
-            if (!(ok = exchange_end(P, X, xs, true))) break;
+            if (!(ok = exchange_end(X))) break;
             int rs = xs;
             xs = next3(xs);
             float A[M], Bc[M], C2[M];
@@ -546,19 +574,19 @@ __global__ void __launch_bounds__(512, 1) seq_bwd_fused_kernel(FusedParams P) {
             for (int t = t0; t < t1;) {
                 rec_step<M, ORDER>(P, g, X, tp, xv, t, t0, t1, rs, xs, sh, A, Bc, C2, ya, yb);
                 if (++t >= t1) break;
-                if (!(ok = exchange_end(P, X, xs, true))) break;
+                if (!(ok = exchange_end(X))) break;
                 rs = xs;
                 xs = next3(xs);
                 rec_step<M, ORDER>(P, g, X, tp, xv, t, t0, t1, rs, xs, sh, A, Bc, C2, yb, ya);
                 if (++t >= t1) break;
-                if (!(ok = exchange_end(P, X, xs, true))) break;
+                if (!(ok = exchange_end(X))) break;
                 rs = xs;
                 xs = next3(xs);
             }
             if (!ok) break;
         }
-        // the stash of the last recompute step was written by this thread
-        // only, so no barrier is needed before the adjoint reads it back
+        // the last recompute step's stash entries were written by this thread
+        // itself, so the adjoint reads them back without a barrier
         // ---- adjoint sweep over the segment ----
         float X1[M], Kc[M], Kg[M], Ky2[M];
         load_bwd_coef<M>(P, g, X1, Kc, Kg, Ky2);
@@ -595,18 +623,20 @@ __global__ void __launch_bounds__(512, 1) seq_bwd_fused_kernel(FusedParams P) {
                             P.grad_x[(size_t)g.inst * P.steps + t] = pick<M>(lam, tp.s(e) & 15);
                 }
             }
-            if (!(ok = exchange_end(P, X, xs, true))) break;
+            if (!(ok = exchange_end(X))) break;
             if (g.colv) {
-                float lg[M];
-                strip_lap<M, ORDER>(P, g, smem + xs * tile, c2g, lg);
+                Column<M> c;
+                load_sides<M>(c, P, g, X.tiles + xs * X.tile);
 #pragma unroll
-                for (int i = 0; i < M; ++i) {
-                    float Ly = *sh.at(t - t0, i);
-                    acc[i] = fadd(acc[i], fmul(fmul(X1[i], fmul(Kc[i], Ly)), lam[i]));
-                    gy1[i] = fadd(fmul(P.k.dt2, lg[i]), fmul(fmul(2.0f, lam[i]), X1[i]));
-                    gy2b[i] = gy2a[i];
-                    gy2a[i] = fmul(Ky2[i], lam[i]);
-                }
+                for (int i = 1; i < M - 1; ++i)
+                    adj_cell(lap_cell<M, ORDER>(P, c, c2g, i), lam[i], *sh.at(t - t0, i), X1[i],
+                             Kc[i], Ky2[i], P.k.dt2, acc[i], gy1[i], gy2a[i], gy2b[i]);
+                xchg_wait(P, X, xs);
+                adj_cell(lap_cell<M, ORDER>(P, c, c2g, 0), lam[0], *sh.at(t - t0, 0), X1[0], Kc[0],
+                         Ky2[0], P.k.dt2, acc[0], gy1[0], gy2a[0], gy2b[0]);
+                adj_cell(lap_cell<M, ORDER>(P, c, c2g, M - 1), lam[M - 1], *sh.at(t - t0, M - 1),
+                         X1[M - 1], Kc[M - 1], Ky2[M - 1], P.k.dt2, acc[M - 1], gy1[M - 1],
+                         gy2a[M - 1], gy2b[M - 1]);
             }
             xs = next3(xs);
         }
@@ -626,9 +656,14 @@ __global__ void __launch_bounds__(512, 1) seq_bwd_fused_kernel(FusedParams P) {
 
 // ---------------------------------------------------------------------------
 // Host side: configuration and launch
-static int tile_ld(int rows) {
+// Column stride of a tile: room for OFF + rows + 1 floats, and conflict-free
+// column accesses of the width the M-cell strips use (float4: LD/4 odd;
+// float2: LD/2 odd; scalar: LD odd).
+static int tile_ld(int rows, int M) {
     int ld = rows + wt::OFF + 1;
-    while (ld % 8 != 4) ++ld;
+    if (M % 4 == 0) { while (ld % 8 != 4) ++ld; }
+    else if (M % 2 == 0) { while (ld % 4 != 2) ++ld; }
+    else { while (ld % 2 != 1) ++ld; }
     return ld;
 }
 
@@ -638,22 +673,33 @@ static int tile_ld(int rows) {
 // sqrt(T) interval with the stash in global memory.  Returns 0 on success.
 int wt_fused_plan(int nx, int ny, int steps, int cluster_req, int seg_req, WtFusedLaunch* L) {
     const int NCP = ((ny + 31) / 32) * 32;
-    const int Ms[2] = {8, 4};
+    const int Ms[3] = {10, 8, 4};
     const int Cs[5] = {4, 2, 8, 1, 16};
     const size_t SMEM_MAX = 227 * 1024 - 64;   // dynamic smem per CTA (static: 28 B)
     for (int ci = 0; ci < 5; ++ci) {
         int C = Cs[ci];
         if (cluster_req > 0 && C != cluster_req) continue;
         if (C > 8) continue;
-        for (int mi = 0; mi < 2; ++mi) {
+        // the M with the fewest padding rows (ties: the larger M)
+        int best = -1, best_pad = 1 << 30;
+        for (int mi = 0; mi < 3; ++mi) {
             int M = Ms[mi];
             int rows = (nx + C - 1) / C;
             int R = ((rows + M - 1) / M) * M;
             if ((C - 1) * R >= nx) continue;   // an empty CTA
+            int threads = (R / M) * NCP;
+            if (threads > (M >= 10 ? 384 : 512)) continue;
+            int pad = C * R - nx;
+            if (pad < best_pad) { best_pad = pad; best = M; }
+        }
+        if (best < 0) continue;
+        {
+            int M = best;
+            int rows = (nx + C - 1) / C;
+            int R = ((rows + M - 1) / M) * M;
             int S = R / M;
             int threads = S * NCP;
-            if (threads > 512) continue;
-            int LD = tile_ld(R);
+            int LD = tile_ld(R, M);
             size_t tiles = 3 * (size_t)(ny + 2) * LD * sizeof(float);
             if (tiles > SMEM_MAX) continue;
             L->C = C; L->M = M; L->R = R; L->S = S; L->NCP = NCP; L->LD = LD;
@@ -698,9 +744,11 @@ static int launch_fused(bool fwd, const wt::FusedParams& P, const WtFusedLaunch&
 
 int wt_launch_fused(bool fwd, const wt::FusedParams& P, const WtFusedLaunch& L, cudaStream_t st) {
     if (P.k.lap_order == WT_LAP_SEQ) {
+        if (L.M == 10) return launch_fused<10, WT_LAP_SEQ>(fwd, P, L, st);
         if (L.M == 8) return launch_fused<8, WT_LAP_SEQ>(fwd, P, L, st);
         if (L.M == 4) return launch_fused<4, WT_LAP_SEQ>(fwd, P, L, st);
     } else {
+        if (L.M == 10) return launch_fused<10, WT_LAP_PAIRED>(fwd, P, L, st);
         if (L.M == 8) return launch_fused<8, WT_LAP_PAIRED>(fwd, P, L, st);
         if (L.M == 4) return launch_fused<4, WT_LAP_PAIRED>(fwd, P, L, st);
     }
