@@ -150,15 +150,17 @@ WT_DEV void mbar_arrive_expect_tx(uint32_t addr, uint32_t bytes) {
                  "r"(bytes)
                  : "memory");
 }
-// Non-blocking probe of phase completion (acquire at cluster scope, so data
-// delivered by remote st.async before the phase completed is visible).
-WT_DEV bool mbar_try_wait_parity(uint32_t addr, uint32_t parity) {
+// Probe of phase completion (acquire at cluster scope, so data delivered by
+// remote st.async before the phase completed is visible).  The thread may be
+// suspended up to `hint_ns` (woken early when the phase completes), so a
+// waiting warp does not spin on the issue slots.
+WT_DEV bool mbar_try_wait_parity(uint32_t addr, uint32_t parity, uint32_t hint_ns) {
     uint32_t ok;
     asm volatile("{\n\t.reg .pred p;\n\t"
-                 "mbarrier.try_wait.parity.acquire.cluster.shared::cta.b64 p, [%1], %2;\n\t"
+                 "mbarrier.try_wait.parity.acquire.cluster.shared::cta.b64 p, [%1], %2, %3;\n\t"
                  "selp.u32 %0, 1, 0, p;\n\t}"
                  : "=r"(ok)
-                 : "r"(addr), "r"(parity)
+                 : "r"(addr), "r"(parity), "r"(hint_ns)
                  : "memory");
     return ok != 0;
 }

@@ -46,6 +46,7 @@ constexpr int OFF = 4;       // first own row in a tile column (16-byte aligned)
 constexpr int SRCMAX = 4;    // source entries one thread may own
 constexpr int PRBMAX = 4;    // probe entries one thread may own
 constexpr uint64_t WAIT_LIMIT_NS = 2000000000ull;   // bounded mbarrier waits (2 s)
+constexpr uint32_t WAIT_HINT_NS = 1000000u;         // suspend a waiting thread up to 1 ms per probe
 
 // load M consecutive floats from a 16-byte aligned (M%4==0) shared address
 template <int M>
@@ -169,9 +170,9 @@ WT_DEV void xchg_wait(const FusedParams& P, Xchg& X, int s) {
     if (!X.waiter) return;
     const uint32_t parity = (X.par >> s) & 1u;
     const uint32_t a = X.mbar + 8u * s;
-    if (!mbar_try_wait_parity(a, parity)) {
+    if (!mbar_try_wait_parity(a, parity, WAIT_HINT_NS)) {
         const uint64_t t0 = global_ns();
-        while (!mbar_try_wait_parity(a, parity)) {
+        while (!mbar_try_wait_parity(a, parity, WAIT_HINT_NS)) {
             if (global_ns() - t0 > WAIT_LIMIT_NS) {
                 atomicExch(P.err, WT_DEVERR_TIMEOUT);
                 *(volatile int*)X.abort = 1;
@@ -464,11 +465,14 @@ __global__ void __launch_bounds__(max_threads<M>(), 1) seq_fwd_fused_kernel(Fuse
 
 // ============================================================================
 // Adjoint with segment recompute.
+// Per-thread stash: step s of the segment holds the thread's M values
+// contiguously at p + s*NT*M (vector stores/loads; the per-lane stride of M
+// floats keeps float2/float4 accesses conflict-free for M = 10 / 8 / 4).
 template <int M>
 struct Stash {
-    float* p;       // this thread's element 0; cell i of step s at p[(s*M + i)*NT]
+    float* p;       // this thread's step-0 entry
     int NT;
-    WT_DEV float* at(int s, int i) const { return p + (size_t)(s * M + i) * NT; }
+    WT_DEV float* step(int s) const { return p + (size_t)s * NT * M; }
 };
 
 // Recompute step: like fwd_step, but stashes Lap(h_{t-1}) instead of writing outputs.
@@ -482,8 +486,7 @@ WT_DEV void rec_step(const FusedParams& P, const Geo& g, Xchg& X, const Taps& tp
     if (!g.colv) return;
     if (tp.ns) apply_sources<M>(P, tp, inout, xv, t + 1 < t1 ? t + 1 : -1);
     if (t + 1 < t1) publish<M>(P, g, X, ws, inout, true);
-#pragma unroll
-    for (int i = 0; i < M; ++i) *sh.at(t - t0, i) = L[i];
+    sts_col<M>(sh.step(t - t0), L);
 }
 
 // Adjoint of one cell (wavetorch/cell.py:36-42 with autograd's accumulation):
@@ -514,8 +517,9 @@ __global__ void __launch_bounds__(max_threads<M>(), 1) seq_bwd_fused_kernel(Fuse
     const size_t bplane = (size_t)P.batch * plane;
     Stash<M> sh;
     sh.NT = NT;
-    sh.p = P.stash_smem ? smem + 3 * tile + threadIdx.x
-                        : P.stash + ((size_t)(g.inst * P.C + g.cta) * P.seg) * M * NT + threadIdx.x;
+    sh.p = P.stash_smem ? smem + 3 * tile + (size_t)threadIdx.x * M
+                        : P.stash + ((size_t)(g.inst * P.C + g.cta) * P.seg) * M * NT +
+                              (size_t)threadIdx.x * M;
 
     // adjoint state: gy1 pending from t+1, gy2 pending from t+1 (a) and t+2 (b).
     // Zero-initialised, so the first arrivals reproduce autograd's "first
@@ -627,16 +631,18 @@ __global__ void __launch_bounds__(max_threads<M>(), 1) seq_bwd_fused_kernel(Fuse
             if (g.colv) {
                 Column<M> c;
                 load_sides<M>(c, P, g, X.tiles + xs * X.tile);
+                float Ly[M];
+                lds_col<M>(Ly, sh.step(t - t0));
 #pragma unroll
                 for (int i = 1; i < M - 1; ++i)
-                    adj_cell(lap_cell<M, ORDER>(P, c, c2g, i), lam[i], *sh.at(t - t0, i), X1[i],
-                             Kc[i], Ky2[i], P.k.dt2, acc[i], gy1[i], gy2a[i], gy2b[i]);
+                    adj_cell(lap_cell<M, ORDER>(P, c, c2g, i), lam[i], Ly[i], X1[i], Kc[i], Ky2[i],
+                             P.k.dt2, acc[i], gy1[i], gy2a[i], gy2b[i]);
                 xchg_wait(P, X, xs);
-                adj_cell(lap_cell<M, ORDER>(P, c, c2g, 0), lam[0], *sh.at(t - t0, 0), X1[0], Kc[0],
-                         Ky2[0], P.k.dt2, acc[0], gy1[0], gy2a[0], gy2b[0]);
-                adj_cell(lap_cell<M, ORDER>(P, c, c2g, M - 1), lam[M - 1], *sh.at(t - t0, M - 1),
-                         X1[M - 1], Kc[M - 1], Ky2[M - 1], P.k.dt2, acc[M - 1], gy1[M - 1],
-                         gy2a[M - 1], gy2b[M - 1]);
+                adj_cell(lap_cell<M, ORDER>(P, c, c2g, 0), lam[0], Ly[0], X1[0], Kc[0], Ky2[0],
+                         P.k.dt2, acc[0], gy1[0], gy2a[0], gy2b[0]);
+                adj_cell(lap_cell<M, ORDER>(P, c, c2g, M - 1), lam[M - 1], Ly[M - 1], X1[M - 1],
+                         Kc[M - 1], Ky2[M - 1], P.k.dt2, acc[M - 1], gy1[M - 1], gy2a[M - 1],
+                         gy2b[M - 1]);
             }
             xs = next3(xs);
         }
