@@ -147,22 +147,30 @@ WT_DEV void xchg_setup(Xchg& X, const FusedParams& P, const Geo& g, float* tiles
     if (threadIdx.x == 0) *abort = 0;
 }
 
-// Publish the thread's M new values into slot `s`: the neighbours' halo rows
-// first (st.async, for the CTA's first/last row), then the own tile column.
+// Push the CTA's first / last row values (this thread's cell 0 / M-1 when it
+// owns them) into the neighbours' halo rows of slot `s` (st.async).
+WT_DEV void send_halo(const FusedParams& P, const Geo& g, const Xchg& X, int s, float first,
+                      float last) {
+    const int colo = (g.col + 1) * P.LD + OFF;
+    if (g.strip == 0 && g.has_up)         // my row 0 -> up neighbour's halo row R
+        st_async_f32(X.up_tile + 4u * (uint32_t)(s * X.tile + colo + P.R), first,
+                     X.up_mbar + 8u * s);
+    if (g.strip == g.S - 1 && g.has_dn)   // my row R-1 -> down neighbour's halo row -1
+        st_async_f32(X.dn_tile + 4u * (uint32_t)(s * X.tile + colo - 1), last,
+                     X.dn_mbar + 8u * s);
+}
+template <int M>
+WT_DEV void store_column(const FusedParams& P, const Geo& g, const Xchg& X, int s,
+                         const float (&v)[M]) {
+    sts_col<M>(X.tiles + s * X.tile + (g.col + 1) * P.LD + OFF + g.xl0, v);
+}
+// Publish the thread's M new values into slot `s`: halo rows, then own column.
 template <int M>
 WT_DEV void publish(const FusedParams& P, const Geo& g, const Xchg& X, int s, const float (&v)[M],
                     bool remote) {
     if (!g.colv) return;
-    const int colo = (g.col + 1) * P.LD + OFF;
-    if (remote) {
-        if (g.strip == 0 && g.has_up)      // my row 0 -> up neighbour's halo row R
-            st_async_f32(X.up_tile + 4u * (uint32_t)(s * X.tile + colo + P.R), v[0],
-                         X.up_mbar + 8u * s);
-        if (g.strip == g.S - 1 && g.has_dn)   // my row R-1 -> down neighbour's halo row -1
-            st_async_f32(X.dn_tile + 4u * (uint32_t)(s * X.tile + colo - 1), v[M - 1],
-                         X.dn_mbar + 8u * s);
-    }
-    sts_col<M>(X.tiles + s * X.tile + colo + g.xl0, v);
+    if (remote) send_halo(P, g, X, s, v[0], v[M - 1]);
+    store_column<M>(P, g, X, s, v);
 }
 
 // Wait until slot s holds the neighbours' halo rows, then re-arm its barrier.
@@ -302,31 +310,6 @@ WT_DEV void load_bwd_coef(const FusedParams& P, const Geo& g, float (&X1)[M], fl
 
 WT_DEV int next3(int s) { return s == 2 ? 0 : s + 1; }
 
-// h_t for the thread's cells from cur = h_{t-1} (registers + tile slot rs) and
-// inout = h_{t-2}; the result overwrites inout (ping-pong register sets).
-// Cells that need no halo row are updated first; then the warps that read a
-// halo wait for it (when `halo` says the slot carries remote rows), so the
-// DSMEM latency overlaps the interior work.  L receives Lap(h_{t-1}).
-template <int M, int ORDER>
-WT_DEV void fwd_update(const FusedParams& P, const Geo& g, Xchg& X, int rs, bool halo,
-                       const float (&A)[M], const float (&Bc)[M], const float (&C2)[M],
-                       const float (&cur)[M], float (&inout)[M], float (&L)[M]) {
-    if (!g.colv) return;   // padding columns read nothing (their tile columns do not exist)
-    Column<M> c;
-    load_sides<M>(c, P, g, X.tiles + rs * X.tile);
-#pragma unroll
-    for (int i = 1; i < M - 1; ++i) {
-        L[i] = lap_cell<M, ORDER>(P, c, cur, i);
-        inout[i] = leapfrog(A[i], Bc[i], C2[i], P.k.two_over, cur[i], inout[i], L[i]);
-    }
-    if (halo) xchg_wait(P, X, rs);
-    L[0] = lap_cell<M, ORDER>(P, c, cur, 0);
-    inout[0] = leapfrog(A[0], Bc[0], C2[0], P.k.two_over, cur[0], inout[0], L[0]);
-    L[M - 1] = lap_cell<M, ORDER>(P, c, cur, M - 1);
-    inout[M - 1] = leapfrog(A[M - 1], Bc[M - 1], C2[M - 1], P.k.two_over, cur[M - 1],
-                            inout[M - 1], L[M - 1]);
-}
-
 // Sources (in table order) with the inputs prefetched one step ahead.
 template <int M>
 WT_DEV void apply_sources(const FusedParams& P, const Taps& tp, float (&y)[M], float (&xv)[SRCMAX],
@@ -339,6 +322,41 @@ WT_DEV void apply_sources(const FusedParams& P, const Taps& tp, float (&y)[M], f
         for (int e = 0; e < SRCMAX; ++e)
             if (e < tp.ns) xv[e] = __ldg(P.x + (size_t)(tp.s(e) >> 4) * P.steps + tnext);
     }
+}
+
+// h_t for the thread's cells from cur = h_{t-1} (registers + tile slot rs) and
+// inout = h_{t-2}; the result overwrites inout (ping-pong register sets).
+// The warps that read a halo row wait for it first (`halo`: slot rs carries
+// remote rows); then the strip's end cells are updated and, when `send`,
+// pushed straight to the neighbours (slot ws) before the interior cells are
+// computed, so the halo is in flight for a whole step before it is needed.
+// L receives Lap(h_{t-1}).  A thread that owns a source cell injects before
+// it sends (sources are few; that thread takes the plain order).
+template <int M, int ORDER>
+WT_DEV void fwd_update(const FusedParams& P, const Geo& g, Xchg& X, const Taps& tp, int rs,
+                       bool halo, int ws, bool send, float (&xv)[SRCMAX], int tnext,
+                       const float (&A)[M], const float (&Bc)[M], const float (&C2)[M],
+                       const float (&cur)[M], float (&inout)[M], float (&L)[M]) {
+    if (!g.colv) return;   // padding columns read nothing (their tile columns do not exist)
+    if (halo) xchg_wait(P, X, rs);
+    Column<M> c;
+    load_sides<M>(c, P, g, X.tiles + rs * X.tile);
+    L[0] = lap_cell<M, ORDER>(P, c, cur, 0);
+    inout[0] = leapfrog(A[0], Bc[0], C2[0], P.k.two_over, cur[0], inout[0], L[0]);
+    L[M - 1] = lap_cell<M, ORDER>(P, c, cur, M - 1);
+    inout[M - 1] = leapfrog(A[M - 1], Bc[M - 1], C2[M - 1], P.k.two_over, cur[M - 1],
+                            inout[M - 1], L[M - 1]);
+    if (send && !tp.ns) send_halo(P, g, X, ws, inout[0], inout[M - 1]);
+#pragma unroll
+    for (int i = 1; i < M - 1; ++i) {
+        L[i] = lap_cell<M, ORDER>(P, c, cur, i);
+        inout[i] = leapfrog(A[i], Bc[i], C2[i], P.k.two_over, cur[i], inout[i], L[i]);
+    }
+    if (tp.ns) {
+        apply_sources<M>(P, tp, inout, xv, tnext);
+        if (send) send_halo(P, g, X, ws, inout[0], inout[M - 1]);
+    }
+    store_column<M>(P, g, X, ws, inout);
 }
 
 struct FwdState {
@@ -372,11 +390,11 @@ WT_DEV void fwd_step(const FusedParams& P, const Geo& g, Xchg& X, const Taps& tp
     }
     --st.ck;
     float L[M];
-    // h_{t-1} came with remote halo rows for every t >= 1 (h_{-1} = 0 is local)
-    fwd_update<M, ORDER>(P, g, X, rs, t >= 1, A, Bc, C2, cur, inout, L);
+    // h_{t-1} came with remote halo rows for every t >= 1 (h_{-1} = 0 is local);
+    // the last step's halos have no reader
+    fwd_update<M, ORDER>(P, g, X, tp, rs, t >= 1, ws, t + 1 < P.steps, st.xv, t + 1, A, Bc, C2,
+                         cur, inout, L);
     if (!g.colv) return;
-    if (tp.ns) apply_sources<M>(P, tp, inout, st.xv, t + 1);
-    publish<M>(P, g, X, ws, inout, t + 1 < P.steps);
     if (tp.np) {
 #pragma unroll
         for (int e = 0; e < PRBMAX; ++e) {
@@ -482,10 +500,9 @@ WT_DEV void rec_step(const FusedParams& P, const Geo& g, Xchg& X, const Taps& tp
                      const Stash<M>& sh, const float (&A)[M], const float (&Bc)[M],
                      const float (&C2)[M], const float (&cur)[M], float (&inout)[M]) {
     float L[M];
-    fwd_update<M, ORDER>(P, g, X, rs, true, A, Bc, C2, cur, inout, L);
+    fwd_update<M, ORDER>(P, g, X, tp, rs, true, ws, t + 1 < t1, xv, t + 1 < t1 ? t + 1 : -1, A,
+                         Bc, C2, cur, inout, L);
     if (!g.colv) return;
-    if (tp.ns) apply_sources<M>(P, tp, inout, xv, t + 1 < t1 ? t + 1 : -1);
-    if (t + 1 < t1) publish<M>(P, g, X, ws, inout, true);
     sts_col<M>(sh.step(t - t0), L);
 }
 
