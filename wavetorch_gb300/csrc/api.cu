@@ -153,7 +153,7 @@ int make_plan(const wt_seq_desc* d, SeqPlan* p) {
         P.o_lam = o; o = up(o + 3 * bp * F);
         P.o_gc = o; o = up(o + bp * F);
     } else {
-        int st = wt_fused_plan(P.nx, P.ny, P.T, d->cluster, d->segment, &P.L);
+        int st = wt_fused_plan(P.nx, P.ny, P.T, P.np, d->cluster, d->segment, &P.L);
         if (st) return st;
         const size_t per_step = (size_t)P.B * P.L.C * P.L.M * P.L.threads * F;
         P.seg = P.L.seg;
@@ -233,7 +233,7 @@ wt::FusedParams fused_params(const wt_scalars* s, const SeqPlan& P, const float*
     std::memset(&F, 0, sizeof(F));
     F.k = wt_make_scalars(s);
     F.batch = P.B; F.nx = P.nx; F.ny = P.ny; F.steps = P.T;
-    F.C = P.L.C; F.R = P.L.R; F.NCP = P.L.NCP; F.LD = P.L.LD; F.seg = P.seg;
+    F.C = P.L.C; F.R = P.L.R; F.NCP = P.L.NCP; F.LD = P.L.LD; F.seg = P.seg; F.PB = P.L.PB;
     F.b = b; F.c = c; F.x = x;
     F.n_src = P.ns;
     F.src_cell = at<int>(ws, P.o_srccell);
@@ -242,6 +242,7 @@ wt::FusedParams fused_params(const wt_scalars* s, const SeqPlan& P, const float*
     F.prb_cell = at<int>(ws, P.o_fcell);
     F.prb_kind = at<int>(ws, P.o_fkind);
     F.prb_col = at<int>(ws, P.o_fcol);
+    F.prb_kind_col = at<int>(ws, P.o_prbkind);
     F.amp = at<float>(ws, P.o_amp);
     F.ckpt = at<float>(ws, P.o_ckpt);
     F.stash = at<float>(ws, P.o_stash);
@@ -308,14 +309,15 @@ extern "C" int wt_seq_fwd(const wt_scalars* s, const wt_seq_desc* d, const float
                                              cudaMemcpyDeviceToDevice, cs);
             if (ce != cudaSuccess) return wt_cuda_status(ce);
         }
-        if (probe_sum) return WT_ERR_UNSUPPORTED;   // the fused form computes it
-        return WT_OK;
+    } else {
+        wt::FusedParams F = fused_params(s, P, b, c, x, workspace);
+        F.out = out;
+        F.fields = d->output_fields ? fields : nullptr;
+        if ((st = wt_launch_fused(true, F, P.L, cs))) return st;
     }
-    wt::FusedParams F = fused_params(s, P, b, c, x, workspace);
-    F.out = out;
-    F.fields = d->output_fields ? fields : nullptr;
-    F.probe_sum = probe_sum;
-    return wt_launch_fused(true, F, P.L, cs);
+    if (probe_sum && P.np > 0)
+        return wt_launch_probe_sum(P.B, P.T, P.np, out, probe_sum, cs);
+    return WT_OK;
 }
 
 extern "C" int wt_seq_bwd(const wt_scalars* s, const wt_seq_desc* d, const float* b,

@@ -44,6 +44,7 @@ struct FusedParams {
     int NCP;        // threads per strip row (ny rounded up to 32)
     int LD;         // tile column stride (floats)
     int seg;        // checkpoint interval
+    int PB;         // probe chunk length (steps staged in shared memory per flush/load)
     const float* b;         // [nx,ny]
     const float* c;         // [nx,ny]
     const float* x;         // [batch][steps]
@@ -55,11 +56,11 @@ struct FusedParams {
     const int* prb_cell;
     const int* prb_kind;
     const int* prb_col;
+    const int* prb_kind_col;    // kind of output column q
     // forward outputs
     float* out;             // [batch][steps][n_prb]
     float* amp;             // [batch][steps][n_prb]
     float* fields;          // [batch][steps][nx][ny] or null
-    float* probe_sum;       // [batch][n_prb] or null
     float* ckpt;            // [nseg][2][batch][nx][ny]
     // adjoint
     const float* grad_out;  // [batch][steps][n_prb]
@@ -75,8 +76,9 @@ struct FusedParams {
 // Launch shape of the fused kernels for one grid size.
 struct WtFusedLaunch {
     int C, M, R, S, NCP, LD, threads;
-    size_t smem_fwd;        // tiles
-    size_t smem_bwd;        // tiles (+ the stash when stash_smem)
+    int PB;                 // probe chunk length
+    size_t smem_fwd;        // tiles + probe ring buffers
+    size_t smem_bwd;        // tiles + seed ring buffers (+ the stash when stash_smem)
     int seg;                // checkpoint interval
     int stash_smem;
 };
@@ -96,5 +98,8 @@ int wt_launch_seq_adj_step(const StepScalars& k, int batch, int nx, int ny, cons
 int wt_launch_seq_adj_reduce(int batch, size_t plane, const float* gc, float* G, int first,
                              cudaStream_t st);
 int wt_launch_fill_zero(float* p, size_t n, cudaStream_t st);
-int wt_fused_plan(int nx, int ny, int steps, int cluster_req, int seg_req, WtFusedLaunch* L);
+int wt_fused_plan(int nx, int ny, int steps, int n_prb, int cluster_req, int seg_req,
+                  WtFusedLaunch* L);
+int wt_launch_probe_sum(int batch, int steps, int n_prb, const float* out, float* sum,
+                        cudaStream_t st);
 int wt_launch_fused(bool fwd, const wt::FusedParams& P, const WtFusedLaunch& L, cudaStream_t st);

@@ -361,15 +361,40 @@ WT_DEV void fwd_update(const FusedParams& P, const Geo& g, Xchg& X, const Taps& 
 
 struct FwdState {
     int ck;                   // steps until the next checkpoint boundary
+    int pc;                   // step index within the probe chunk
+    int pb;                   // probe ring buffer in use (0/1)
     float xv[SRCMAX];         // this step's source inputs
-    float psum[PRBMAX], pcmp[PRBMAX];
 };
+
+// Shared probe ring buffers of the forward: [2][n_prb][PB] raw amplitudes
+// plus an ownership flag per probe column.  A probe's owner thread stores one
+// value per step; every PB steps the whole CTA writes the finished chunk to
+// the outputs, so the per-step cost on the owner's warp is one shared store.
+struct ProbeRing {
+    float* buf;
+    int* own;
+};
+
+// Write chunk `b` (steps t0 .. t0+n-1) of the probes this CTA owns.
+WT_DEV void flush_probes(const FusedParams& P, const Geo& g, const ProbeRing& pr, int b, int t0,
+                         int n) {
+    const int tot = P.n_prb * P.PB;
+    for (int idx = threadIdx.x; idx < tot; idx += blockDim.x) {
+        const int q = idx / P.PB, tt = idx - q * P.PB;
+        if (tt >= n || !pr.own[q]) continue;
+        const float v = pr.buf[(b * P.n_prb + q) * P.PB + tt];
+        const size_t oi = ((size_t)g.inst * P.steps + t0 + tt) * P.n_prb + q;
+        P.out[oi] = (pr.own[q] == 2) ? fmul(v, v) : v;   // own: 1 amplitude, 2 intensity
+        P.amp[oi] = v;
+    }
+}
 
 // One step of the forward kernel (everything but the closing barrier).
 template <int M, int ORDER>
 WT_DEV void fwd_step(const FusedParams& P, const Geo& g, Xchg& X, const Taps& tp, FwdState& st,
-                     int t, int rs, int ws, const float (&A)[M], const float (&Bc)[M],
-                     const float (&C2)[M], const float (&cur)[M], float (&inout)[M]) {
+                     const ProbeRing& pr, int t, int rs, int ws, const float (&A)[M],
+                     const float (&Bc)[M], const float (&C2)[M], const float (&cur)[M],
+                     float (&inout)[M]) {
     const size_t plane = (size_t)P.nx * P.ny;
     const size_t bplane = (size_t)P.batch * plane;
     if (st.ck == 0) {
@@ -396,21 +421,10 @@ WT_DEV void fwd_step(const FusedParams& P, const Geo& g, Xchg& X, const Taps& tp
                          cur, inout, L);
     if (!g.colv) return;
     if (tp.np) {
+        float* row = pr.buf + (size_t)st.pb * P.n_prb * P.PB + st.pc;
 #pragma unroll
-        for (int e = 0; e < PRBMAX; ++e) {
-            if (e >= tp.np) continue;
-            const int pe = tp.p(e);
-            float v = pick<M>(inout, pe & 15);
-            float o = (pe & 16) ? fmul(v, v) : v;
-            size_t oi = ((size_t)g.inst * P.steps + t) * P.n_prb + (pe >> 5);
-            P.out[oi] = o;
-            P.amp[oi] = v;
-            // Kahan-compensated running time sum
-            float yk = fsub(o, st.pcmp[e]);
-            float tk = fadd(st.psum[e], yk);
-            st.pcmp[e] = fsub(fsub(tk, st.psum[e]), yk);
-            st.psum[e] = tk;
-        }
+        for (int e = 0; e < PRBMAX; ++e)
+            if (e < tp.np) row[(tp.p(e) >> 5) * P.PB] = pick<M>(inout, tp.p(e) & 15);
     }
     if (P.fields) {
         float* fo = P.fields + ((size_t)g.inst * P.steps + t) * plane;
@@ -423,9 +437,11 @@ WT_DEV void fwd_step(const FusedParams& P, const Geo& g, Xchg& X, const Taps& tp
 }
 
 // CTA barrier closing an exchange; false when the CTA must leave its loop.
-WT_DEV bool exchange_end(const Xchg& X) {
+// The abort word (set only after a 2 s wait gave up) is read every 32nd
+// barrier: all threads read it after the same barrier, so they agree.
+WT_DEV bool exchange_end(const Xchg& X, int k) {
     __syncthreads();
-    return *(volatile int*)X.abort == 0;
+    return (k & 31) != 0 || *(volatile int*)X.abort == 0;
 }
 
 template <int M>
@@ -440,7 +456,11 @@ __global__ void __launch_bounds__(max_threads<M>(), 1) seq_fwd_fused_kernel(Fuse
     __shared__ int abort_flag;
     const Geo g = make_geo(P, M);
     const int tile = (P.ny + 2) * P.LD;
+    ProbeRing pr;
+    pr.buf = smem + 3 * tile;
+    pr.own = reinterpret_cast<int*>(pr.buf + 2 * P.n_prb * P.PB);
     zero_smem(smem, 3 * tile);
+    for (int q = threadIdx.x; q < P.n_prb; q += blockDim.x) pr.own[q] = 0;
     Xchg X;
     xchg_setup(X, P, g, smem, tile, mbar, &abort_flag);
 
@@ -452,32 +472,37 @@ __global__ void __launch_bounds__(max_threads<M>(), 1) seq_fwd_fused_kernel(Fuse
     build_taps<M>(P, g, tp);
     FwdState st;
     st.ck = P.seg;
-#pragma unroll
-    for (int e = 0; e < PRBMAX; ++e) st.psum[e] = st.pcmp[e] = 0.f;
+    st.pc = 0;
+    st.pb = 0;
 #pragma unroll
     for (int e = 0; e < SRCMAX; ++e)
         st.xv[e] = e < tp.ns ? __ldg(P.x + (size_t)(tp.s(e) >> 4) * P.steps) : 0.f;
-    cluster_sync_all();   // zeroed tiles and initialised barriers, cluster-wide
+    __syncthreads();      // ownership flags cleared before the owners mark theirs
+    if (g.colv && tp.np) {
+#pragma unroll
+        for (int e = 0; e < PRBMAX; ++e)
+            if (e < tp.np) pr.own[tp.p(e) >> 5] = (tp.p(e) & 16) ? 2 : 1;
+    }
+    cluster_sync_all();   // zeroed tiles, flags and initialised barriers, cluster-wide
 
     // ya holds h_{t-1} at even t, yb at odd t (the update overwrites h_{t-2})
     int rs = 0;           // slot holding h_{t-1} (h_{-1} = 0 is slot 0)
+    int chunk0 = 0;       // first step of the probe chunk being filled
     for (int t = 0; t < P.steps;) {
         int ws = next3(rs);
-        fwd_step<M, ORDER>(P, g, X, tp, st, t, rs, ws, A, Bc, C2, ya, yb);
-        if (!exchange_end(X)) break;
+        fwd_step<M, ORDER>(P, g, X, tp, st, pr, t, rs, ws, A, Bc, C2, ya, yb);
+        if (!exchange_end(X, t)) break;
         rs = ws;
+        if (++st.pc == P.PB) { flush_probes(P, g, pr, st.pb, chunk0, P.PB); st.pc = 0; st.pb ^= 1; chunk0 = t + 1; }
         if (++t >= P.steps) break;
         ws = next3(rs);
-        fwd_step<M, ORDER>(P, g, X, tp, st, t, rs, ws, A, Bc, C2, yb, ya);
-        if (!exchange_end(X)) break;
+        fwd_step<M, ORDER>(P, g, X, tp, st, pr, t, rs, ws, A, Bc, C2, yb, ya);
+        if (!exchange_end(X, t)) break;
         rs = ws;
+        if (++st.pc == P.PB) { flush_probes(P, g, pr, st.pb, chunk0, P.PB); st.pc = 0; st.pb ^= 1; chunk0 = t + 1; }
         ++t;
     }
-    if (P.probe_sum && g.colv && tp.np) {
-#pragma unroll
-        for (int e = 0; e < PRBMAX; ++e)
-            if (e < tp.np) P.probe_sum[(size_t)g.inst * P.n_prb + (tp.p(e) >> 5)] = st.psum[e];
-    }
+    if (st.pc > 0) flush_probes(P, g, pr, st.pb, chunk0, st.pc);
     cluster_sync_all();
 }
 
@@ -506,6 +531,25 @@ WT_DEV void rec_step(const FusedParams& P, const Geo& g, Xchg& X, const Taps& tp
     sts_col<M>(sh.step(t - t0), L);
 }
 
+// Stage the adjoint seeds of chunk c (adjoint steps u = c*PB .. c*PB+PB-1,
+// i.e. t = T-1-u) of every probe column into ring buffer c & 1:
+// intensity g * (2 y) (autograd's PowBackward), amplitude g.
+WT_DEV void stage_seeds(const FusedParams& P, const Geo& g, float* seeds, int c) {
+    float* dst = seeds + (size_t)(c & 1) * P.n_prb * P.PB;
+    const int tot = P.n_prb * P.PB;
+    for (int idx = threadIdx.x; idx < tot; idx += blockDim.x) {
+        const int q = idx / P.PB, k = idx - q * P.PB;
+        const int t = P.steps - 1 - (c * P.PB + k);
+        float sd = 0.f;
+        if (t >= 0) {
+            const size_t oi = ((size_t)g.inst * P.steps + t) * P.n_prb + q;
+            const float gv = __ldg(P.grad_out + oi);
+            sd = __ldg(P.prb_kind_col + q) ? fmul(gv, fmul(2.0f, __ldg(P.amp + oi))) : gv;
+        }
+        dst[q * P.PB + k] = sd;
+    }
+}
+
 // Adjoint of one cell (wavetorch/cell.py:36-42 with autograd's accumulation):
 // dL/dc += (X1 * (Kc * Lap(h_{t-1}))) * lam; pending grad_y1 / grad_y2 terms.
 WT_DEV void adj_cell(float lg, float lam, float Ly, float X1, float Kc, float Ky2, float dt2,
@@ -532,9 +576,12 @@ __global__ void __launch_bounds__(max_threads<M>(), 1) seq_bwd_fused_kernel(Fuse
 
     const size_t plane = (size_t)P.nx * P.ny;
     const size_t bplane = (size_t)P.batch * plane;
+    // adjoint seeds of all probe columns, staged per chunk of PB adjoint
+    // steps: seeds[2][n_prb][PB], u = T-1-t counts adjoint steps
+    float* seeds = smem + 3 * tile;
     Stash<M> sh;
     sh.NT = NT;
-    sh.p = P.stash_smem ? smem + 3 * tile + (size_t)threadIdx.x * M
+    sh.p = P.stash_smem ? seeds + ((2 * P.n_prb * P.PB + 3) & ~3) + (size_t)threadIdx.x * M
                         : P.stash + ((size_t)(g.inst * P.C + g.cta) * P.seg) * M * NT +
                               (size_t)threadIdx.x * M;
 
@@ -544,19 +591,8 @@ __global__ void __launch_bounds__(max_threads<M>(), 1) seq_bwd_fused_kernel(Fuse
     float gy1[M], gy2a[M], gy2b[M], acc[M];
 #pragma unroll
     for (int i = 0; i < M; ++i) gy1[i] = gy2a[i] = gy2b[i] = acc[i] = 0.f;
-    // probe seeds prefetched one step ahead: grad_out and amplitude
-    float sg[PRBMAX], sa[PRBMAX];
-#pragma unroll
-    for (int e = 0; e < PRBMAX; ++e) sg[e] = sa[e] = 0.f;
-    if (tp.np && g.colv) {
-#pragma unroll
-        for (int e = 0; e < PRBMAX; ++e)
-            if (e < tp.np) {
-                size_t oi = ((size_t)g.inst * P.steps + (P.steps - 1)) * P.n_prb + (tp.p(e) >> 5);
-                sg[e] = __ldg(P.grad_out + oi);
-                sa[e] = __ldg(P.amp + oi);
-            }
-    }
+    stage_seeds(P, g, seeds, 0);
+    int u = 0;            // adjoint steps done
 
     cluster_sync_all();
     const int nseg = (P.steps + P.seg - 1) / P.seg;
@@ -583,7 +619,7 @@ __global__ void __launch_bounds__(max_threads<M>(), 1) seq_bwd_fused_kernel(Fuse
                 }
             }
             publish<M>(P, g, X, xs, ya, true);
-            if (!(ok = exchange_end(X))) break;
+            if (!(ok = exchange_end(X, 0))) break;
             int rs = xs;
             xs = next3(xs);
             float A[M], Bc[M], C2[M];
@@ -595,12 +631,12 @@ __global__ void __launch_bounds__(max_threads<M>(), 1) seq_bwd_fused_kernel(Fuse
             for (int t = t0; t < t1;) {
                 rec_step<M, ORDER>(P, g, X, tp, xv, t, t0, t1, rs, xs, sh, A, Bc, C2, ya, yb);
                 if (++t >= t1) break;
-                if (!(ok = exchange_end(X))) break;
+                if (!(ok = exchange_end(X, t))) break;
                 rs = xs;
                 xs = next3(xs);
                 rec_step<M, ORDER>(P, g, X, tp, xv, t, t0, t1, rs, xs, sh, A, Bc, C2, yb, ya);
                 if (++t >= t1) break;
-                if (!(ok = exchange_end(X))) break;
+                if (!(ok = exchange_end(X, t))) break;
                 rs = xs;
                 xs = next3(xs);
             }
@@ -618,21 +654,15 @@ __global__ void __launch_bounds__(max_threads<M>(), 1) seq_bwd_fused_kernel(Fuse
                 lam[i] = fadd(gy2b[i], gy1[i]);
                 c2g[i] = 0.f;
             }
+            if (u % P.PB == 0 && u + P.PB < P.steps)   // next chunk, a barrier ahead of use
+                stage_seeds(P, g, seeds, u / P.PB + 1);
             if (g.colv) {
                 if (tp.np) {
                     // probe seeds, descending reference order (list order)
+                    const float* sr = seeds + (size_t)((u / P.PB) & 1) * P.n_prb * P.PB + u % P.PB;
 #pragma unroll
-                    for (int e = 0; e < PRBMAX; ++e) {
-                        if (e >= tp.np) continue;
-                        const int pe = tp.p(e);
-                        float sd = (pe & 16) ? fmul(sg[e], fmul(2.0f, sa[e])) : sg[e];
-                        add_at<M>(lam, pe & 15, sd);
-                        if (t > 0) {
-                            size_t oi = ((size_t)g.inst * P.steps + (t - 1)) * P.n_prb + (pe >> 5);
-                            sg[e] = __ldg(P.grad_out + oi);
-                            sa[e] = __ldg(P.amp + oi);
-                        }
-                    }
+                    for (int e = 0; e < PRBMAX; ++e)
+                        if (e < tp.np) add_at<M>(lam, tp.p(e) & 15, sr[(tp.p(e) >> 5) * P.PB]);
                 }
 #pragma unroll
                 for (int i = 0; i < M; ++i) c2g[i] = fmul(Kg[i], lam[i]);
@@ -644,7 +674,8 @@ __global__ void __launch_bounds__(max_threads<M>(), 1) seq_bwd_fused_kernel(Fuse
                             P.grad_x[(size_t)g.inst * P.steps + t] = pick<M>(lam, tp.s(e) & 15);
                 }
             }
-            if (!(ok = exchange_end(X))) break;
+            if (!(ok = exchange_end(X, u))) break;
+            ++u;
             if (g.colv) {
                 Column<M> c;
                 load_sides<M>(c, P, g, X.tiles + xs * X.tile);
@@ -691,14 +722,20 @@ static int tile_ld(int rows, int M) {
 }
 
 // Pick (C, M) for a grid: clusters of C CTAs, M cells per thread, at most
-// 512 threads per CTA; then the checkpoint interval: the largest stash that
-// fits in shared memory next to the three tiles (at least 4 steps), else a
-// sqrt(T) interval with the stash in global memory.  Returns 0 on success.
-int wt_fused_plan(int nx, int ny, int steps, int cluster_req, int seg_req, WtFusedLaunch* L) {
+// 512 threads per CTA (384 for 10-cell strips); then the checkpoint
+// interval: the largest stash that fits in shared memory next to the three
+// tiles and the probe ring buffers (at least 4 steps), else a sqrt(T)
+// interval with the stash in global memory.  Returns 0 on success.
+int wt_fused_plan(int nx, int ny, int steps, int n_prb, int cluster_req, int seg_req,
+                  WtFusedLaunch* L) {
     const int NCP = ((ny + 31) / 32) * 32;
     const int Ms[3] = {10, 8, 4};
     const int Cs[5] = {4, 2, 8, 1, 16};
     const size_t SMEM_MAX = 227 * 1024 - 64;   // dynamic smem per CTA (static: 28 B)
+    const int PB = n_prb > 0 ? std::max(1, std::min(32, 2048 / n_prb)) : 32;
+    auto r16 = [](size_t v) { return (v + 15) / 16 * 16; };
+    const size_t aux_fwd = r16((size_t)(2 * n_prb * PB + n_prb) * 4);
+    const size_t aux_bwd = r16((size_t)(2 * n_prb * PB) * 4);
     for (int ci = 0; ci < 5; ++ci) {
         int C = Cs[ci];
         if (cluster_req > 0 && C != cluster_req) continue;
@@ -716,28 +753,54 @@ int wt_fused_plan(int nx, int ny, int steps, int cluster_req, int seg_req, WtFus
             if (pad < best_pad) { best_pad = pad; best = M; }
         }
         if (best < 0) continue;
-        {
-            int M = best;
-            int rows = (nx + C - 1) / C;
-            int R = ((rows + M - 1) / M) * M;
-            int S = R / M;
-            int threads = S * NCP;
-            int LD = tile_ld(R, M);
-            size_t tiles = 3 * (size_t)(ny + 2) * LD * sizeof(float);
-            if (tiles > SMEM_MAX) continue;
-            L->C = C; L->M = M; L->R = R; L->S = S; L->NCP = NCP; L->LD = LD;
-            L->threads = threads; L->smem_fwd = tiles;
-            const size_t per_step = (size_t)M * threads * sizeof(float);
-            const int fit = (int)((SMEM_MAX - tiles) / per_step);
-            int seg = seg_req > 0 ? seg_req : (fit >= 4 ? fit : (int)std::ceil(std::sqrt((double)steps)));
-            seg = std::max(1, std::min(seg, steps));
-            L->seg = seg;
-            L->stash_smem = seg <= fit;
-            L->smem_bwd = tiles + (L->stash_smem ? (size_t)seg * per_step : 0);
-            return 0;
-        }
+        int M = best;
+        int rows = (nx + C - 1) / C;
+        int R = ((rows + M - 1) / M) * M;
+        int S = R / M;
+        int threads = S * NCP;
+        int LD = tile_ld(R, M);
+        size_t tiles = 3 * (size_t)(ny + 2) * LD * sizeof(float);
+        if (tiles + std::max(aux_fwd, aux_bwd) > SMEM_MAX) continue;
+        L->C = C; L->M = M; L->R = R; L->S = S; L->NCP = NCP; L->LD = LD;
+        L->threads = threads; L->PB = PB;
+        L->smem_fwd = tiles + aux_fwd;
+        const size_t per_step = (size_t)M * threads * sizeof(float);
+        const int fit = (int)((SMEM_MAX - tiles - aux_bwd) / per_step);
+        int seg = seg_req > 0 ? seg_req : (fit >= 4 ? fit : (int)std::ceil(std::sqrt((double)steps)));
+        seg = std::max(1, std::min(seg, steps));
+        L->seg = seg;
+        L->stash_smem = seg <= fit;
+        L->smem_bwd = tiles + aux_bwd + (L->stash_smem ? (size_t)seg * per_step : 0);
+        return 0;
     }
     return WT_ERR_UNSUPPORTED;
+}
+
+// Kahan-compensated time sums of the probe series: one thread per
+// (instance, column), sequential over t.
+__global__ void probe_sum_kernel(int batch, int steps, int n_prb, const float* __restrict__ out,
+                                 float* __restrict__ sum) {
+    int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= batch * n_prb) return;
+    const int b = idx / n_prb, q = idx - b * n_prb;
+    const float* p = out + (size_t)b * steps * n_prb + q;
+    float s = 0.f, comp = 0.f;
+    for (int t = 0; t < steps; ++t) {
+        float y = fsub(__ldg(p + (size_t)t * n_prb), comp);
+        float tk = fadd(s, y);
+        comp = fsub(fsub(tk, s), y);
+        s = tk;
+    }
+    sum[idx] = s;
+}
+
+int wt_launch_probe_sum(int batch, int steps, int n_prb, const float* out, float* sum,
+                        cudaStream_t st) {
+    const int n = batch * n_prb;
+    if (n == 0) return WT_OK;
+    probe_sum_kernel<<<(n + 127) / 128, 128, 0, st>>>(batch, steps, n_prb, out, sum);
+    wt_count_launches(1);
+    return wt_cuda_status(cudaGetLastError());
 }
 
 template <int M, int ORDER>
