@@ -223,6 +223,7 @@ WT_DEV void zero_smem(float* s, int n) {
 //   source e: (input row << 4) | cell index i      probe e: (column << 5) | (kind << 4) | i
 struct Taps {
     int ns, np;
+    bool src_edge;        // a source sits on a cell this thread sends as a halo
     int s0, s1, s2, s3;
     int p0, p1, p2, p3;
     WT_DEV int s(int e) const { return e == 0 ? s0 : e == 1 ? s1 : e == 2 ? s2 : s3; }
@@ -261,6 +262,14 @@ WT_DEV void build_taps(const FusedParams& P, const Geo& g, Taps& tp) {
     tp.ns = min(ns, SRCMAX); tp.np = min(np, PRBMAX);
     tp.s0 = s0; tp.s1 = s1; tp.s2 = s2; tp.s3 = s3;
     tp.p0 = p0; tp.p1 = p1; tp.p2 = p2; tp.p3 = p3;
+    tp.src_edge = false;
+#pragma unroll
+    for (int e = 0; e < SRCMAX; ++e) {
+        const int i = tp.s(e) & 15;
+        if (e < tp.ns && ((i == 0 && g.strip == 0 && g.has_up) ||
+                          (i == M - 1 && g.strip == g.S - 1 && g.has_dn)))
+            tp.src_edge = true;
+    }
 }
 
 // select v[i] for a runtime i without dynamic register indexing
@@ -346,7 +355,7 @@ WT_DEV void fwd_update(const FusedParams& P, const Geo& g, Xchg& X, const Taps& 
     L[M - 1] = lap_cell<M, ORDER>(P, c, cur, M - 1);
     inout[M - 1] = leapfrog(A[M - 1], Bc[M - 1], C2[M - 1], P.k.two_over, cur[M - 1],
                             inout[M - 1], L[M - 1]);
-    if (send && !tp.ns) send_halo(P, g, X, ws, inout[0], inout[M - 1]);
+    if (send && !tp.src_edge) send_halo(P, g, X, ws, inout[0], inout[M - 1]);
 #pragma unroll
     for (int i = 1; i < M - 1; ++i) {
         L[i] = lap_cell<M, ORDER>(P, c, cur, i);
@@ -354,13 +363,12 @@ WT_DEV void fwd_update(const FusedParams& P, const Geo& g, Xchg& X, const Taps& 
     }
     if (tp.ns) {
         apply_sources<M>(P, tp, inout, xv, tnext);
-        if (send) send_halo(P, g, X, ws, inout[0], inout[M - 1]);
+        if (send && tp.src_edge) send_halo(P, g, X, ws, inout[0], inout[M - 1]);
     }
     store_column<M>(P, g, X, ws, inout);
 }
 
 struct FwdState {
-    int ck;                   // steps until the next checkpoint boundary
     int pc;                   // step index within the probe chunk
     int pb;                   // probe ring buffer in use (0/1)
     float xv[SRCMAX];         // this step's source inputs
@@ -389,31 +397,31 @@ WT_DEV void flush_probes(const FusedParams& P, const Geo& g, const ProbeRing& pr
     }
 }
 
+// Checkpoint of segment t/seg: the state before step t, (h_{t-1}, h_{t-2}).
+template <int M>
+WT_DEV void store_checkpoint(const FusedParams& P, const Geo& g, int t, const float (&h1)[M],
+                             const float (&h2)[M]) {
+    if (!g.colv) return;
+    const size_t plane = (size_t)P.nx * P.ny;
+    const size_t bplane = (size_t)P.batch * plane;
+    float* cp = P.ckpt + (size_t)(t / P.seg) * 2 * bplane + (size_t)g.inst * plane;
+#pragma unroll
+    for (int i = 0; i < M; ++i) {
+        int gx = g.gx0 + i;
+        if (gx < P.nx) {
+            size_t cell = (size_t)gx * P.ny + g.col;
+            __stcg(cp + cell, h1[i]);
+            __stcg(cp + bplane + cell, h2[i]);
+        }
+    }
+}
+
 // One step of the forward kernel (everything but the closing barrier).
-template <int M, int ORDER>
+template <int M, int ORDER, bool FIELDS>
 WT_DEV void fwd_step(const FusedParams& P, const Geo& g, Xchg& X, const Taps& tp, FwdState& st,
                      const ProbeRing& pr, int t, int rs, int ws, const float (&A)[M],
                      const float (&Bc)[M], const float (&C2)[M], const float (&cur)[M],
                      float (&inout)[M]) {
-    const size_t plane = (size_t)P.nx * P.ny;
-    const size_t bplane = (size_t)P.batch * plane;
-    if (st.ck == 0) {
-        st.ck = P.seg;
-        // state before step t: (h_{t-1}, h_{t-2}) -> checkpoint of segment t/seg
-        if (g.colv) {
-            float* cp = P.ckpt + (size_t)(t / P.seg) * 2 * bplane + (size_t)g.inst * plane;
-#pragma unroll
-            for (int i = 0; i < M; ++i) {
-                int gx = g.gx0 + i;
-                if (gx < P.nx) {
-                    size_t cell = (size_t)gx * P.ny + g.col;
-                    __stcg(cp + cell, cur[i]);
-                    __stcg(cp + bplane + cell, inout[i]);
-                }
-            }
-        }
-    }
-    --st.ck;
     float L[M];
     // h_{t-1} came with remote halo rows for every t >= 1 (h_{-1} = 0 is local);
     // the last step's halos have no reader
@@ -426,7 +434,8 @@ WT_DEV void fwd_step(const FusedParams& P, const Geo& g, Xchg& X, const Taps& tp
         for (int e = 0; e < PRBMAX; ++e)
             if (e < tp.np) row[(tp.p(e) >> 5) * P.PB] = pick<M>(inout, tp.p(e) & 15);
     }
-    if (P.fields) {
+    if (FIELDS) {
+        const size_t plane = (size_t)P.nx * P.ny;
         float* fo = P.fields + ((size_t)g.inst * P.steps + t) * plane;
 #pragma unroll
         for (int i = 0; i < M; ++i) {
@@ -449,7 +458,7 @@ constexpr int max_threads() { return M >= 10 ? 384 : 512; }
 
 // ============================================================================
 // Forward
-template <int M, int ORDER>
+template <int M, int ORDER, bool FIELDS>
 __global__ void __launch_bounds__(max_threads<M>(), 1) seq_fwd_fused_kernel(FusedParams P) {
     extern __shared__ __align__(16) float smem[];
     __shared__ __align__(8) uint64_t mbar[3];
@@ -471,7 +480,6 @@ __global__ void __launch_bounds__(max_threads<M>(), 1) seq_fwd_fused_kernel(Fuse
     Taps tp;
     build_taps<M>(P, g, tp);
     FwdState st;
-    st.ck = P.seg;
     st.pc = 0;
     st.pb = 0;
 #pragma unroll
@@ -485,22 +493,30 @@ __global__ void __launch_bounds__(max_threads<M>(), 1) seq_fwd_fused_kernel(Fuse
     }
     cluster_sync_all();   // zeroed tiles, flags and initialised barriers, cluster-wide
 
-    // ya holds h_{t-1} at even t, yb at odd t (the update overwrites h_{t-2})
+    // ya holds h_{t-1} at even t, yb at odd t (the update overwrites h_{t-2});
+    // the outer loop runs one checkpoint segment per iteration
     int rs = 0;           // slot holding h_{t-1} (h_{-1} = 0 is slot 0)
     int chunk0 = 0;       // first step of the probe chunk being filled
-    for (int t = 0; t < P.steps;) {
-        int ws = next3(rs);
-        fwd_step<M, ORDER>(P, g, X, tp, st, pr, t, rs, ws, A, Bc, C2, ya, yb);
-        if (!exchange_end(X, t)) break;
-        rs = ws;
-        if (++st.pc == P.PB) { flush_probes(P, g, pr, st.pb, chunk0, P.PB); st.pc = 0; st.pb ^= 1; chunk0 = t + 1; }
-        if (++t >= P.steps) break;
-        ws = next3(rs);
-        fwd_step<M, ORDER>(P, g, X, tp, st, pr, t, rs, ws, A, Bc, C2, yb, ya);
-        if (!exchange_end(X, t)) break;
-        rs = ws;
-        if (++st.pc == P.PB) { flush_probes(P, g, pr, st.pb, chunk0, P.PB); st.pc = 0; st.pb ^= 1; chunk0 = t + 1; }
-        ++t;
+    bool ok = true;
+    for (int t0 = 0; t0 < P.steps && ok; t0 += P.seg) {
+        if (t0 > 0) {
+            if (t0 & 1) store_checkpoint<M>(P, g, t0, yb, ya);
+            else        store_checkpoint<M>(P, g, t0, ya, yb);
+        }
+        const int t1 = min(P.steps, t0 + P.seg);
+        for (int t = t0; t < t1; ++t) {
+            const int ws = next3(rs);
+            if (t & 1) fwd_step<M, ORDER, FIELDS>(P, g, X, tp, st, pr, t, rs, ws, A, Bc, C2, yb, ya);
+            else       fwd_step<M, ORDER, FIELDS>(P, g, X, tp, st, pr, t, rs, ws, A, Bc, C2, ya, yb);
+            if (!(ok = exchange_end(X, t))) break;
+            rs = ws;
+            if (++st.pc == P.PB) {
+                flush_probes(P, g, pr, st.pb, chunk0, P.PB);
+                st.pc = 0;
+                st.pb ^= 1;
+                chunk0 = t + 1;
+            }
+        }
     }
     if (st.pc > 0) flush_probes(P, g, pr, st.pb, chunk0, st.pc);
     cluster_sync_all();
@@ -806,8 +822,9 @@ int wt_launch_probe_sum(int batch, int steps, int n_prb, const float* out, float
 template <int M, int ORDER>
 static int launch_fused(bool fwd, const wt::FusedParams& P, const WtFusedLaunch& L,
                         cudaStream_t st) {
-    void (*kern)(wt::FusedParams) = fwd ? wt::seq_fwd_fused_kernel<M, ORDER>
-                                        : wt::seq_bwd_fused_kernel<M, ORDER>;
+    void (*kern)(wt::FusedParams) = !fwd ? wt::seq_bwd_fused_kernel<M, ORDER>
+                                    : P.fields ? wt::seq_fwd_fused_kernel<M, ORDER, true>
+                                               : wt::seq_fwd_fused_kernel<M, ORDER, false>;
     size_t smem = fwd ? L.smem_fwd : L.smem_bwd;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return wt_cuda_status(e);
