@@ -161,20 +161,22 @@ int make_plan(const wt_seq_desc* d, SeqPlan* p) {
         P.o_ckpt = o; o = up(o + (size_t)P.nseg * 2 * bp * F);
         P.o_stash = o; o = up(o + (P.L.stash_smem ? 0 : (size_t)P.seg * per_step));
         P.o_gcpart = o; o = up(o + bp * F);
-        // per-thread tap capacity of the fused kernels
-        std::vector<int> cnt;
-        auto key = [&](int cell) {
-            int gx = cell / P.ny, gy = cell % P.ny;
-            int cta = gx / P.L.R, strip = (gx % P.L.R) / P.L.M;
-            return ((size_t)cta * P.L.S + strip) * P.L.NCP + gy;
-        };
-        size_t nkeys = (size_t)P.L.C * P.L.S * P.L.NCP;
-        cnt.assign(nkeys, 0);
-        for (int i = 0; i < P.ns; ++i)
-            if (++cnt[key(d->sources_host[i].cell)] > 4) return WT_ERR_UNSUPPORTED;
-        cnt.assign(nkeys, 0);
-        for (int i = 0; i < P.np; ++i)
-            if (++cnt[key(d->probes_host[i].cell)] > 4) return WT_ERR_UNSUPPORTED;
+        // per-thread tap capacity of both fused kernels (4 sources, 4 probes)
+        for (int layout = 0; layout < 2; ++layout) {
+            const int R = layout ? P.L.fR : P.L.R, M = layout ? P.L.fM : P.L.M;
+            const int S = R / M;
+            std::vector<int> cnt((size_t)P.L.C * S * P.L.NCP, 0);
+            auto key = [&](int cell) {
+                int gx = cell / P.ny, gy = cell % P.ny;
+                int cta = gx / R, strip = (gx % R) / M;
+                return ((size_t)cta * S + strip) * P.L.NCP + gy;
+            };
+            for (int i = 0; i < P.ns; ++i)
+                if (++cnt[key(d->sources_host[i].cell)] > 4) return WT_ERR_UNSUPPORTED;
+            std::fill(cnt.begin(), cnt.end(), 0);
+            for (int i = 0; i < P.np; ++i)
+                if (++cnt[key(d->probes_host[i].cell)] > 4) return WT_ERR_UNSUPPORTED;
+        }
     }
     P.total = o;
     return WT_OK;
@@ -234,6 +236,7 @@ wt::FusedParams fused_params(const wt_scalars* s, const SeqPlan& P, const float*
     F.k = wt_make_scalars(s);
     F.batch = P.B; F.nx = P.nx; F.ny = P.ny; F.steps = P.T;
     F.C = P.L.C; F.R = P.L.R; F.NCP = P.L.NCP; F.LD = P.L.LD; F.seg = P.seg; F.PB = P.L.PB;
+    // (R and LD are set per kernel at launch: the two kernels use different strips)
     F.b = b; F.c = c; F.x = x;
     F.n_src = P.ns;
     F.src_cell = at<int>(ws, P.o_srccell);

@@ -75,7 +75,9 @@ struct FusedParams {
 
 // Launch shape of the fused kernels for one grid size.
 struct WtFusedLaunch {
-    int C, M, R, S, NCP, LD, threads;
+    int C, NCP;
+    int M, R, S, LD, threads;          // adjoint kernel strips
+    int fM, fR, fS, fLD, fthreads;     // forward kernel strips (fewer registers: more threads)
     int PB;                 // probe chunk length
     size_t smem_fwd;        // tiles + probe ring buffers
     size_t smem_bwd;        // tiles + seed ring buffers (+ the stash when stash_smem)

@@ -453,13 +453,15 @@ WT_DEV bool exchange_end(const Xchg& X, int k) {
     return (k & 31) != 0 || *(volatile int*)X.abort == 0;
 }
 
-template <int M>
-constexpr int max_threads() { return M >= 10 ? 384 : 512; }
+// Threads per CTA a strip height allows (register budget per thread): the
+// forward keeps 5 values per cell, the adjoint about twice as many.
+constexpr int fwd_max_threads(int M) { return M <= 5 ? 768 : M == 6 ? 640 : M == 8 ? 512 : 384; }
+constexpr int bwd_max_threads(int M) { return M >= 10 ? 384 : 512; }
 
 // ============================================================================
 // Forward
 template <int M, int ORDER, bool FIELDS>
-__global__ void __launch_bounds__(max_threads<M>(), 1) seq_fwd_fused_kernel(FusedParams P) {
+__global__ void __launch_bounds__(fwd_max_threads(M), 1) seq_fwd_fused_kernel(FusedParams P) {
     extern __shared__ __align__(16) float smem[];
     __shared__ __align__(8) uint64_t mbar[3];
     __shared__ int abort_flag;
@@ -577,7 +579,7 @@ WT_DEV void adj_cell(float lg, float lam, float Ly, float X1, float Kc, float Ky
 }
 
 template <int M, int ORDER>
-__global__ void __launch_bounds__(max_threads<M>(), 1) seq_bwd_fused_kernel(FusedParams P) {
+__global__ void __launch_bounds__(bwd_max_threads(M), 1) seq_bwd_fused_kernel(FusedParams P) {
     extern __shared__ __align__(16) float smem[];
     __shared__ __align__(8) uint64_t mbar[3];
     __shared__ int abort_flag;
@@ -737,15 +739,32 @@ static int tile_ld(int rows, int M) {
     return ld;
 }
 
-// Pick (C, M) for a grid: clusters of C CTAs, M cells per thread, at most
-// 512 threads per CTA (384 for 10-cell strips); then the checkpoint
-// interval: the largest stash that fits in shared memory next to the three
-// tiles and the probe ring buffers (at least 4 steps), else a sqrt(T)
-// interval with the stash in global memory.  Returns 0 on success.
+// Strip height with the fewest padding rows for R rows per CTA (ties: the
+// first in `Ms`), within the thread budget of that height.
+static int pick_strip(int nx, int C, int NCP, const int* Ms, int nM, bool fwd) {
+    int best = -1, best_pad = 1 << 30;
+    for (int mi = 0; mi < nM; ++mi) {
+        int M = Ms[mi];
+        int rows = (nx + C - 1) / C;
+        int R = ((rows + M - 1) / M) * M;
+        if ((C - 1) * R >= nx) continue;   // an empty CTA
+        if ((R / M) * NCP > (fwd ? wt::fwd_max_threads(M) : wt::bwd_max_threads(M))) continue;
+        int pad = C * R - nx;
+        if (pad < best_pad) { best_pad = pad; best = M; }
+    }
+    return best;
+}
+
+// Pick the cluster size C and the strip heights (the adjoint kernel favours
+// tall strips: its per-cell state is large; the forward favours more
+// threads); then the checkpoint interval: the largest stash that fits in
+// shared memory next to the three tiles and the probe ring buffers (at least
+// 4 steps), else a sqrt(T) interval with the stash in global memory.
 int wt_fused_plan(int nx, int ny, int steps, int n_prb, int cluster_req, int seg_req,
                   WtFusedLaunch* L) {
     const int NCP = ((ny + 31) / 32) * 32;
-    const int Ms[3] = {10, 8, 4};
+    const int Mb[3] = {10, 8, 4};
+    const int Mf[5] = {5, 6, 8, 10, 4};
     const int Cs[5] = {4, 2, 8, 1, 16};
     const size_t SMEM_MAX = 227 * 1024 - 64;   // dynamic smem per CTA (static: 28 B)
     const int PB = n_prb > 0 ? std::max(1, std::min(32, 2048 / n_prb)) : 32;
@@ -756,31 +775,20 @@ int wt_fused_plan(int nx, int ny, int steps, int n_prb, int cluster_req, int seg
         int C = Cs[ci];
         if (cluster_req > 0 && C != cluster_req) continue;
         if (C > 8) continue;
-        // the M with the fewest padding rows (ties: the larger M)
-        int best = -1, best_pad = 1 << 30;
-        for (int mi = 0; mi < 3; ++mi) {
-            int M = Ms[mi];
-            int rows = (nx + C - 1) / C;
-            int R = ((rows + M - 1) / M) * M;
-            if ((C - 1) * R >= nx) continue;   // an empty CTA
-            int threads = (R / M) * NCP;
-            if (threads > (M >= 10 ? 384 : 512)) continue;
-            int pad = C * R - nx;
-            if (pad < best_pad) { best_pad = pad; best = M; }
-        }
-        if (best < 0) continue;
-        int M = best;
-        int rows = (nx + C - 1) / C;
-        int R = ((rows + M - 1) / M) * M;
-        int S = R / M;
-        int threads = S * NCP;
-        int LD = tile_ld(R, M);
-        size_t tiles = 3 * (size_t)(ny + 2) * LD * sizeof(float);
-        if (tiles + std::max(aux_fwd, aux_bwd) > SMEM_MAX) continue;
-        L->C = C; L->M = M; L->R = R; L->S = S; L->NCP = NCP; L->LD = LD;
-        L->threads = threads; L->PB = PB;
-        L->smem_fwd = tiles + aux_fwd;
-        const size_t per_step = (size_t)M * threads * sizeof(float);
+        const int M = pick_strip(nx, C, NCP, Mb, 3, false);
+        const int fM = pick_strip(nx, C, NCP, Mf, 5, true);
+        if (M < 0 || fM < 0) continue;
+        const int rows = (nx + C - 1) / C;
+        const int R = ((rows + M - 1) / M) * M, fR = ((rows + fM - 1) / fM) * fM;
+        const int LD = tile_ld(R, M), fLD = tile_ld(fR, fM);
+        const size_t tiles = 3 * (size_t)(ny + 2) * LD * sizeof(float);
+        const size_t ftiles = 3 * (size_t)(ny + 2) * fLD * sizeof(float);
+        if (tiles + aux_bwd > SMEM_MAX || ftiles + aux_fwd > SMEM_MAX) continue;
+        L->C = C; L->NCP = NCP; L->PB = PB;
+        L->M = M; L->R = R; L->S = R / M; L->LD = LD; L->threads = (R / M) * NCP;
+        L->fM = fM; L->fR = fR; L->fS = fR / fM; L->fLD = fLD; L->fthreads = (fR / fM) * NCP;
+        L->smem_fwd = ftiles + aux_fwd;
+        const size_t per_step = (size_t)M * L->threads * sizeof(float);
         const int fit = (int)((SMEM_MAX - tiles - aux_bwd) / per_step);
         int seg = seg_req > 0 ? seg_req : (fit >= 4 ? fit : (int)std::ceil(std::sqrt((double)steps)));
         seg = std::max(1, std::min(seg, steps));
@@ -819,23 +827,18 @@ int wt_launch_probe_sum(int batch, int steps, int n_prb, const float* out, float
     return wt_cuda_status(cudaGetLastError());
 }
 
-template <int M, int ORDER>
-static int launch_fused(bool fwd, const wt::FusedParams& P, const WtFusedLaunch& L,
-                        cudaStream_t st) {
-    void (*kern)(wt::FusedParams) = !fwd ? wt::seq_bwd_fused_kernel<M, ORDER>
-                                    : P.fields ? wt::seq_fwd_fused_kernel<M, ORDER, true>
-                                               : wt::seq_fwd_fused_kernel<M, ORDER, false>;
-    size_t smem = fwd ? L.smem_fwd : L.smem_bwd;
+static int launch_kernel(void (*kern)(wt::FusedParams), const wt::FusedParams& P, int C,
+                         int threads, size_t smem, cudaStream_t st) {
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return wt_cuda_status(e);
     cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3(L.C * P.batch, 1, 1);
-    cfg.blockDim = dim3(L.threads, 1, 1);
+    cfg.gridDim = dim3(C * P.batch, 1, 1);
+    cfg.blockDim = dim3(threads, 1, 1);
     cfg.dynamicSmemBytes = smem;
     cfg.stream = st;
     cudaLaunchAttribute attr[1];
     attr[0].id = cudaLaunchAttributeClusterDimension;
-    attr[0].val.clusterDim.x = L.C;
+    attr[0].val.clusterDim.x = C;
     attr[0].val.clusterDim.y = 1;
     attr[0].val.clusterDim.z = 1;
     cfg.attrs = attr;
@@ -845,15 +848,45 @@ static int launch_fused(bool fwd, const wt::FusedParams& P, const WtFusedLaunch&
     return wt_cuda_status(e);
 }
 
-int wt_launch_fused(bool fwd, const wt::FusedParams& P, const WtFusedLaunch& L, cudaStream_t st) {
-    if (P.k.lap_order == WT_LAP_SEQ) {
-        if (L.M == 10) return launch_fused<10, WT_LAP_SEQ>(fwd, P, L, st);
-        if (L.M == 8) return launch_fused<8, WT_LAP_SEQ>(fwd, P, L, st);
-        if (L.M == 4) return launch_fused<4, WT_LAP_SEQ>(fwd, P, L, st);
+template <int M, int ORDER>
+static int launch_fwd(const wt::FusedParams& P0, const WtFusedLaunch& L, cudaStream_t st) {
+    wt::FusedParams P = P0;
+    P.R = L.fR;
+    P.LD = L.fLD;
+    return launch_kernel(P.fields ? wt::seq_fwd_fused_kernel<M, ORDER, true>
+                                  : wt::seq_fwd_fused_kernel<M, ORDER, false>,
+                         P, L.C, L.fthreads, L.smem_fwd, st);
+}
+
+template <int M, int ORDER>
+static int launch_bwd(const wt::FusedParams& P0, const WtFusedLaunch& L, cudaStream_t st) {
+    wt::FusedParams P = P0;
+    P.R = L.R;
+    P.LD = L.LD;
+    return launch_kernel(wt::seq_bwd_fused_kernel<M, ORDER>, P, L.C, L.threads, L.smem_bwd, st);
+}
+
+template <int ORDER>
+static int launch_order(bool fwd, const wt::FusedParams& P, const WtFusedLaunch& L, cudaStream_t st) {
+    if (fwd) {
+        switch (L.fM) {
+            case 10: return launch_fwd<10, ORDER>(P, L, st);
+            case 8: return launch_fwd<8, ORDER>(P, L, st);
+            case 6: return launch_fwd<6, ORDER>(P, L, st);
+            case 5: return launch_fwd<5, ORDER>(P, L, st);
+            case 4: return launch_fwd<4, ORDER>(P, L, st);
+        }
     } else {
-        if (L.M == 10) return launch_fused<10, WT_LAP_PAIRED>(fwd, P, L, st);
-        if (L.M == 8) return launch_fused<8, WT_LAP_PAIRED>(fwd, P, L, st);
-        if (L.M == 4) return launch_fused<4, WT_LAP_PAIRED>(fwd, P, L, st);
+        switch (L.M) {
+            case 10: return launch_bwd<10, ORDER>(P, L, st);
+            case 8: return launch_bwd<8, ORDER>(P, L, st);
+            case 4: return launch_bwd<4, ORDER>(P, L, st);
+        }
     }
     return WT_ERR_UNSUPPORTED;
+}
+
+int wt_launch_fused(bool fwd, const wt::FusedParams& P, const WtFusedLaunch& L, cudaStream_t st) {
+    return P.k.lap_order == WT_LAP_SEQ ? launch_order<WT_LAP_SEQ>(fwd, P, L, st)
+                                       : launch_order<WT_LAP_PAIRED>(fwd, P, L, st);
 }
