@@ -220,7 +220,7 @@ WT_DEV void zero_smem(float* s, int n) {
 
 // Per-thread source list (table order) and probe list (descending order),
 // packed into scalar words so they stay in registers:
-//   source e: (input row << 4) | cell index i      probe e: (column << 5) | (kind << 4) | i
+//   source e: (input row << 5) | cell index i      probe e: (column << 6) | (kind << 5) | i
 struct Taps {
     int ns, np;
     bool src_edge;        // a source sits on a cell this thread sends as a halo
@@ -228,6 +228,11 @@ struct Taps {
     int p0, p1, p2, p3;
     WT_DEV int s(int e) const { return e == 0 ? s0 : e == 1 ? s1 : e == 2 ? s2 : s3; }
     WT_DEV int p(int e) const { return e == 0 ? p0 : e == 1 ? p1 : e == 2 ? p2 : p3; }
+    WT_DEV int src_i(int e) const { return s(e) & 31; }
+    WT_DEV int src_row(int e) const { return s(e) >> 5; }
+    WT_DEV int prb_i(int e) const { return p(e) & 31; }
+    WT_DEV int prb_col(int e) const { return p(e) >> 6; }
+    WT_DEV bool prb_intensity(int e) const { return (p(e) & 32) != 0; }
 };
 
 template <int M>
@@ -241,7 +246,7 @@ WT_DEV void build_taps(const FusedParams& P, const Geo& g, Taps& tp) {
             int i = cx - g.gx0;
             if (cy == g.col && i >= 0 && i < M) {
                 int row = __ldg(P.src_row + e);
-                int v = ((row < 0 ? g.inst : row) << 4) | i;
+                int v = ((row < 0 ? g.inst : row) << 5) | i;
                 if (ns == 0) s0 = v; else if (ns == 1) s1 = v; else if (ns == 2) s2 = v;
                 else if (ns == 3) s3 = v; else atomicExch(P.err, WT_DEVERR_BOUNDS);
                 ++ns;
@@ -252,7 +257,7 @@ WT_DEV void build_taps(const FusedParams& P, const Geo& g, Taps& tp) {
             int cx = cell / P.ny, cy = cell - cx * P.ny;
             int i = cx - g.gx0;
             if (cy == g.col && i >= 0 && i < M) {
-                int v = (__ldg(P.prb_col + e) << 5) | (__ldg(P.prb_kind + e) << 4) | i;
+                int v = (__ldg(P.prb_col + e) << 6) | (__ldg(P.prb_kind + e) << 5) | i;
                 if (np == 0) p0 = v; else if (np == 1) p1 = v; else if (np == 2) p2 = v;
                 else if (np == 3) p3 = v; else atomicExch(P.err, WT_DEVERR_BOUNDS);
                 ++np;
@@ -265,7 +270,7 @@ WT_DEV void build_taps(const FusedParams& P, const Geo& g, Taps& tp) {
     tp.src_edge = false;
 #pragma unroll
     for (int e = 0; e < SRCMAX; ++e) {
-        const int i = tp.s(e) & 15;
+        const int i = tp.src_i(e);
         if (e < tp.ns && ((i == 0 && g.strip == 0 && g.has_up) ||
                           (i == M - 1 && g.strip == g.S - 1 && g.has_dn)))
             tp.src_edge = true;
@@ -325,11 +330,11 @@ WT_DEV void apply_sources(const FusedParams& P, const Taps& tp, float (&y)[M], f
                           int tnext) {
 #pragma unroll
     for (int e = 0; e < SRCMAX; ++e)
-        if (e < tp.ns) add_at<M>(y, tp.s(e) & 15, xv[e]);
+        if (e < tp.ns) add_at<M>(y, tp.src_i(e), xv[e]);
     if (tnext >= 0 && tnext < P.steps) {
 #pragma unroll
         for (int e = 0; e < SRCMAX; ++e)
-            if (e < tp.ns) xv[e] = __ldg(P.x + (size_t)(tp.s(e) >> 4) * P.steps + tnext);
+            if (e < tp.ns) xv[e] = __ldg(P.x + (size_t)tp.src_row(e) * P.steps + tnext);
     }
 }
 
@@ -432,7 +437,7 @@ WT_DEV void fwd_step(const FusedParams& P, const Geo& g, Xchg& X, const Taps& tp
         float* row = pr.buf + (size_t)st.pb * P.n_prb * P.PB + st.pc;
 #pragma unroll
         for (int e = 0; e < PRBMAX; ++e)
-            if (e < tp.np) row[(tp.p(e) >> 5) * P.PB] = pick<M>(inout, tp.p(e) & 15);
+            if (e < tp.np) row[tp.prb_col(e) * P.PB] = pick<M>(inout, tp.prb_i(e));
     }
     if (FIELDS) {
         const size_t plane = (size_t)P.nx * P.ny;
@@ -455,7 +460,9 @@ WT_DEV bool exchange_end(const Xchg& X, int k) {
 
 // Threads per CTA a strip height allows (register budget per thread): the
 // forward keeps 5 values per cell, the adjoint about twice as many.
-constexpr int fwd_max_threads(int M) { return M <= 5 ? 768 : M == 6 ? 640 : M == 8 ? 512 : 384; }
+constexpr int fwd_max_threads(int M) {
+    return M <= 5 ? 768 : M == 6 ? 640 : M == 8 ? 512 : M <= 10 ? 384 : 256;
+}
 constexpr int bwd_max_threads(int M) { return M >= 10 ? 384 : 512; }
 
 // ============================================================================
@@ -486,12 +493,12 @@ __global__ void __launch_bounds__(fwd_max_threads(M), 1) seq_fwd_fused_kernel(Fu
     st.pb = 0;
 #pragma unroll
     for (int e = 0; e < SRCMAX; ++e)
-        st.xv[e] = e < tp.ns ? __ldg(P.x + (size_t)(tp.s(e) >> 4) * P.steps) : 0.f;
+        st.xv[e] = e < tp.ns ? __ldg(P.x + (size_t)tp.src_row(e) * P.steps) : 0.f;
     __syncthreads();      // ownership flags cleared before the owners mark theirs
     if (g.colv && tp.np) {
 #pragma unroll
         for (int e = 0; e < PRBMAX; ++e)
-            if (e < tp.np) pr.own[tp.p(e) >> 5] = (tp.p(e) & 16) ? 2 : 1;
+            if (e < tp.np) pr.own[tp.prb_col(e)] = tp.prb_intensity(e) ? 2 : 1;
     }
     cluster_sync_all();   // zeroed tiles, flags and initialised barriers, cluster-wide
 
@@ -645,7 +652,7 @@ __global__ void __launch_bounds__(bwd_max_threads(M), 1) seq_bwd_fused_kernel(Fu
             float xv[SRCMAX];
 #pragma unroll
             for (int e = 0; e < SRCMAX; ++e)
-                xv[e] = (e < tp.ns) ? __ldg(P.x + (size_t)(tp.s(e) >> 4) * P.steps + t0) : 0.f;
+                xv[e] = (e < tp.ns) ? __ldg(P.x + (size_t)tp.src_row(e) * P.steps + t0) : 0.f;
             for (int t = t0; t < t1;) {
                 rec_step<M, ORDER>(P, g, X, tp, xv, t, t0, t1, rs, xs, sh, A, Bc, C2, ya, yb);
                 if (++t >= t1) break;
@@ -680,7 +687,7 @@ __global__ void __launch_bounds__(bwd_max_threads(M), 1) seq_bwd_fused_kernel(Fu
                     const float* sr = seeds + (size_t)((u / P.PB) & 1) * P.n_prb * P.PB + u % P.PB;
 #pragma unroll
                     for (int e = 0; e < PRBMAX; ++e)
-                        if (e < tp.np) add_at<M>(lam, tp.p(e) & 15, sr[(tp.p(e) >> 5) * P.PB]);
+                        if (e < tp.np) add_at<M>(lam, tp.prb_i(e), sr[tp.prb_col(e) * P.PB]);
                 }
 #pragma unroll
                 for (int i = 0; i < M; ++i) c2g[i] = fmul(Kg[i], lam[i]);
@@ -688,8 +695,8 @@ __global__ void __launch_bounds__(bwd_max_threads(M), 1) seq_bwd_fused_kernel(Fu
                 if (P.grad_x && tp.ns) {
 #pragma unroll
                     for (int e = 0; e < SRCMAX; ++e)
-                        if (e < tp.ns && (tp.s(e) >> 4) == g.inst)
-                            P.grad_x[(size_t)g.inst * P.steps + t] = pick<M>(lam, tp.s(e) & 15);
+                        if (e < tp.ns && tp.src_row(e) == g.inst)
+                            P.grad_x[(size_t)g.inst * P.steps + t] = pick<M>(lam, tp.src_i(e));
                 }
             }
             if (!(ok = exchange_end(X, u))) break;
@@ -764,7 +771,7 @@ int wt_fused_plan(int nx, int ny, int steps, int n_prb, int cluster_req, int seg
                   WtFusedLaunch* L) {
     const int NCP = ((ny + 31) / 32) * 32;
     const int Mb[3] = {10, 8, 4};
-    const int Mf[5] = {5, 6, 8, 10, 4};
+    const int Mf[7] = {10, 15, 30, 8, 6, 5, 4};
     const int Cs[5] = {4, 2, 8, 1, 16};
     const size_t SMEM_MAX = 227 * 1024 - 64;   // dynamic smem per CTA (static: 28 B)
     const int PB = n_prb > 0 ? std::max(1, std::min(32, 2048 / n_prb)) : 32;
@@ -776,7 +783,7 @@ int wt_fused_plan(int nx, int ny, int steps, int n_prb, int cluster_req, int seg
         if (cluster_req > 0 && C != cluster_req) continue;
         if (C > 8) continue;
         const int M = pick_strip(nx, C, NCP, Mb, 3, false);
-        const int fM = pick_strip(nx, C, NCP, Mf, 5, true);
+        const int fM = pick_strip(nx, C, NCP, Mf, 7, true);
         if (M < 0 || fM < 0) continue;
         const int rows = (nx + C - 1) / C;
         const int R = ((rows + M - 1) / M) * M, fR = ((rows + fM - 1) / fM) * fM;
@@ -870,6 +877,8 @@ template <int ORDER>
 static int launch_order(bool fwd, const wt::FusedParams& P, const WtFusedLaunch& L, cudaStream_t st) {
     if (fwd) {
         switch (L.fM) {
+            case 30: return launch_fwd<30, ORDER>(P, L, st);
+            case 15: return launch_fwd<15, ORDER>(P, L, st);
             case 10: return launch_fwd<10, ORDER>(P, L, st);
             case 8: return launch_fwd<8, ORDER>(P, L, st);
             case 6: return launch_fwd<6, ORDER>(P, L, st);
