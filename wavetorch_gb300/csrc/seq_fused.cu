@@ -324,72 +324,18 @@ WT_DEV void load_bwd_coef(const FusedParams& P, const Geo& g, float (&X1)[M], fl
 
 WT_DEV int next3(int s) { return s == 2 ? 0 : s + 1; }
 
-// ---- rare per-thread work, kept out of line -------------------------------
-// Only the few threads that own a source or probe cell run these; as real
-// calls they cannot be if-converted into the step of every other thread.
-template <int M>
-struct Vals {
-    float v[M];
-};
-template <int M>
-struct SrcState {
-    Vals<M> y;
-    float xv[SRCMAX];
-};
-
-// Sources (in table order): add this step's inputs, prefetch the next step's.
-template <int M>
-__device__ __noinline__ SrcState<M> sources_step(SrcState<M> s, const FusedParams& P,
-                                                 const Taps tp, int tnext) {
-#pragma unroll
-    for (int e = 0; e < SRCMAX; ++e)
-        if (e < tp.ns) add_at<M>(s.y.v, tp.src_i(e), s.xv[e]);
-    if (tnext >= 0 && tnext < P.steps) {
-#pragma unroll
-        for (int e = 0; e < SRCMAX; ++e)
-            if (e < tp.ns) s.xv[e] = __ldg(P.x + (size_t)tp.src_row(e) * P.steps + tnext);
-    }
-    return s;
-}
-
-// Probe amplitudes of this step into the shared ring (row = this step's column).
-template <int M>
-__device__ __noinline__ void probes_step(const Vals<M> y, const Taps tp, float* row, int PB) {
-#pragma unroll
-    for (int e = 0; e < PRBMAX; ++e)
-        if (e < tp.np) row[tp.prb_col(e) * PB] = pick<M>(y.v, tp.prb_i(e));
-}
-
-// Adjoint seeds (descending reference order) from the staged ring.
-template <int M>
-__device__ __noinline__ Vals<M> seeds_step(Vals<M> lam, const Taps tp, const float* sr, int PB) {
-#pragma unroll
-    for (int e = 0; e < PRBMAX; ++e)
-        if (e < tp.np) add_at<M>(lam.v, tp.prb_i(e), sr[tp.prb_col(e) * PB]);
-    return lam;
-}
-
-// dL/dx of this step for own-row sources.
-template <int M>
-__device__ __noinline__ void gradx_step(const Vals<M> lam, const Taps tp, float* gx, int inst) {
-#pragma unroll
-    for (int e = 0; e < SRCMAX; ++e)
-        if (e < tp.ns && tp.src_row(e) == inst) *gx = pick<M>(lam.v, tp.src_i(e));
-}
-
+// Sources (in table order) with the inputs prefetched one step ahead.
 template <int M>
 WT_DEV void apply_sources(const FusedParams& P, const Taps& tp, float (&y)[M], float (&xv)[SRCMAX],
                           int tnext) {
-    SrcState<M> s;
 #pragma unroll
-    for (int i = 0; i < M; ++i) s.y.v[i] = y[i];
+    for (int e = 0; e < SRCMAX; ++e)
+        if (e < tp.ns) add_at<M>(y, tp.src_i(e), xv[e]);
+    if (tnext >= 0 && tnext < P.steps) {
 #pragma unroll
-    for (int e = 0; e < SRCMAX; ++e) s.xv[e] = xv[e];
-    s = sources_step<M>(s, P, tp, tnext);
-#pragma unroll
-    for (int i = 0; i < M; ++i) y[i] = s.y.v[i];
-#pragma unroll
-    for (int e = 0; e < SRCMAX; ++e) xv[e] = s.xv[e];
+        for (int e = 0; e < SRCMAX; ++e)
+            if (e < tp.ns) xv[e] = __ldg(P.x + (size_t)tp.src_row(e) * P.steps + tnext);
+    }
 }
 
 // h_t for the thread's cells from cur = h_{t-1} (registers + tile slot rs) and
@@ -488,10 +434,10 @@ WT_DEV void fwd_step(const FusedParams& P, const Geo& g, Xchg& X, const Taps& tp
                          cur, inout, L);
     if (!g.colv) return;
     if (tp.np) {
-        Vals<M> y;
+        float* row = pr.buf + (size_t)st.pb * P.n_prb * P.PB + st.pc;
 #pragma unroll
-        for (int i = 0; i < M; ++i) y.v[i] = inout[i];
-        probes_step<M>(y, tp, pr.buf + (size_t)st.pb * P.n_prb * P.PB + st.pc, P.PB);
+        for (int e = 0; e < PRBMAX; ++e)
+            if (e < tp.np) row[tp.prb_col(e) * P.PB] = pick<M>(inout, tp.prb_i(e));
     }
     if (FIELDS) {
         const size_t plane = (size_t)P.nx * P.ny;
@@ -738,23 +684,19 @@ __global__ void __launch_bounds__(bwd_max_threads(M), 1) seq_bwd_fused_kernel(Fu
             if (g.colv) {
                 if (tp.np) {
                     // probe seeds, descending reference order (list order)
-                    Vals<M> l;
+                    const float* sr = seeds + (size_t)((u / P.PB) & 1) * P.n_prb * P.PB + u % P.PB;
 #pragma unroll
-                    for (int i = 0; i < M; ++i) l.v[i] = lam[i];
-                    l = seeds_step<M>(l, tp,
-                                      seeds + (size_t)((u / P.PB) & 1) * P.n_prb * P.PB + u % P.PB,
-                                      P.PB);
-#pragma unroll
-                    for (int i = 0; i < M; ++i) lam[i] = l.v[i];
+                    for (int e = 0; e < PRBMAX; ++e)
+                        if (e < tp.np) add_at<M>(lam, tp.prb_i(e), sr[tp.prb_col(e) * P.PB]);
                 }
 #pragma unroll
                 for (int i = 0; i < M; ++i) c2g[i] = fmul(Kg[i], lam[i]);
                 publish<M>(P, g, X, xs, c2g, true);
                 if (P.grad_x && tp.ns) {
-                    Vals<M> l;
 #pragma unroll
-                    for (int i = 0; i < M; ++i) l.v[i] = lam[i];
-                    gradx_step<M>(l, tp, P.grad_x + (size_t)g.inst * P.steps + t, g.inst);
+                    for (int e = 0; e < SRCMAX; ++e)
+                        if (e < tp.ns && tp.src_row(e) == g.inst)
+                            P.grad_x[(size_t)g.inst * P.steps + t] = pick<M>(lam, tp.src_i(e));
                 }
             }
             if (!(ok = exchange_end(X, u))) break;
