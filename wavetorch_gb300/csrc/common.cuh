@@ -171,6 +171,17 @@ WT_DEV void st_async_f32(uint32_t remote, float v, uint32_t remote_mbar) {
                  "r"(__float_as_uint(v)), "r"(remote_mbar)
                  : "memory");
 }
+// Relaxed 8-byte store into another CTA's shared memory (shared::cluster
+// address) and relaxed 8-byte load from this CTA's shared memory; aligned
+// 8-byte accesses are single-copy atomic, so a {value, tag} word is never torn.
+WT_DEV void st_cluster_u64(uint32_t remote, unsigned long long v) {
+    asm volatile("st.relaxed.cluster.shared::cluster.b64 [%0], %1;" ::"r"(remote), "l"(v) : "memory");
+}
+WT_DEV unsigned long long ld_cluster_u64(uint32_t local) {
+    unsigned long long v;
+    asm volatile("ld.relaxed.cluster.shared::cta.b64 %0, [%1];" : "=l"(v) : "r"(local) : "memory");
+    return v;
+}
 WT_DEV uint64_t global_ns() {
     uint64_t t;
     asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));

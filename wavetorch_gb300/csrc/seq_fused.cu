@@ -11,20 +11,16 @@
 //
 // Exchange.  Each step every thread writes its M new values into a
 // column-major shared-memory tile  F[col+1][OFF + row]  (zero columns at
-// y = -1 and y = ny, one halo row above and below the CTA's rows).  The CTA's
-// first and last rows are pushed into the neighbouring CTAs' halo rows with
-// st.async (DSMEM), which completes transaction bytes on the receiver's
-// mbarrier for that tile.  Per step: one __syncthreads for the CTA's own
-// tile, and an mbarrier wait (acquire.cluster) by the warps that read halos.
-// Tiles rotate over three slots, so a neighbour can never overwrite a halo
-// row that is still being read: it writes slot s only after consuming this
-// CTA's data of the next slot, which this CTA sent after finishing its reads
-// of slot s.  No cluster-wide barrier or release fence runs in the step loop,
-// so global stores (outputs, checkpoints) never stall the exchange.
+// y = -1 and y = ny), double buffered, with one __syncthreads per step.  The
+// CTA's first and last rows also go to the neighbouring CTAs as tagged
+// 64-bit words (see the exchange section below); only the thread that needs
+// a neighbour's value waits for it, so nothing on the cluster path is a
+// barrier or a fence, and global stores never stall the exchange.
 //
 // Waits are bounded (~2 s).  A wait that gives up records WT_DEVERR_TIMEOUT
-// in the status word, every CTA leaves its loop at the next step, and the
-// cluster meets at one final barrier before exiting.
+// in the status word, the CTA leaves its loop within 32 steps, its
+// neighbours' waits then give up too, and the cluster meets at one final
+// barrier before exiting.
 //
 // Adjoint.  The forward stores the pair (h_{t-1}, h_{t-2}) every `seg` steps.
 // The adjoint walks the segments backwards: it reloads the checkpoint,
@@ -45,8 +41,7 @@ namespace wt {
 constexpr int OFF = 4;       // first own row in a tile column (16-byte aligned)
 constexpr int SRCMAX = 4;    // source entries one thread may own
 constexpr int PRBMAX = 4;    // probe entries one thread may own
-constexpr uint64_t WAIT_LIMIT_NS = 2000000000ull;   // bounded mbarrier waits (2 s)
-constexpr uint32_t WAIT_HINT_NS = 1000000u;         // suspend a waiting thread up to 1 ms per probe
+constexpr uint64_t WAIT_LIMIT_NS = 2000000000ull;   // bounded halo waits (2 s)
 
 // load M consecutive floats from a 16-byte aligned (M%4==0) shared address
 template <int M>
@@ -106,111 +101,120 @@ WT_DEV Geo make_geo(const FusedParams& P, int M) {
 }
 
 // ---- neighbour exchange ----------------------------------------------------
+// Inside a CTA the strips exchange through a double-buffered column-major
+// tile (one __syncthreads per exchange).  Between the CTAs of a cluster only
+// the boundary rows travel: each value goes as one 64-bit word {float bits,
+// tag = exchange index + 1} stored with st.relaxed.cluster into the
+// receiving CTA's halo array [2][NCP] (parity of the exchange index), and
+// the single thread that needs it spins on that word until the tag matches
+// (an aligned 8-byte store is single-copy atomic, so the value is valid
+// whenever the tag is).  No barrier, fence or mbarrier is on this path.
+//
+// Double buffering is enough: a neighbour writes parity p for exchange k+2
+// only after it received this CTA's exchange k+1 value, which this CTA's
+// same thread sent after reading its exchange-k word.
 struct Xchg {
     float* tiles;           // slot 0 (slots are `tile` floats apart)
     int tile;               // floats per slot
-    uint32_t mbar;          // shared address of 3 consecutive mbarriers
-    uint32_t up_tile, dn_tile;   // slot-0 shared::cluster addresses in the neighbours
-    uint32_t up_mbar, dn_mbar;
-    uint32_t expect;        // halo bytes per phase
-    uint32_t par;           // bit p: parity of the next wait on slot p
-    bool waiter;            // reads a halo row (or arms the barriers)
-    bool armer;
+    unsigned long long* hup;    // [2][NCP] words from the up neighbour (its last row)
+    unsigned long long* hdn;    // [2][NCP] words from the down neighbour (its first row)
+    uint32_t up_hdn;        // shared::cluster address of the up neighbour's hdn
+    uint32_t dn_hup;        // shared::cluster address of the down neighbour's hup
+    int NCP;
     int* abort;             // CTA-wide abort flag (shared)
 };
 
+// smem layout: [2 tile slots][hup 2*NCP words][hdn 2*NCP words] (+ callers' areas)
 WT_DEV void xchg_setup(Xchg& X, const FusedParams& P, const Geo& g, float* tiles, int tile,
-                       uint64_t* mbar, int* abort) {
+                       int* abort) {
     X.tiles = tiles;
     X.tile = tile;
-    X.mbar = smem_addr(mbar);
-    X.par = 0;
+    X.NCP = P.NCP;
+    X.hup = reinterpret_cast<unsigned long long*>(tiles + 2 * tile);
+    X.hdn = X.hup + 2 * P.NCP;
     X.abort = abort;
-    X.expect = (uint32_t)((g.has_up + g.has_dn) * P.ny * 4);
-    const bool remote = P.C > 1;
-    X.armer = remote && threadIdx.x == 0;
-    X.waiter = remote && ((g.strip == 0 && g.has_up) || (g.strip == g.S - 1 && g.has_dn) || X.armer);
-    X.up_tile = X.dn_tile = X.up_mbar = X.dn_mbar = 0;
-    if (g.has_up) {
-        X.up_tile = map_shared_rank(tiles, g.cta - 1);
-        X.up_mbar = map_shared_rank(mbar, g.cta - 1);
-    }
-    if (g.has_dn) {
-        X.dn_tile = map_shared_rank(tiles, g.cta + 1);
-        X.dn_mbar = map_shared_rank(mbar, g.cta + 1);
-    }
-    if (X.armer) {
-        for (int p = 0; p < 3; ++p) mbar_init(X.mbar + 8 * p, 1);
-        fence_mbarrier_init_cluster();
-        for (int p = 0; p < 3; ++p) mbar_arrive_expect_tx(X.mbar + 8 * p, X.expect);
-    }
+    for (int i = threadIdx.x; i < 4 * P.NCP; i += blockDim.x) X.hup[i] = 0ull;   // tag 0: nothing yet
+    X.up_hdn = g.has_up ? map_shared_rank(X.hdn, g.cta - 1) : 0u;
+    X.dn_hup = g.has_dn ? map_shared_rank(X.hup, g.cta + 1) : 0u;
     if (threadIdx.x == 0) *abort = 0;
 }
 
-// Push the CTA's first / last row values (this thread's cell 0 / M-1 when it
-// owns them) into the neighbours' halo rows of slot `s` (st.async).
-WT_DEV void send_halo(const FusedParams& P, const Geo& g, const Xchg& X, int s, float first,
-                      float last) {
-    const int colo = (g.col + 1) * P.LD + OFF;
-    if (g.strip == 0 && g.has_up)         // my row 0 -> up neighbour's halo row R
-        st_async_f32(X.up_tile + 4u * (uint32_t)(s * X.tile + colo + P.R), first,
-                     X.up_mbar + 8u * s);
-    if (g.strip == g.S - 1 && g.has_dn)   // my row R-1 -> down neighbour's halo row -1
-        st_async_f32(X.dn_tile + 4u * (uint32_t)(s * X.tile + colo - 1), last,
-                     X.dn_mbar + 8u * s);
+// Words (bytes) of the exchange area that follows the two tile slots.
+constexpr int xchg_words(int NCP) { return 4 * NCP; }
+
+// Send the CTA's first / last row values of exchange k (this thread's cell
+// 0 / M-1 when its strip is a CTA boundary strip).
+WT_DEV void send_halo(const Geo& g, const Xchg& X, int k, float first, float last) {
+    const unsigned long long tag = (unsigned long long)(uint32_t)(k + 1) << 32;
+    const uint32_t off = 8u * (uint32_t)((k & 1) * X.NCP + g.col);
+    if (g.strip == 0 && g.has_up) st_cluster_u64(X.up_hdn + off, tag | __float_as_uint(first));
+    if (g.strip == g.S - 1 && g.has_dn) st_cluster_u64(X.dn_hup + off, tag | __float_as_uint(last));
 }
+
+// Wait (bounded) for exchange k's word at w and return its value.
+WT_DEV float recv_word(const FusedParams& P, const Xchg& X, const unsigned long long* w, int k) {
+    const uint32_t a = smem_addr(w);
+    const uint32_t tag = (uint32_t)(k + 1);
+    unsigned long long v = ld_cluster_u64(a);
+    if ((uint32_t)(v >> 32) != tag) {
+        const uint64_t t0 = global_ns();
+        for (uint32_t it = 1;; ++it) {
+            v = ld_cluster_u64(a);
+            if ((uint32_t)(v >> 32) == tag) break;
+            if ((it & 1023u) == 0 && global_ns() - t0 > WAIT_LIMIT_NS) {
+                atomicExch(P.err, WT_DEVERR_TIMEOUT);
+                *(volatile int*)X.abort = 1;
+                return 0.f;
+            }
+        }
+    }
+    return __uint_as_float((uint32_t)v);
+}
+
 template <int M>
 WT_DEV void store_column(const FusedParams& P, const Geo& g, const Xchg& X, int s,
                          const float (&v)[M]) {
     sts_col<M>(X.tiles + s * X.tile + (g.col + 1) * P.LD + OFF + g.xl0, v);
 }
-// Publish the thread's M new values into slot `s`: halo rows, then own column.
+
+// Publish the thread's M values as exchange k: halo words, then own column
+// into tile slot s.
 template <int M>
-WT_DEV void publish(const FusedParams& P, const Geo& g, const Xchg& X, int s, const float (&v)[M],
-                    bool remote) {
+WT_DEV void publish(const FusedParams& P, const Geo& g, const Xchg& X, int s, int k,
+                    const float (&v)[M]) {
     if (!g.colv) return;
-    if (remote) send_halo(P, g, X, s, v[0], v[M - 1]);
+    send_halo(g, X, k, v[0], v[M - 1]);
     store_column<M>(P, g, X, s, v);
 }
 
-// Wait until slot s holds the neighbours' halo rows, then re-arm its barrier.
-WT_DEV void xchg_wait(const FusedParams& P, Xchg& X, int s) {
-    if (!X.waiter) return;
-    const uint32_t parity = (X.par >> s) & 1u;
-    const uint32_t a = X.mbar + 8u * s;
-    if (!mbar_try_wait_parity(a, parity, WAIT_HINT_NS)) {
-        const uint64_t t0 = global_ns();
-        while (!mbar_try_wait_parity(a, parity, WAIT_HINT_NS)) {
-            if (global_ns() - t0 > WAIT_LIMIT_NS) {
-                atomicExch(P.err, WT_DEVERR_TIMEOUT);
-                *(volatile int*)X.abort = 1;
-                break;
-            }
-        }
-    }
-    X.par ^= 1u << s;
-    if (X.armer) mbar_arrive_expect_tx(a, X.expect);
-}
-
 // The thread's column of slot `slot`: left/right neighbour columns of its M
-// cells, and the two cells just above and below its strip.
+// cells, and the two cells just above and below its strip (from the tile, or
+// for a CTA boundary strip the neighbour's word of exchange k; k < 0: none,
+// the tile's zero halo rows stand for the field h_{-1} = 0).
 template <int M>
 struct Column {
     float lf[M], rt[M];
-    const float* colp;     // own cell 0 in the slot
+    float up, dn;
 };
 template <int M>
-WT_DEV void load_sides(Column<M>& c, const FusedParams& P, const Geo& g, const float* slot) {
-    c.colp = slot + (g.col + 1) * P.LD + OFF + g.xl0;
-    lds_col<M>(c.lf, c.colp - P.LD);
-    lds_col<M>(c.rt, c.colp + P.LD);
+WT_DEV void load_sides(Column<M>& c, const FusedParams& P, const Geo& g, const Xchg& X, int slot,
+                       int k) {
+    const float* colp = X.tiles + slot * X.tile + (g.col + 1) * P.LD + OFF + g.xl0;
+    lds_col<M>(c.lf, colp - P.LD);
+    lds_col<M>(c.rt, colp + P.LD);
+    c.up = colp[-1];
+    c.dn = colp[M];
+    if (k >= 0) {
+        if (g.strip == 0 && g.has_up) c.up = recv_word(P, X, X.hup + (k & 1) * X.NCP + g.col, k);
+        if (g.strip == g.S - 1 && g.has_dn) c.dn = recv_word(P, X, X.hdn + (k & 1) * X.NCP + g.col, k);
+    }
 }
-// Laplacian of cell i (0 < i < M-1 use registers for up/down; the ends read
-// the tile: a halo row for the CTA's boundary strips).
+
+// Laplacian of cell i (0 < i < M-1 use registers for up/down).
 template <int M, int ORDER>
 WT_DEV float lap_cell(const FusedParams& P, const Column<M>& c, const float (&ctr)[M], int i) {
-    float u = i == 0 ? c.colp[-1] : ctr[i - 1];
-    float d = i == M - 1 ? c.colp[M] : ctr[i + 1];
+    float u = i == 0 ? c.up : ctr[i - 1];
+    float d = i == M - 1 ? c.dn : ctr[i + 1];
     return lap5<ORDER>(u, c.lf[i], ctr[i], c.rt[i], d, P.k.lap_w, P.k.lap_w4);
 }
 
@@ -322,7 +326,6 @@ WT_DEV void load_bwd_coef(const FusedParams& P, const Geo& g, float (&X1)[M], fl
     }
 }
 
-WT_DEV int next3(int s) { return s == 2 ? 0 : s + 1; }
 
 // Sources (in table order) with the inputs prefetched one step ahead.
 template <int M>
@@ -338,29 +341,27 @@ WT_DEV void apply_sources(const FusedParams& P, const Taps& tp, float (&y)[M], f
     }
 }
 
-// h_t for the thread's cells from cur = h_{t-1} (registers + tile slot rs) and
-// inout = h_{t-2}; the result overwrites inout (ping-pong register sets).
-// The warps that read a halo row wait for it first (`halo`: slot rs carries
-// remote rows); then the strip's end cells are updated and, when `send`,
-// pushed straight to the neighbours (slot ws) before the interior cells are
-// computed, so the halo is in flight for a whole step before it is needed.
-// L receives Lap(h_{t-1}).  A thread that owns a source cell injects before
-// it sends (sources are few; that thread takes the plain order).
+// h_t for the thread's cells from cur = h_{t-1} (registers + tile slot rs,
+// halo words of exchange kr) and inout = h_{t-2}; the result overwrites inout
+// (ping-pong register sets) and is published as exchange ks into slot ws
+// (ks < 0: no halo words, the last step's have no reader).  The strip's end
+// cells are updated and sent first, so a neighbour's halo is in flight while
+// the interior cells are computed.  L receives Lap(h_{t-1}).  A thread that
+// owns a source cell on a halo row injects before it sends.
 template <int M, int ORDER>
-WT_DEV void fwd_update(const FusedParams& P, const Geo& g, Xchg& X, const Taps& tp, int rs,
-                       bool halo, int ws, bool send, float (&xv)[SRCMAX], int tnext,
+WT_DEV void fwd_update(const FusedParams& P, const Geo& g, const Xchg& X, const Taps& tp, int rs,
+                       int kr, int ws, int ks, float (&xv)[SRCMAX], int tnext,
                        const float (&A)[M], const float (&Bc)[M], const float (&C2)[M],
                        const float (&cur)[M], float (&inout)[M], float (&L)[M]) {
     if (!g.colv) return;   // padding columns read nothing (their tile columns do not exist)
-    if (halo) xchg_wait(P, X, rs);
     Column<M> c;
-    load_sides<M>(c, P, g, X.tiles + rs * X.tile);
+    load_sides<M>(c, P, g, X, rs, kr);
     L[0] = lap_cell<M, ORDER>(P, c, cur, 0);
     inout[0] = leapfrog(A[0], Bc[0], C2[0], P.k.two_over, cur[0], inout[0], L[0]);
     L[M - 1] = lap_cell<M, ORDER>(P, c, cur, M - 1);
     inout[M - 1] = leapfrog(A[M - 1], Bc[M - 1], C2[M - 1], P.k.two_over, cur[M - 1],
                             inout[M - 1], L[M - 1]);
-    if (send && !tp.src_edge) send_halo(P, g, X, ws, inout[0], inout[M - 1]);
+    if (ks >= 0 && !tp.src_edge) send_halo(g, X, ks, inout[0], inout[M - 1]);
 #pragma unroll
     for (int i = 1; i < M - 1; ++i) {
         L[i] = lap_cell<M, ORDER>(P, c, cur, i);
@@ -368,7 +369,7 @@ WT_DEV void fwd_update(const FusedParams& P, const Geo& g, Xchg& X, const Taps& 
     }
     if (tp.ns) {
         apply_sources<M>(P, tp, inout, xv, tnext);
-        if (send && tp.src_edge) send_halo(P, g, X, ws, inout[0], inout[M - 1]);
+        if (ks >= 0 && tp.src_edge) send_halo(g, X, ks, inout[0], inout[M - 1]);
     }
     store_column<M>(P, g, X, ws, inout);
 }
@@ -423,15 +424,14 @@ WT_DEV void store_checkpoint(const FusedParams& P, const Geo& g, int t, const fl
 
 // One step of the forward kernel (everything but the closing barrier).
 template <int M, int ORDER, bool FIELDS>
-WT_DEV void fwd_step(const FusedParams& P, const Geo& g, Xchg& X, const Taps& tp, FwdState& st,
-                     const ProbeRing& pr, int t, int rs, int ws, const float (&A)[M],
+WT_DEV void fwd_step(const FusedParams& P, const Geo& g, const Xchg& X, const Taps& tp,
+                     FwdState& st, const ProbeRing& pr, int t, const float (&A)[M],
                      const float (&Bc)[M], const float (&C2)[M], const float (&cur)[M],
                      float (&inout)[M]) {
     float L[M];
-    // h_{t-1} came with remote halo rows for every t >= 1 (h_{-1} = 0 is local);
-    // the last step's halos have no reader
-    fwd_update<M, ORDER>(P, g, X, tp, rs, t >= 1, ws, t + 1 < P.steps, st.xv, t + 1, A, Bc, C2,
-                         cur, inout, L);
+    // exchange t carries h_t; tile slot (t+1)&1 holds it (h_{-1} = 0 is slot 0)
+    fwd_update<M, ORDER>(P, g, X, tp, t & 1, t - 1, (t + 1) & 1, t + 1 < P.steps ? t : -1, st.xv,
+                         t + 1, A, Bc, C2, cur, inout, L);
     if (!g.colv) return;
     if (tp.np) {
         float* row = pr.buf + (size_t)st.pb * P.n_prb * P.PB + st.pc;
@@ -470,17 +470,16 @@ constexpr int bwd_max_threads(int M) { return M >= 10 ? 384 : 512; }
 template <int M, int ORDER, bool FIELDS>
 __global__ void __launch_bounds__(fwd_max_threads(M), 1) seq_fwd_fused_kernel(FusedParams P) {
     extern __shared__ __align__(16) float smem[];
-    __shared__ __align__(8) uint64_t mbar[3];
     __shared__ int abort_flag;
     const Geo g = make_geo(P, M);
     const int tile = (P.ny + 2) * P.LD;
     ProbeRing pr;
-    pr.buf = smem + 3 * tile;
+    pr.buf = smem + 2 * tile + 2 * xchg_words(P.NCP);
     pr.own = reinterpret_cast<int*>(pr.buf + 2 * P.n_prb * P.PB);
-    zero_smem(smem, 3 * tile);
+    zero_smem(smem, 2 * tile);
     for (int q = threadIdx.x; q < P.n_prb; q += blockDim.x) pr.own[q] = 0;
     Xchg X;
-    xchg_setup(X, P, g, smem, tile, mbar, &abort_flag);
+    xchg_setup(X, P, g, smem, tile, &abort_flag);
 
     float A[M], Bc[M], C2[M], ya[M], yb[M];
     load_fwd_coef<M>(P, g, A, Bc, C2);
@@ -500,11 +499,10 @@ __global__ void __launch_bounds__(fwd_max_threads(M), 1) seq_fwd_fused_kernel(Fu
         for (int e = 0; e < PRBMAX; ++e)
             if (e < tp.np) pr.own[tp.prb_col(e)] = tp.prb_intensity(e) ? 2 : 1;
     }
-    cluster_sync_all();   // zeroed tiles, flags and initialised barriers, cluster-wide
+    cluster_sync_all();   // zeroed tiles, halo words and flags, cluster-wide
 
     // ya holds h_{t-1} at even t, yb at odd t (the update overwrites h_{t-2});
     // the outer loop runs one checkpoint segment per iteration
-    int rs = 0;           // slot holding h_{t-1} (h_{-1} = 0 is slot 0)
     int chunk0 = 0;       // first step of the probe chunk being filled
     bool ok = true;
     for (int t0 = 0; t0 < P.steps && ok; t0 += P.seg) {
@@ -514,11 +512,9 @@ __global__ void __launch_bounds__(fwd_max_threads(M), 1) seq_fwd_fused_kernel(Fu
         }
         const int t1 = min(P.steps, t0 + P.seg);
         for (int t = t0; t < t1; ++t) {
-            const int ws = next3(rs);
-            if (t & 1) fwd_step<M, ORDER, FIELDS>(P, g, X, tp, st, pr, t, rs, ws, A, Bc, C2, yb, ya);
-            else       fwd_step<M, ORDER, FIELDS>(P, g, X, tp, st, pr, t, rs, ws, A, Bc, C2, ya, yb);
+            if (t & 1) fwd_step<M, ORDER, FIELDS>(P, g, X, tp, st, pr, t, A, Bc, C2, yb, ya);
+            else       fwd_step<M, ORDER, FIELDS>(P, g, X, tp, st, pr, t, A, Bc, C2, ya, yb);
             if (!(ok = exchange_end(X, t))) break;
-            rs = ws;
             if (++st.pc == P.PB) {
                 flush_probes(P, g, pr, st.pb, chunk0, P.PB);
                 st.pc = 0;
@@ -545,13 +541,14 @@ struct Stash {
 
 // Recompute step: like fwd_step, but stashes Lap(h_{t-1}) instead of writing outputs.
 template <int M, int ORDER>
-WT_DEV void rec_step(const FusedParams& P, const Geo& g, Xchg& X, const Taps& tp,
-                     float (&xv)[SRCMAX], int t, int t0, int t1, int rs, int ws,
+WT_DEV void rec_step(const FusedParams& P, const Geo& g, const Xchg& X, const Taps& tp,
+                     float (&xv)[SRCMAX], int t, int t0, int t1, int kx,
                      const Stash<M>& sh, const float (&A)[M], const float (&Bc)[M],
                      const float (&C2)[M], const float (&cur)[M], float (&inout)[M]) {
     float L[M];
-    fwd_update<M, ORDER>(P, g, X, tp, rs, true, ws, t + 1 < t1, xv, t + 1 < t1 ? t + 1 : -1, A,
-                         Bc, C2, cur, inout, L);
+    // reads exchange kx (slot kx&1), publishes exchange kx+1 when the segment goes on
+    fwd_update<M, ORDER>(P, g, X, tp, kx & 1, kx, (kx + 1) & 1, t + 1 < t1 ? kx + 1 : -1, xv,
+                         t + 1 < t1 ? t + 1 : -1, A, Bc, C2, cur, inout, L);
     if (!g.colv) return;
     sts_col<M>(sh.step(t - t0), L);
 }
@@ -588,14 +585,13 @@ WT_DEV void adj_cell(float lg, float lam, float Ly, float X1, float Kc, float Ky
 template <int M, int ORDER>
 __global__ void __launch_bounds__(bwd_max_threads(M), 1) seq_bwd_fused_kernel(FusedParams P) {
     extern __shared__ __align__(16) float smem[];
-    __shared__ __align__(8) uint64_t mbar[3];
     __shared__ int abort_flag;
     const Geo g = make_geo(P, M);
     const int NT = blockDim.x;
     const int tile = (P.ny + 2) * P.LD;
-    zero_smem(smem, 3 * tile);
+    zero_smem(smem, 2 * tile);
     Xchg X;
-    xchg_setup(X, P, g, smem, tile, mbar, &abort_flag);
+    xchg_setup(X, P, g, smem, tile, &abort_flag);
     Taps tp;
     build_taps<M>(P, g, tp);
 
@@ -603,7 +599,7 @@ __global__ void __launch_bounds__(bwd_max_threads(M), 1) seq_bwd_fused_kernel(Fu
     const size_t bplane = (size_t)P.batch * plane;
     // adjoint seeds of all probe columns, staged per chunk of PB adjoint
     // steps: seeds[2][n_prb][PB], u = T-1-t counts adjoint steps
-    float* seeds = smem + 3 * tile;
+    float* seeds = smem + 2 * tile + 2 * xchg_words(P.NCP);
     Stash<M> sh;
     sh.NT = NT;
     sh.p = P.stash_smem ? seeds + ((2 * P.n_prb * P.PB + 3) & ~3) + (size_t)threadIdx.x * M
@@ -621,7 +617,7 @@ __global__ void __launch_bounds__(bwd_max_threads(M), 1) seq_bwd_fused_kernel(Fu
 
     cluster_sync_all();
     const int nseg = (P.steps + P.seg - 1) / P.seg;
-    int xs = 0;           // next slot to publish into
+    int kx = 0;           // exchange index (tile slot kx & 1)
     bool ok = true;
     for (int sgi = nseg - 1; sgi >= 0 && ok; --sgi) {
         const int t0 = sgi * P.seg;
@@ -643,10 +639,8 @@ __global__ void __launch_bounds__(bwd_max_threads(M), 1) seq_bwd_fused_kernel(Fu
                     }
                 }
             }
-            publish<M>(P, g, X, xs, ya, true);
+            publish<M>(P, g, X, kx & 1, kx, ya);
             if (!(ok = exchange_end(X, 0))) break;
-            int rs = xs;
-            xs = next3(xs);
             float A[M], Bc[M], C2[M];
             load_fwd_coef<M>(P, g, A, Bc, C2);
             float xv[SRCMAX];
@@ -654,16 +648,14 @@ __global__ void __launch_bounds__(bwd_max_threads(M), 1) seq_bwd_fused_kernel(Fu
             for (int e = 0; e < SRCMAX; ++e)
                 xv[e] = (e < tp.ns) ? __ldg(P.x + (size_t)tp.src_row(e) * P.steps + t0) : 0.f;
             for (int t = t0; t < t1;) {
-                rec_step<M, ORDER>(P, g, X, tp, xv, t, t0, t1, rs, xs, sh, A, Bc, C2, ya, yb);
+                rec_step<M, ORDER>(P, g, X, tp, xv, t, t0, t1, kx, sh, A, Bc, C2, ya, yb);
+                ++kx;             // exchange kx consumed (the last one of the segment too)
                 if (++t >= t1) break;
                 if (!(ok = exchange_end(X, t))) break;
-                rs = xs;
-                xs = next3(xs);
-                rec_step<M, ORDER>(P, g, X, tp, xv, t, t0, t1, rs, xs, sh, A, Bc, C2, yb, ya);
+                rec_step<M, ORDER>(P, g, X, tp, xv, t, t0, t1, kx, sh, A, Bc, C2, yb, ya);
+                ++kx;
                 if (++t >= t1) break;
                 if (!(ok = exchange_end(X, t))) break;
-                rs = xs;
-                xs = next3(xs);
             }
             if (!ok) break;
         }
@@ -691,7 +683,7 @@ __global__ void __launch_bounds__(bwd_max_threads(M), 1) seq_bwd_fused_kernel(Fu
                 }
 #pragma unroll
                 for (int i = 0; i < M; ++i) c2g[i] = fmul(Kg[i], lam[i]);
-                publish<M>(P, g, X, xs, c2g, true);
+                publish<M>(P, g, X, kx & 1, kx, c2g);
                 if (P.grad_x && tp.ns) {
 #pragma unroll
                     for (int e = 0; e < SRCMAX; ++e)
@@ -703,21 +695,24 @@ __global__ void __launch_bounds__(bwd_max_threads(M), 1) seq_bwd_fused_kernel(Fu
             ++u;
             if (g.colv) {
                 Column<M> c;
-                load_sides<M>(c, P, g, X.tiles + xs * X.tile);
+                load_sides<M>(c, P, g, X, kx & 1, -1);   // interior first; halo words below
                 float Ly[M];
                 lds_col<M>(Ly, sh.step(t - t0));
 #pragma unroll
                 for (int i = 1; i < M - 1; ++i)
                     adj_cell(lap_cell<M, ORDER>(P, c, c2g, i), lam[i], Ly[i], X1[i], Kc[i], Ky2[i],
                              P.k.dt2, acc[i], gy1[i], gy2a[i], gy2b[i]);
-                xchg_wait(P, X, xs);
+                if (g.strip == 0 && g.has_up)
+                    c.up = recv_word(P, X, X.hup + (kx & 1) * X.NCP + g.col, kx);
+                if (g.strip == g.S - 1 && g.has_dn)
+                    c.dn = recv_word(P, X, X.hdn + (kx & 1) * X.NCP + g.col, kx);
                 adj_cell(lap_cell<M, ORDER>(P, c, c2g, 0), lam[0], Ly[0], X1[0], Kc[0], Ky2[0],
                          P.k.dt2, acc[0], gy1[0], gy2a[0], gy2b[0]);
                 adj_cell(lap_cell<M, ORDER>(P, c, c2g, M - 1), lam[M - 1], Ly[M - 1], X1[M - 1],
                          Kc[M - 1], Ky2[M - 1], P.k.dt2, acc[M - 1], gy1[M - 1], gy2a[M - 1],
                          gy2b[M - 1]);
             }
-            xs = next3(xs);
+            ++kx;
         }
     }
     if (g.colv && ok) {
@@ -762,11 +757,11 @@ static int pick_strip(int nx, int C, int NCP, const int* Ms, int nM, bool fwd) {
     return best;
 }
 
-// Pick the cluster size C and the strip heights (the adjoint kernel favours
-// tall strips: its per-cell state is large; the forward favours more
-// threads); then the checkpoint interval: the largest stash that fits in
-// shared memory next to the three tiles and the probe ring buffers (at least
-// 4 steps), else a sqrt(T) interval with the stash in global memory.
+// Pick the cluster size C and the strip heights (10-cell strips where they
+// fit: per-step overhead amortised over more cells); then the checkpoint
+// interval: the largest stash that fits in shared memory next to the two
+// tiles, the halo words and the probe ring buffers (at least 4 steps), else
+// a sqrt(T) interval with the stash in global memory.
 int wt_fused_plan(int nx, int ny, int steps, int n_prb, int cluster_req, int seg_req,
                   WtFusedLaunch* L) {
     const int NCP = ((ny + 31) / 32) * 32;
@@ -788,8 +783,10 @@ int wt_fused_plan(int nx, int ny, int steps, int n_prb, int cluster_req, int seg
         const int rows = (nx + C - 1) / C;
         const int R = ((rows + M - 1) / M) * M, fR = ((rows + fM - 1) / fM) * fM;
         const int LD = tile_ld(R, M), fLD = tile_ld(fR, fM);
-        const size_t tiles = 3 * (size_t)(ny + 2) * LD * sizeof(float);
-        const size_t ftiles = 3 * (size_t)(ny + 2) * fLD * sizeof(float);
+        // two tile slots + the halo words [2 parities][up, down][NCP]
+        const size_t words = (size_t)wt::xchg_words(NCP) * 8;
+        const size_t tiles = 2 * (size_t)(ny + 2) * LD * sizeof(float) + words;
+        const size_t ftiles = 2 * (size_t)(ny + 2) * fLD * sizeof(float) + words;
         if (tiles + aux_bwd > SMEM_MAX || ftiles + aux_fwd > SMEM_MAX) continue;
         L->C = C; L->NCP = NCP; L->PB = PB;
         L->M = M; L->R = R; L->S = R / M; L->LD = LD; L->threads = (R / M) * NCP;
