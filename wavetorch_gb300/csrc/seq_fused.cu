@@ -140,7 +140,7 @@ WT_DEV void xchg_setup(Xchg& X, const FusedParams& P, const Geo& g, float* tiles
 }
 
 // Words (bytes) of the exchange area that follows the two tile slots.
-__host__ __device__ constexpr int xchg_words(int NCP) { return 4 * NCP; }
+constexpr int xchg_words(int NCP) { return 4 * NCP; }
 
 // Send the CTA's first / last row values of exchange k (this thread's cell
 // 0 / M-1 when its strip is a CTA boundary strip).
@@ -151,27 +151,23 @@ WT_DEV void send_halo(const Geo& g, const Xchg& X, int k, float first, float las
     if (g.strip == g.S - 1 && g.has_dn) st_cluster_u64(X.dn_hup + off, tag | __float_as_uint(last));
 }
 
-// Spin (bounded) until the word at shared address a carries `tag`; out of
-// line so the step's code stays small (the first probe usually succeeds).
-__device__ __noinline__ unsigned long long spin_word(int* err, int* abort, uint32_t a, uint32_t tag) {
-    const uint64_t t0 = global_ns();
-    for (uint32_t it = 1;; ++it) {
-        unsigned long long v = ld_cluster_u64(a);
-        if ((uint32_t)(v >> 32) == tag) return v;
-        if ((it & 1023u) == 0 && global_ns() - t0 > WAIT_LIMIT_NS) {
-            atomicExch(err, WT_DEVERR_TIMEOUT);
-            *(volatile int*)abort = 1;
-            return 0ull;
-        }
-    }
-}
-
-// Exchange k's value from the word at w (waiting for it when needed).
+// Wait (bounded) for exchange k's word at w and return its value.
 WT_DEV float recv_word(const FusedParams& P, const Xchg& X, const unsigned long long* w, int k) {
     const uint32_t a = smem_addr(w);
     const uint32_t tag = (uint32_t)(k + 1);
     unsigned long long v = ld_cluster_u64(a);
-    if ((uint32_t)(v >> 32) != tag) v = spin_word(P.err, X.abort, a, tag);
+    if ((uint32_t)(v >> 32) != tag) {
+        const uint64_t t0 = global_ns();
+        for (uint32_t it = 1;; ++it) {
+            v = ld_cluster_u64(a);
+            if ((uint32_t)(v >> 32) == tag) break;
+            if ((it & 1023u) == 0 && global_ns() - t0 > WAIT_LIMIT_NS) {
+                atomicExch(P.err, WT_DEVERR_TIMEOUT);
+                *(volatile int*)X.abort = 1;
+                return 0.f;
+            }
+        }
+    }
     return __uint_as_float((uint32_t)v);
 }
 
@@ -394,7 +390,7 @@ struct ProbeRing {
 };
 
 // Write chunk `b` (steps t0 .. t0+n-1) of the probes this CTA owns.
-__device__ __noinline__ void flush_probes(const FusedParams& P, const Geo& g, const ProbeRing& pr, int b, int t0,
+WT_DEV void flush_probes(const FusedParams& P, const Geo& g, const ProbeRing& pr, int b, int t0,
                          int n) {
     const int tot = P.n_prb * P.PB;
     for (int idx = threadIdx.x; idx < tot; idx += blockDim.x) {
@@ -505,18 +501,19 @@ __global__ void __launch_bounds__(fwd_max_threads(M), 1) seq_fwd_fused_kernel(Fu
     }
     cluster_sync_all();   // zeroed tiles, halo words and flags, cluster-wide
 
-    // ya holds h_{t-1}, yb h_{t-2}; the outer loop runs one checkpoint
-    // segment per iteration
+    // ya holds h_{t-1} at even t, yb at odd t (the update overwrites h_{t-2});
+    // the outer loop runs one checkpoint segment per iteration
     int chunk0 = 0;       // first step of the probe chunk being filled
     bool ok = true;
     for (int t0 = 0; t0 < P.steps && ok; t0 += P.seg) {
-        if (t0 > 0) store_checkpoint<M>(P, g, t0, ya, yb);
+        if (t0 > 0) {
+            if (t0 & 1) store_checkpoint<M>(P, g, t0, yb, ya);
+            else        store_checkpoint<M>(P, g, t0, ya, yb);
+        }
         const int t1 = min(P.steps, t0 + P.seg);
         for (int t = t0; t < t1; ++t) {
-            // one copy of the step: ya = h_{t-1}, yb = h_{t-2} -> h_t, then rotate
-            fwd_step<M, ORDER, FIELDS>(P, g, X, tp, st, pr, t, A, Bc, C2, ya, yb);
-#pragma unroll
-            for (int i = 0; i < M; ++i) { float h = ya[i]; ya[i] = yb[i]; yb[i] = h; }
+            if (t & 1) fwd_step<M, ORDER, FIELDS>(P, g, X, tp, st, pr, t, A, Bc, C2, yb, ya);
+            else       fwd_step<M, ORDER, FIELDS>(P, g, X, tp, st, pr, t, A, Bc, C2, ya, yb);
             if (!(ok = exchange_end(X, t))) break;
             if (++st.pc == P.PB) {
                 flush_probes(P, g, pr, st.pb, chunk0, P.PB);
@@ -652,9 +649,11 @@ __global__ void __launch_bounds__(bwd_max_threads(M), 1) seq_bwd_fused_kernel(Fu
                 xv[e] = (e < tp.ns) ? __ldg(P.x + (size_t)tp.src_row(e) * P.steps + t0) : 0.f;
             for (int t = t0; t < t1;) {
                 rec_step<M, ORDER>(P, g, X, tp, xv, t, t0, t1, kx, sh, A, Bc, C2, ya, yb);
-#pragma unroll
-                for (int i = 0; i < M; ++i) { float h = ya[i]; ya[i] = yb[i]; yb[i] = h; }
                 ++kx;             // exchange kx consumed (the last one of the segment too)
+                if (++t >= t1) break;
+                if (!(ok = exchange_end(X, t))) break;
+                rec_step<M, ORDER>(P, g, X, tp, xv, t, t0, t1, kx, sh, A, Bc, C2, yb, ya);
+                ++kx;
                 if (++t >= t1) break;
                 if (!(ok = exchange_end(X, t))) break;
             }
