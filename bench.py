@@ -150,13 +150,17 @@ def measured_peaks():
 
 
 def committed_traffic(kernel: str):
-    """Per-launch DRAM bytes of `kernel` from the committed ncu summary."""
-    p = os.path.join(HERE, "profiles", "traffic.json")
+    """Per-launch DRAM bytes of `kernel` from the committed ncu summary
+    (`profiles/traffic.txt`: `name bytes` lines, `#` comments)."""
+    p = os.path.join(HERE, "profiles", "traffic.txt")
     if not os.path.exists(p):
         return None
     with open(p) as fh:
-        d = json.load(fh)
-    return d.get(kernel)
+        for line in fh:
+            f = line.split("#", 1)[0].split()
+            if len(f) == 2 and f[0] == kernel:
+                return int(f[1])
+    return None
 
 
 # ---------------------------------------------------------------------------

@@ -96,6 +96,20 @@ def test_fused_tap_capacity(lib):
     assert lib.wt_seq_workspace_bytes(C.byref(d), C.byref(n)) == _lib.WT_OK
 
 
+def test_fused_plan_size_limit(lib):
+    """The fused form plans instances that fit one cluster (up to 160x160);
+    WaveRNN sends larger grids to the plain form."""
+    from wavetorch_gb300.functional import SeqSpec, fused_supported
+    assert fused_supported(SeqSpec(2, 160, 160, 100, [(5, -1)], [(7, 1, 0)]))
+    assert not fused_supported(SeqSpec(2, 161, 161, 100, [(5, -1)], [(7, 1, 0)]))
+    assert not fused_supported(SeqSpec(1, 1024, 1024, 100, [(5, -1)], [(7, 1, 0)]))
+    # the plain form takes any grid
+    spec = SeqSpec(1, 1024, 1024, 100, [(5, -1)], [(7, 1, 0)], form=0)
+    d, keep = spec.desc()
+    n = C.c_size_t(0)
+    assert lib.wt_seq_workspace_bytes(C.byref(d), C.byref(n)) == 0
+
+
 def test_step_entry_points_validate_before_touching_the_device(lib):
     from wavetorch_gb300 import _lib
     sc = _lib.Scalars(0.707, 1.0, 0)

@@ -13,6 +13,7 @@ else raises (there is no CPU path).
 from __future__ import annotations
 
 import ctypes as C
+import dataclasses
 from dataclasses import dataclass
 from typing import Optional, Sequence
 
@@ -144,6 +145,15 @@ def seq_workspace_bytes(spec: SeqSpec) -> int:
     n = C.c_size_t(0)
     _lib.check(_lib.load().wt_seq_workspace_bytes(C.byref(d), C.byref(n)), "wt_seq_workspace_bytes")
     return int(n.value)
+
+
+def fused_supported(spec: SeqSpec) -> bool:
+    """Whether the fused form can plan this sequence: the whole instance must
+    fit on one thread-block cluster (square grids up to 160x160 cells).  Any
+    other error is left for the real call to report."""
+    d, keep = dataclasses.replace(spec, form=_lib.WT_FORM_FUSED).desc()
+    n = C.c_size_t(0)
+    return _lib.load().wt_seq_workspace_bytes(C.byref(d), C.byref(n)) != _lib.WT_ERR_UNSUPPORTED
 
 
 def seq_forward(spec: SeqSpec, sc: _lib.Scalars, b, c, x, want_sum: bool = False):

@@ -4,7 +4,8 @@ For the reference's own source and probe types and a linear cell, the whole
 loop is one :class:`~wavetorch_gb300.functional.WaveSeqFn` call:
 
 * ``form='fused'`` (default): persistent cluster kernels, sqrt(T)-style
-  checkpoints and segment recompute in the adjoint;
+  checkpoints and segment recompute in the adjoint; grids too large for one
+  thread-block cluster run in the plain form instead;
 * ``form='plain'``: one forward kernel per step with every field kept, and one
   adjoint kernel per step -- the reference's dataflow, bit-exact with it;
 * ``form='step'``: the reference's Python loop structure, each step a
@@ -16,7 +17,7 @@ from __future__ import annotations
 import torch
 
 from . import _lib
-from .functional import SeqSpec, WaveSeqFn, lap_order, scalars
+from .functional import SeqSpec, WaveSeqFn, fused_supported, lap_order, scalars
 from .probe import WaveProbe
 from .source import WaveSource
 
@@ -109,6 +110,8 @@ class WaveRNN(torch.nn.Module):
                        [] if fields_out else ptab,
                        form=_FORMS[form if form in _FORMS else "fused"], segment=self.segment,
                        cluster=self.cluster, output_fields=fields_out)
+        if spec.form == _lib.WT_FORM_FUSED and not fused_supported(spec):
+            spec.form = _lib.WT_FORM_PLAIN   # instance too large for one cluster
         b = geom.b
         out = WaveSeqFn.apply(c, b, x.contiguous(), spec, sc)
         if fields_out:
