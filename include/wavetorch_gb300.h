@@ -187,6 +187,29 @@ int wt_rho_to_c_bwd(const wt_geom_desc* g, const float* rho, const float* blur_k
 /* Bytes of `work` the two calls above need (2 * nx * ny floats). */
 int wt_rho_to_c_work_bytes(const wt_geom_desc* g, size_t* bytes);
 
+/* The forward above for callers that cannot hand the library a work buffer:
+ * code that runs where no allocator is at hand (a C or ctypes caller without
+ * torch or a memory pool) or where allocating is not allowed (a loop whose
+ * device memory was budgeted up front, where a cudaMalloc would also
+ * synchronise the device).  It writes the same c as wt_rho_to_c_fwd and
+ * allocates nothing: its scratch is one array of WT_RHO_TO_C_NOALLOC_MAX_CELLS
+ * x 2 floats (8 MiB) in the library's own static device memory.
+ *   - Grids of more than WT_RHO_TO_C_NOALLOC_MAX_CELLS cells are refused with
+ *     WT_ERR_UNSUPPORTED before anything runs; use wt_rho_to_c_fwd for them.
+ *   - The first call on each device looks up that device's copy of the array
+ *     (with the device current); make it before any stream capture begins.
+ *   - Every call on a device shares that one array.  No part of it has to
+ *     start at zero (each call writes every element it reads), but calls
+ *     whose executions overlap (different streams, or host threads, without
+ *     ordering between them) race on it and may return wrong c.
+ *   - It keeps no state for wt_rho_to_c_bwd: a backward needs the forward
+ *     with a caller-owned `work`.
+ * No counterpart in the reference, whose rho -> c runs in torch ops that
+ * allocate their intermediates.                                             */
+#define WT_RHO_TO_C_NOALLOC_MAX_CELLS 1048576   /* 1024 x 1024 */
+int wt_rho_to_c_fwd_noalloc(const wt_geom_desc* g, const float* rho, const float* blur_kernel,
+                            float* c, wt_stream_t stream);
+
 #ifdef __cplusplus
 }
 #endif

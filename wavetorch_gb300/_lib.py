@@ -29,7 +29,7 @@ EXPORTED = [
     "wt_version", "wt_status_string", "wt_last_error", "wt_kernel_launches",
     "wt_step_fwd", "wt_step_bwd",
     "wt_seq_workspace_bytes", "wt_seq_fwd", "wt_seq_bwd", "wt_seq_device_status",
-    "wt_rho_to_c_fwd", "wt_rho_to_c_bwd", "wt_rho_to_c_work_bytes",
+    "wt_rho_to_c_fwd", "wt_rho_to_c_bwd", "wt_rho_to_c_work_bytes", "wt_rho_to_c_fwd_noalloc",
 ]
 
 
@@ -92,6 +92,7 @@ def _declare(lib):
     lib.wt_rho_to_c_fwd.argtypes = [P(GeomDesc), _VP, _VP, _VP, _VP, _VP]
     lib.wt_rho_to_c_bwd.argtypes = [P(GeomDesc), _VP, _VP, _VP, _VP, _VP, _VP]
     lib.wt_rho_to_c_work_bytes.argtypes = [P(GeomDesc), P(C.c_size_t)]
+    lib.wt_rho_to_c_fwd_noalloc.argtypes = [P(GeomDesc), _VP, _VP, _VP, _VP]
     for name in EXPORTED:
         if name not in ("wt_version", "wt_status_string", "wt_last_error", "wt_kernel_launches"):
             getattr(lib, name).restype = C.c_int

@@ -169,3 +169,45 @@ extern "C" int wt_rho_to_c_bwd(const wt_geom_desc* d, const float* rho, const fl
     // odd n starts in tmp and ends in grad_rho, even n starts and ends in grad_rho.
     return wt_cuda_status(cudaGetLastError());
 }
+
+// ---------------------------------------------------------------------------
+// wt_rho_to_c_fwd_noalloc: the same forward with its scratch (tanh values and
+// blurred density, 2 floats per cell) in this file-scope array instead of a
+// caller-owned buffer.  Each device has its own copy; the address of the
+// current device's copy is looked up once and cached.
+#include <mutex>
+
+static __device__ __align__(256) float g_rho_to_c_scratch[2 * (size_t)WT_RHO_TO_C_NOALLOC_MAX_CELLS];
+
+static constexpr int NOALLOC_MAX_DEVICES = 64;
+static std::mutex g_noalloc_mu;
+static float* g_noalloc_scratch[NOALLOC_MAX_DEVICES] = {};
+
+// Address of the current device's scratch array (looked up on first use).
+static int noalloc_scratch(float** out) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return wt_cuda_status(e);
+    if (dev < 0 || dev >= NOALLOC_MAX_DEVICES) return WT_ERR_UNSUPPORTED;
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    if (!g_noalloc_scratch[dev]) {
+        void* p = nullptr;
+        e = cudaGetSymbolAddress(&p, g_rho_to_c_scratch);
+        if (e != cudaSuccess) return wt_cuda_status(e);
+        g_noalloc_scratch[dev] = static_cast<float*>(p);
+    }
+    *out = g_noalloc_scratch[dev];
+    return WT_OK;
+}
+
+extern "C" int wt_rho_to_c_fwd_noalloc(const wt_geom_desc* d, const float* rho,
+                                       const float* blur_kernel, float* c, wt_stream_t stream) {
+    if (!d || d->nx <= 0 || d->ny <= 0) return WT_ERR_INVALID;
+    if ((size_t)d->nx * (size_t)d->ny > (size_t)WT_RHO_TO_C_NOALLOC_MAX_CELLS)
+        return WT_ERR_UNSUPPORTED;
+    if (!rho || !c || (d->blur_n > 0 && !blur_kernel)) return WT_ERR_INVALID;
+    float* work = nullptr;
+    int st = noalloc_scratch(&work);
+    if (st) return st;
+    return wt_rho_to_c_fwd(d, rho, blur_kernel, c, work, stream);
+}
