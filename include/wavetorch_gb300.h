@@ -125,10 +125,21 @@ typedef struct wt_seq_desc {
     int32_t n_probes;
     const wt_probe_entry* probes_host;     /* host array, n_probes entries   */
     int32_t form;                          /* WT_FORM_PLAIN / WT_FORM_FUSED  */
-    int32_t segment;                       /* checkpoint interval, 0 = auto  */
+    int32_t segment;                       /* fused adjoint mode, see below  */
     int32_t cluster;                       /* CTAs per instance, 0 = auto    */
     int32_t output_fields;                 /* 1: also write every field      */
 } wt_seq_desc;
+
+/* `segment` chooses how the fused form's adjoint gets the forward's fields:
+ *   -1  tape: the forward stores Lap(h_{t-1}) of every cell and step
+ *       (about steps x batch x nx x ny floats of workspace, plus the padding
+ *       of the kernels' strips) and the adjoint streams it back; no
+ *       recompute.
+ *   >0  checkpoints every `segment` steps; the adjoint recomputes each
+ *       segment's forward (workspace ~ 2 fields per segment).
+ *    0  automatic: the tape when it takes at most 16 GiB, else checkpoints at
+ *       the largest interval whose recompute stash fits in shared memory.
+ * Both modes give identical results.  The plain form ignores it.            */
 
 /* Bytes of workspace that wt_seq_fwd must be given and that must be handed,
  * unchanged, to wt_seq_bwd (checkpoints or the full field history, plus the

@@ -112,14 +112,15 @@ def test_zero_input_is_silent(cuda):
 
 
 def test_ragged_segments(cuda):
-    """Checkpoint intervals that do not divide T give the same adjoint."""
+    """Checkpoint intervals that do not divide T, and the tape mode, give the
+    same adjoint."""
     b, c, x, _, src, prb = cfg1_problem(cuda, B=3, N=120, steps=301)
     B, steps = x.shape
     sc = scalars(0.707, 1.0, lap_order(B, 120, 120, 1.0))
     g = torch.randn(B, steps, 3, generator=torch.Generator().manual_seed(8)).to(cuda)
     ref_spec = SeqSpec(B, 120, 120, steps, src, prb, form=_lib.WT_FORM_PLAIN)
     _, gref = run(ref_spec, sc, b, c, x, g)
-    for seg in (1, 7, 64, 301, 1000):
+    for seg in (1, 7, 64, 301, 1000, -1):   # -1: tape mode
         spec = SeqSpec(B, 120, 120, steps, src, prb, form=_lib.WT_FORM_FUSED, segment=seg)
         _, gf = run(spec, sc, b, c, x, g)
         assert rel(gf.cpu().numpy(), gref.cpu().numpy()) <= 1e-6, seg
@@ -143,3 +144,21 @@ def test_cluster_sizes_agree(cuda, cluster):
                       sc, b, c, x, g)
     assert torch.equal(p_out, f_out)
     assert rel(f_gc.cpu().numpy(), p_gc.cpu().numpy()) <= 1e-6
+
+
+def test_tape_and_checkpoint_modes_agree_bitwise(cuda):
+    """B=32, 120x120, first 700 steps: the adjoint that streams the stored
+    Laplacians back and the one that recomputes segments from checkpoints do
+    the same arithmetic on the same values, so dL/dc is identical."""
+    b, c, x, _, src, prb = cfg1_problem(cuda, B=32, N=120, steps=3500)
+    x = x[:, :700].contiguous()
+    B, steps = x.shape
+    sc = scalars(0.707, 1.0, lap_order(B, 120, 120, 1.0))
+    g = torch.randn(B, steps, 3, generator=torch.Generator().manual_seed(12)).to(cuda)
+    res = {}
+    for seg in (-1, 0, 11, 50):
+        spec = SeqSpec(B, 120, 120, steps, src, prb, form=_lib.WT_FORM_FUSED, segment=seg)
+        res[seg] = run(spec, sc, b, c, x, g)
+    for seg in (0, 11, 50):
+        assert torch.equal(res[seg][0], res[-1][0]), seg
+        assert torch.equal(res[seg][1], res[-1][1]), seg

@@ -182,3 +182,31 @@ def test_cfg0_error_vs_fp64_is_at_the_reference_floor(cuda):
     ours = rel(y.detach().cpu().numpy(), d["out64"])
     theirs = rel(d["out"], d["out64"])
     assert ours <= 2 * theirs + 1e-6
+
+
+def test_in_place_edits_of_coordinates_and_scalars_are_seen(cuda):
+    """The host keeps copies of small device buffers (probe and source
+    coordinates, dt) to avoid a device read per forward; an in-place edit of
+    such a buffer must reach the next forward."""
+    d = golden("cfg1_small")
+    m = build_model(d, cuda, "fused")
+    x = T(d["x"], cuda)
+    with torch.no_grad():
+        y1 = m(x)
+        px = int(m.probes[0].x.item())
+        m.probes[0].x.fill_(px + 3)
+        m.sources[0].y.add_(2)
+        y2 = m(x)
+        m.cell.dt.fill_(0.5)
+        y3 = m(x)
+    ref = build_model(d, cuda, "fused")
+    with torch.no_grad():
+        ref.probes[0].x.fill_(px + 3)
+        ref.sources[0].y.add_(2)
+        r2 = ref(x)
+        ref.cell.dt.fill_(0.5)
+        r3 = ref(x)
+    assert not torch.equal(y1, y2)
+    assert torch.equal(y2, r2)
+    assert not torch.equal(y2, y3)
+    assert torch.equal(y3, r3)

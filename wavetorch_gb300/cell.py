@@ -7,7 +7,7 @@ import numpy as np
 import torch
 
 from .functional import WaveStepFn, _f32
-from .utils import to_tensor
+from .utils import host_scalar, to_tensor
 
 
 def saturable_damping(u, uth, b0):
@@ -47,11 +47,11 @@ class WaveCell(torch.nn.Module):
     def scalars(self):
         """Python values of (dt, h, satdamp_b0, satdamp_uth, c_nl) -- one host
         read per sequence instead of one per step."""
-        return (_f32(self.dt), _f32(self.geom.h), float(self.satdamp_b0), float(self.satdamp_uth),
-                float(self.c_nl))
+        return (_f32(self.dt), _f32(self.geom.h), float(host_scalar(self.satdamp_b0)),
+                float(host_scalar(self.satdamp_uth)), float(host_scalar(self.c_nl)))
 
     def is_linear(self) -> bool:
-        return not (float(self.satdamp_b0) > 0 or float(self.c_nl) != 0)
+        return not (float(host_scalar(self.satdamp_b0)) > 0 or float(host_scalar(self.c_nl)) != 0)
 
     def forward(self, h1, h2, c_linear, rho, _scalars=None):
         """Take a step through time: returns (y_{t+1}, y_t).

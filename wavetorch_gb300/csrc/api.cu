@@ -90,6 +90,10 @@ extern "C" int wt_step_bwd(const wt_scalars* s, int32_t batch, int32_t nx, int32
 namespace {
 
 constexpr size_t ALIGN = 256;
+// Automatic choice of the fused adjoint's mode: the tape (every step's
+// Laplacian, T x batch x nx x pitch floats) when it takes at most this many
+// bytes, else checkpoints with segment recompute.
+constexpr size_t WT_TAPE_AUTO_MAX_BYTES = (size_t)16 << 30;
 size_t up(size_t v) { return (v + ALIGN - 1) / ALIGN * ALIGN; }
 
 struct SeqPlan {
@@ -104,9 +108,10 @@ struct SeqPlan {
     // float areas
     size_t o_amp;
     size_t o_hist, o_zero, o_lam, o_gc;             // plain
-    size_t o_ckpt, o_stash, o_gcpart;               // fused
+    size_t o_ckpt, o_stash, o_gcpart, o_lap;        // fused
     size_t total;
     int seg, nseg;
+    bool tape;                                      // fused: tape mode
     WtFusedLaunch L;
 };
 
@@ -153,13 +158,29 @@ int make_plan(const wt_seq_desc* d, SeqPlan* p) {
         P.o_lam = o; o = up(o + 3 * bp * F);
         P.o_gc = o; o = up(o + bp * F);
     } else {
+        if (d->segment < -1) return WT_ERR_INVALID;
         int st = wt_fused_plan(P.nx, P.ny, P.T, P.np, d->cluster, d->segment, &P.L);
         if (st) return st;
-        const size_t per_step = (size_t)P.B * P.L.C * P.L.M * P.L.threads * F;
-        P.seg = P.L.seg;
-        P.nseg = (P.T + P.seg - 1) / P.seg;
-        P.o_ckpt = o; o = up(o + (size_t)P.nseg * 2 * bp * F);
-        P.o_stash = o; o = up(o + (P.L.stash_smem ? 0 : (size_t)P.seg * per_step));
+        const size_t tape_bytes = (size_t)P.T * P.B * P.L.C * P.L.threads * P.L.M * F;
+        P.tape = P.L.nbuf >= 2 &&
+                 (d->segment == -1 || (d->segment == 0 && tape_bytes <= WT_TAPE_AUTO_MAX_BYTES));
+        if (d->segment == -1 && !P.tape) return WT_ERR_UNSUPPORTED;
+        if (P.tape) {
+            // the forward runs on the adjoint's strips so that the tape's
+            // per-thread layout is the same on both sides
+            P.L.fM = P.L.M; P.L.fR = P.L.R; P.L.fS = P.L.S; P.L.fLD = P.L.LD;
+            P.L.fthreads = P.L.threads;
+            P.L.smem_fwd = P.L.smem_fwd_tape;
+            P.seg = P.T;      // no checkpoints
+            P.nseg = 1;
+            P.o_lap = o; o = up(o + tape_bytes);
+        } else {
+            const size_t per_step = (size_t)P.B * P.L.C * P.L.M * P.L.threads * F;
+            P.seg = P.L.seg;
+            P.nseg = (P.T + P.seg - 1) / P.seg;
+            P.o_ckpt = o; o = up(o + (size_t)P.nseg * 2 * bp * F);
+            P.o_stash = o; o = up(o + (P.L.stash_smem ? 0 : (size_t)P.seg * per_step));
+        }
         P.o_gcpart = o; o = up(o + bp * F);
         // per-thread tap capacity of both fused kernels (4 sources, 4 probes)
         for (int layout = 0; layout < 2; ++layout) {
@@ -223,6 +244,37 @@ int upload_tables(const wt_seq_desc* d, const SeqPlan& P, void* ws, cudaStream_t
         H(P.o_fcol)[j] = i;
     }
     H(P.o_err)[0] = 0;
+    // Small tables go to the device inside a kernel's parameters, so the host
+    // does not wait: the per-cell maps (plain form only) are filled with -1
+    // and every other entry is written explicitly.
+    static thread_local wt::IntScatter sc;
+    sc.n = 0;
+    auto put = [&](size_t off_bytes, size_t count, bool skip_minus1) {
+        const int* src = H(off_bytes);
+        for (size_t i = 0; i < count; ++i) {
+            if (skip_minus1 && src[i] == -1) continue;
+            if (sc.n == wt::INT_SCATTER_CAP) return false;
+            sc.idx[sc.n] = (int)(off_bytes / sizeof(int) + i);
+            sc.val[sc.n++] = src[i];
+        }
+        return true;
+    };
+    const bool plain = P.form == WT_FORM_PLAIN;
+    bool fits = (!plain || (put(P.o_srcmap, P.plane, true) && put(P.o_prbmap, P.plane, true))) &&
+                put(P.o_srcnext, P.ns, false) && put(P.o_srcrow, P.ns, false) &&
+                put(P.o_srccell, P.ns, false) && put(P.o_prbnext, P.np, false) &&
+                put(P.o_prbkind, P.np, false) && put(P.o_fcell, P.np, false) &&
+                put(P.o_fkind, P.np, false) && put(P.o_fcol, P.np, false) && put(P.o_err, 1, false);
+    int rc;
+    if (fits) {
+        int* base = at<int>(ws, 0);
+        if (plain) {
+            if ((rc = wt_launch_fill_int(base + P.o_srcmap / sizeof(int), P.plane, -1, st))) return rc;
+            if ((rc = wt_launch_fill_int(base + P.o_prbmap / sizeof(int), P.plane, -1, st))) return rc;
+        }
+        return wt_launch_scatter_ints(base, sc, st);
+    }
+    // too many entries for one parameter block: one staged copy of all tables
     cudaError_t e = cudaMemcpyAsync(ws, h.data(), P.tables_end, cudaMemcpyHostToDevice, st);
     if (e != cudaSuccess) return wt_cuda_status(e);
     // pageable source: make sure the staging copy has consumed `h`
@@ -247,9 +299,11 @@ wt::FusedParams fused_params(const wt_scalars* s, const SeqPlan& P, const float*
     F.prb_col = at<int>(ws, P.o_fcol);
     F.prb_kind_col = at<int>(ws, P.o_prbkind);
     F.amp = at<float>(ws, P.o_amp);
-    F.ckpt = at<float>(ws, P.o_ckpt);
-    F.stash = at<float>(ws, P.o_stash);
+    F.ckpt = P.tape ? nullptr : at<float>(ws, P.o_ckpt);
+    F.stash = P.tape ? nullptr : at<float>(ws, P.o_stash);
     F.stash_smem = P.L.stash_smem;
+    F.lap = P.tape ? at<float>(ws, P.o_lap) : nullptr;
+    F.nbuf = P.L.nbuf;
     F.gc_part = at<float>(ws, P.o_gcpart);
     F.err = at<int>(ws, P.o_err);
     return F;

@@ -182,6 +182,20 @@ WT_DEV unsigned long long ld_cluster_u64(uint32_t local) {
     asm volatile("ld.relaxed.cluster.shared::cta.b64 %0, [%1];" : "=l"(v) : "r"(local) : "memory");
     return v;
 }
+// Order this thread's earlier generic-proxy shared-memory accesses before
+// later asynchronous-proxy (bulk copy) accesses to the same memory.
+WT_DEV void fence_proxy_async_smem() {
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+// Bulk copy of `bytes` (a multiple of 16; both addresses 16-byte aligned)
+// from global memory into this CTA's shared memory; completion is counted
+// as transaction bytes on the mbarrier at `mbar`.
+WT_DEV void bulk_g2s(uint32_t dst, const void* src, uint32_t bytes, uint32_t mbar) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
+        "l"(src), "r"(bytes), "r"(mbar)
+        : "memory");
+}
 WT_DEV uint64_t global_ns() {
     uint64_t t;
     asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));

@@ -68,7 +68,20 @@ struct FusedParams {
     float* grad_x;          // [batch][steps] or null
     float* stash;           // global stash [batch][C][seg][M][nthreads] (unless in smem)
     int stash_smem;         // 1: the stash lives in shared memory after the tiles
+    // tape mode: the forward stores Lap(h_{t-1}) of every cell and step, the
+    // adjoint streams it back instead of recomputing segments
+    float* lap;             // [steps][batch][C][M/V][threads][V] or null (checkpoint mode)
+    int nbuf;               // tape slices in the adjoint's shared-memory ring
     int* err;
+};
+
+// Up to INT_SCATTER_CAP int writes base[idx[i]] = val[i], passed by value as
+// kernel parameters (24 KB, within the 32 KB parameter limit).
+constexpr int INT_SCATTER_CAP = 3000;
+struct IntScatter {
+    int n;
+    int idx[INT_SCATTER_CAP];
+    int val[INT_SCATTER_CAP];
 };
 
 }  // namespace wt
@@ -83,6 +96,11 @@ struct WtFusedLaunch {
     size_t smem_bwd;        // tiles + seed ring buffers (+ the stash when stash_smem)
     int seg;                // checkpoint interval
     int stash_smem;
+    // tape mode (see FusedParams::lap): possible when `nbuf` >= 2 slices fit;
+    // the forward then runs on the adjoint's strips (M, R, LD, threads)
+    int nbuf;
+    size_t smem_tape;       // adjoint shared memory in tape mode
+    size_t smem_fwd_tape;   // forward shared memory in tape mode
 };
 
 int wt_launch_step_fwd(const StepScalars& k, int batch, int nx, int ny, int coef_batched,
@@ -100,6 +118,8 @@ int wt_launch_seq_adj_step(const StepScalars& k, int batch, int nx, int ny, cons
 int wt_launch_seq_adj_reduce(int batch, size_t plane, const float* gc, float* G, int first,
                              cudaStream_t st);
 int wt_launch_fill_zero(float* p, size_t n, cudaStream_t st);
+int wt_launch_fill_int(int* p, size_t n, int v, cudaStream_t st);
+int wt_launch_scatter_ints(int* base, const wt::IntScatter& s, cudaStream_t st);
 int wt_fused_plan(int nx, int ny, int steps, int n_prb, int cluster_req, int seg_req,
                   WtFusedLaunch* L);
 int wt_launch_probe_sum(int batch, int steps, int n_prb, const float* out, float* sum,

@@ -78,6 +78,45 @@ WT_DEV void sts_col(float* p, const float (&s)[M]) {
     }
 }
 
+// Chunk-major block of a CTA's M values per thread: chunk j (V = 4, 2 or 1
+// consecutive values, the widest vector M allows) of thread `tid` sits at
+// (j * NT + tid) * V.  A warp's access to one chunk is one contiguous run
+// (coalesced in global memory, conflict-free in shared memory).
+template <int M>
+constexpr int chunk_width() { return M % 4 == 0 ? 4 : M % 2 == 0 ? 2 : 1; }
+
+template <int M>
+WT_DEV void st_chunks(float* base, int NT, int tid, const float (&s)[M]) {
+    constexpr int V = chunk_width<M>();
+#pragma unroll
+    for (int j = 0; j < M / V; ++j) {
+        float* p = base + ((size_t)j * NT + tid) * V;
+        if constexpr (V == 4)
+            *reinterpret_cast<float4*>(p) = make_float4(s[4 * j], s[4 * j + 1], s[4 * j + 2], s[4 * j + 3]);
+        else if constexpr (V == 2)
+            *reinterpret_cast<float2*>(p) = make_float2(s[2 * j], s[2 * j + 1]);
+        else
+            *p = s[j];
+    }
+}
+template <int M>
+WT_DEV void ld_chunks(float (&d)[M], const float* base, int NT, int tid) {
+    constexpr int V = chunk_width<M>();
+#pragma unroll
+    for (int j = 0; j < M / V; ++j) {
+        const float* p = base + ((size_t)j * NT + tid) * V;
+        if constexpr (V == 4) {
+            float4 v = *reinterpret_cast<const float4*>(p);
+            d[4 * j] = v.x; d[4 * j + 1] = v.y; d[4 * j + 2] = v.z; d[4 * j + 3] = v.w;
+        } else if constexpr (V == 2) {
+            float2 v = *reinterpret_cast<const float2*>(p);
+            d[2 * j] = v.x; d[2 * j + 1] = v.y;
+        } else {
+            d[j] = *p;
+        }
+    }
+}
+
 // Thread geometry shared by both kernels.
 struct Geo {
     int inst, cta, col, strip, xl0, gx0, S;
@@ -433,6 +472,9 @@ WT_DEV void fwd_step(const FusedParams& P, const Geo& g, const Xchg& X, const Ta
     fwd_update<M, ORDER>(P, g, X, tp, t & 1, t - 1, (t + 1) & 1, t + 1 < P.steps ? t : -1, st.xv,
                          t + 1, A, Bc, C2, cur, inout, L);
     if (!g.colv) return;
+    if (P.lap)            // tape for the adjoint: this thread's M values of Lap(h_{t-1})
+        st_chunks<M>(P.lap + (((size_t)t * P.batch + g.inst) * P.C + g.cta) * blockDim.x * M,
+                     blockDim.x, threadIdx.x, L);
     if (tp.np) {
         float* row = pr.buf + (size_t)st.pb * P.n_prb * P.PB + st.pc;
 #pragma unroll
@@ -726,6 +768,152 @@ __global__ void __launch_bounds__(bwd_max_threads(M), 1) seq_bwd_fused_kernel(Fu
     cluster_sync_all();
 }
 
+// ============================================================================
+// Adjoint in tape mode: the forward stored Lap(h_{t-1}) of every cell and
+// step, so the adjoint runs its T steps in one sweep with no recompute.  The
+// tape is laid out [step][instance][cta][chunk][thread] (chunk-major, see
+// st_chunks): both kernels use the same strips, so a CTA's values of one
+// step are one contiguous slice, written with coalesced vector stores and
+// read back from shared memory without bank conflicts.  Slices
+// arrive by bulk copy into a ring of `nbuf` shared-memory slots, issued by
+// thread 0 nbuf-1 steps ahead of use; slot t % nbuf holds step t, and its
+// mbarrier's phase parity for step t is ((T-1-t) / nbuf) & 1.
+struct TapeRing {
+    float* buf;                     // nbuf slices
+    unsigned long long* full;       // nbuf mbarriers
+    int slice;                      // floats per slice (threads * M)
+};
+
+WT_DEV void tape_issue(const FusedParams& P, const Geo& g, const TapeRing& r, int t) {
+    const int s = t % P.nbuf;
+    const float* src = P.lap + (((size_t)t * P.batch + g.inst) * P.C + g.cta) * r.slice;
+    const uint32_t mb = smem_addr(r.full + s);
+    const uint32_t bytes = (uint32_t)(r.slice * sizeof(float));
+    mbar_arrive_expect_tx(mb, bytes);
+    bulk_g2s(smem_addr(r.buf + (size_t)s * r.slice), src, bytes, mb);
+}
+
+// Bounded wait for step t's slice (parity of its use of the slot).
+WT_DEV bool tape_wait(const FusedParams& P, const Xchg& X, const TapeRing& r, int t) {
+    const uint32_t mb = smem_addr(r.full + t % P.nbuf);
+    const uint32_t par = (uint32_t)(((P.steps - 1 - t) / P.nbuf) & 1);
+    if (mbar_try_wait_parity(mb, par, 1000000u)) return true;
+    const uint64_t t0 = global_ns();
+    while (!mbar_try_wait_parity(mb, par, 1000000u)) {
+        if (global_ns() - t0 > WAIT_LIMIT_NS) {
+            atomicExch(P.err, WT_DEVERR_TIMEOUT);
+            *(volatile int*)X.abort = 1;
+            return false;
+        }
+    }
+    return true;
+}
+
+template <int M, int ORDER>
+__global__ void __launch_bounds__(bwd_max_threads(M), 1) seq_bwd_tape_kernel(FusedParams P) {
+    extern __shared__ __align__(16) float smem[];
+    __shared__ int abort_flag;
+    const Geo g = make_geo(P, M);
+    const int tile = (P.ny + 2) * P.LD;
+    zero_smem(smem, 2 * tile);
+    Xchg X;
+    xchg_setup(X, P, g, smem, tile, &abort_flag);
+    Taps tp;
+    build_taps<M>(P, g, tp);
+
+    const size_t plane = (size_t)P.nx * P.ny;
+    float* seeds = smem + 2 * tile + 2 * xchg_words(P.NCP);
+    TapeRing ring;
+    ring.buf = seeds + ((2 * P.n_prb * P.PB + 3) & ~3);
+    ring.slice = (int)blockDim.x * M;
+    ring.full = reinterpret_cast<unsigned long long*>(ring.buf + (size_t)P.nbuf * ring.slice);
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < P.nbuf; ++s) mbar_init(smem_addr(ring.full + s), 1);
+        fence_mbarrier_init_cluster();
+    }
+
+    float X1[M], Kc[M], Kg[M], Ky2[M];
+    load_bwd_coef<M>(P, g, X1, Kc, Kg, Ky2);
+    float gy1[M], gy2a[M], gy2b[M], acc[M];
+#pragma unroll
+    for (int i = 0; i < M; ++i) gy1[i] = gy2a[i] = gy2b[i] = acc[i] = 0.f;
+    stage_seeds(P, g, seeds, 0);
+    cluster_sync_all();   // zeroed tiles, ring and halo words; barriers initialised
+
+    int lo = P.steps;     // lowest step issued (thread 0)
+    if (threadIdx.x == 0) {
+        for (int j = 0; j < P.nbuf && P.steps - 1 - j >= 0; ++j) tape_issue(P, g, ring, lo = P.steps - 1 - j);
+    }
+    bool ok = true;
+    for (int u = 0; u < P.steps; ++u) {
+        const int t = P.steps - 1 - u;
+        float lam[M], c2g[M];
+#pragma unroll
+        for (int i = 0; i < M; ++i) {
+            lam[i] = fadd(gy2b[i], gy1[i]);
+            c2g[i] = 0.f;
+        }
+        if (u % P.PB == 0 && u + P.PB < P.steps)   // next chunk, a barrier ahead of use
+            stage_seeds(P, g, seeds, u / P.PB + 1);
+        if (g.colv) {
+            if (tp.np) {
+                const float* sr = seeds + (size_t)((u / P.PB) & 1) * P.n_prb * P.PB + u % P.PB;
+#pragma unroll
+                for (int e = 0; e < PRBMAX; ++e)
+                    if (e < tp.np) add_at<M>(lam, tp.prb_i(e), sr[tp.prb_col(e) * P.PB]);
+            }
+#pragma unroll
+            for (int i = 0; i < M; ++i) c2g[i] = fmul(Kg[i], lam[i]);
+            publish<M>(P, g, X, u & 1, u, c2g);
+            if (P.grad_x && tp.ns) {
+#pragma unroll
+                for (int e = 0; e < SRCMAX; ++e)
+                    if (e < tp.ns && tp.src_row(e) == g.inst)
+                        P.grad_x[(size_t)g.inst * P.steps + t] = pick<M>(lam, tp.src_i(e));
+            }
+        }
+        if (!(ok = exchange_end(X, u))) break;
+        // step t+1's slice was read before this barrier: refill its slot
+        if (threadIdx.x == 0 && u > 0 && t + 1 - P.nbuf >= 0) {
+            fence_proxy_async_smem();
+            tape_issue(P, g, ring, lo = t + 1 - P.nbuf);
+        }
+        if (g.colv) {
+            Column<M> c;
+            load_sides<M>(c, P, g, X, u & 1, -1);   // interior first; halo words below
+            tape_wait(P, X, ring, t);
+            float Ly[M];
+            ld_chunks<M>(Ly, ring.buf + (size_t)(t % P.nbuf) * ring.slice, blockDim.x, threadIdx.x);
+#pragma unroll
+            for (int i = 1; i < M - 1; ++i)
+                adj_cell(lap_cell<M, ORDER>(P, c, c2g, i), lam[i], Ly[i], X1[i], Kc[i], Ky2[i],
+                         P.k.dt2, acc[i], gy1[i], gy2a[i], gy2b[i]);
+            if (g.strip == 0 && g.has_up) c.up = recv_word(P, X, X.hup + (u & 1) * X.NCP + g.col, u);
+            if (g.strip == g.S - 1 && g.has_dn)
+                c.dn = recv_word(P, X, X.hdn + (u & 1) * X.NCP + g.col, u);
+            adj_cell(lap_cell<M, ORDER>(P, c, c2g, 0), lam[0], Ly[0], X1[0], Kc[0], Ky2[0],
+                     P.k.dt2, acc[0], gy1[0], gy2a[0], gy2b[0]);
+            adj_cell(lap_cell<M, ORDER>(P, c, c2g, M - 1), lam[M - 1], Ly[M - 1], X1[M - 1],
+                     Kc[M - 1], Ky2[M - 1], P.k.dt2, acc[M - 1], gy1[M - 1], gy2a[M - 1],
+                     gy2b[M - 1]);
+        }
+    }
+    if (!ok && threadIdx.x == 0) {
+        // leaving early: let the copies still in flight land first (the last
+        // nbuf issued steps hold one copy per slot; waits are bounded)
+        for (int s = lo; s < lo + P.nbuf && s < P.steps; ++s) tape_wait(P, X, ring, s);
+    }
+    if (g.colv && ok) {
+        float* o = P.gc_part + (size_t)g.inst * plane;
+#pragma unroll
+        for (int i = 0; i < M; ++i) {
+            int gx = g.gx0 + i;
+            if (gx < P.nx) o[(size_t)gx * P.ny + g.col] = acc[i];
+        }
+    }
+    cluster_sync_all();
+}
+
 }  // namespace wt
 
 // ---------------------------------------------------------------------------
@@ -799,6 +987,16 @@ int wt_fused_plan(int nx, int ny, int steps, int n_prb, int cluster_req, int seg
         L->seg = seg;
         L->stash_smem = seg <= fit;
         L->smem_bwd = tiles + aux_bwd + (L->stash_smem ? (size_t)seg * per_step : 0);
+        // tape mode: both kernels on the adjoint's strips; the adjoint keeps
+        // a ring of up to 8 slices (threads x M floats) plus one mbarrier per
+        // slice; one slice must stay below the mbarrier's transaction-count
+        // limit (2^20 - 1 bytes)
+        const size_t slice = per_step;
+        const int tfit = slice < (1u << 20) ? (int)((SMEM_MAX - tiles - aux_bwd) / (slice + 8)) : 0;
+        L->nbuf = std::min(8, tfit);
+        L->smem_tape = tiles + aux_bwd + (size_t)L->nbuf * (slice + 8);
+        L->smem_fwd_tape = tiles + aux_fwd;
+        if (tiles + aux_fwd > SMEM_MAX || L->threads > wt::fwd_max_threads(M)) L->nbuf = 0;
         return 0;
     }
     return WT_ERR_UNSUPPORTED;
@@ -867,6 +1065,8 @@ static int launch_bwd(const wt::FusedParams& P0, const WtFusedLaunch& L, cudaStr
     wt::FusedParams P = P0;
     P.R = L.R;
     P.LD = L.LD;
+    if (P.lap)
+        return launch_kernel(wt::seq_bwd_tape_kernel<M, ORDER>, P, L.C, L.threads, L.smem_tape, st);
     return launch_kernel(wt::seq_bwd_fused_kernel<M, ORDER>, P, L.C, L.threads, L.smem_bwd, st);
 }
 

@@ -340,3 +340,32 @@ int wt_launch_fill_zero(float* p, size_t n, cudaStream_t st) {
     wt_count_launches(1);
     return wt_cuda_status(cudaGetLastError());
 }
+
+// ---------------------------------------------------------------------------
+// Lookup tables of the sequence entry points, written without a host copy:
+// the -1 fill of the per-cell maps, then the entries themselves, carried in
+// the kernel's parameters (so the host never waits for a staging copy).
+namespace wt {
+__global__ void fill_int_kernel(int* __restrict__ p, size_t n, int v) {
+    size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) p[i] = v;
+}
+__global__ void scatter_ints_kernel(int* __restrict__ base, IntScatter s) {
+    for (int i = threadIdx.x; i < s.n; i += blockDim.x) base[s.idx[i]] = s.val[i];
+}
+}  // namespace wt
+
+int wt_launch_fill_int(int* p, size_t n, int v, cudaStream_t st) {
+    if (n == 0) return WT_OK;
+    int thr = 256;
+    wt::fill_int_kernel<<<(unsigned)((n + thr - 1) / thr), thr, 0, st>>>(p, n, v);
+    wt_count_launches(1);
+    return wt_cuda_status(cudaGetLastError());
+}
+
+int wt_launch_scatter_ints(int* base, const wt::IntScatter& s, cudaStream_t st) {
+    if (s.n <= 0) return WT_OK;
+    wt::scatter_ints_kernel<<<1, 256, 0, st>>>(base, s);
+    wt_count_launches(1);
+    return wt_cuda_status(cudaGetLastError());
+}

@@ -14,12 +14,14 @@ from __future__ import annotations
 
 import ctypes as C
 import dataclasses
+import struct
 from dataclasses import dataclass
 from typing import Optional, Sequence
 
 import torch
 
 from . import _lib
+from .utils import host_scalar
 
 ONEDNN_MIN_CELLS = 20480   # torch CPU conv2d uses oneDNN above this (batch 1)
 
@@ -56,10 +58,9 @@ def _require_cuda_f32(name: str, t: torch.Tensor) -> torch.Tensor:
 
 
 def _f32(v) -> float:
-    """float32 value of a python number or 0-d tensor."""
-    if isinstance(v, torch.Tensor):
-        v = v.detach().float().cpu().item()
-    return float(torch.tensor(float(v), dtype=torch.float32).item())
+    """float32 value of a python number or one-element tensor (device tensors
+    are read once and cached, see utils.host_scalar)."""
+    return struct.unpack("f", struct.pack("f", float(host_scalar(v))))[0]
 
 
 def scalars(dt, h, order: int) -> _lib.Scalars:

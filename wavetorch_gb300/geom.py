@@ -15,7 +15,7 @@ import torch
 
 from . import _lib
 from .functional import RhoToCFn, _f32
-from .utils import to_tensor
+from .utils import host_scalar, to_tensor
 
 
 def disk_kernel(radius: int) -> torch.Tensor:
@@ -208,7 +208,7 @@ class WaveGeometryFreeForm(WaveGeometry):
     def geom_desc(self) -> _lib.GeomDesc:
         k = self.blur_kernel.shape[-1]
         return _lib.GeomDesc(self.domain_shape[0], self.domain_shape[1], (k - 1) // 2,
-                             int(self.blur_N.item()), _f32(self.eta), _f32(self.beta),
+                             int(host_scalar(self.blur_N)), _f32(self.eta), _f32(self.beta),
                              _f32(self.c0), _f32(self.c1))
 
     @property

@@ -9,7 +9,7 @@ from __future__ import annotations
 
 import torch
 
-from .utils import to_tensor
+from .utils import host_list, to_tensor
 
 
 class WaveProbe(torch.nn.Module):
@@ -26,8 +26,8 @@ class WaveProbe(torch.nn.Module):
 
     def cells(self):
         """Flat list of (x, y) cells this probe reads, in output order."""
-        xs = self.x.reshape(-1).tolist()
-        ys = self.y.reshape(-1).tolist()
+        xs = host_list(self.x)
+        ys = host_list(self.y)
         if len(xs) != len(ys):
             raise ValueError("probe x and y must have the same length")
         return list(zip(xs, ys))

@@ -8,7 +8,7 @@ from __future__ import annotations
 
 import torch
 
-from .utils import to_tensor
+from .utils import host_list, to_tensor
 
 
 def bresenham(r0, c0, r1, c1):
@@ -57,8 +57,8 @@ class WaveSource(torch.nn.Module):
 
     def cells(self):
         """Flat list of (x, y) cells this source drives."""
-        xs = self.x.reshape(-1).tolist()
-        ys = self.y.reshape(-1).tolist()
+        xs = host_list(self.x)
+        ys = host_list(self.y)
         return list(zip(xs, ys))
 
     def plot(self, ax, color='r'):

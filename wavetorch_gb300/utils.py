@@ -1,6 +1,8 @@
 """Host-side helpers mirroring wavetorch/utils.py (dtype switch, loss glue)."""
 from __future__ import annotations
 
+import weakref
+
 import numpy as np
 import torch
 
@@ -13,6 +15,37 @@ def to_tensor(x, dtype=None):
     if isinstance(x, torch.Tensor):
         return x.detach().clone().type(dtype)
     return torch.tensor(x, dtype=dtype)
+
+
+# Host copies of small device tensors (coordinates, physics scalars), keyed by
+# the tensor object and checked against its version counter, which every
+# in-place change bumps.  Reading a CUDA tensor on the host synchronises the
+# device, so without this each forward would stall the GPU once per value.
+_HOST_VALUES = {}
+
+
+def host_list(t: torch.Tensor) -> list:
+    """Python list of the values of a small tensor, read from the device only
+    when the tensor object is new or was modified in place."""
+    if t.device.type == "cpu":
+        return t.reshape(-1).tolist()
+    key, ver = id(t), t._version
+    hit = _HOST_VALUES.get(key)
+    if hit is not None and hit[0]() is t and hit[1] == ver:
+        return hit[2]
+    vals = t.reshape(-1).tolist()
+    _HOST_VALUES[key] = (weakref.ref(t, lambda _r, k=key: _HOST_VALUES.pop(k, None)), ver, vals)
+    return vals
+
+
+def host_scalar(t) -> float:
+    """Python value of a one-element tensor (or a number), cached like host_list."""
+    if isinstance(t, torch.Tensor):
+        v = host_list(t)
+        if len(v) != 1:
+            raise ValueError("expected a one-element tensor")
+        return v[0]
+    return t
 
 
 def set_dtype(dtype=None):
