@@ -784,8 +784,7 @@ struct TapeRing {
     int slice;                      // floats per slice (threads * M)
 };
 
-WT_DEV void tape_issue(const FusedParams& P, const Geo& g, const TapeRing& r, int t) {
-    const int s = t % P.nbuf;
+WT_DEV void tape_issue(const FusedParams& P, const Geo& g, const TapeRing& r, int t, int s) {
     const float* src = P.lap + (((size_t)t * P.batch + g.inst) * P.C + g.cta) * r.slice;
     const uint32_t mb = smem_addr(r.full + s);
     const uint32_t bytes = (uint32_t)(r.slice * sizeof(float));
@@ -793,10 +792,9 @@ WT_DEV void tape_issue(const FusedParams& P, const Geo& g, const TapeRing& r, in
     bulk_g2s(smem_addr(r.buf + (size_t)s * r.slice), src, bytes, mb);
 }
 
-// Bounded wait for step t's slice (parity of its use of the slot).
-WT_DEV bool tape_wait(const FusedParams& P, const Xchg& X, const TapeRing& r, int t) {
-    const uint32_t mb = smem_addr(r.full + t % P.nbuf);
-    const uint32_t par = (uint32_t)(((P.steps - 1 - t) / P.nbuf) & 1);
+// Bounded wait for the phase of parity `par` of slot s.
+WT_DEV bool tape_wait(const FusedParams& P, const Xchg& X, const TapeRing& r, int s, uint32_t par) {
+    const uint32_t mb = smem_addr(r.full + s);
     if (mbar_try_wait_parity(mb, par, 1000000u)) return true;
     const uint64_t t0 = global_ns();
     while (!mbar_try_wait_parity(mb, par, 1000000u)) {
@@ -842,8 +840,17 @@ __global__ void __launch_bounds__(bwd_max_threads(M), 1) seq_bwd_tape_kernel(Fus
 
     int lo = P.steps;     // lowest step issued (thread 0)
     if (threadIdx.x == 0) {
-        for (int j = 0; j < P.nbuf && P.steps - 1 - j >= 0; ++j) tape_issue(P, g, ring, lo = P.steps - 1 - j);
+        for (int j = 0; j < P.nbuf && P.steps - 1 - j >= 0; ++j) {
+            lo = P.steps - 1 - j;
+            tape_issue(P, g, ring, lo, lo % P.nbuf);
+        }
     }
+    // per-step counters kept incrementally (no division on the step path):
+    // slot = t % nbuf, phase bit s = parity of the next wait on slot s,
+    // pk = u % PB, pc = u / PB
+    int slot = (P.steps - 1) % P.nbuf;
+    uint32_t phase = 0;
+    int pk = 0, pc = 0;
     bool ok = true;
     for (int u = 0; u < P.steps; ++u) {
         const int t = P.steps - 1 - u;
@@ -853,11 +860,11 @@ __global__ void __launch_bounds__(bwd_max_threads(M), 1) seq_bwd_tape_kernel(Fus
             lam[i] = fadd(gy2b[i], gy1[i]);
             c2g[i] = 0.f;
         }
-        if (u % P.PB == 0 && u + P.PB < P.steps)   // next chunk, a barrier ahead of use
-            stage_seeds(P, g, seeds, u / P.PB + 1);
+        if (pk == 0 && u + P.PB < P.steps)   // next chunk, a barrier ahead of use
+            stage_seeds(P, g, seeds, pc + 1);
         if (g.colv) {
             if (tp.np) {
-                const float* sr = seeds + (size_t)((u / P.PB) & 1) * P.n_prb * P.PB + u % P.PB;
+                const float* sr = seeds + (size_t)(pc & 1) * P.n_prb * P.PB + pk;
 #pragma unroll
                 for (int e = 0; e < PRBMAX; ++e)
                     if (e < tp.np) add_at<M>(lam, tp.prb_i(e), sr[tp.prb_col(e) * P.PB]);
@@ -876,14 +883,16 @@ __global__ void __launch_bounds__(bwd_max_threads(M), 1) seq_bwd_tape_kernel(Fus
         // step t+1's slice was read before this barrier: refill its slot
         if (threadIdx.x == 0 && u > 0 && t + 1 - P.nbuf >= 0) {
             fence_proxy_async_smem();
-            tape_issue(P, g, ring, lo = t + 1 - P.nbuf);
+            lo = t + 1 - P.nbuf;
+            tape_issue(P, g, ring, lo, slot + 1 == P.nbuf ? 0 : slot + 1);
         }
         if (g.colv) {
             Column<M> c;
             load_sides<M>(c, P, g, X, u & 1, -1);   // interior first; halo words below
-            tape_wait(P, X, ring, t);
+            tape_wait(P, X, ring, slot, (phase >> slot) & 1u);
+            phase ^= 1u << slot;
             float Ly[M];
-            ld_chunks<M>(Ly, ring.buf + (size_t)(t % P.nbuf) * ring.slice, blockDim.x, threadIdx.x);
+            ld_chunks<M>(Ly, ring.buf + (size_t)slot * ring.slice, blockDim.x, threadIdx.x);
 #pragma unroll
             for (int i = 1; i < M - 1; ++i)
                 adj_cell(lap_cell<M, ORDER>(P, c, c2g, i), lam[i], Ly[i], X1[i], Kc[i], Ky2[i],
@@ -897,11 +906,15 @@ __global__ void __launch_bounds__(bwd_max_threads(M), 1) seq_bwd_tape_kernel(Fus
                      Kc[M - 1], Ky2[M - 1], P.k.dt2, acc[M - 1], gy1[M - 1], gy2a[M - 1],
                      gy2b[M - 1]);
         }
+        slot = slot == 0 ? P.nbuf - 1 : slot - 1;
+        if (++pk == P.PB) { pk = 0; ++pc; }
     }
     if (!ok && threadIdx.x == 0) {
         // leaving early: let the copies still in flight land first (the last
-        // nbuf issued steps hold one copy per slot; waits are bounded)
-        for (int s = lo; s < lo + P.nbuf && s < P.steps; ++s) tape_wait(P, X, ring, s);
+        // nbuf issued steps hold one copy per slot, step s in slot s % nbuf
+        // at parity ((T-1-s) / nbuf) & 1; waits are bounded)
+        for (int s = lo; s < lo + P.nbuf && s < P.steps; ++s)
+            tape_wait(P, X, ring, s % P.nbuf, (uint32_t)(((P.steps - 1 - s) / P.nbuf) & 1));
     }
     if (g.colv && ok) {
         float* o = P.gc_part + (size_t)g.inst * plane;
