@@ -157,6 +157,16 @@ def fused_supported(spec: SeqSpec) -> bool:
     return _lib.load().wt_seq_workspace_bytes(C.byref(d), C.byref(n)) != _lib.WT_ERR_UNSUPPORTED
 
 
+def fused_uses_tape(spec: SeqSpec) -> bool:
+    """Whether the fused adjoint of this sequence runs in tape mode (the
+    forward stores every step's Laplacian) rather than from checkpoints."""
+    if spec.form != _lib.WT_FORM_FUSED or spec.segment > 0:
+        return False
+    if spec.segment == -1:
+        return True
+    return seq_workspace_bytes(spec) == seq_workspace_bytes(dataclasses.replace(spec, segment=-1))
+
+
 def seq_forward(spec: SeqSpec, sc: _lib.Scalars, b, c, x, want_sum: bool = False):
     """Run the forward sequence; returns (out, fields, probe_sum, workspace)."""
     dev = c.device
