@@ -175,6 +175,63 @@ def case_nonlinear(wt):
     return as32(r)
 
 
+def loss64(wt, kw, rho):
+    """Loss of the model of `kw` at density `rho`, run in float64."""
+    geom = wt.WaveGeometryFreeForm((kw["N"], kw["N"]), 1.0, c0=1.0, c1=0.5, abs_N=kw["abs_N"],
+                                   abs_sig=3.0, abs_p=2, rho=rho)
+    with torch.no_grad():
+        geom.rho.copy_(rho)        # keep the perturbed entry (the ctor constrains)
+    cell = wt.WaveCell(0.707, geom, satdamp_b0=kw["satdamp_b0"], satdamp_uth=kw["satdamp_uth"],
+                       c_nl=kw["c_nl"])
+    model = wt.WaveRNN(cell, [s() for s in kw["sources"]], [p() for p in kw["probes"]])
+    with torch.no_grad():
+        y = model(torch.from_numpy(kw["x"]).to(torch.float64))
+        return torch.nn.CrossEntropyLoss()(wt.utils.normalize_power(y.sum(dim=1)),
+                                           torch.from_numpy(kw["labels"])).item()
+
+
+def case_fd64(wt, nonlinear):
+    """Central finite differences of the loss in float64 at 16 random design
+    entries of rho (eps = 1e-5), next to the float64 autograd gradient."""
+    N, T, B, abs_N = 40, 60, 2, 8
+    g = torch.Generator().manual_seed(13 if nonlinear else 14)
+    rho0 = torch.rand(N, N, generator=g)
+    x, labels = vowel_like(B, T, seed=13 if nonlinear else 14)
+    x = (x * np.float32(0.2)).astype(np.float32)
+    kw = dict(N=N, abs_N=abs_N, x=x, labels=labels,
+              sources=[lambda: wt.WaveSource(10, 20)],
+              probes=[lambda y=y: wt.WaveIntensityProbe(30, y) for y in (12, 20, 28)],
+              satdamp_b0=0.05 if nonlinear else 0.0,
+              satdamp_uth=float(np.sqrt(0.1)) if nonlinear else 0.0,
+              c_nl=0.1 if nonlinear else 0.0)
+    wt.utils.set_dtype('float64')
+    try:
+        r64 = run_model(wt, N=N, abs_N=abs_N, B=B, T=T, x=x, labels=labels,
+                        sources=kw["sources"], probes=kw["probes"], rho0=rho0,
+                        satdamp_b0=kw["satdamp_b0"], satdamp_uth=kw["satdamp_uth"],
+                        c_nl=kw["c_nl"], dtype=torch.float64)
+        rho = torch.from_numpy(r64["rho"])                 # constrained density
+        design = np.argwhere((r64["b"] == 0).reshape(-1)).reshape(-1)
+        pick = np.random.default_rng(15).choice(design, 16, replace=False)
+        eps = 1e-5
+        fd = []
+        for i in pick:
+            rp, rm = rho.clone(), rho.clone()
+            rp.view(-1)[i] += eps
+            rm.view(-1)[i] -= eps
+            fd.append((loss64(wt, kw, rp) - loss64(wt, kw, rm)) / (2 * eps))
+    finally:
+        wt.utils.set_dtype('float32')
+    res = {"rho": r64["rho"].astype(np.float32), "x": x, "labels": labels,
+           "fd_index": pick.astype(np.int64), "fd_grad": np.array(fd, np.float64),
+           "grad_rho64": r64["grad_rho"].reshape(-1)[pick], "eps": np.array(eps),
+           "satdamp_b0": np.array(kw["satdamp_b0"]), "satdamp_uth": np.array(kw["satdamp_uth"]),
+           "c_nl": np.array(kw["c_nl"])}
+    res.update(meta(N=N, T=T, B=B, abs_N=abs_N, sources=[(10 * N + 20, -1)],
+                    probes=[(30 * N + y, 1, i) for i, y in enumerate((12, 20, 28))]))
+    return res
+
+
 def case_step(wt, B, N, dt, h, seed):
     """One TimeStep forward/backward on random inputs (the check of
     study/utils/test_grad.py, with stored values)."""
@@ -229,6 +286,8 @@ def main():
         "multi": lambda: case_multi(wt),
         "line": lambda: case_line(wt),
         "nonlinear": lambda: case_nonlinear(wt),
+        "fd64_linear": lambda: case_fd64(wt, False),
+        "fd64_nonlinear": lambda: case_fd64(wt, True),
         "step_b2_h025": lambda: case_step(wt, 2, 16, 0.1, 0.25, 5),
         "step_b1_h1": lambda: case_step(wt, 1, 14, 0.5, 1.0, 6),
         "step_b20_h1": lambda: case_step(wt, 20, 10, 0.707, 1.0, 7),

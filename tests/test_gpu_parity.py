@@ -210,3 +210,22 @@ def test_in_place_edits_of_coordinates_and_scalars_are_seen(cuda):
     assert torch.equal(y2, r2)
     assert not torch.equal(y2, y3)
     assert torch.equal(y3, r3)
+
+
+@pytest.mark.parametrize("name,form", [("fd64_linear", "fused"), ("fd64_linear", "plain"),
+                                       ("fd64_nonlinear", "step")])
+def test_grad_rho_against_fp64_central_differences(cuda, name, form):
+    """dL/drho (float32, hand-written adjoint) at 16 random design cells
+    against central differences of the reference run in float64 (eps 1e-5;
+    they agree with the reference's float64 autograd to 3e-9).  Tolerance:
+    1e-4 of the largest of the 16 derivatives."""
+    d = golden(name)
+    m = build_model(d, cuda, form, cnl=float(d["c_nl"]), b0=float(d["satdamp_b0"]),
+                    uth=float(d["satdamp_uth"]))
+    y = m(T(d["x"], cuda))
+    loss = torch.nn.CrossEntropyLoss()(wt.utils.normalize_power(y.sum(dim=1)),
+                                       T(d["labels"], cuda))
+    loss.backward()
+    ours = m.cell.geom.rho.grad.reshape(-1).cpu().numpy().astype(np.float64)[d["fd_index"]]
+    fd = d["fd_grad"]
+    assert np.abs(ours - fd).max() <= 1e-4 * np.abs(fd).max()

@@ -86,3 +86,13 @@ def test_fp32_vs_fp64_floor():
     d = golden("cfg0_small")
     assert rel(d["out"], d["out64"]) < 1e-4
     assert rel(d["grad_rho"], d["grad_rho64"]) < 1e-4
+
+
+@pytest.mark.parametrize("name", ["fd64_linear", "fd64_nonlinear"])
+def test_fp64_finite_difference_fixtures_match_reference_autograd(name):
+    """The central differences (float64, eps 1e-5) that pin the GPU gradients
+    agree with the reference's own float64 autograd gradient."""
+    d = golden(name)
+    fd, ag = d["fd_grad"], d["grad_rho64"]
+    assert fd.shape == (16,)
+    assert np.abs(fd - ag).max() <= 1e-7 * np.abs(fd).max()
