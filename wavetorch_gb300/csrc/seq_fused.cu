@@ -323,16 +323,31 @@ WT_DEV void build_taps(const FusedParams& P, const Geo& g, Taps& tp) {
 // select v[i] for a runtime i without dynamic register indexing
 template <int M>
 WT_DEV float pick(const float (&v)[M], int i) {
-    float r = 0.f;
-#pragma unroll
-    for (int j = 0; j < M; ++j) r = (j == i) ? v[j] : r;
-    return r;
+    static_assert(M <= 32, "strips of at most 32 cells");
+    // a jump on i (one thread of a warp typically), not M predicated selects
+#define WT_PICK(J) case J: if constexpr (J < M) return v[J]; break;
+    switch (i) {
+        WT_PICK(0) WT_PICK(1) WT_PICK(2) WT_PICK(3) WT_PICK(4) WT_PICK(5) WT_PICK(6) WT_PICK(7)
+        WT_PICK(8) WT_PICK(9) WT_PICK(10) WT_PICK(11) WT_PICK(12) WT_PICK(13) WT_PICK(14)
+        WT_PICK(15) WT_PICK(16) WT_PICK(17) WT_PICK(18) WT_PICK(19) WT_PICK(20) WT_PICK(21)
+        WT_PICK(22) WT_PICK(23) WT_PICK(24) WT_PICK(25) WT_PICK(26) WT_PICK(27) WT_PICK(28)
+        WT_PICK(29) WT_PICK(30) WT_PICK(31)
+    }
+#undef WT_PICK
+    return 0.f;
 }
 template <int M>
 WT_DEV void add_at(float (&v)[M], int i, float a) {
-#pragma unroll
-    for (int j = 0; j < M; ++j)
-        if (j == i) v[j] = fadd(v[j], a);
+    static_assert(M <= 32, "strips of at most 32 cells");
+#define WT_ADD(J) case J: if constexpr (J < M) v[J] = fadd(v[J], a); break;
+    switch (i) {
+        WT_ADD(0) WT_ADD(1) WT_ADD(2) WT_ADD(3) WT_ADD(4) WT_ADD(5) WT_ADD(6) WT_ADD(7)
+        WT_ADD(8) WT_ADD(9) WT_ADD(10) WT_ADD(11) WT_ADD(12) WT_ADD(13) WT_ADD(14)
+        WT_ADD(15) WT_ADD(16) WT_ADD(17) WT_ADD(18) WT_ADD(19) WT_ADD(20) WT_ADD(21)
+        WT_ADD(22) WT_ADD(23) WT_ADD(24) WT_ADD(25) WT_ADD(26) WT_ADD(27) WT_ADD(28)
+        WT_ADD(29) WT_ADD(30) WT_ADD(31)
+    }
+#undef WT_ADD
 }
 
 // Per-cell coefficients of one phase, re-formed from b and c.
@@ -624,6 +639,15 @@ WT_DEV void adj_cell(float lg, float lam, float Ly, float X1, float Kc, float Ky
     gy2a = fmul(Ky2, lam);
 }
 
+// adj_cell with the two pending grad_y2 terms in alternating arrays: g2 holds
+// the term of two steps ago on entry and this step's term on exit.
+WT_DEV void adj_cell_pp(float lg, float lam, float Ly, float X1, float Kc, float Ky2, float dt2,
+                        float& acc, float& gy1, float& g2) {
+    acc = fadd(acc, fmul(fmul(X1, fmul(Kc, Ly)), lam));
+    gy1 = fadd(fmul(dt2, lg), fmul(fmul(2.0f, lam), X1));
+    g2 = fmul(Ky2, lam);
+}
+
 template <int M, int ORDER>
 __global__ void __launch_bounds__(bwd_max_threads(M), 1) seq_bwd_fused_kernel(FusedParams P) {
     extern __shared__ __align__(16) float smem[];
@@ -852,12 +876,14 @@ __global__ void __launch_bounds__(bwd_max_threads(M), 1) seq_bwd_tape_kernel(Fus
     uint32_t phase = 0;
     int pk = 0, pc = 0;
     bool ok = true;
-    for (int u = 0; u < P.steps; ++u) {
+    // One adjoint step; g2 holds the grad_y2 term written two steps ago and
+    // receives this step's (the two arrays alternate, so nothing is copied).
+    auto step = [&](int u, float (&g2)[M]) -> bool {
         const int t = P.steps - 1 - u;
         float lam[M], c2g[M];
 #pragma unroll
         for (int i = 0; i < M; ++i) {
-            lam[i] = fadd(gy2b[i], gy1[i]);
+            lam[i] = fadd(g2[i], gy1[i]);
             c2g[i] = 0.f;
         }
         if (pk == 0 && u + P.PB < P.steps)   // next chunk, a barrier ahead of use
@@ -879,7 +905,7 @@ __global__ void __launch_bounds__(bwd_max_threads(M), 1) seq_bwd_tape_kernel(Fus
                         P.grad_x[(size_t)g.inst * P.steps + t] = pick<M>(lam, tp.src_i(e));
             }
         }
-        if (!(ok = exchange_end(X, u))) break;
+        if (!exchange_end(X, u)) return false;
         // step t+1's slice was read before this barrier: refill its slot
         if (threadIdx.x == 0 && u > 0 && t + 1 - P.nbuf >= 0) {
             fence_proxy_async_smem();
@@ -895,20 +921,21 @@ __global__ void __launch_bounds__(bwd_max_threads(M), 1) seq_bwd_tape_kernel(Fus
             ld_chunks<M>(Ly, ring.buf + (size_t)slot * ring.slice, blockDim.x, threadIdx.x);
 #pragma unroll
             for (int i = 1; i < M - 1; ++i)
-                adj_cell(lap_cell<M, ORDER>(P, c, c2g, i), lam[i], Ly[i], X1[i], Kc[i], Ky2[i],
-                         P.k.dt2, acc[i], gy1[i], gy2a[i], gy2b[i]);
+                adj_cell_pp(lap_cell<M, ORDER>(P, c, c2g, i), lam[i], Ly[i], X1[i], Kc[i], Ky2[i],
+                            P.k.dt2, acc[i], gy1[i], g2[i]);
             if (g.strip == 0 && g.has_up) c.up = recv_word(P, X, X.hup + (u & 1) * X.NCP + g.col, u);
             if (g.strip == g.S - 1 && g.has_dn)
                 c.dn = recv_word(P, X, X.hdn + (u & 1) * X.NCP + g.col, u);
-            adj_cell(lap_cell<M, ORDER>(P, c, c2g, 0), lam[0], Ly[0], X1[0], Kc[0], Ky2[0],
-                     P.k.dt2, acc[0], gy1[0], gy2a[0], gy2b[0]);
-            adj_cell(lap_cell<M, ORDER>(P, c, c2g, M - 1), lam[M - 1], Ly[M - 1], X1[M - 1],
-                     Kc[M - 1], Ky2[M - 1], P.k.dt2, acc[M - 1], gy1[M - 1], gy2a[M - 1],
-                     gy2b[M - 1]);
+            adj_cell_pp(lap_cell<M, ORDER>(P, c, c2g, 0), lam[0], Ly[0], X1[0], Kc[0], Ky2[0],
+                        P.k.dt2, acc[0], gy1[0], g2[0]);
+            adj_cell_pp(lap_cell<M, ORDER>(P, c, c2g, M - 1), lam[M - 1], Ly[M - 1], X1[M - 1],
+                        Kc[M - 1], Ky2[M - 1], P.k.dt2, acc[M - 1], gy1[M - 1], g2[M - 1]);
         }
         slot = slot == 0 ? P.nbuf - 1 : slot - 1;
         if (++pk == P.PB) { pk = 0; ++pc; }
-    }
+        return true;
+    };
+    for (int u = 0; u < P.steps && ok; ++u) ok = (u & 1) ? step(u, gy2a) : step(u, gy2b);
     if (!ok && threadIdx.x == 0) {
         // leaving early: let the copies still in flight land first (the last
         // nbuf issued steps hold one copy per slot, step s in slot s % nbuf
@@ -1009,7 +1036,7 @@ int wt_fused_plan(int nx, int ny, int steps, int n_prb, int cluster_req, int seg
         L->nbuf = std::min(8, tfit);
         L->smem_tape = tiles + aux_bwd + (size_t)L->nbuf * (slice + 8);
         L->smem_fwd_tape = tiles + aux_fwd;
-        if (tiles + aux_fwd > SMEM_MAX || L->threads > wt::fwd_max_threads(M)) L->nbuf = 0;
+        if (L->smem_fwd_tape > SMEM_MAX || L->threads > wt::fwd_max_threads(M)) L->nbuf = 0;
         return 0;
     }
     return WT_ERR_UNSUPPORTED;
