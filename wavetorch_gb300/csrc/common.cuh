@@ -150,26 +150,17 @@ WT_DEV void mbar_arrive_expect_tx(uint32_t addr, uint32_t bytes) {
                  "r"(bytes)
                  : "memory");
 }
-// Probe of phase completion (acquire at cluster scope, so data delivered by
-// remote st.async before the phase completed is visible).  The thread may be
-// suspended up to `hint_ns` (woken early when the phase completes), so a
-// waiting warp does not spin on the issue slots.
-WT_DEV bool mbar_try_wait_parity(uint32_t addr, uint32_t parity, uint32_t hint_ns) {
+// Probe of phase completion with acquire semantics at CTA scope: enough for
+// data a bulk copy wrote into this CTA's own shared memory.
+WT_DEV bool mbar_try_wait_parity_cta(uint32_t addr, uint32_t parity) {
     uint32_t ok;
     asm volatile("{\n\t.reg .pred p;\n\t"
-                 "mbarrier.try_wait.parity.acquire.cluster.shared::cta.b64 p, [%1], %2, %3;\n\t"
+                 "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
                  "selp.u32 %0, 1, 0, p;\n\t}"
                  : "=r"(ok)
-                 : "r"(addr), "r"(parity), "r"(hint_ns)
+                 : "r"(addr), "r"(parity)
                  : "memory");
     return ok != 0;
-}
-// Asynchronous 4-byte store into another CTA's shared memory that completes
-// `4` transaction bytes on that CTA's mbarrier (both shared::cluster addresses).
-WT_DEV void st_async_f32(uint32_t remote, float v, uint32_t remote_mbar) {
-    asm volatile("st.async.shared::cluster.mbarrier::complete_tx::bytes.b32 [%0], %1, [%2];" ::"r"(remote),
-                 "r"(__float_as_uint(v)), "r"(remote_mbar)
-                 : "memory");
 }
 // Relaxed 8-byte store into another CTA's shared memory (shared::cluster
 // address) and relaxed 8-byte load from this CTA's shared memory; aligned

@@ -320,36 +320,6 @@ WT_DEV void build_taps(const FusedParams& P, const Geo& g, Taps& tp) {
     }
 }
 
-// select v[i] for a runtime i without dynamic register indexing
-template <int M>
-WT_DEV float pick(const float (&v)[M], int i) {
-    static_assert(M <= 32, "strips of at most 32 cells");
-    // a jump on i (one thread of a warp typically), not M predicated selects
-#define WT_PICK(J) case J: if constexpr (J < M) return v[J]; break;
-    switch (i) {
-        WT_PICK(0) WT_PICK(1) WT_PICK(2) WT_PICK(3) WT_PICK(4) WT_PICK(5) WT_PICK(6) WT_PICK(7)
-        WT_PICK(8) WT_PICK(9) WT_PICK(10) WT_PICK(11) WT_PICK(12) WT_PICK(13) WT_PICK(14)
-        WT_PICK(15) WT_PICK(16) WT_PICK(17) WT_PICK(18) WT_PICK(19) WT_PICK(20) WT_PICK(21)
-        WT_PICK(22) WT_PICK(23) WT_PICK(24) WT_PICK(25) WT_PICK(26) WT_PICK(27) WT_PICK(28)
-        WT_PICK(29) WT_PICK(30) WT_PICK(31)
-    }
-#undef WT_PICK
-    return 0.f;
-}
-template <int M>
-WT_DEV void add_at(float (&v)[M], int i, float a) {
-    static_assert(M <= 32, "strips of at most 32 cells");
-#define WT_ADD(J) case J: if constexpr (J < M) v[J] = fadd(v[J], a); break;
-    switch (i) {
-        WT_ADD(0) WT_ADD(1) WT_ADD(2) WT_ADD(3) WT_ADD(4) WT_ADD(5) WT_ADD(6) WT_ADD(7)
-        WT_ADD(8) WT_ADD(9) WT_ADD(10) WT_ADD(11) WT_ADD(12) WT_ADD(13) WT_ADD(14)
-        WT_ADD(15) WT_ADD(16) WT_ADD(17) WT_ADD(18) WT_ADD(19) WT_ADD(20) WT_ADD(21)
-        WT_ADD(22) WT_ADD(23) WT_ADD(24) WT_ADD(25) WT_ADD(26) WT_ADD(27) WT_ADD(28)
-        WT_ADD(29) WT_ADD(30) WT_ADD(31)
-    }
-#undef WT_ADD
-}
-
 // Per-cell coefficients of one phase, re-formed from b and c.
 template <int M>
 WT_DEV void load_fwd_coef(const FusedParams& P, const Geo& g, float (&A)[M], float (&Bc)[M],
@@ -381,13 +351,25 @@ WT_DEV void load_bwd_coef(const FusedParams& P, const Geo& g, float (&X1)[M], fl
 }
 
 
-// Sources (in table order) with the inputs prefetched one step ahead.
+// The thread's own column of tile slot `slot` (its M cells).
 template <int M>
-WT_DEV void apply_sources(const FusedParams& P, const Taps& tp, float (&y)[M], float (&xv)[SRCMAX],
-                          int tnext) {
+WT_DEV float* own_column(const FusedParams& P, const Geo& g, const Xchg& X, int slot) {
+    return X.tiles + slot * X.tile + (g.col + 1) * P.LD + OFF + g.xl0;
+}
+
+// Sources (in table order) with the inputs prefetched one step ahead.  A
+// source's cell index varies by thread, and indexing registers by a runtime
+// value costs a jump per step on the warp that owns the source; so the
+// injection goes through the thread's column of the tile (already stored):
+// add there, then reload the column into registers.
+template <int M>
+WT_DEV void apply_sources(const FusedParams& P, const Geo& g, const Xchg& X, const Taps& tp,
+                          int slot, float (&y)[M], float (&xv)[SRCMAX], int tnext) {
+    float* colp = own_column<M>(P, g, X, slot);
 #pragma unroll
     for (int e = 0; e < SRCMAX; ++e)
-        if (e < tp.ns) add_at<M>(y, tp.src_i(e), xv[e]);
+        if (e < tp.ns) colp[tp.src_i(e)] = fadd(colp[tp.src_i(e)], xv[e]);
+    lds_col<M>(y, colp);
     if (tnext >= 0 && tnext < P.steps) {
 #pragma unroll
         for (int e = 0; e < SRCMAX; ++e)
@@ -421,11 +403,11 @@ WT_DEV void fwd_update(const FusedParams& P, const Geo& g, const Xchg& X, const 
         L[i] = lap_cell<M, ORDER>(P, c, cur, i);
         inout[i] = leapfrog(A[i], Bc[i], C2[i], P.k.two_over, cur[i], inout[i], L[i]);
     }
+    store_column<M>(P, g, X, ws, inout);
     if (tp.ns) {
-        apply_sources<M>(P, tp, inout, xv, tnext);
+        apply_sources<M>(P, g, X, tp, ws, inout, xv, tnext);
         if (ks >= 0 && tp.src_edge) send_halo(g, X, ks, inout[0], inout[M - 1]);
     }
-    store_column<M>(P, g, X, ws, inout);
 }
 
 struct FwdState {
@@ -490,11 +472,12 @@ WT_DEV void fwd_step(const FusedParams& P, const Geo& g, const Xchg& X, const Ta
     if (P.lap)            // tape for the adjoint: this thread's M values of Lap(h_{t-1})
         st_chunks<M>(P.lap + (((size_t)t * P.batch + g.inst) * P.C + g.cta) * blockDim.x * M,
                      blockDim.x, threadIdx.x, L);
-    if (tp.np) {
+    if (tp.np) {          // probe values from the column just stored (no register indexing)
+        const float* colp = own_column<M>(P, g, X, (t + 1) & 1);
         float* row = pr.buf + (size_t)st.pb * P.n_prb * P.PB + st.pc;
 #pragma unroll
         for (int e = 0; e < PRBMAX; ++e)
-            if (e < tp.np) row[tp.prb_col(e) * P.PB] = pick<M>(inout, tp.prb_i(e));
+            if (e < tp.np) row[tp.prb_col(e) * P.PB] = colp[tp.prb_i(e)];
     }
     if (FIELDS) {
         const size_t plane = (size_t)P.nx * P.ny;
@@ -629,6 +612,31 @@ WT_DEV void stage_seeds(const FusedParams& P, const Geo& g, float* seeds, int c)
     }
 }
 
+// Probe seeds into lam (descending reference order) and dL/dx at the
+// source, for the few threads that own such cells.  The cells' indices vary by
+// thread, so instead of indexing registers by a runtime value the thread
+// passes lam through its own column of the tile slot it is about to publish
+// into (that column has no readers until the publish): store, add the seeds
+// at their cells, read dL/dx, reload.
+template <int M>
+WT_DEV void seed_and_read(const FusedParams& P, const Geo& g, const Xchg& X, const Taps& tp,
+                          int slot, int t, float (&lam)[M], const float* sr) {
+    float* colp = own_column<M>(P, g, X, slot);
+    sts_col<M>(colp, lam);
+    if (tp.np) {
+#pragma unroll
+        for (int e = 0; e < PRBMAX; ++e)
+            if (e < tp.np) colp[tp.prb_i(e)] = fadd(colp[tp.prb_i(e)], sr[tp.prb_col(e) * P.PB]);
+        lds_col<M>(lam, colp);
+    }
+    if (P.grad_x && tp.ns) {
+#pragma unroll
+        for (int e = 0; e < SRCMAX; ++e)
+            if (e < tp.ns && tp.src_row(e) == g.inst)
+                P.grad_x[(size_t)g.inst * P.steps + t] = colp[tp.src_i(e)];
+    }
+}
+
 // Adjoint of one cell (wavetorch/cell.py:36-42 with autograd's accumulation):
 // dL/dc += (X1 * (Kc * Lap(h_{t-1}))) * lam; pending grad_y1 / grad_y2 terms.
 WT_DEV void adj_cell(float lg, float lam, float Ly, float X1, float Kc, float Ky2, float dt2,
@@ -740,22 +748,12 @@ __global__ void __launch_bounds__(bwd_max_threads(M), 1) seq_bwd_fused_kernel(Fu
             if (u % P.PB == 0 && u + P.PB < P.steps)   // next chunk, a barrier ahead of use
                 stage_seeds(P, g, seeds, u / P.PB + 1);
             if (g.colv) {
-                if (tp.np) {
-                    // probe seeds, descending reference order (list order)
-                    const float* sr = seeds + (size_t)((u / P.PB) & 1) * P.n_prb * P.PB + u % P.PB;
-#pragma unroll
-                    for (int e = 0; e < PRBMAX; ++e)
-                        if (e < tp.np) add_at<M>(lam, tp.prb_i(e), sr[tp.prb_col(e) * P.PB]);
-                }
+                if (tp.np || (P.grad_x && tp.ns))
+                    seed_and_read<M>(P, g, X, tp, kx & 1, t, lam,
+                                     seeds + (size_t)((u / P.PB) & 1) * P.n_prb * P.PB + u % P.PB);
 #pragma unroll
                 for (int i = 0; i < M; ++i) c2g[i] = fmul(Kg[i], lam[i]);
                 publish<M>(P, g, X, kx & 1, kx, c2g);
-                if (P.grad_x && tp.ns) {
-#pragma unroll
-                    for (int e = 0; e < SRCMAX; ++e)
-                        if (e < tp.ns && tp.src_row(e) == g.inst)
-                            P.grad_x[(size_t)g.inst * P.steps + t] = pick<M>(lam, tp.src_i(e));
-                }
             }
             if (!(ok = exchange_end(X, u))) break;
             ++u;
@@ -819,9 +817,9 @@ WT_DEV void tape_issue(const FusedParams& P, const Geo& g, const TapeRing& r, in
 // Bounded wait for the phase of parity `par` of slot s.
 WT_DEV bool tape_wait(const FusedParams& P, const Xchg& X, const TapeRing& r, int s, uint32_t par) {
     const uint32_t mb = smem_addr(r.full + s);
-    if (mbar_try_wait_parity(mb, par, 1000000u)) return true;
+    if (mbar_try_wait_parity_cta(mb, par)) return true;
     const uint64_t t0 = global_ns();
-    while (!mbar_try_wait_parity(mb, par, 1000000u)) {
+    while (!mbar_try_wait_parity_cta(mb, par)) {
         if (global_ns() - t0 > WAIT_LIMIT_NS) {
             atomicExch(P.err, WT_DEVERR_TIMEOUT);
             *(volatile int*)X.abort = 1;
@@ -889,21 +887,12 @@ __global__ void __launch_bounds__(bwd_max_threads(M), 1) seq_bwd_tape_kernel(Fus
         if (pk == 0 && u + P.PB < P.steps)   // next chunk, a barrier ahead of use
             stage_seeds(P, g, seeds, pc + 1);
         if (g.colv) {
-            if (tp.np) {
-                const float* sr = seeds + (size_t)(pc & 1) * P.n_prb * P.PB + pk;
-#pragma unroll
-                for (int e = 0; e < PRBMAX; ++e)
-                    if (e < tp.np) add_at<M>(lam, tp.prb_i(e), sr[tp.prb_col(e) * P.PB]);
-            }
+            if (tp.np || (P.grad_x && tp.ns))
+                seed_and_read<M>(P, g, X, tp, u & 1, t, lam,
+                                 seeds + (size_t)(pc & 1) * P.n_prb * P.PB + pk);
 #pragma unroll
             for (int i = 0; i < M; ++i) c2g[i] = fmul(Kg[i], lam[i]);
             publish<M>(P, g, X, u & 1, u, c2g);
-            if (P.grad_x && tp.ns) {
-#pragma unroll
-                for (int e = 0; e < SRCMAX; ++e)
-                    if (e < tp.ns && tp.src_row(e) == g.inst)
-                        P.grad_x[(size_t)g.inst * P.steps + t] = pick<M>(lam, tp.src_i(e));
-            }
         }
         if (!exchange_end(X, u)) return false;
         // step t+1's slice was read before this barrier: refill its slot
