@@ -200,10 +200,12 @@ class WaveGeometryFreeForm(WaveGeometry):
             raise ValueError('The domain initialization is invalid')
 
     def constrain_to_design_region(self):
-        """Zero the density outside the design region and inside the PML."""
+        """Zero the density outside the design region and inside the PML
+        (wavetorch/geom.py:201-205).  A masked fill on the device: unlike
+        boolean-index assignment it needs no device-to-host round trip, so an
+        optimiser step followed by this call stays asynchronous."""
         with torch.no_grad():
-            self.rho[self.design_region == 0] = 0.0
-            self.rho[self.b > 0] = 0.0
+            self.rho.masked_fill_((self.design_region == 0) | (self.b > 0), 0.0)
 
     def geom_desc(self) -> _lib.GeomDesc:
         k = self.blur_kernel.shape[-1]
