@@ -210,6 +210,50 @@ WT_DEV float recv_word(const FusedParams& P, const Xchg& X, const unsigned long 
     return __uint_as_float((uint32_t)v);
 }
 
+// Per-thread addresses of the forward's step path, formed once before the
+// loop (recomputing them every step cost a quarter of the step's
+// instructions): the thread's column in tile slot 0 (slot 1 is `tile` floats
+// further), and for the CTA's boundary strips the halo words it reads and
+// the neighbour words it writes, for exchange parity 0 (parity 1 is `pstride`
+// bytes further).  0 where the thread has no such word.
+struct Lane {
+    float* col0;
+    int tile;
+    uint32_t rup, rdn, sup, sdn, pstride;
+};
+
+WT_DEV Lane make_lane(const FusedParams& P, const Geo& g, const Xchg& X) {
+    Lane l;
+    l.col0 = X.tiles + (g.col + 1) * P.LD + OFF + g.xl0;
+    l.tile = X.tile;
+    const bool top = g.strip == 0 && g.has_up, bot = g.strip == g.S - 1 && g.has_dn;
+    l.rup = top ? smem_addr(X.hup + g.col) : 0u;
+    l.rdn = bot ? smem_addr(X.hdn + g.col) : 0u;
+    l.sup = top ? X.up_hdn + 8u * (uint32_t)g.col : 0u;
+    l.sdn = bot ? X.dn_hup + 8u * (uint32_t)g.col : 0u;
+    l.pstride = 8u * (uint32_t)X.NCP;
+    return l;
+}
+
+// Wait (bounded) for exchange k's word at shared address a and return its value.
+WT_DEV float recv_at(const FusedParams& P, const Xchg& X, uint32_t a, int k) {
+    const uint32_t tag = (uint32_t)(k + 1);
+    unsigned long long v = ld_cluster_u64(a);
+    if ((uint32_t)(v >> 32) != tag) {
+        const uint64_t t0 = global_ns();
+        for (uint32_t it = 1;; ++it) {
+            v = ld_cluster_u64(a);
+            if ((uint32_t)(v >> 32) == tag) break;
+            if ((it & 1023u) == 0 && global_ns() - t0 > WAIT_LIMIT_NS) {
+                atomicExch(P.err, WT_DEVERR_TIMEOUT);
+                *(volatile int*)X.abort = 1;
+                return 0.f;
+            }
+        }
+    }
+    return __uint_as_float((uint32_t)v);
+}
+
 template <int M>
 WT_DEV void store_column(const FusedParams& P, const Geo& g, const Xchg& X, int s,
                          const float (&v)[M]) {
@@ -410,6 +454,51 @@ WT_DEV void fwd_update(const FusedParams& P, const Geo& g, const Xchg& X, const 
     }
 }
 
+// fwd_update for the forward kernel's step loop, on precomputed addresses:
+// step t reads tile slot RS = t & 1 and the halo words of exchange t-1
+// (parity RS ^ 1), writes slot RS ^ 1 and sends exchange t (parity RS).
+template <int M, int ORDER, int RS>
+WT_DEV void fwd_update_lane(const FusedParams& P, const Geo& g, const Xchg& X, const Lane& ln,
+                            const Taps& tp, int t, bool send, float (&xv)[SRCMAX],
+                            const float (&A)[M], const float (&Bc)[M], const float (&C2)[M],
+                            const float (&cur)[M], float (&inout)[M], float (&L)[M]) {
+    if (!g.colv) return;
+    const float* rcol = ln.col0 + RS * ln.tile;
+    float* wcol = ln.col0 + (RS ^ 1) * ln.tile;
+    Column<M> c;
+    lds_col<M>(c.lf, rcol - P.LD);
+    lds_col<M>(c.rt, rcol + P.LD);
+    c.up = rcol[-1];
+    c.dn = rcol[M];
+    if (t > 0) {
+        if (ln.rup) c.up = recv_at(P, X, ln.rup + (RS ^ 1) * ln.pstride, t - 1);
+        if (ln.rdn) c.dn = recv_at(P, X, ln.rdn + (RS ^ 1) * ln.pstride, t - 1);
+    }
+    L[0] = lap_cell<M, ORDER>(P, c, cur, 0);
+    inout[0] = leapfrog(A[0], Bc[0], C2[0], P.k.two_over, cur[0], inout[0], L[0]);
+    L[M - 1] = lap_cell<M, ORDER>(P, c, cur, M - 1);
+    inout[M - 1] = leapfrog(A[M - 1], Bc[M - 1], C2[M - 1], P.k.two_over, cur[M - 1],
+                            inout[M - 1], L[M - 1]);
+    const unsigned long long tag = (unsigned long long)(uint32_t)(t + 1) << 32;
+    if (send && !tp.src_edge) {
+        if (ln.sup) st_cluster_u64(ln.sup + RS * ln.pstride, tag | __float_as_uint(inout[0]));
+        if (ln.sdn) st_cluster_u64(ln.sdn + RS * ln.pstride, tag | __float_as_uint(inout[M - 1]));
+    }
+#pragma unroll
+    for (int i = 1; i < M - 1; ++i) {
+        L[i] = lap_cell<M, ORDER>(P, c, cur, i);
+        inout[i] = leapfrog(A[i], Bc[i], C2[i], P.k.two_over, cur[i], inout[i], L[i]);
+    }
+    sts_col<M>(wcol, inout);
+    if (tp.ns) {
+        apply_sources<M>(P, g, X, tp, RS ^ 1, inout, xv, t + 1);
+        if (send && tp.src_edge) {
+            if (ln.sup) st_cluster_u64(ln.sup + RS * ln.pstride, tag | __float_as_uint(inout[0]));
+            if (ln.sdn) st_cluster_u64(ln.sdn + RS * ln.pstride, tag | __float_as_uint(inout[M - 1]));
+        }
+    }
+}
+
 struct FwdState {
     int pc;                   // step index within the probe chunk
     int pb;                   // probe ring buffer in use (0/1)
@@ -459,21 +548,34 @@ WT_DEV void store_checkpoint(const FusedParams& P, const Geo& g, int t, const fl
 }
 
 // One step of the forward kernel (everything but the closing barrier).
-template <int M, int ORDER, bool FIELDS>
-WT_DEV void fwd_step(const FusedParams& P, const Geo& g, const Xchg& X, const Taps& tp,
-                     FwdState& st, const ProbeRing& pr, int t, const float (&A)[M],
-                     const float (&Bc)[M], const float (&C2)[M], const float (&cur)[M],
-                     float (&inout)[M]) {
+// RS = t & 1 (the tile slot holding h_{t-1}); tape points at this thread's
+// chunk 0 of step t's tape slice.
+template <int M, int ORDER, bool FIELDS, int RS>
+WT_DEV void fwd_step(const FusedParams& P, const Geo& g, const Xchg& X, const Lane& ln,
+                     const Taps& tp, FwdState& st, const ProbeRing& pr, int t, float* tape,
+                     const float (&A)[M], const float (&Bc)[M], const float (&C2)[M],
+                     const float (&cur)[M], float (&inout)[M]) {
     float L[M];
-    // exchange t carries h_t; tile slot (t+1)&1 holds it (h_{-1} = 0 is slot 0)
-    fwd_update<M, ORDER>(P, g, X, tp, t & 1, t - 1, (t + 1) & 1, t + 1 < P.steps ? t : -1, st.xv,
-                         t + 1, A, Bc, C2, cur, inout, L);
+    // exchange t carries h_t; tile slot RS ^ 1 holds it (h_{-1} = 0 is slot 0)
+    fwd_update_lane<M, ORDER, RS>(P, g, X, ln, tp, t, t + 1 < P.steps, st.xv, A, Bc, C2, cur,
+                                  inout, L);
     if (!g.colv) return;
-    if (P.lap)            // tape for the adjoint: this thread's M values of Lap(h_{t-1})
-        st_chunks<M>(P.lap + (((size_t)t * P.batch + g.inst) * P.C + g.cta) * blockDim.x * M,
-                     blockDim.x, threadIdx.x, L);
+    if (tape) {           // tape for the adjoint: this thread's M values of Lap(h_{t-1})
+        constexpr int V = chunk_width<M>();
+        const int stride = (int)blockDim.x * V;
+#pragma unroll
+        for (int j = 0; j < M / V; ++j) {
+            float* p = tape + j * stride;
+            if constexpr (V == 4)
+                *reinterpret_cast<float4*>(p) = make_float4(L[4 * j], L[4 * j + 1], L[4 * j + 2], L[4 * j + 3]);
+            else if constexpr (V == 2)
+                *reinterpret_cast<float2*>(p) = make_float2(L[2 * j], L[2 * j + 1]);
+            else
+                *p = L[j];
+        }
+    }
     if (tp.np) {          // probe values from the column just stored (no register indexing)
-        const float* colp = own_column<M>(P, g, X, (t + 1) & 1);
+        const float* colp = ln.col0 + (RS ^ 1) * ln.tile;
         float* row = pr.buf + (size_t)st.pb * P.n_prb * P.PB + st.pc;
 #pragma unroll
         for (int e = 0; e < PRBMAX; ++e)
@@ -543,6 +645,12 @@ __global__ void __launch_bounds__(fwd_max_threads(M), 1) seq_fwd_fused_kernel(Fu
 
     // ya holds h_{t-1} at even t, yb at odd t (the update overwrites h_{t-2});
     // the outer loop runs one checkpoint segment per iteration
+    const Lane ln = make_lane(P, g, X);
+    // tape: this thread's chunk 0 of step 0's slice, advanced one step at a time
+    float* tape = P.lap ? P.lap + ((size_t)g.inst * P.C + g.cta) * blockDim.x * M +
+                              (size_t)threadIdx.x * chunk_width<M>()
+                        : nullptr;
+    const size_t tape_step = (size_t)P.batch * P.C * blockDim.x * M;
     int chunk0 = 0;       // first step of the probe chunk being filled
     bool ok = true;
     for (int t0 = 0; t0 < P.steps && ok; t0 += P.seg) {
@@ -552,8 +660,9 @@ __global__ void __launch_bounds__(fwd_max_threads(M), 1) seq_fwd_fused_kernel(Fu
         }
         const int t1 = min(P.steps, t0 + P.seg);
         for (int t = t0; t < t1; ++t) {
-            if (t & 1) fwd_step<M, ORDER, FIELDS>(P, g, X, tp, st, pr, t, A, Bc, C2, yb, ya);
-            else       fwd_step<M, ORDER, FIELDS>(P, g, X, tp, st, pr, t, A, Bc, C2, ya, yb);
+            if (t & 1) fwd_step<M, ORDER, FIELDS, 1>(P, g, X, ln, tp, st, pr, t, tape, A, Bc, C2, yb, ya);
+            else       fwd_step<M, ORDER, FIELDS, 0>(P, g, X, ln, tp, st, pr, t, tape, A, Bc, C2, ya, yb);
+            if (tape) tape += tape_step;
             if (!(ok = exchange_end(X, t))) break;
             if (++st.pc == P.PB) {
                 flush_probes(P, g, pr, st.pb, chunk0, P.PB);
