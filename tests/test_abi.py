@@ -97,11 +97,13 @@ def test_fused_tap_capacity(lib):
 
 
 def test_fused_plan_size_limit(lib):
-    """The fused form plans instances that fit one cluster (up to 160x160);
-    WaveRNN sends larger grids to the plain form."""
+    """The fused form plans instances that fit one cluster (up to 256x256,
+    with 16-CTA clusters above 160); WaveRNN sends larger grids to the plain
+    form."""
     from wavetorch_gb300.functional import SeqSpec, fused_supported
-    assert fused_supported(SeqSpec(2, 160, 160, 100, [(5, -1)], [(7, 1, 0)]))
-    assert not fused_supported(SeqSpec(2, 161, 161, 100, [(5, -1)], [(7, 1, 0)]))
+    for n in (160, 161, 200, 256):
+        assert fused_supported(SeqSpec(2, n, n, 100, [(5, -1)], [(7, 1, 0)])), n
+    assert not fused_supported(SeqSpec(2, 257, 257, 100, [(5, -1)], [(7, 1, 0)]))
     assert not fused_supported(SeqSpec(1, 1024, 1024, 100, [(5, -1)], [(7, 1, 0)]))
     # the plain form takes any grid
     spec = SeqSpec(1, 1024, 1024, 100, [(5, -1)], [(7, 1, 0)], form=0)

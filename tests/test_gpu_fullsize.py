@@ -162,3 +162,24 @@ def test_tape_and_checkpoint_modes_agree_bitwise(cuda):
     for seg in (0, 11, 50):
         assert torch.equal(res[seg][0], res[-1][0]), seg
         assert torch.equal(res[seg][1], res[-1][1]), seg
+
+
+@pytest.mark.parametrize("N", [200, 256])
+def test_large_grids_fused_agree_with_plain(cuda, N):
+    """Grids above 160x160 run on 16-CTA clusters: forward identical to the
+    plain form (bit-exact with the reference), dL/dc within 1e-6."""
+    geom = wt.WaveGeometryFreeForm((N, N), 1.0, c0=1.0, c1=0.5, abs_N=20, abs_sig=3.0, abs_p=2,
+                                   rho=torch.rand(N, N, generator=torch.Generator().manual_seed(N))).to(cuda)
+    with torch.no_grad():
+        c = geom.c.contiguous()
+    b = geom.b.contiguous()
+    B, steps = 2, 300
+    x = torch.from_numpy(vowel_like(B, steps, seed=N)[0]).to(cuda)
+    src = [(20 * N + N // 2, -1)]
+    prb = [((N - 20) * N + N // 2 + d, 1, i) for i, d in enumerate((-15, 0, 15))]
+    sc = scalars(0.707, 1.0, lap_order(B, N, N, 1.0))
+    g = torch.randn(B, steps, 3, generator=torch.Generator().manual_seed(1)).to(cuda)
+    p_out, p_gc = run(SeqSpec(B, N, N, steps, src, prb, form=_lib.WT_FORM_PLAIN), sc, b, c, x, g)
+    f_out, f_gc = run(SeqSpec(B, N, N, steps, src, prb, form=_lib.WT_FORM_FUSED), sc, b, c, x, g)
+    assert torch.equal(p_out, f_out)
+    assert rel(f_gc.cpu().numpy(), p_gc.cpu().numpy()) <= 1e-6

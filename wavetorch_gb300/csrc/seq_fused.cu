@@ -1069,13 +1069,13 @@ static int tile_ld(int rows, int M) {
 
 // Strip height with the fewest padding rows for R rows per CTA (ties: the
 // first in `Ms`), within the thread budget of that height.
-static int pick_strip(int nx, int C, int NCP, const int* Ms, int nM, bool fwd) {
+static int pick_strip(int nx, int C, int NCP, const int* Ms, int nM, bool fwd, bool allow_empty) {
     int best = -1, best_pad = 1 << 30;
     for (int mi = 0; mi < nM; ++mi) {
         int M = Ms[mi];
         int rows = (nx + C - 1) / C;
         int R = ((rows + M - 1) / M) * M;
-        if ((C - 1) * R >= nx) continue;   // an empty CTA
+        if (!allow_empty && (C - 1) * R >= nx) continue;   // a CTA of padding rows only
         if ((R / M) * NCP > (fwd ? wt::fwd_max_threads(M) : wt::bwd_max_threads(M))) continue;
         int pad = C * R - nx;
         if (pad < best_pad) { best_pad = pad; best = M; }
@@ -1102,9 +1102,11 @@ int wt_fused_plan(int nx, int ny, int steps, int n_prb, int cluster_req, int seg
     for (int ci = 0; ci < 5; ++ci) {
         int C = Cs[ci];
         if (cluster_req > 0 && C != cluster_req) continue;
-        if (C > 8) continue;
-        const int M = pick_strip(nx, C, NCP, Mb, 3, false);
-        const int fM = pick_strip(nx, C, NCP, Mf, 7, true);
+        // 16 CTAs (a non-portable cluster size) only for grids the portable
+        // sizes cannot hold; there the last CTAs may hold padding rows only
+        const bool big = C > 8;
+        const int M = pick_strip(nx, C, NCP, Mb, 3, false, big);
+        const int fM = pick_strip(nx, C, NCP, Mf, 7, true, big);
         if (M < 0 || fM < 0) continue;
         const int rows = (nx + C - 1) / C;
         const int R = ((rows + M - 1) / M) * M, fR = ((rows + fM - 1) / fM) * fM;
@@ -1171,6 +1173,10 @@ static int launch_kernel(void (*kern)(wt::FusedParams), const wt::FusedParams& P
                          int threads, size_t smem, cudaStream_t st) {
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return wt_cuda_status(e);
+    if (C > 8) {
+        e = cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+        if (e != cudaSuccess) return wt_cuda_status(e);
+    }
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(C * P.batch, 1, 1);
     cfg.blockDim = dim3(threads, 1, 1);

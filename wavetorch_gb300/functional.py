@@ -150,7 +150,8 @@ def seq_workspace_bytes(spec: SeqSpec) -> int:
 
 def fused_supported(spec: SeqSpec) -> bool:
     """Whether the fused form can plan this sequence: the whole instance must
-    fit on one thread-block cluster (square grids up to 160x160 cells).  Any
+    fit on one thread-block cluster (square grids up to 256x256 cells, with
+    16-CTA clusters above 160x160).  Any
     other error is left for the real call to report."""
     d, keep = dataclasses.replace(spec, form=_lib.WT_FORM_FUSED).desc()
     n = C.c_size_t(0)
