@@ -128,6 +128,7 @@ typedef struct wt_seq_desc {
     int32_t segment;                       /* fused adjoint mode, see below  */
     int32_t cluster;                       /* CTAs per instance, 0 = auto    */
     int32_t output_fields;                 /* 1: also write every field      */
+    int32_t coef_batched;                  /* 1: one geometry per instance   */
 } wt_seq_desc;
 
 /* `segment` chooses how the fused form's adjoint gets the forward's fields:
@@ -145,6 +146,12 @@ typedef struct wt_seq_desc {
  * unchanged, to wt_seq_bwd (checkpoints or the full field history, plus the
  * per-step probe amplitudes).                                               */
 int wt_seq_workspace_bytes(const wt_seq_desc* d, size_t* bytes);
+
+/* `coef_batched` = 1 gives every instance its own geometry: b and c are
+ * [batch,nx,ny] and wt_seq_bwd's grad_c is [batch,nx,ny] (dLoss/dc of each
+ * instance, not summed).  The reference has one geometry per WaveRNN; this
+ * serves batches of different models of the same grid size (ragged batches).
+ * Fused form only: the plain form returns WT_ERR_UNSUPPORTED for it.        */
 
 /* Forward.  b, c: [nx,ny]; x: [batch,steps]; out: [batch,steps,n_probes];
  * fields (only if output_fields): [batch,steps,nx,ny]; probe_sum (nullable):

@@ -130,6 +130,20 @@ def test_fused_adjoint_modes(lib):
     assert lib.wt_seq_workspace_bytes(C.byref(d), C.byref(n)) == _lib.WT_ERR_INVALID
 
 
+def test_per_instance_geometry_flag(lib):
+    """coef_batched: fused form only; anything but 0/1 is invalid."""
+    from wavetorch_gb300 import _lib
+    n = C.c_size_t(0)
+    d, keep = _desc(form=1)
+    d.coef_batched = 1
+    assert lib.wt_seq_workspace_bytes(C.byref(d), C.byref(n)) == _lib.WT_OK
+    d, keep = _desc(form=0)
+    d.coef_batched = 1
+    assert lib.wt_seq_workspace_bytes(C.byref(d), C.byref(n)) == _lib.WT_ERR_UNSUPPORTED
+    d.coef_batched = 2
+    assert lib.wt_seq_workspace_bytes(C.byref(d), C.byref(n)) == _lib.WT_ERR_INVALID
+
+
 def test_step_entry_points_validate_before_touching_the_device(lib):
     from wavetorch_gb300 import _lib
     sc = _lib.Scalars(0.707, 1.0, 0)

@@ -1,0 +1,54 @@
+"""Ragged batches: models of different grid sizes and step counts advanced as
+one captured CUDA graph give each model the loss and dL/drho it gets when run
+alone through WaveRNN (tolerance 1e-5, the parity bar: the ragged step forms
+the loss gradient in closed form, autograd op by op)."""
+import numpy as np
+import pytest
+import torch
+
+import wavetorch_gb300 as wt
+from wavetorch_gb300.data import vowel_like
+from wavetorch_gb300.ragged import RaggedBatch
+
+pytestmark = pytest.mark.gpu
+
+
+def rel(a, b):
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    return np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300)
+
+
+def make(N, seed, dev):
+    geom = wt.WaveGeometryFreeForm((N, N), 1.0, c0=1.0, c1=0.5, abs_N=20, abs_sig=3.0, abs_p=2,
+                                   rho=torch.rand(N, N, generator=torch.Generator().manual_seed(seed)))
+    cell = wt.WaveCell(0.707, geom)
+    return wt.WaveRNN(cell, wt.WaveSource(20, N // 2),
+                      [wt.WaveIntensityProbe(N - 20, N // 2 + d) for d in (-15, 0, 15)]).to(dev)
+
+
+@pytest.mark.parametrize("graph", [False, True])
+def test_ragged_step_matches_models_run_alone(cuda, graph):
+    # enough steps for the wave to reach the probes (N - 40 cells away at
+    # about 0.7 cells per step), else every intensity is 0 and the loss 0/0
+    sizes = [64, 64, 100, 150, 200, 256]
+    steps = [150, 120, 200, 260, 330, 400]
+    models = [make(N, 100 + i, cuda) for i, N in enumerate(sizes)]
+    inputs, labels = [], []
+    for i, T in enumerate(steps):
+        x, lab = vowel_like(1, T, seed=200 + i)
+        inputs.append(torch.from_numpy(x[0]).to(cuda))
+        labels.append(int(lab[0]))
+    rb = RaggedBatch(models, inputs, labels, graph=graph)
+    for _ in range(2):                       # replays are repeatable
+        losses = rb.step().clone()
+    torch.cuda.synchronize()
+    grads = [m.cell.geom.rho.grad.clone() for m in models]
+    for i, m in enumerate(models):
+        m.cell.geom.rho.grad = None
+        y = m(inputs[i][None])
+        loss = torch.nn.CrossEntropyLoss()(wt.utils.normalize_power(y.sum(dim=1)),
+                                           torch.tensor([labels[i]], device=cuda))
+        loss.backward()
+        assert abs(losses[i].item() - loss.item()) <= 1e-5 * abs(loss.item()), i
+        assert rel(grads[i].cpu().numpy(), m.cell.geom.rho.grad.cpu().numpy()) <= 1e-5, i

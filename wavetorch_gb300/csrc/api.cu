@@ -97,7 +97,7 @@ constexpr size_t WT_TAPE_AUTO_MAX_BYTES = (size_t)16 << 30;
 size_t up(size_t v) { return (v + ALIGN - 1) / ALIGN * ALIGN; }
 
 struct SeqPlan {
-    int B, nx, ny, T, ns, np, form;
+    int B, nx, ny, T, ns, np, form, coef_batched;
     size_t plane;
     // int tables
     size_t o_srcmap, o_srcnext, o_srcrow, o_srccell;
@@ -121,6 +121,8 @@ int make_plan(const wt_seq_desc* d, SeqPlan* p) {
     if ((d->n_sources > 0 && !d->sources_host) || (d->n_probes > 0 && !d->probes_host))
         return WT_ERR_INVALID;
     if (d->form != WT_FORM_PLAIN && d->form != WT_FORM_FUSED) return WT_ERR_INVALID;
+    if (d->coef_batched != 0 && d->coef_batched != 1) return WT_ERR_INVALID;
+    if (d->coef_batched && d->form != WT_FORM_FUSED) return WT_ERR_UNSUPPORTED;
     const long long cells = (long long)d->nx * d->ny;
     if (cells > (1LL << 30)) return WT_ERR_INVALID;
     for (int i = 0; i < d->n_sources; ++i) {
@@ -135,6 +137,7 @@ int make_plan(const wt_seq_desc* d, SeqPlan* p) {
     std::memset(&P, 0, sizeof(P));
     P.B = d->batch; P.nx = d->nx; P.ny = d->ny; P.T = d->steps;
     P.ns = d->n_sources; P.np = d->n_probes; P.form = d->form;
+    P.coef_batched = d->coef_batched;
     P.plane = (size_t)cells;
     const size_t I = sizeof(int), F = sizeof(float);
     size_t o = 0;
@@ -290,6 +293,7 @@ wt::FusedParams fused_params(const wt_scalars* s, const SeqPlan& P, const float*
     F.C = P.L.C; F.R = P.L.R; F.NCP = P.L.NCP; F.LD = P.L.LD; F.seg = P.seg; F.PB = P.L.PB;
     // (R and LD are set per kernel at launch: the two kernels use different strips)
     F.b = b; F.c = c; F.x = x;
+    F.coef_stride = P.coef_batched ? P.plane : 0;
     F.n_src = P.ns;
     F.src_cell = at<int>(ws, P.o_srccell);
     F.src_row = at<int>(ws, P.o_srcrow);
@@ -430,7 +434,9 @@ extern "C" int wt_seq_bwd(const wt_scalars* s, const wt_seq_desc* d, const float
     wt::FusedParams F = fused_params(s, P, b, c, x, workspace);
     F.grad_out = grad_out;
     F.grad_x = grad_x;
+    if (P.coef_batched) F.gc_part = grad_c;   // per-instance dL/dc is the result
     if ((st = wt_launch_fused(false, F, P.L, cs))) return st;
+    if (P.coef_batched) return WT_OK;
     return wt_launch_seq_adj_reduce(P.B, plane, F.gc_part, grad_c, 1, cs);
 }
 

@@ -45,8 +45,9 @@ struct FusedParams {
     int LD;         // tile column stride (floats)
     int seg;        // checkpoint interval
     int PB;         // probe chunk length (steps staged in shared memory per flush/load)
-    const float* b;         // [nx,ny]
-    const float* c;         // [nx,ny]
+    const float* b;         // [nx,ny], or [batch][nx][ny] when coef_stride != 0
+    const float* c;         // likewise
+    size_t coef_stride;     // floats between instances' b / c (0: shared by the batch)
     const float* x;         // [batch][steps]
     // sources in table order, probes in descending reference order
     int n_src;

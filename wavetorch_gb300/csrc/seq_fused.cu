@@ -33,6 +33,8 @@
 // registers at a time.
 #include <algorithm>
 #include <cmath>
+#include <map>
+#include <mutex>
 
 #include "internal.cuh"
 
@@ -373,7 +375,7 @@ WT_DEV void load_fwd_coef(const FusedParams& P, const Geo& g, float (&A)[M], flo
         A[i] = Bc[i] = C2[i] = 0.f;
         int gx = g.gx0 + i;
         if (g.colv && gx < P.nx) {
-            size_t cell = (size_t)gx * P.ny + g.col;
+            size_t cell = P.coef_stride * g.inst + (size_t)gx * P.ny + g.col;
             FwdCoef f = fwd_coef(__ldg(P.b + cell), __ldg(P.c + cell), P.k);
             A[i] = f.A; Bc[i] = f.Bc; C2[i] = f.c2;
         }
@@ -387,7 +389,7 @@ WT_DEV void load_bwd_coef(const FusedParams& P, const Geo& g, float (&X1)[M], fl
         X1[i] = Kc[i] = Kg[i] = Ky2[i] = 0.f;
         int gx = g.gx0 + i;
         if (g.colv && gx < P.nx) {
-            size_t cell = (size_t)gx * P.ny + g.col;
+            size_t cell = P.coef_stride * g.inst + (size_t)gx * P.ny + g.col;
             BwdCoef k = bwd_coef(__ldg(P.b + cell), __ldg(P.c + cell), P.k);
             X1[i] = k.X1; Kc[i] = k.Kc; Kg[i] = k.Kg; Ky2[i] = k.Ky2;
         }
@@ -1169,14 +1171,36 @@ int wt_launch_probe_sum(int batch, int steps, int n_prb, const float* out, float
     return wt_cuda_status(cudaGetLastError());
 }
 
-static int launch_kernel(void (*kern)(wt::FusedParams), const wt::FusedParams& P, int C,
-                         int threads, size_t smem, cudaStream_t st) {
-    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+// Kernel attributes (dynamic shared memory size, non-portable cluster size)
+// are set once per kernel and device, and raised when a launch needs more:
+// not repeated on every launch, which keeps launches cheap on the host and
+// free of extra runtime calls while a stream is being captured.
+static int ensure_attributes(void (*kern)(wt::FusedParams), size_t smem, bool nonportable) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return wt_cuda_status(e);
-    if (C > 8) {
+    static std::mutex mu;
+    static std::map<std::pair<int, const void*>, std::pair<size_t, bool>> done;
+    std::lock_guard<std::mutex> lock(mu);
+    auto& v = done[{dev, reinterpret_cast<const void*>(kern)}];
+    if (v.first < smem) {
+        e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return wt_cuda_status(e);
+        v.first = smem;
+    }
+    if (nonportable && !v.second) {
         e = cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
         if (e != cudaSuccess) return wt_cuda_status(e);
+        v.second = true;
     }
+    return WT_OK;
+}
+
+static int launch_kernel(void (*kern)(wt::FusedParams), const wt::FusedParams& P, int C,
+                         int threads, size_t smem, cudaStream_t st) {
+    int rc = ensure_attributes(kern, smem, C > 8);
+    if (rc) return rc;
+    cudaError_t e;
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(C * P.batch, 1, 1);
     cfg.blockDim = dim3(threads, 1, 1);

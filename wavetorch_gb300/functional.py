@@ -129,6 +129,7 @@ class SeqSpec:
     segment: int = 0
     cluster: int = 0
     output_fields: bool = False
+    coef_batched: bool = False      # one geometry (b, c) per instance
 
     def desc(self):
         ns, np_ = len(self.sources), len(self.probes)
@@ -137,7 +138,7 @@ class SeqSpec:
         d = _lib.SeqDesc(self.batch, self.nx, self.ny, self.steps, ns,
                          C.cast(src, C.POINTER(_lib.SourceEntry)), np_,
                          C.cast(prb, C.POINTER(_lib.ProbeEntry)), self.form, self.segment,
-                         self.cluster, int(self.output_fields))
+                         self.cluster, int(self.output_fields), int(self.coef_batched))
         return d, (src, prb)   # keep the arrays alive with the descriptor
 
 
@@ -189,7 +190,7 @@ def seq_forward(spec: SeqSpec, sc: _lib.Scalars, b, c, x, want_sum: bool = False
 def seq_backward(spec: SeqSpec, sc: _lib.Scalars, b, c, x, grad_out, ws, want_x: bool):
     dev = c.device
     d, keep = spec.desc()
-    gc = torch.empty((spec.nx, spec.ny), device=dev)
+    gc = torch.empty(((spec.batch,) if spec.coef_batched else ()) + (spec.nx, spec.ny), device=dev)
     gx = torch.empty((spec.batch, spec.steps), device=dev) if want_x else None
     _lib.check(_lib.load().wt_seq_bwd(C.byref(sc), C.byref(d), _ptr(b), _ptr(c), _ptr(x),
                                       _ptr(grad_out), _ptr(gc), _ptr(gx), _ptr(ws), ws.numel(),

@@ -1,0 +1,243 @@
+"""Ragged batches: many single-instance wave models of different grid sizes
+and step counts, advanced together as one CUDA graph.
+
+The reference trains one ``WaveRNN`` at a time; a user with many models (a
+sweep over grid sizes, an ensemble) runs them one after another.  Here the
+instances are grouped by grid size and source/probe layout; a group runs as
+one fused sequence launch with one geometry per instance (``coef_batched``),
+its shorter inputs zero-padded to the group's longest step count and the
+loss masked to each instance's own steps, so its forward fields, losses and
+gradients are those of the instance run alone.  Every group runs on its own
+stream; one training step (rho -> c for every instance, the fused forwards,
+the losses and their gradients, the fused adjoints, c -> rho) is captured
+once into a CUDA graph and replayed.  A small autotuner times the cluster
+sizes each group's grid admits and keeps the fastest.
+
+Loss per instance: ``CrossEntropy(normalize_power(sum_t I), label)``, the
+reference's training loss (wavetorch/train.py:61-62, utils.py:35-36); its
+gradient with respect to the probe series is formed in closed form.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import time
+from dataclasses import dataclass, field
+from typing import Dict, List, Optional, Sequence
+
+import torch
+
+from . import _lib
+from .functional import (SeqSpec, _ptr, _stream, fused_supported, lap_order, scalars,
+                         seq_backward, seq_forward)
+from .geom import WaveGeometryFreeForm
+from .probe import WaveProbe
+from .source import WaveSource
+
+# cluster size chosen per (grid, source/probe layout) by the autotuner
+_TUNED: Dict[tuple, int] = {}
+
+
+@dataclass
+class _Group:
+    key: tuple
+    idx: List[int]
+    N: int
+    T: int
+    spec: SeqSpec
+    sc: _lib.Scalars
+    b: torch.Tensor                 # [G, N, N]
+    c: torch.Tensor                 # [G, N, N] (rho -> c writes each slice)
+    x: torch.Tensor                 # [G, T] zero-padded inputs
+    mask: torch.Tensor              # [G, T, 1] 1 for t < T_i
+    labels: torch.Tensor            # [G]
+    onehot: torch.Tensor            # [G, P]
+    work: List[torch.Tensor] = field(default_factory=list)   # rho -> c scratch per instance
+    stream: Optional[torch.cuda.Stream] = None
+
+
+def _check_model(m) -> None:
+    if not isinstance(m.cell.geom, WaveGeometryFreeForm):
+        raise TypeError("ragged batches need WaveGeometryFreeForm geometries")
+    if not m.cell.is_linear():
+        raise TypeError("ragged batches need linear cells (no saturable damping or Kerr term)")
+    if not all(isinstance(s, WaveSource) for s in m.sources) or \
+            not all(isinstance(p, WaveProbe) for p in m.probes):
+        raise TypeError("ragged batches need point sources and probes")
+
+
+class RaggedBatch:
+    """One training step over many models.
+
+    models: single-instance ``WaveRNN`` models (FreeForm geometry, linear
+    cell, point sources and probes), on one CUDA device.
+    inputs: one 1-D float32 input series per model (lengths may differ).
+    labels: one class index per model.
+
+    ``step()`` runs rho -> c, the forwards, the losses and the adjoints of all
+    models and leaves each model's ``cell.geom.rho.grad`` (overwritten, not
+    accumulated) and returns the per-model losses [n_models].
+    """
+
+    def __init__(self, models: Sequence, inputs: Sequence[torch.Tensor], labels, *,
+                 autotune: bool = True, graph: bool = True, segment: int = 0):
+        if not (len(models) == len(inputs) == len(labels)) or not models:
+            raise ValueError("models, inputs and labels must be non-empty and of equal length")
+        self.models = list(models)
+        dev = self.models[0].cell.geom.rho.device
+        if dev.type != "cuda":
+            raise RuntimeError("ragged batches run on CUDA devices only")
+        self.device = dev
+        for m in self.models:
+            _check_model(m)
+        self.T = [int(v.numel()) for v in inputs]
+        self.n = len(self.models)
+        # group by grid, physics scalars and source/probe layout
+        keys = {}
+        for i, m in enumerate(self.models):
+            nx, ny = m.cell.geom.domain_shape
+            if nx != ny:
+                raise ValueError("ragged batches take square grids")
+            dt, h = m.cell.scalars()[:2]
+            ptab, L = m.probe_table()
+            if L != 1:
+                raise ValueError("ragged batches take single-cell probes")
+            key = (nx, dt, h, tuple(m.source_table(1)), tuple(ptab), tuple(m.cell.geom.b.shape))
+            keys.setdefault(key, []).append(i)
+        self.groups: List[_Group] = []
+        for key, idx in sorted(keys.items(), key=lambda kv: -kv[0][0]):
+            N, dt, h, src, prb = key[0], key[1], key[2], list(key[3]), list(key[4])
+            G, T = len(idx), max(self.T[i] for i in idx)
+            x = torch.zeros(G, T, device=dev)
+            mask = torch.zeros(G, T, 1, device=dev)
+            for j, i in enumerate(idx):
+                x[j, :self.T[i]] = inputs[i].to(dev, torch.float32).reshape(-1)
+                mask[j, :self.T[i]] = 1.0
+            b = torch.stack([self.models[i].cell.geom.b for i in idx]).contiguous()
+            spec = SeqSpec(G, N, N, T, src, prb, form=_lib.WT_FORM_FUSED, segment=segment,
+                           coef_batched=True)
+            if not fused_supported(spec):
+                raise ValueError(f"a {N}x{N} grid is too large for the fused form")
+            # each model is an instance of its own: the Laplacian order of a batch of one
+            sc = scalars(dt, h, lap_order(1, N, N, h))
+            lab = torch.as_tensor([int(labels[i]) for i in idx], device=dev)
+            onehot = torch.nn.functional.one_hot(lab, len(prb)).to(torch.float32)
+            grp = _Group(key, idx, N, T, spec, sc, b, torch.empty(G, N, N, device=dev), x, mask,
+                         lab, onehot)
+            nwork = C.c_size_t(0)
+            for i in idx:
+                gd = self.models[i].cell.geom.geom_desc()
+                _lib.check(_lib.load().wt_rho_to_c_work_bytes(C.byref(gd), C.byref(nwork)),
+                           "wt_rho_to_c_work_bytes")
+                grp.work.append(torch.empty(nwork.value // 4, device=dev))
+            grp.stream = torch.cuda.Stream(device=dev)
+            self.groups.append(grp)
+        for m in self.models:
+            m.cell.geom.rho.grad = torch.zeros_like(m.cell.geom.rho)
+        if autotune:
+            self._autotune()
+        self.losses: Optional[torch.Tensor] = None
+        self.graph: Optional[torch.cuda.CUDAGraph] = None
+        if graph:
+            self._capture()
+
+    # -- one step, eagerly ------------------------------------------------
+    def _run(self) -> torch.Tensor:
+        lib = _lib.load()
+        main = torch.cuda.current_stream(self.device)
+        start = torch.cuda.Event()
+        start.record(main)
+        parts = [None] * self.n
+        done = []
+        for grp in self.groups:
+            grp.stream.wait_event(start)
+            with torch.cuda.stream(grp.stream):
+                st = _stream(self.device)
+                for j, i in enumerate(grp.idx):            # rho -> c into the group's stack
+                    geom = self.models[i].cell.geom
+                    _lib.check(lib.wt_rho_to_c_fwd(C.byref(geom.geom_desc()), _ptr(geom.rho),
+                                                   _ptr(geom.blur_kernel[0, 0]), _ptr(grp.c[j]),
+                                                   _ptr(grp.work[j]), st), "wt_rho_to_c_fwd")
+                out, _, _, ws = seq_forward(grp.spec, grp.sc, grp.b, grp.c, grp.x)
+                # loss = CE(normalize_power(sum over the instance's own steps))
+                I = (out * grp.mask).sum(dim=1)                     # [G, P]
+                S = I.sum(dim=1, keepdim=True)
+                p = I / S
+                lp = torch.log_softmax(p, dim=1)
+                loss = -lp.gather(1, grp.labels[:, None])[:, 0]     # [G]
+                dp = torch.softmax(p, dim=1) - grp.onehot
+                dI = (dp - (dp * p).sum(dim=1, keepdim=True)) / S   # dloss/dI
+                gout = (dI[:, None, :] * grp.mask).contiguous()     # dloss/d out, [G, T, P]
+                gc, _ = seq_backward(grp.spec, grp.sc, grp.b, grp.c, grp.x, gout, ws, False)
+                for j, i in enumerate(grp.idx):            # c -> rho
+                    geom = self.models[i].cell.geom
+                    _lib.check(lib.wt_rho_to_c_bwd(C.byref(geom.geom_desc()), _ptr(geom.rho),
+                                                   _ptr(geom.blur_kernel[0, 0]), _ptr(gc[j]),
+                                                   _ptr(geom.rho.grad), _ptr(grp.work[j]), st),
+                               "wt_rho_to_c_bwd")
+                for j, i in enumerate(grp.idx):
+                    parts[i] = loss[j:j + 1]
+                ev = torch.cuda.Event()
+                ev.record(grp.stream)
+                done.append(ev)
+        for ev in done:
+            main.wait_event(ev)
+        return torch.cat(parts)
+
+    def _capture(self) -> None:
+        side = torch.cuda.Stream(device=self.device)
+        side.wait_stream(torch.cuda.current_stream(self.device))
+        with torch.cuda.stream(side):
+            for _ in range(2):
+                self._run()
+        torch.cuda.current_stream(self.device).wait_stream(side)
+        torch.cuda.synchronize(self.device)
+        self.graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(self.graph):
+            self.losses = self._run()
+
+    def step(self) -> torch.Tensor:
+        """One training step of every model; returns the losses [n_models]."""
+        if self.graph is not None:
+            self.graph.replay()
+            return self.losses
+        return self._run()
+
+    # -- autotuner ----------------------------------------------------------
+    def _autotune(self, steps: int = 96) -> None:
+        """Pick each group's cluster size by timing a short forward + adjoint
+        of its instances for every size its grid admits (cached per layout)."""
+        for grp in self.groups:
+            if grp.key in _TUNED:
+                grp.spec.cluster = _TUNED[grp.key]
+                continue
+            T = min(grp.T, steps)
+            best, best_t = 0, float("inf")
+            x = grp.x[:, :T].contiguous()
+            g = torch.ones(len(grp.idx), T, len(grp.spec.probes), device=self.device)
+            c = torch.ones_like(grp.c) * 0.75
+            for cl in (1, 2, 4, 8, 16):
+                spec = SeqSpec(len(grp.idx), grp.N, grp.N, T, grp.spec.sources, grp.spec.probes,
+                               form=_lib.WT_FORM_FUSED, segment=grp.spec.segment, cluster=cl,
+                               coef_batched=True)
+                if not fused_supported(spec):
+                    continue
+                try:
+                    ts = []
+                    for r in range(3):
+                        torch.cuda.synchronize(self.device)
+                        t0 = time.perf_counter()
+                        _, _, _, ws = seq_forward(spec, grp.sc, grp.b, c, x)
+                        seq_backward(spec, grp.sc, grp.b, c, x, g, ws, False)
+                        torch.cuda.synchronize(self.device)
+                        if r:
+                            ts.append(time.perf_counter() - t0)
+                except _lib.WaveKernelError:
+                    continue
+                if min(ts) < best_t:
+                    best, best_t = cl, min(ts)
+            _TUNED[grp.key] = best
+            grp.spec.cluster = best
+
+    def cell_steps(self) -> int:
+        """Cell-steps of one training step (each model's N^2 x T_i)."""
+        return sum(self.models[i].cell.geom.domain_shape[0] ** 2 * self.T[i] for i in range(self.n))
