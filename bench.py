@@ -52,6 +52,9 @@ def parse():
     p.add_argument("--T", type=int, default=WORKLOAD["steps"])
     p.add_argument("--kernels-only", action="store_true",
                    help="run only the sequence kernels (forward + adjoint) -- the profiling case")
+    p.add_argument("--workload", choices=["batched", "ragged"], default="batched",
+                   help="ragged: many models of different grid sizes / step counts in one graph")
+    p.add_argument("--instances", type=int, default=256, help="models in the ragged workload")
     return p.parse_args()
 
 
@@ -453,8 +456,106 @@ def run_kernels_only(args):
                       "cell_steps_per_s": B * N * N * T / ((f + bw) / 1e3)}))
 
 
+def run_ragged(args):
+    """Ragged workload: `instances` single-instance models, grid side
+    U{64..256} (PML 20), step count U{500..4000}, the vowel-like generator
+    with independent seeds, source (20, N/2), intensity probes (N-20,
+    N/2 + {-15, 0, 15}); one training step of all models as one CUDA graph.
+    Compared with the per-model loops a user of the reference would run:
+    each model alone through WaveRNN, plain form and fused form, timed on a
+    16-model subsample and scaled by cell-steps."""
+    import numpy as np
+    import torch
+    import wavetorch_gb300 as wt
+    from wavetorch_gb300.data import vowel_like
+    from wavetorch_gb300.ragged import RaggedBatch
+    world, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    rng = np.random.default_rng(4321 + rank)
+    n = args.instances
+    sizes = rng.integers(64, 257, n)
+    steps = rng.integers(500, 4001, n)
+    models, inputs, labels = [], [], []
+    for i in range(n):
+        N = int(sizes[i])
+        geom = wt.WaveGeometryFreeForm((N, N), 1.0, c0=1.0, c1=0.5, abs_N=20, abs_sig=3.0, abs_p=2,
+                                       rho=torch.rand(N, N, generator=torch.Generator().manual_seed(i)))
+        models.append(wt.WaveRNN(wt.WaveCell(0.707, geom), wt.WaveSource(20, N // 2),
+                                 [wt.WaveIntensityProbe(N - 20, N // 2 + d) for d in (-15, 0, 15)]
+                                 ).to(dev))
+        x, lab = vowel_like(1, int(steps[i]), seed=1000 + i)
+        inputs.append(torch.from_numpy(x[0]).to(dev))
+        labels.append(int(lab[0]))
+    t0 = time.perf_counter()
+    rb = RaggedBatch(models, inputs, labels)
+    t_setup = time.perf_counter() - t0
+    cell_steps = rb.cell_steps()
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
+    stream = torch.cuda.current_stream(dev)
+    for _ in range(args.warmup):
+        rb.step()
+    torch.cuda.synchronize(dev)
+    ts = []
+    with ClockSampler(local) as clk:
+        for _ in range(args.steps):
+            flush.zero_()
+            e = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+            e[0].record(stream)
+            rb.step()
+            e[1].record(stream)
+            torch.cuda.synchronize(dev)
+            ts.append(e[0].elapsed_time(e[1]) / 1e3)
+    t_step = statistics.mean(ts)
+    # per-model loops on a 16-model subsample
+    sub = list(range(min(16, n)))
+    sub_cells = sum(int(sizes[i]) ** 2 * int(steps[i]) for i in sub)
+    loops = {}
+    for form in ("plain", "fused"):
+        tot = 0.0
+        for i in sub:
+            m = models[i]
+            m.form = form
+            lab = torch.tensor([labels[i]], device=dev)
+            for r in range(2):
+                torch.cuda.synchronize(dev)
+                a = time.perf_counter()
+                m.cell.geom.rho.grad = None
+                y = m(inputs[i][None])
+                loss = torch.nn.CrossEntropyLoss()(wt.utils.normalize_power(y.sum(dim=1)), lab)
+                loss.backward()
+                torch.cuda.synchronize(dev)
+                if r:
+                    tot += time.perf_counter() - a
+        loops[form] = sub_cells / tot
+    line = {
+        "metric": "cell-steps/s fwd+adjoint, ragged batch of models in one CUDA graph",
+        "value": cell_steps / t_step, "unit": "cell-steps/s", "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": t_step * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "fp32",
+        "data": "synthetic (seeded vowel-like waveforms, random-init rho)",
+        "config": {"workload": f"ragged: {n} models, N ~ U{{64..256}} (PML 20), T ~ U{{500..4000}}, "
+                               "fwd + adjoint to dL/drho per model",
+                   "instances": n, "groups": len(rb.groups), "cell_steps": cell_steps,
+                   "l2": "flushed (512 MiB write) before every timed step",
+                   "setup_s": t_setup},
+        "per_model_loop": {"plain_cell_steps_per_s": loops["plain"],
+                           "fused_cell_steps_per_s": loops["fused"],
+                           "ragged_over_plain_loop": (cell_steps / t_step) / loops["plain"],
+                           "ragged_over_fused_loop": (cell_steps / t_step) / loops["fused"],
+                           "sample": f"{len(sub)} models, {sub_cells} cell-steps, each alone "
+                                     "through WaveRNN (forward, CE loss, backward)"},
+        "clocks": clk.summary(),
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
+    if args.workload == "ragged" and args.impl == "ours":
+        run_ragged(args)
+        return
     if args.kernels_only:
         run_kernels_only(args)
     elif args.impl == "reference":

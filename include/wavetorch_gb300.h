@@ -140,6 +140,7 @@ typedef struct wt_seq_desc {
  *       segment's forward (workspace ~ 2 fields per segment).
  *    0  automatic: the tape when it takes at most 16 GiB, else checkpoints at
  *       the largest interval whose recompute stash fits in shared memory.
+ *   -2  checkpoints at that automatic interval (never the tape).
  * Both modes give identical results.  The plain form ignores it.            */
 
 /* Bytes of workspace that wt_seq_fwd must be given and that must be handed,

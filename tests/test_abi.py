@@ -114,7 +114,8 @@ def test_fused_plan_size_limit(lib):
 
 def test_fused_adjoint_modes(lib):
     """segment -1: tape (T x batch x nx x ny floats plus strip padding); > 0:
-    checkpoints; 0: the tape up to 16 GiB, else checkpoints; < -1 invalid."""
+    checkpoints; 0: the tape up to 16 GiB, else checkpoints; -2: checkpoints
+    at the automatic interval; below -2 invalid."""
     from wavetorch_gb300 import _lib
     from wavetorch_gb300.functional import SeqSpec, seq_workspace_bytes
     prb = [(80 * 120 + y, 1, i) for i, y in enumerate((35, 50, 65))]
@@ -125,7 +126,8 @@ def test_fused_adjoint_modes(lib):
     assert sz(32, 11) < 2 * 2**30
     assert sz(128, 0) < 8 * 2**30         # a 25.8 GB tape: checkpoints instead
     assert sz(128, -1) > 4 * tape
-    d, keep = SeqSpec(32, 120, 120, 3500, [(2460, -1)], prb, segment=-2).desc()
+    assert sz(32, -2) < 2 * 2**30            # -2: checkpoints at the automatic interval
+    d, keep = SeqSpec(32, 120, 120, 3500, [(2460, -1)], prb, segment=-3).desc()
     n = C.c_size_t(0)
     assert lib.wt_seq_workspace_bytes(C.byref(d), C.byref(n)) == _lib.WT_ERR_INVALID
 

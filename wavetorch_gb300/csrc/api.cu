@@ -161,7 +161,7 @@ int make_plan(const wt_seq_desc* d, SeqPlan* p) {
         P.o_lam = o; o = up(o + 3 * bp * F);
         P.o_gc = o; o = up(o + bp * F);
     } else {
-        if (d->segment < -1) return WT_ERR_INVALID;
+        if (d->segment < -2) return WT_ERR_INVALID;
         int st = wt_fused_plan(P.nx, P.ny, P.T, P.np, d->cluster, d->segment, &P.L);
         if (st) return st;
         const size_t tape_bytes = (size_t)P.T * P.B * P.L.C * P.L.threads * P.L.M * F;

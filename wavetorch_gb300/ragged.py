@@ -28,7 +28,7 @@ import torch
 
 from . import _lib
 from .functional import (SeqSpec, _ptr, _stream, fused_supported, lap_order, scalars,
-                         seq_backward, seq_forward)
+                         seq_backward, seq_forward, seq_workspace_bytes)
 from .geom import WaveGeometryFreeForm
 from .probe import WaveProbe
 from .source import WaveSource
@@ -131,6 +131,8 @@ class RaggedBatch:
                 grp.work.append(torch.empty(nwork.value // 4, device=dev))
             grp.stream = torch.cuda.Stream(device=dev)
             self.groups.append(grp)
+        if segment == 0:
+            self._fit_memory()
         for m in self.models:
             m.cell.geom.rho.grad = torch.zeros_like(m.cell.geom.rho)
         if autotune:
@@ -139,6 +141,24 @@ class RaggedBatch:
         self.graph: Optional[torch.cuda.CUDAGraph] = None
         if graph:
             self._capture()
+
+    def _fit_memory(self, share: float = 0.3) -> None:
+        """Groups whose tapes would take the workspaces past `share` of the
+        device's memory (largest first) use checkpoints instead (segment -2)."""
+        total_mem = torch.cuda.get_device_properties(self.device).total_memory
+        sizes = [seq_workspace_bytes(g.spec) for g in self.groups]
+        total = sum(sizes)
+        for k in sorted(range(len(self.groups)), key=lambda k: -sizes[k]):
+            if total <= share * total_mem:
+                break
+            g = self.groups[k]
+            g.spec.segment = -2
+            new = seq_workspace_bytes(g.spec)
+            total += new - sizes[k]
+
+    def workspace_bytes(self) -> int:
+        """Device bytes the sequence workspaces of one step take."""
+        return sum(seq_workspace_bytes(g.spec) for g in self.groups)
 
     # -- one step, eagerly ------------------------------------------------
     def _run(self) -> torch.Tensor:
@@ -191,6 +211,7 @@ class RaggedBatch:
                 self._run()
         torch.cuda.current_stream(self.device).wait_stream(side)
         torch.cuda.synchronize(self.device)
+        torch.cuda.empty_cache()   # the warm-up's workspaces: the graph gets its own pool
         self.graph = torch.cuda.CUDAGraph()
         with torch.cuda.graph(self.graph):
             self.losses = self._run()
