@@ -178,6 +178,33 @@ int wt_seq_bwd(const wt_scalars* s, const wt_seq_desc* d,
 int wt_seq_device_status(const wt_seq_desc* d, const void* workspace, size_t workspace_bytes,
                          wt_stream_t stream);
 
+/* ---- the nonlinear cell ----------------------------------------------------
+ * WaveCell with satdamp_b0 > 0 and/or c_nl != 0 (wavetorch/cell.py:8-9,
+ * :93-101): every step, at every cell,
+ *   b = b_pml + rho * satdamp_b0 / (1 + |h1 / satdamp_uth|^2)   (if b0 > 0)
+ *   c = c_lin + (rho * c_nl) * h1^2                              (if c_nl != 0)
+ * with h1 the field one step ago, then the leapfrog step with these b and c.
+ * Fused form only, with the adjoint reading a two-part tape (Lap(h1), h1:
+ * twice the linear tape); `segment` must be 0 or -1 and output_fields 0.
+ * b: b_pml, c_lin: the linear speed, rho: the density the nonlinear terms
+ * are weighted with (the geometry's raw rho), each [nx,ny] (or
+ * [batch,nx,ny] with coef_batched).  The backward returns dLoss/dc_lin in
+ * grad_c and the direct dLoss/drho through b and c in grad_rho (both
+ * [nx,ny] summed over the batch, or per instance with coef_batched).      */
+typedef struct wt_nonlinear {
+    float satdamp_b0, satdamp_uth, c_nl;   /* float32 values of the buffers */
+} wt_nonlinear;
+
+int wt_seq_workspace_bytes_nl(const wt_seq_desc* d, size_t* bytes);
+int wt_seq_fwd_nl(const wt_scalars* s, const wt_seq_desc* d, const wt_nonlinear* nl,
+                  const float* b, const float* c_lin, const float* rho, const float* x,
+                  float* out, float* probe_sum, void* workspace, size_t workspace_bytes,
+                  wt_stream_t stream);
+int wt_seq_bwd_nl(const wt_scalars* s, const wt_seq_desc* d, const wt_nonlinear* nl,
+                  const float* b, const float* c_lin, const float* rho, const float* x,
+                  const float* grad_out, float* grad_c, float* grad_rho, float* grad_x,
+                  void* workspace, size_t workspace_bytes, wt_stream_t stream);
+
 /* ======================================================================== *
  * 3. Free-form geometry: rho -> c (wavetorch/geom.py:207-233).              *
  * ======================================================================== */

@@ -213,3 +213,27 @@ def test_per_instance_geometries(cuda, N):
         o1, g1 = run(one, sc, bs, cs[i], x[i:i + 1].contiguous(), g[i:i + 1].contiguous())
         assert torch.equal(out[i:i + 1], o1), i
         assert rel(gc[i].cpu().numpy(), g1.cpu().numpy()) <= 1e-6, i
+
+
+@pytest.mark.parametrize("b0,cnl", [(0.05, 0.1), (0.05, 0.0), (0.0, 0.1)])
+def test_nonlinear_fused_matches_step_form(cuda, b0, cnl):
+    """B=4, 120x120, 400 steps, nonlinearity where rho > 0.5: the fused
+    nonlinear sequence forms b and c with the same float32 operations as the
+    per-step form, so the probe series agree bit for bit; dL/drho within 1e-5."""
+    N, B, steps = 120, 4, 400
+    rho0 = torch.rand(N, N, generator=torch.Generator().manual_seed(21))
+    x = torch.from_numpy(vowel_like(B, steps, seed=21)[0] * np.float32(0.2)).to(cuda)
+    labels = torch.tensor([0, 1, 2, 1], device=cuda)
+    res = {}
+    for form in ("step", "fused"):
+        geom = wt.WaveGeometryFreeForm((N, N), 1.0, c0=1.0, c1=0.5, abs_N=20, abs_sig=3.0, abs_p=2,
+                                       rho=rho0)
+        cell = wt.WaveCell(0.707, geom, satdamp_b0=b0, satdamp_uth=float(np.sqrt(0.1)), c_nl=cnl)
+        m = wt.WaveRNN(cell, wt.WaveSource(20, 60),
+                       [wt.WaveIntensityProbe(80, y) for y in (35, 50, 65)], form=form).to(cuda)
+        y = m(x)
+        loss = torch.nn.CrossEntropyLoss()(wt.utils.normalize_power(y.sum(dim=1)), labels)
+        loss.backward()
+        res[form] = (y.detach(), m.cell.geom.rho.grad.detach())
+    assert torch.equal(res["step"][0], res["fused"][0])
+    assert rel(res["fused"][1].cpu().numpy(), res["step"][1].cpu().numpy()) <= 1e-5

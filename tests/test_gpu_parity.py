@@ -161,9 +161,13 @@ def test_end_to_end_training_step(cuda, name, form):
     assert rel(m.cell.geom.rho.grad.cpu().numpy(), d["grad_rho"]) <= E2E_TOL[name]
 
 
-def test_nonlinear_step_form(cuda):
+@pytest.mark.parametrize("form", ["step", "fused"])
+def test_nonlinear_cell(cuda, form):
+    """Saturable damping and Kerr term: the per-step form (torch ops for b, c)
+    and the fused form (b, c formed in the kernels, hand-written adjoint
+    through them) against the reference."""
     d = golden("nonlinear")
-    m = build_model(d, cuda, "step", cnl=float(d["c_nl"]), b0=float(d["satdamp_b0"]),
+    m = build_model(d, cuda, form, cnl=float(d["c_nl"]), b0=float(d["satdamp_b0"]),
                     uth=float(d["satdamp_uth"]))
     y = m(T(d["x"], cuda))
     loss = torch.nn.CrossEntropyLoss()(wt.utils.normalize_power(y.sum(dim=1)),
@@ -213,7 +217,7 @@ def test_in_place_edits_of_coordinates_and_scalars_are_seen(cuda):
 
 
 @pytest.mark.parametrize("name,form", [("fd64_linear", "fused"), ("fd64_linear", "plain"),
-                                       ("fd64_nonlinear", "step")])
+                                       ("fd64_nonlinear", "step"), ("fd64_nonlinear", "fused")])
 def test_grad_rho_against_fp64_central_differences(cuda, name, form):
     """dL/drho (float32, hand-written adjoint) at 16 random design cells
     against central differences of the reference run in float64 (eps 1e-5;

@@ -29,6 +29,7 @@ EXPORTED = [
     "wt_version", "wt_status_string", "wt_last_error", "wt_kernel_launches",
     "wt_step_fwd", "wt_step_bwd",
     "wt_seq_workspace_bytes", "wt_seq_fwd", "wt_seq_bwd", "wt_seq_device_status",
+    "wt_seq_workspace_bytes_nl", "wt_seq_fwd_nl", "wt_seq_bwd_nl",
     "wt_rho_to_c_fwd", "wt_rho_to_c_bwd", "wt_rho_to_c_work_bytes", "wt_rho_to_c_fwd_noalloc",
 ]
 
@@ -57,6 +58,10 @@ class SeqDesc(C.Structure):
         ("form", C.c_int32), ("segment", C.c_int32), ("cluster", C.c_int32),
         ("output_fields", C.c_int32), ("coef_batched", C.c_int32),
     ]
+
+
+class NonLinear(C.Structure):
+    _fields_ = [("satdamp_b0", C.c_float), ("satdamp_uth", C.c_float), ("c_nl", C.c_float)]
 
 
 class GeomDesc(C.Structure):
@@ -89,6 +94,11 @@ def _declare(lib):
     lib.wt_seq_bwd.argtypes = [P(Scalars), P(SeqDesc), _VP, _VP, _VP, _VP, _VP, _VP, _VP,
                                C.c_size_t, _VP]
     lib.wt_seq_device_status.argtypes = [P(SeqDesc), _VP, C.c_size_t, _VP]
+    lib.wt_seq_workspace_bytes_nl.argtypes = [P(SeqDesc), P(C.c_size_t)]
+    lib.wt_seq_fwd_nl.argtypes = [P(Scalars), P(SeqDesc), P(NonLinear), _VP, _VP, _VP, _VP, _VP,
+                                  _VP, _VP, C.c_size_t, _VP]
+    lib.wt_seq_bwd_nl.argtypes = [P(Scalars), P(SeqDesc), P(NonLinear), _VP, _VP, _VP, _VP, _VP,
+                                  _VP, _VP, _VP, _VP, C.c_size_t, _VP]
     lib.wt_rho_to_c_fwd.argtypes = [P(GeomDesc), _VP, _VP, _VP, _VP, _VP]
     lib.wt_rho_to_c_bwd.argtypes = [P(GeomDesc), _VP, _VP, _VP, _VP, _VP, _VP]
     lib.wt_rho_to_c_work_bytes.argtypes = [P(GeomDesc), P(C.c_size_t)]

@@ -108,14 +108,14 @@ struct SeqPlan {
     // float areas
     size_t o_amp;
     size_t o_hist, o_zero, o_lam, o_gc;             // plain
-    size_t o_ckpt, o_stash, o_gcpart, o_lap;        // fused
+    size_t o_ckpt, o_stash, o_gcpart, o_lap, o_grho; // fused
     size_t total;
     int seg, nseg;
     bool tape;                                      // fused: tape mode
     WtFusedLaunch L;
 };
 
-int make_plan(const wt_seq_desc* d, SeqPlan* p) {
+int make_plan(const wt_seq_desc* d, SeqPlan* p, bool nl = false) {
     if (!d || d->batch <= 0 || d->nx <= 0 || d->ny <= 0 || d->steps <= 0) return WT_ERR_INVALID;
     if (d->n_sources < 0 || d->n_probes < 0) return WT_ERR_INVALID;
     if ((d->n_sources > 0 && !d->sources_host) || (d->n_probes > 0 && !d->probes_host))
@@ -164,9 +164,18 @@ int make_plan(const wt_seq_desc* d, SeqPlan* p) {
         if (d->segment < -2) return WT_ERR_INVALID;
         int st = wt_fused_plan(P.nx, P.ny, P.T, P.np, d->cluster, d->segment, &P.L);
         if (st) return st;
-        const size_t tape_bytes = (size_t)P.T * P.B * P.L.C * P.L.threads * P.L.M * F;
-        P.tape = P.L.nbuf >= 2 &&
-                 (d->segment == -1 || (d->segment == 0 && tape_bytes <= WT_TAPE_AUTO_MAX_BYTES));
+        const size_t tape_bytes = (size_t)(nl ? 2 : 1) * P.T * P.B * P.L.C * P.L.threads * P.L.M * F;
+        if (nl) {
+            // the nonlinear adjoint runs from a two-part tape only (it reads
+            // the field of the next slot as well, so at least 3 slots)
+            if (d->segment > 0 || d->segment == -2 || d->output_fields || P.L.nbuf_nl < 3)
+                return WT_ERR_UNSUPPORTED;
+            P.L.nbuf = P.L.nbuf_nl;
+            P.tape = true;
+        } else {
+            P.tape = P.L.nbuf >= 2 &&
+                     (d->segment == -1 || (d->segment == 0 && tape_bytes <= WT_TAPE_AUTO_MAX_BYTES));
+        }
         if (d->segment == -1 && !P.tape) return WT_ERR_UNSUPPORTED;
         if (P.tape) {
             // the forward runs on the adjoint's strips so that the tape's
@@ -185,6 +194,7 @@ int make_plan(const wt_seq_desc* d, SeqPlan* p) {
             P.o_stash = o; o = up(o + (P.L.stash_smem ? 0 : (size_t)P.seg * per_step));
         }
         P.o_gcpart = o; o = up(o + bp * F);
+        if (nl) { P.o_grho = o; o = up(o + bp * F); }
         // per-thread tap capacity of both fused kernels (4 sources, 4 probes)
         for (int layout = 0; layout < 2; ++layout) {
             const int R = layout ? P.L.fR : P.L.R, M = layout ? P.L.fM : P.L.M;
@@ -454,4 +464,81 @@ extern "C" int wt_seq_device_status(const wt_seq_desc* d, const void* workspace,
     if (h == WT_DEVERR_BOUNDS) return WT_ERR_INVALID;
     if (h == WT_DEVERR_TIMEOUT) return WT_ERR_TIMEOUT;
     return WT_OK;
+}
+
+// ---------------------------------------------------------------------------
+// 3. sequences of the nonlinear cell (fused form, tape mode)
+static bool nl_ok(const wt_nonlinear* nl) {
+    return nl && std::isfinite(nl->satdamp_b0) && std::isfinite(nl->satdamp_uth) &&
+           std::isfinite(nl->c_nl) && (nl->satdamp_b0 <= 0.f || nl->satdamp_uth != 0.f);
+}
+
+extern "C" int wt_seq_workspace_bytes_nl(const wt_seq_desc* d, size_t* bytes) {
+    if (!bytes) return WT_ERR_INVALID;
+    SeqPlan P;
+    int st = make_plan(d, &P, true);
+    if (st) return st;
+    if (P.form != WT_FORM_FUSED) return WT_ERR_UNSUPPORTED;
+    *bytes = P.total;
+    return WT_OK;
+}
+
+static void nl_params(wt::FusedParams& F, const SeqPlan& P, const wt_nonlinear* nl, const float* rho,
+                      void* ws) {
+    F.rho = rho;
+    F.b0 = nl->satdamp_b0;
+    F.uth = nl->satdamp_uth;
+    F.cnl = nl->c_nl;
+    F.grho_part = at<float>(ws, P.o_grho);
+}
+
+extern "C" int wt_seq_fwd_nl(const wt_scalars* s, const wt_seq_desc* d, const wt_nonlinear* nl,
+                             const float* b, const float* c_lin, const float* rho, const float* x,
+                             float* out, float* probe_sum, void* workspace, size_t workspace_bytes,
+                             wt_stream_t stream) {
+    if (!scalars_ok(s) || !nl_ok(nl)) return WT_ERR_INVALID;
+    SeqPlan P;
+    int st = make_plan(d, &P, true);
+    if (st) return st;
+    if (P.form != WT_FORM_FUSED) return WT_ERR_UNSUPPORTED;
+    if (!b || !c_lin || !rho || !workspace || workspace_bytes < P.total) return WT_ERR_INVALID;
+    if (P.ns > 0 && !x) return WT_ERR_INVALID;
+    if (P.np > 0 && !out) return WT_ERR_INVALID;
+    cudaStream_t cs = (cudaStream_t)stream;
+    if ((st = upload_tables(d, P, workspace, cs))) return st;
+    wt::FusedParams F = fused_params(s, P, b, c_lin, x, workspace);
+    nl_params(F, P, nl, rho, workspace);
+    F.out = out;
+    if ((st = wt_launch_fused_nl(true, F, P.L, cs))) return st;
+    if (probe_sum && P.np > 0) return wt_launch_probe_sum(P.B, P.T, P.np, out, probe_sum, cs);
+    return WT_OK;
+}
+
+extern "C" int wt_seq_bwd_nl(const wt_scalars* s, const wt_seq_desc* d, const wt_nonlinear* nl,
+                             const float* b, const float* c_lin, const float* rho, const float* x,
+                             const float* grad_out, float* grad_c, float* grad_rho, float* grad_x,
+                             void* workspace, size_t workspace_bytes, wt_stream_t stream) {
+    if (!scalars_ok(s) || !nl_ok(nl)) return WT_ERR_INVALID;
+    SeqPlan P;
+    int st = make_plan(d, &P, true);
+    if (st) return st;
+    if (P.form != WT_FORM_FUSED) return WT_ERR_UNSUPPORTED;
+    if (!b || !c_lin || !rho || !grad_c || !grad_rho || !workspace || workspace_bytes < P.total)
+        return WT_ERR_INVALID;
+    if (P.np > 0 && !grad_out) return WT_ERR_INVALID;
+    if (grad_x) {
+        int own = 0;
+        for (int i = 0; i < P.ns; ++i) own += d->sources_host[i].in_row < 0;
+        if (own != 1 || P.ns != 1) return WT_ERR_UNSUPPORTED;
+    }
+    cudaStream_t cs = (cudaStream_t)stream;
+    wt::FusedParams F = fused_params(s, P, b, c_lin, x, workspace);
+    nl_params(F, P, nl, rho, workspace);
+    F.grad_out = grad_out;
+    F.grad_x = grad_x;
+    if (P.coef_batched) { F.gc_part = grad_c; F.grho_part = grad_rho; }
+    if ((st = wt_launch_fused_nl(false, F, P.L, cs))) return st;
+    if (P.coef_batched) return WT_OK;
+    if ((st = wt_launch_seq_adj_reduce(P.B, P.plane, F.gc_part, grad_c, 1, cs))) return st;
+    return wt_launch_seq_adj_reduce(P.B, P.plane, F.grho_part, grad_rho, 1, cs);
 }

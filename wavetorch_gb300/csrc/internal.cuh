@@ -73,6 +73,11 @@ struct FusedParams {
     // adjoint streams it back instead of recomputing segments
     float* lap;             // [steps][batch][C][M/V][threads][V] or null (checkpoint mode)
     int nbuf;               // tape slices in the adjoint's shared-memory ring
+    // nonlinear cell (wavetorch/cell.py:8-9, :93-101): b and c formed every
+    // step from the field; the tape then holds Lap(h_{t-1}) and h_{t-1}
+    const float* rho;       // density (as b, c: shared or per instance)
+    float b0, uth, cnl;     // satdamp_b0, satdamp_uth, c_nl (float32 values)
+    float* grho_part;       // [batch][nx][ny] per-instance direct dL/drho
     int* err;
 };
 
@@ -102,6 +107,8 @@ struct WtFusedLaunch {
     int nbuf;
     size_t smem_tape;       // adjoint shared memory in tape mode
     size_t smem_fwd_tape;   // forward shared memory in tape mode
+    size_t smem_bwd_base;   // adjoint shared memory before the tape ring
+    int nbuf_nl;            // ring slices of the nonlinear adjoint (two-part slices)
 };
 
 int wt_launch_step_fwd(const StepScalars& k, int batch, int nx, int ny, int coef_batched,
@@ -126,3 +133,5 @@ int wt_fused_plan(int nx, int ny, int steps, int n_prb, int cluster_req, int seg
 int wt_launch_probe_sum(int batch, int steps, int n_prb, const float* out, float* sum,
                         cudaStream_t st);
 int wt_launch_fused(bool fwd, const wt::FusedParams& P, const WtFusedLaunch& L, cudaStream_t st);
+// Nonlinear cell, tape mode: nbuf ring slices of two parts (Lap, field).
+int wt_launch_fused_nl(bool fwd, const wt::FusedParams& P, const WtFusedLaunch& L, cudaStream_t st);

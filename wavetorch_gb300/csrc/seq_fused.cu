@@ -35,6 +35,7 @@
 #include <cmath>
 #include <map>
 #include <mutex>
+#include <type_traits>
 
 #include "internal.cuh"
 
@@ -99,6 +100,38 @@ WT_DEV void st_chunks(float* base, int NT, int tid, const float (&s)[M]) {
             *reinterpret_cast<float2*>(p) = make_float2(s[2 * j], s[2 * j + 1]);
         else
             *p = s[j];
+    }
+}
+// st_chunks from the thread's own chunk-0 address p (stride: floats between chunks).
+template <int M>
+WT_DEV void st_chunks_at(float* p, int stride, const float (&s)[M]) {
+    constexpr int V = chunk_width<M>();
+#pragma unroll
+    for (int j = 0; j < M / V; ++j) {
+        float* q = p + j * stride;
+        if constexpr (V == 4)
+            *reinterpret_cast<float4*>(q) = make_float4(s[4 * j], s[4 * j + 1], s[4 * j + 2], s[4 * j + 3]);
+        else if constexpr (V == 2)
+            *reinterpret_cast<float2*>(q) = make_float2(s[2 * j], s[2 * j + 1]);
+        else
+            *q = s[j];
+    }
+}
+template <int M>
+WT_DEV void ld_chunks_at(float (&d)[M], const float* p, int stride) {
+    constexpr int V = chunk_width<M>();
+#pragma unroll
+    for (int j = 0; j < M / V; ++j) {
+        const float* q = p + j * stride;
+        if constexpr (V == 4) {
+            float4 v = *reinterpret_cast<const float4*>(q);
+            d[4 * j] = v.x; d[4 * j + 1] = v.y; d[4 * j + 2] = v.z; d[4 * j + 3] = v.w;
+        } else if constexpr (V == 2) {
+            float2 v = *reinterpret_cast<const float2*>(q);
+            d[2 * j] = v.x; d[2 * j + 1] = v.y;
+        } else {
+            d[j] = *q;
+        }
     }
 }
 template <int M>
@@ -456,13 +489,46 @@ WT_DEV void fwd_update(const FusedParams& P, const Geo& g, const Xchg& X, const 
     }
 }
 
+// Field-dependent coefficients of the nonlinear cell, in the reference's
+// operation order (wavetorch/cell.py:8-9, :93-101):
+//   sat = b0 / (1 + |h1 / uth|^2),  b = b_pml + rho * sat     (if b0 > 0)
+//   c = c_lin + (rho * c_nl) * h1^2                           (if c_nl != 0)
+struct NLCoef { float b, c, sat, q; };
+WT_DEV NLCoef nl_coef(const FusedParams& P, float bpml, float clin, float rho, float h1) {
+    NLCoef r;
+    r.b = bpml; r.c = clin; r.sat = 0.f; r.q = 0.f;
+    if (P.b0 > 0.f) {
+        r.q = fdiv(h1, P.uth);
+        const float a = fabsf(r.q);
+        r.sat = fdiv(P.b0, fadd(1.0f, fmul(a, a)));
+        r.b = fadd(bpml, fmul(rho, r.sat));
+    }
+    if (P.cnl != 0.f) r.c = fadd(clin, fmul(fmul(rho, P.cnl), fmul(h1, h1)));
+    return r;
+}
+
 // fwd_update for the forward kernel's step loop, on precomputed addresses:
 // step t reads tile slot RS = t & 1 and the halo words of exchange t-1
 // (parity RS ^ 1), writes slot RS ^ 1 and sends exchange t (parity RS).
-template <int M, int ORDER, int RS>
+// Nonlinear cell (NL): k0, k1, k2 hold b_pml, c_lin and rho, and the update
+// coefficients are formed from them and h_{t-1} every step; linear: k0, k1,
+// k2 are the update coefficients A, Bc, c^2 themselves.
+template <bool NL>
+WT_DEV void cell_coef(const FusedParams& P, float k0, float k1, float k2, float h1, float& A,
+                      float& Bc, float& C2) {
+    if constexpr (NL) {
+        const NLCoef n = nl_coef(P, k0, k1, k2, h1);
+        const FwdCoef f = fwd_coef(n.b, n.c, P.k);
+        A = f.A; Bc = f.Bc; C2 = f.c2;
+    } else {
+        A = k0; Bc = k1; C2 = k2;
+    }
+}
+
+template <int M, int ORDER, int RS, bool NL = false>
 WT_DEV void fwd_update_lane(const FusedParams& P, const Geo& g, const Xchg& X, const Lane& ln,
                             const Taps& tp, int t, bool send, float (&xv)[SRCMAX],
-                            const float (&A)[M], const float (&Bc)[M], const float (&C2)[M],
+                            const float (&k0)[M], const float (&k1)[M], const float (&k2)[M],
                             const float (&cur)[M], float (&inout)[M], float (&L)[M]) {
     if (!g.colv) return;
     const float* rcol = ln.col0 + RS * ln.tile;
@@ -476,21 +542,21 @@ WT_DEV void fwd_update_lane(const FusedParams& P, const Geo& g, const Xchg& X, c
         if (ln.rup) c.up = recv_at(P, X, ln.rup + (RS ^ 1) * ln.pstride, t - 1);
         if (ln.rdn) c.dn = recv_at(P, X, ln.rdn + (RS ^ 1) * ln.pstride, t - 1);
     }
-    L[0] = lap_cell<M, ORDER>(P, c, cur, 0);
-    inout[0] = leapfrog(A[0], Bc[0], C2[0], P.k.two_over, cur[0], inout[0], L[0]);
-    L[M - 1] = lap_cell<M, ORDER>(P, c, cur, M - 1);
-    inout[M - 1] = leapfrog(A[M - 1], Bc[M - 1], C2[M - 1], P.k.two_over, cur[M - 1],
-                            inout[M - 1], L[M - 1]);
+    auto update = [&](int i) {
+        float A, Bc, C2;
+        cell_coef<NL>(P, k0[i], k1[i], k2[i], cur[i], A, Bc, C2);
+        L[i] = lap_cell<M, ORDER>(P, c, cur, i);
+        inout[i] = leapfrog(A, Bc, C2, P.k.two_over, cur[i], inout[i], L[i]);
+    };
+    update(0);
+    update(M - 1);
     const unsigned long long tag = (unsigned long long)(uint32_t)(t + 1) << 32;
     if (send && !tp.src_edge) {
         if (ln.sup) st_cluster_u64(ln.sup + RS * ln.pstride, tag | __float_as_uint(inout[0]));
         if (ln.sdn) st_cluster_u64(ln.sdn + RS * ln.pstride, tag | __float_as_uint(inout[M - 1]));
     }
 #pragma unroll
-    for (int i = 1; i < M - 1; ++i) {
-        L[i] = lap_cell<M, ORDER>(P, c, cur, i);
-        inout[i] = leapfrog(A[i], Bc[i], C2[i], P.k.two_over, cur[i], inout[i], L[i]);
-    }
+    for (int i = 1; i < M - 1; ++i) update(i);
     sts_col<M>(wcol, inout);
     if (tp.ns) {
         apply_sources<M>(P, g, X, tp, RS ^ 1, inout, xv, t + 1);
@@ -672,6 +738,104 @@ __global__ void __launch_bounds__(fwd_max_threads(M), 1) seq_fwd_fused_kernel(Fu
                 st.pb ^= 1;
                 chunk0 = t + 1;
             }
+        }
+    }
+    if (st.pc > 0) flush_probes(P, g, pr, st.pb, chunk0, st.pc);
+    cluster_sync_all();
+}
+
+// ============================================================================
+// Nonlinear cell, forward (tape mode): as seq_fwd_fused_kernel, with b and c
+// formed every step from h_{t-1} (nl_coef) and a two-part tape per step:
+// Lap(h_{t-1}) and h_{t-1}, each chunk-major (threads x M floats).
+template <int M>
+WT_DEV void load_nl_coef(const FusedParams& P, const Geo& g, float (&bp)[M], float (&cl)[M],
+                         float (&rh)[M]) {
+#pragma unroll
+    for (int i = 0; i < M; ++i) {
+        bp[i] = cl[i] = rh[i] = 0.f;
+        int gx = g.gx0 + i;
+        if (g.colv && gx < P.nx) {
+            size_t cell = P.coef_stride * g.inst + (size_t)gx * P.ny + g.col;
+            bp[i] = __ldg(P.b + cell);
+            cl[i] = __ldg(P.c + cell);
+            rh[i] = __ldg(P.rho + cell);
+        }
+    }
+}
+
+template <int M, int ORDER, int RS>
+WT_DEV void fwd_step_nl(const FusedParams& P, const Geo& g, const Xchg& X, const Lane& ln,
+                        const Taps& tp, FwdState& st, const ProbeRing& pr, int t, float* tape,
+                        const float (&bp)[M], const float (&cl)[M], const float (&rh)[M],
+                        const float (&cur)[M], float (&inout)[M]) {
+    float L[M];
+    fwd_update_lane<M, ORDER, RS, true>(P, g, X, ln, tp, t, t + 1 < P.steps, st.xv, bp, cl, rh,
+                                        cur, inout, L);
+    if (!g.colv) return;
+    const int stride = (int)blockDim.x * chunk_width<M>();
+    st_chunks_at<M>(tape, stride, L);
+    st_chunks_at<M>(tape + (size_t)blockDim.x * M, stride, cur);
+    if (tp.np) {
+        const float* colp = ln.col0 + (RS ^ 1) * ln.tile;
+        float* row = pr.buf + (size_t)st.pb * P.n_prb * P.PB + st.pc;
+#pragma unroll
+        for (int e = 0; e < PRBMAX; ++e)
+            if (e < tp.np) row[tp.prb_col(e) * P.PB] = colp[tp.prb_i(e)];
+    }
+}
+
+template <int M, int ORDER>
+__global__ void __launch_bounds__(fwd_max_threads(M), 1) seq_fwd_nl_kernel(FusedParams P) {
+    extern __shared__ __align__(16) float smem[];
+    __shared__ int abort_flag;
+    const Geo g = make_geo(P, M);
+    const int tile = (P.ny + 2) * P.LD;
+    ProbeRing pr;
+    pr.buf = smem + 2 * tile + 2 * xchg_words(P.NCP);
+    pr.own = reinterpret_cast<int*>(pr.buf + 2 * P.n_prb * P.PB);
+    zero_smem(smem, 2 * tile);
+    for (int q = threadIdx.x; q < P.n_prb; q += blockDim.x) pr.own[q] = 0;
+    Xchg X;
+    xchg_setup(X, P, g, smem, tile, &abort_flag);
+
+    float bp[M], cl[M], rh[M], ya[M], yb[M];
+    load_nl_coef<M>(P, g, bp, cl, rh);
+#pragma unroll
+    for (int i = 0; i < M; ++i) ya[i] = yb[i] = 0.f;
+    Taps tp;
+    build_taps<M>(P, g, tp);
+    FwdState st;
+    st.pc = 0;
+    st.pb = 0;
+#pragma unroll
+    for (int e = 0; e < SRCMAX; ++e)
+        st.xv[e] = e < tp.ns ? __ldg(P.x + (size_t)tp.src_row(e) * P.steps) : 0.f;
+    __syncthreads();
+    if (g.colv && tp.np) {
+#pragma unroll
+        for (int e = 0; e < PRBMAX; ++e)
+            if (e < tp.np) pr.own[tp.prb_col(e)] = tp.prb_intensity(e) ? 2 : 1;
+    }
+    cluster_sync_all();
+
+    const Lane ln = make_lane(P, g, X);
+    const size_t part = (size_t)blockDim.x * M;       // floats per tape part
+    float* tape = P.lap + ((size_t)g.inst * P.C + g.cta) * 2 * part +
+                  (size_t)threadIdx.x * chunk_width<M>();
+    const size_t tape_step = (size_t)P.batch * P.C * 2 * part;
+    int chunk0 = 0;
+    bool ok = true;
+    for (int t = 0; t < P.steps; ++t) {
+        if (t & 1) fwd_step_nl<M, ORDER, 1>(P, g, X, ln, tp, st, pr, t, tape, bp, cl, rh, yb, ya);
+        else       fwd_step_nl<M, ORDER, 0>(P, g, X, ln, tp, st, pr, t, tape, bp, cl, rh, ya, yb);
+        tape += tape_step;
+        if (!(ok = exchange_end(X, t))) break;
+        if (++st.pc == P.PB) {
+            flush_probes(P, g, pr, st.pb, chunk0, P.PB);
+            st.pc = 0;
+            st.pb ^= 1;
+            chunk0 = t + 1;
         }
     }
     if (st.pc > 0) flush_probes(P, g, pr, st.pb, chunk0, st.pc);
@@ -1054,6 +1218,186 @@ __global__ void __launch_bounds__(bwd_max_threads(M), 1) seq_bwd_tape_kernel(Fus
     cluster_sync_all();
 }
 
+// ============================================================================
+// Nonlinear cell, adjoint (tape mode).  Per step s, with g = lam_s and the
+// tape's Lap(h1), h1 = h_{s-1} (slot s) and h2 = h_{s-2} (part 1 of slot
+// s-1), TimeStep's backward (wavetorch/cell.py:33-42) at the step's own b, c,
+// then autograd's chain through b(h1, rho) and c(h1, rho):
+//   dL/dh1  += grad_b * rho * dsat/dh1 + grad_c * (rho c_nl) * 2 h1
+//   dL/drho += grad_b * sat + grad_c * h1^2 * c_nl      (direct; accr)
+//   dL/dc_lin += grad_c                                  (accc)
+WT_DEV void adj_cell_nl(const FusedParams& P, float lg, float lam, float Ly, float h1, float h2,
+                        float bp, float cl, float rh, float& accc, float& accr, float& gy1,
+                        float& g2) {
+    const NLCoef n = nl_coef(P, bp, cl, rh, h1);
+    const float dt = P.k.dt, dt2 = P.k.dt2;
+    const float v = fadd(fmul(n.b, dt), 1.0f);                          // b*dt + 1
+    const float X1 = fdiv(1.0f, v);
+    const float gc = fmul(fmul(X1, fmul(fmul(fmul(2.0f, n.c), dt2), Ly)), lam);
+    float gh = fadd(fmul(dt2, lg), fmul(fmul(2.0f, lam), X1));            // grad_y1
+    g2 = fmul(fmul(fsub(fmul(n.b, dt), 1.0f), X1), lam);                  // grad_y2
+    accc = fadd(accc, gc);
+    float dr = 0.f;
+    if (P.b0 > 0.f) {
+        const float kb1 = fmul(-fdiv(1.0f, fmul(v, v)), dt);
+        const float inner = fsub(fadd(fmul(fmul(fmul(n.c, n.c), dt2), Ly), fmul(2.0f, h1)),
+                                 fmul(2.0f, h2));
+        const float gb = fmul(fmul(kb1, inner), lam);                     // grad_b
+        dr = fmul(gb, n.sat);                                             // b = b_pml + rho*sat
+        const float gs = fmul(gb, rh);
+        const float a = fabsf(n.q);                                       // sat = b0 / d
+        const float d = fadd(1.0f, fmul(a, a));
+        const float gd = fdiv(fmul(-gs, P.b0), fmul(d, d));
+        const float ga = fmul(gd, fmul(2.0f, a));                         // d = 1 + a^2
+        const float gq = n.q > 0.f ? ga : (n.q < 0.f ? -ga : 0.f);        // a = |q|
+        gh = fadd(gh, fdiv(gq, P.uth));                                   // q = h1 / uth
+    }
+    if (P.cnl != 0.f) {                                                   // c = c_lin + (rho c_nl) h1^2
+        dr = fadd(dr, fmul(fmul(gc, fmul(h1, h1)), P.cnl));
+        gh = fadd(gh, fmul(fmul(gc, fmul(rh, P.cnl)), fmul(2.0f, h1)));
+    }
+    accr = fadd(accr, dr);
+    gy1 = gh;
+}
+
+template <int M, int ORDER>
+__global__ void __launch_bounds__(bwd_max_threads(M), 1) seq_bwd_nl_kernel(FusedParams P) {
+    extern __shared__ __align__(16) float smem[];
+    __shared__ int abort_flag;
+    const Geo g = make_geo(P, M);
+    const int tile = (P.ny + 2) * P.LD;
+    zero_smem(smem, 2 * tile);
+    Xchg X;
+    xchg_setup(X, P, g, smem, tile, &abort_flag);
+    Taps tp;
+    build_taps<M>(P, g, tp);
+
+    const size_t plane = (size_t)P.nx * P.ny;
+    float* seeds = smem + 2 * tile + 2 * xchg_words(P.NCP);
+    TapeRing ring;
+    ring.buf = seeds + ((2 * P.n_prb * P.PB + 3) & ~3);
+    ring.slice = 2 * (int)blockDim.x * M;             // two parts: Lap(h1), h1
+    ring.full = reinterpret_cast<unsigned long long*>(ring.buf + (size_t)P.nbuf * ring.slice);
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < P.nbuf; ++s) mbar_init(smem_addr(ring.full + s), 1);
+        fence_mbarrier_init_cluster();
+    }
+
+    float bp[M], cl[M], rh[M];
+    load_nl_coef<M>(P, g, bp, cl, rh);
+    float gy1[M], gy2a[M], gy2b[M], accc[M], accr[M];
+#pragma unroll
+    for (int i = 0; i < M; ++i) gy1[i] = gy2a[i] = gy2b[i] = accc[i] = accr[i] = 0.f;
+    stage_seeds(P, g, seeds, 0);
+    cluster_sync_all();
+
+    int lo = P.steps;
+    if (threadIdx.x == 0) {
+        for (int j = 0; j < P.nbuf && P.steps - 1 - j >= 0; ++j) {
+            lo = P.steps - 1 - j;
+            tape_issue(P, g, ring, lo, lo % P.nbuf);
+        }
+    }
+    const Lane ln = make_lane(P, g, X);
+    const int part = (int)blockDim.x * M;
+    const int stride = (int)blockDim.x * chunk_width<M>();
+    const int lane_off = threadIdx.x * chunk_width<M>();
+    int slot = (P.steps - 1) % P.nbuf;
+    uint32_t phase = 0;
+    int pk = 0, pc = 0;
+    bool ok = true;
+    auto step = [&](auto par, int u, float (&g2)[M]) -> bool {
+        constexpr int PAR = decltype(par)::value;
+        const int t = P.steps - 1 - u;
+        float* col = ln.col0 + PAR * ln.tile;
+        const int prev = slot == 0 ? P.nbuf - 1 : slot - 1;     // slot of step t-1
+        // the step's fields come first: c2g needs b and c at h1
+        float h1[M], h2[M], lam[M], c2g[M];
+        if (g.colv) {
+            tape_wait(P, X, ring, slot, (phase >> slot) & 1u);
+            ld_chunks_at<M>(h1, ring.buf + (size_t)slot * ring.slice + part + lane_off, stride);
+            if (t > 0) {
+                tape_wait(P, X, ring, prev, (phase >> prev) & 1u);
+                ld_chunks_at<M>(h2, ring.buf + (size_t)prev * ring.slice + part + lane_off, stride);
+            } else {
+#pragma unroll
+                for (int i = 0; i < M; ++i) h2[i] = 0.f;
+            }
+        }
+#pragma unroll
+        for (int i = 0; i < M; ++i) {
+            lam[i] = fadd(g2[i], gy1[i]);
+            c2g[i] = 0.f;
+        }
+        if (pk == 0 && u + P.PB < P.steps)
+            stage_seeds(P, g, seeds, pc + 1);
+        if (g.colv) {
+            if (tp.np || (P.grad_x && tp.ns))
+                seed_and_read<M>(P, g, X, tp, PAR, t, lam, seeds + (size_t)(pc & 1) * P.n_prb * P.PB + pk);
+#pragma unroll
+            for (int i = 0; i < M; ++i) {
+                const NLCoef n = nl_coef(P, bp[i], cl[i], rh[i], h1[i]);
+                const float X1 = fdiv(1.0f, fadd(fmul(n.b, P.k.dt), 1.0f));
+                c2g[i] = fmul(fmul(X1, fmul(n.c, n.c)), lam[i]);   // (b*dt+1)^-1 * c^2 * g
+            }
+            const unsigned long long tag = (unsigned long long)(uint32_t)(u + 1) << 32;
+            if (ln.sup) st_cluster_u64(ln.sup + PAR * ln.pstride, tag | __float_as_uint(c2g[0]));
+            if (ln.sdn) st_cluster_u64(ln.sdn + PAR * ln.pstride, tag | __float_as_uint(c2g[M - 1]));
+            sts_col<M>(col, c2g);
+        }
+        if (!exchange_end(X, u)) return false;
+        if (threadIdx.x == 0 && u > 0 && t + 1 - P.nbuf >= 0) {
+            fence_proxy_async_smem();
+            lo = t + 1 - P.nbuf;
+            tape_issue(P, g, ring, lo, slot + 1 == P.nbuf ? 0 : slot + 1);
+        }
+        if (g.colv) {
+            Column<M> c;
+            lds_col<M>(c.lf, col - P.LD);
+            lds_col<M>(c.rt, col + P.LD);
+            c.up = col[-1];
+            c.dn = col[M];
+            float Ly[M];
+            ld_chunks_at<M>(Ly, ring.buf + (size_t)slot * ring.slice + lane_off, stride);
+            phase ^= 1u << slot;
+#pragma unroll
+            for (int i = 1; i < M - 1; ++i)
+                adj_cell_nl(P, lap_cell<M, ORDER>(P, c, c2g, i), lam[i], Ly[i], h1[i], h2[i], bp[i],
+                            cl[i], rh[i], accc[i], accr[i], gy1[i], g2[i]);
+            if (ln.rup) c.up = recv_at(P, X, ln.rup + PAR * ln.pstride, u);
+            if (ln.rdn) c.dn = recv_at(P, X, ln.rdn + PAR * ln.pstride, u);
+            adj_cell_nl(P, lap_cell<M, ORDER>(P, c, c2g, 0), lam[0], Ly[0], h1[0], h2[0], bp[0],
+                        cl[0], rh[0], accc[0], accr[0], gy1[0], g2[0]);
+            adj_cell_nl(P, lap_cell<M, ORDER>(P, c, c2g, M - 1), lam[M - 1], Ly[M - 1], h1[M - 1],
+                        h2[M - 1], bp[M - 1], cl[M - 1], rh[M - 1], accc[M - 1], accr[M - 1],
+                        gy1[M - 1], g2[M - 1]);
+        }
+        slot = prev;
+        if (++pk == P.PB) { pk = 0; ++pc; }
+        return true;
+    };
+    for (int u = 0; u < P.steps && ok; ++u)
+        ok = (u & 1) ? step(std::integral_constant<int, 1>{}, u, gy2a)
+                     : step(std::integral_constant<int, 0>{}, u, gy2b);
+    if (!ok && threadIdx.x == 0) {
+        for (int s = lo; s < lo + P.nbuf && s < P.steps; ++s)
+            tape_wait(P, X, ring, s % P.nbuf, (uint32_t)(((P.steps - 1 - s) / P.nbuf) & 1));
+    }
+    if (g.colv && ok) {
+        float* oc = P.gc_part + (size_t)g.inst * plane;
+        float* orh = P.grho_part + (size_t)g.inst * plane;
+#pragma unroll
+        for (int i = 0; i < M; ++i) {
+            int gx = g.gx0 + i;
+            if (gx < P.nx) {
+                oc[(size_t)gx * P.ny + g.col] = accc[i];
+                orh[(size_t)gx * P.ny + g.col] = accr[i];
+            }
+        }
+    }
+    cluster_sync_all();
+}
+
 }  // namespace wt
 
 // ---------------------------------------------------------------------------
@@ -1138,6 +1482,9 @@ int wt_fused_plan(int nx, int ny, int steps, int n_prb, int cluster_req, int seg
         L->nbuf = std::min(8, tfit);
         L->smem_tape = tiles + aux_bwd + (size_t)L->nbuf * (slice + 8);
         L->smem_fwd_tape = tiles + aux_fwd;
+        L->smem_bwd_base = tiles + aux_bwd;
+        const int nfit = 2 * slice < (1u << 20) ? (int)((SMEM_MAX - tiles - aux_bwd) / (2 * slice + 8)) : 0;
+        L->nbuf_nl = std::min(8, nfit);
         if (L->smem_fwd_tape > SMEM_MAX || L->threads > wt::fwd_max_threads(M)) L->nbuf = 0;
         return 0;
     }
@@ -1258,6 +1605,31 @@ static int launch_order(bool fwd, const wt::FusedParams& P, const WtFusedLaunch&
         }
     }
     return WT_ERR_UNSUPPORTED;
+}
+
+template <int M, int ORDER>
+static int launch_nl(bool fwd, const wt::FusedParams& P0, const WtFusedLaunch& L, cudaStream_t st) {
+    wt::FusedParams P = P0;
+    P.R = L.R;
+    P.LD = L.LD;
+    if (fwd) return launch_kernel(wt::seq_fwd_nl_kernel<M, ORDER>, P, L.C, L.threads, L.smem_fwd_tape, st);
+    const size_t smem = L.smem_bwd_base + (size_t)P.nbuf * (2 * (size_t)L.threads * M * sizeof(float) + 8);
+    return launch_kernel(wt::seq_bwd_nl_kernel<M, ORDER>, P, L.C, L.threads, smem, st);
+}
+
+template <int ORDER>
+static int launch_nl_order(bool fwd, const wt::FusedParams& P, const WtFusedLaunch& L, cudaStream_t st) {
+    switch (L.M) {
+        case 10: return launch_nl<10, ORDER>(fwd, P, L, st);
+        case 8: return launch_nl<8, ORDER>(fwd, P, L, st);
+        case 4: return launch_nl<4, ORDER>(fwd, P, L, st);
+    }
+    return WT_ERR_UNSUPPORTED;
+}
+
+int wt_launch_fused_nl(bool fwd, const wt::FusedParams& P, const WtFusedLaunch& L, cudaStream_t st) {
+    return P.k.lap_order == WT_LAP_SEQ ? launch_nl_order<WT_LAP_SEQ>(fwd, P, L, st)
+                                       : launch_nl_order<WT_LAP_PAIRED>(fwd, P, L, st);
 }
 
 int wt_launch_fused(bool fwd, const wt::FusedParams& P, const WtFusedLaunch& L, cudaStream_t st) {

@@ -231,6 +231,62 @@ class WaveSeqFn(torch.autograd.Function):
 
 
 # ---------------------------------------------------------------------------
+def nl_supported(spec: SeqSpec) -> bool:
+    """Whether the fused nonlinear sequence can plan this shape (its adjoint
+    needs a two-part tape ring in shared memory)."""
+    d, keep = dataclasses.replace(spec, form=_lib.WT_FORM_FUSED).desc()
+    n = C.c_size_t(0)
+    return _lib.load().wt_seq_workspace_bytes_nl(C.byref(d), C.byref(n)) == _lib.WT_OK
+
+
+class WaveSeqNLFn(torch.autograd.Function):
+    """The whole time loop of a nonlinear cell (saturable damping and/or Kerr
+    term, wavetorch/cell.py:8-9, :93-101) in the fused form: b and c are
+    formed every step from the field inside the kernels.  Inputs: the linear
+    speed c_lin, the density rho that weights the nonlinear terms, b_pml, x.
+    Gradients: dL/dc_lin and the direct dL/drho (rho also reaches c_lin
+    through the projection; autograd adds both)."""
+
+    @staticmethod
+    def forward(ctx, c_lin, rho, b, x, spec: SeqSpec, sc: _lib.Scalars, nl: _lib.NonLinear):
+        c_lin = _require_cuda_f32("c", c_lin)
+        rho = _require_cuda_f32("rho", rho)
+        b = _require_cuda_f32("b", b)
+        x = _require_cuda_f32("x", x)
+        dev = c_lin.device
+        d, keep = spec.desc()
+        n = C.c_size_t(0)
+        lib = _lib.load()
+        _lib.check(lib.wt_seq_workspace_bytes_nl(C.byref(d), C.byref(n)), "wt_seq_workspace_bytes_nl")
+        ws = torch.empty(int(n.value), dtype=torch.uint8, device=dev)
+        out = torch.empty((spec.batch, spec.steps, len(spec.probes)), device=dev)
+        _lib.check(lib.wt_seq_fwd_nl(C.byref(sc), C.byref(d), C.byref(nl), _ptr(b), _ptr(c_lin),
+                                     _ptr(rho), _ptr(x), _ptr(out), None, _ptr(ws), ws.numel(),
+                                     _stream(dev)), "wt_seq_fwd_nl")
+        ctx.spec, ctx.sc, ctx.nl = spec, sc, nl
+        ctx.save_for_backward(c_lin, rho, b, x, ws)
+        return out
+
+    @staticmethod
+    def backward(ctx, grad_out):
+        c_lin, rho, b, x, ws = ctx.saved_tensors
+        spec = ctx.spec
+        g = _require_cuda_f32("grad_out", grad_out)
+        dev = g.device
+        shape = ((spec.batch,) if spec.coef_batched else ()) + (spec.nx, spec.ny)
+        gc = torch.empty(shape, device=dev)
+        gr = torch.empty(shape, device=dev)
+        gx = torch.empty((spec.batch, spec.steps), device=dev) if ctx.needs_input_grad[3] else None
+        d, keep = spec.desc()
+        _lib.check(_lib.load().wt_seq_bwd_nl(C.byref(ctx.sc), C.byref(d), C.byref(ctx.nl), _ptr(b),
+                                             _ptr(c_lin), _ptr(rho), _ptr(x), _ptr(g), _ptr(gc),
+                                             _ptr(gr), _ptr(gx), _ptr(ws), ws.numel(), _stream(dev)),
+                   "wt_seq_bwd_nl")
+        return (gc if ctx.needs_input_grad[0] else None), (gr if ctx.needs_input_grad[1] else None), \
+            None, gx, None, None, None
+
+
+# ---------------------------------------------------------------------------
 class RhoToCFn(torch.autograd.Function):
     """c = c0 + (c1 - c0) * P(blur^n(rho)) (wavetorch/geom.py:207-233)."""
 

@@ -17,7 +17,8 @@ from __future__ import annotations
 import torch
 
 from . import _lib
-from .functional import SeqSpec, WaveSeqFn, fused_supported, lap_order, scalars
+from .functional import (SeqSpec, WaveSeqFn, WaveSeqNLFn, fused_supported, lap_order,
+                         nl_supported, scalars)
 from .probe import WaveProbe
 from .source import WaveSource
 
@@ -79,10 +80,32 @@ class WaveRNN(torch.nn.Module):
                 table.append((x * ny + y, probe.kind, p))
         return table, L
 
-    def _seq_ok(self) -> bool:
-        return (self.cell.is_linear()
-                and all(isinstance(s, WaveSource) for s in self.sources)
+    def _taps_ok(self) -> bool:
+        return (all(isinstance(s, WaveSource) for s in self.sources)
                 and all(isinstance(p, WaveProbe) for p in self.probes))
+
+    def _seq_ok(self) -> bool:
+        return self.cell.is_linear() and self._taps_ok()
+
+    def _forward_nonlinear(self, x, c):
+        """The nonlinear cell's time loop as one fused sequence (b and c formed
+        every step inside the kernels), or None when the shape does not fit
+        the fused form (the caller then steps it)."""
+        geom = self.cell.geom
+        nx, ny = geom.domain_shape
+        batch, steps = x.shape[0], x.shape[1]
+        dt, h, b0, uth, cnl = self.cell.scalars()
+        ptab, L = self.probe_table()
+        spec = SeqSpec(batch, nx, ny, steps, self.source_table(batch), ptab,
+                       form=_lib.WT_FORM_FUSED, segment=self.segment, cluster=self.cluster)
+        if not nl_supported(spec):
+            return None
+        sc = scalars(dt, h, lap_order(batch, nx, ny, h))
+        nl = _lib.NonLinear(b0, uth, cnl)
+        out = WaveSeqNLFn.apply(c, geom.rho, geom.b, x.contiguous(), spec, sc, nl)
+        if L != 1:
+            out = out.view(batch, steps, L, len(self.probes))
+        return out
 
     # -- forward ----------------------------------------------------------
     def forward(self, x, output_fields=False, form: str | None = None):
@@ -101,6 +124,11 @@ class WaveRNN(torch.nn.Module):
         if use_seq and fields_out and torch.is_grad_enabled() and (
                 c.requires_grad or x.requires_grad):
             use_seq = False   # field outputs are differentiated step by step
+        if (form == "fused" and not fields_out and not self.cell.is_linear()
+                and self._taps_ok()):
+            out = self._forward_nonlinear(x, c)
+            if out is not None:
+                return out
         if not use_seq:
             return self._forward_steps(x, c, fields_out)
         dt, h = self.cell.scalars()[:2]
