@@ -240,6 +240,35 @@ def run_ours(args):
     value = world * cell_steps / t_step
     grad_fused = model.cell.geom.rho.grad.detach().clone()
 
+    # ---- the same step with the loss fused into the sequence ----
+    from wavetorch_gb300.losses import cross_entropy_normalize_power
+
+    def fused_loss_step():
+        model.cell.geom.rho.grad = None
+        loss, _ = cross_entropy_normalize_power(model, x, labels)
+        loss.backward()
+
+    fused_loss = None
+    if args.form == "fused":
+        for _ in range(2):
+            fused_loss_step()
+        torch.cuda.synchronize(dev)
+        tl = []
+        for k in range(args.steps):
+            flush.zero_()
+            e = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+            e[0].record(stream)
+            fused_loss_step()
+            e[1].record(stream)
+            torch.cuda.synchronize(dev)
+            tl.append(e[0].elapsed_time(e[1]) / 1e3)
+        t_fl = max_over_ranks(statistics.mean(tl), world, dev)
+        g_fl = model.cell.geom.rho.grad.detach()
+        fused_loss = {"value": world * cell_steps / t_fl, "ms_per_step": t_fl * 1e3,
+                      "grad_rel_diff": float((g_fl - grad_fused).norm() / grad_fused.norm()),
+                      "note": "wavetorch_gb300.losses.cross_entropy_normalize_power: the "
+                              "reference's loss computed from the forward's probe sums"}
+
     # ---- end to end through the public API with host buffers ----
     x_host = torch.from_numpy(x_np).pin_memory()
     l_host = torch.from_numpy(lab_np).pin_memory()
@@ -357,6 +386,7 @@ def run_ours(args):
                          "ms_fwd_kernel": t_f * 1e3, "ms_bwd_kernels": t_b * 1e3},
             "cpu_baseline": cpu,
             "plain_form": plain,
+            "fused_loss": fused_loss,
             "clocks": clk.summary(),
             "gpu_launches": int(launches),
         }

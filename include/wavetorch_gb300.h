@@ -178,6 +178,22 @@ int wt_seq_bwd(const wt_scalars* s, const wt_seq_desc* d,
 int wt_seq_device_status(const wt_seq_desc* d, const void* workspace, size_t workspace_bytes,
                          wt_stream_t stream);
 
+/* ---- the training loss, fused ---------------------------------------------
+ * The reference trains on CrossEntropy(normalize_power(sum_t out), label)
+ * (wavetorch/train.py:61-62, utils.py:35-36): the loss depends on the probe
+ * series only through its time sums.  wt_loss_ce_normalize_power takes those
+ * sums ([batch,n_probes], e.g. wt_seq_fwd's Kahan probe_sum) and int64 labels
+ * [batch], and writes the batch-mean loss (one float) and dLoss/dsum
+ * [batch,n_probes].  wt_seq_bwd_sum is wt_seq_bwd for such a loss: it takes
+ * grad_sum instead of a [batch,steps,n_probes] grad_out (fused form only).
+ * No counterpart in the reference, which runs the loss as torch ops.       */
+int wt_loss_ce_normalize_power(int32_t batch, int32_t n_probes, const float* probe_sum,
+                               const int64_t* labels, float* loss, float* grad_sum,
+                               wt_stream_t stream);
+int wt_seq_bwd_sum(const wt_scalars* s, const wt_seq_desc* d, const float* b, const float* c,
+                   const float* x, const float* grad_sum, float* grad_c, void* workspace,
+                   size_t workspace_bytes, wt_stream_t stream);
+
 /* ---- the nonlinear cell ----------------------------------------------------
  * WaveCell with satdamp_b0 > 0 and/or c_nl != 0 (wavetorch/cell.py:8-9,
  * :93-101): every step, at every cell,

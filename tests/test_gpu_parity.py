@@ -233,3 +233,34 @@ def test_grad_rho_against_fp64_central_differences(cuda, name, form):
     ours = m.cell.geom.rho.grad.reshape(-1).cpu().numpy().astype(np.float64)[d["fd_index"]]
     fd = d["fd_grad"]
     assert np.abs(ours - fd).max() <= 1e-4 * np.abs(fd).max()
+
+
+@pytest.mark.parametrize("name", ["cfg0_small", "cfg1_small", "multi"])
+def test_fused_training_loss(cuda, name):
+    """The loss fused with the sequence (Kahan time sums, one loss kernel,
+    per-probe adjoint weights) against the reference's loss and gradient."""
+    from wavetorch_gb300.losses import cross_entropy_normalize_power
+    d = golden(name)
+    m = build_model(d, cuda, "fused")
+    loss, y = cross_entropy_normalize_power(m, T(d["x"], cuda), T(d["labels"], cuda))
+    loss.backward()
+    assert abs(loss.item() - float(d["loss"])) <= 1e-5 * abs(float(d["loss"]))
+    assert rel(y.cpu().numpy(), d["out"]) <= 1e-5
+    assert rel(m.cell.geom.rho.grad.cpu().numpy(), d["grad_rho"]) <= E2E_TOL[name]
+
+
+@pytest.mark.parametrize("name", SEQ_CASES)
+def test_kahan_probe_sums(cuda, name):
+    """Time sums of the probe series: the fused forward accumulates them in
+    its probe flushes, the plain form in a separate kernel; same Kahan
+    arithmetic on the same (bit-exact) outputs, so equal bit for bit, and
+    within float32 rounding of a float64 sum."""
+    d = golden(name)
+    b, c, x = T(d["b"], cuda), T(d["c"], cuda), T(d["x"], cuda)
+    sums = {}
+    for form in ("plain", "fused"):
+        _, _, ps, _ = seq_forward(spec_of(d, form), sc_of(d), b, c, x, want_sum=True)
+        sums[form] = ps.cpu().numpy()
+    assert np.array_equal(sums["plain"], sums["fused"])
+    ref = d["out"].astype(np.float64).sum(axis=1)
+    assert np.abs(sums["fused"] - ref).max() <= 1e-6 * np.abs(ref).max()

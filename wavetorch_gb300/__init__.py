@@ -4,7 +4,7 @@ Drop-in modules with the reference's names and constructor signatures; the
 time loop, its adjoint and the rho -> c map run as hand-written sm_103a CUDA
 kernels behind the C ABI in ``include/wavetorch_gb300.h``.
 """
-from . import cell, geom, probe, rnn, source, utils, io, functional  # noqa: F401
+from . import cell, geom, probe, rnn, source, utils, io, functional, losses, ragged  # noqa: F401
 from .cell import WaveCell, TimeStep
 from .geom import WaveGeometry, WaveGeometryHoley, WaveGeometryFreeForm
 from .probe import WaveProbe, WaveIntensityProbe

@@ -29,6 +29,7 @@ EXPORTED = [
     "wt_version", "wt_status_string", "wt_last_error", "wt_kernel_launches",
     "wt_step_fwd", "wt_step_bwd",
     "wt_seq_workspace_bytes", "wt_seq_fwd", "wt_seq_bwd", "wt_seq_device_status",
+    "wt_loss_ce_normalize_power", "wt_seq_bwd_sum",
     "wt_seq_workspace_bytes_nl", "wt_seq_fwd_nl", "wt_seq_bwd_nl",
     "wt_rho_to_c_fwd", "wt_rho_to_c_bwd", "wt_rho_to_c_work_bytes", "wt_rho_to_c_fwd_noalloc",
 ]
@@ -94,6 +95,9 @@ def _declare(lib):
     lib.wt_seq_bwd.argtypes = [P(Scalars), P(SeqDesc), _VP, _VP, _VP, _VP, _VP, _VP, _VP,
                                C.c_size_t, _VP]
     lib.wt_seq_device_status.argtypes = [P(SeqDesc), _VP, C.c_size_t, _VP]
+    lib.wt_loss_ce_normalize_power.argtypes = [i32, i32, _VP, _VP, _VP, _VP, _VP]
+    lib.wt_seq_bwd_sum.argtypes = [P(Scalars), P(SeqDesc), _VP, _VP, _VP, _VP, _VP, _VP,
+                                   C.c_size_t, _VP]
     lib.wt_seq_workspace_bytes_nl.argtypes = [P(SeqDesc), P(C.c_size_t)]
     lib.wt_seq_fwd_nl.argtypes = [P(Scalars), P(SeqDesc), P(NonLinear), _VP, _VP, _VP, _VP, _VP,
                                   _VP, _VP, C.c_size_t, _VP]

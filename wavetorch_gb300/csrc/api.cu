@@ -384,7 +384,8 @@ extern "C" int wt_seq_fwd(const wt_scalars* s, const wt_seq_desc* d, const float
         wt::FusedParams F = fused_params(s, P, b, c, x, workspace);
         F.out = out;
         F.fields = d->output_fields ? fields : nullptr;
-        if ((st = wt_launch_fused(true, F, P.L, cs))) return st;
+        F.psum = P.np > 0 ? probe_sum : nullptr;   // summed in the probe flushes
+        return wt_launch_fused(true, F, P.L, cs);
     }
     if (probe_sum && P.np > 0)
         return wt_launch_probe_sum(P.B, P.T, P.np, out, probe_sum, cs);
@@ -509,9 +510,8 @@ extern "C" int wt_seq_fwd_nl(const wt_scalars* s, const wt_seq_desc* d, const wt
     wt::FusedParams F = fused_params(s, P, b, c_lin, x, workspace);
     nl_params(F, P, nl, rho, workspace);
     F.out = out;
-    if ((st = wt_launch_fused_nl(true, F, P.L, cs))) return st;
-    if (probe_sum && P.np > 0) return wt_launch_probe_sum(P.B, P.T, P.np, out, probe_sum, cs);
-    return WT_OK;
+    F.psum = P.np > 0 ? probe_sum : nullptr;
+    return wt_launch_fused_nl(true, F, P.L, cs);
 }
 
 extern "C" int wt_seq_bwd_nl(const wt_scalars* s, const wt_seq_desc* d, const wt_nonlinear* nl,
@@ -541,4 +541,35 @@ extern "C" int wt_seq_bwd_nl(const wt_scalars* s, const wt_seq_desc* d, const wt
     if (P.coef_batched) return WT_OK;
     if ((st = wt_launch_seq_adj_reduce(P.B, P.plane, F.gc_part, grad_c, 1, cs))) return st;
     return wt_launch_seq_adj_reduce(P.B, P.plane, F.grho_part, grad_rho, 1, cs);
+}
+
+// ---------------------------------------------------------------------------
+// 4. the training loss fused with the sequence
+extern "C" int wt_loss_ce_normalize_power(int32_t batch, int32_t n_probes, const float* probe_sum,
+                                          const int64_t* labels, float* loss, float* grad_sum,
+                                          wt_stream_t stream) {
+    if (batch <= 0 || n_probes <= 0 || !probe_sum || !labels || !loss || !grad_sum)
+        return WT_ERR_INVALID;
+    return wt_launch_loss_ce_np(batch, n_probes, probe_sum, labels, loss, grad_sum,
+                                (cudaStream_t)stream);
+}
+
+extern "C" int wt_seq_bwd_sum(const wt_scalars* s, const wt_seq_desc* d, const float* b,
+                              const float* c, const float* x, const float* grad_sum,
+                              float* grad_c, void* workspace, size_t workspace_bytes,
+                              wt_stream_t stream) {
+    if (!scalars_ok(s)) return WT_ERR_INVALID;
+    SeqPlan P;
+    int st = make_plan(d, &P);
+    if (st) return st;
+    if (P.form != WT_FORM_FUSED) return WT_ERR_UNSUPPORTED;
+    if (!b || !c || !grad_c || !grad_sum || !workspace || workspace_bytes < P.total)
+        return WT_ERR_INVALID;
+    cudaStream_t cs = (cudaStream_t)stream;
+    wt::FusedParams F = fused_params(s, P, b, c, x, workspace);
+    F.grad_w = grad_sum;
+    if (P.coef_batched) F.gc_part = grad_c;
+    if ((st = wt_launch_fused(false, F, P.L, cs))) return st;
+    if (P.coef_batched) return WT_OK;
+    return wt_launch_seq_adj_reduce(P.B, P.plane, F.gc_part, grad_c, 1, cs);
 }

@@ -62,9 +62,11 @@ struct FusedParams {
     float* out;             // [batch][steps][n_prb]
     float* amp;             // [batch][steps][n_prb]
     float* fields;          // [batch][steps][nx][ny] or null
+    float* psum;            // [batch][n_prb] Kahan time sums of out, or null
     float* ckpt;            // [nseg][2][batch][nx][ny]
     // adjoint
     const float* grad_out;  // [batch][steps][n_prb]
+    const float* grad_w;    // [batch][n_prb] dLoss/d(sum_t out), used instead of grad_out if set
     float* gc_part;         // [batch][nx][ny] per-instance dL/dc
     float* grad_x;          // [batch][steps] or null
     float* stash;           // global stash [batch][C][seg][M][nthreads] (unless in smem)
@@ -132,6 +134,8 @@ int wt_fused_plan(int nx, int ny, int steps, int n_prb, int cluster_req, int seg
                   WtFusedLaunch* L);
 int wt_launch_probe_sum(int batch, int steps, int n_prb, const float* out, float* sum,
                         cudaStream_t st);
+int wt_launch_loss_ce_np(int batch, int n_prb, const float* sum, const int64_t* labels,
+                         float* loss, float* grad_sum, cudaStream_t st);
 int wt_launch_fused(bool fwd, const wt::FusedParams& P, const WtFusedLaunch& L, cudaStream_t st);
 // Nonlinear cell, tape mode: nbuf ring slices of two parts (Lap, field).
 int wt_launch_fused_nl(bool fwd, const wt::FusedParams& P, const WtFusedLaunch& L, cudaStream_t st);

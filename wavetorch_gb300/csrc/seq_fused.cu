@@ -580,6 +580,7 @@ struct FwdState {
 struct ProbeRing {
     float* buf;
     int* own;
+    float* ksum;    // [2][n_prb]: running Kahan sum and compensation of each owned column
 };
 
 // Write chunk `b` (steps t0 .. t0+n-1) of the probes this CTA owns.
@@ -594,6 +595,30 @@ WT_DEV void flush_probes(const FusedParams& P, const Geo& g, const ProbeRing& pr
         P.out[oi] = (pr.own[q] == 2) ? fmul(v, v) : v;   // own: 1 amplitude, 2 intensity
         P.amp[oi] = v;
     }
+    if (!P.psum) return;
+    // Kahan-compensated time sums of the outputs, one thread per column, in
+    // step order (the arithmetic of probe_sum_kernel)
+    for (int q = threadIdx.x; q < P.n_prb; q += blockDim.x) {
+        if (!pr.own[q]) continue;
+        float s = pr.ksum[q], comp = pr.ksum[P.n_prb + q];
+        const float* vb = pr.buf + (size_t)(b * P.n_prb + q) * P.PB;
+        for (int tt = 0; tt < n; ++tt) {
+            const float v = vb[tt];
+            const float y = fsub((pr.own[q] == 2) ? fmul(v, v) : v, comp);
+            const float tk = fadd(s, y);
+            comp = fsub(fsub(tk, s), y);
+            s = tk;
+        }
+        pr.ksum[q] = s;
+        pr.ksum[P.n_prb + q] = comp;
+    }
+}
+
+// The owned columns' sums, at the end of the forward.
+WT_DEV void write_probe_sums(const FusedParams& P, const Geo& g, const ProbeRing& pr) {
+    if (!P.psum) return;
+    for (int q = threadIdx.x; q < P.n_prb; q += blockDim.x)
+        if (pr.own[q]) P.psum[(size_t)g.inst * P.n_prb + q] = pr.ksum[q];
 }
 
 // Checkpoint of segment t/seg: the state before step t, (h_{t-1}, h_{t-2}).
@@ -686,8 +711,12 @@ __global__ void __launch_bounds__(fwd_max_threads(M), 1) seq_fwd_fused_kernel(Fu
     ProbeRing pr;
     pr.buf = smem + 2 * tile + 2 * xchg_words(P.NCP);
     pr.own = reinterpret_cast<int*>(pr.buf + 2 * P.n_prb * P.PB);
+    pr.ksum = reinterpret_cast<float*>(pr.own + P.n_prb);
     zero_smem(smem, 2 * tile);
-    for (int q = threadIdx.x; q < P.n_prb; q += blockDim.x) pr.own[q] = 0;
+    for (int q = threadIdx.x; q < P.n_prb; q += blockDim.x) {
+        pr.own[q] = 0;
+        pr.ksum[q] = pr.ksum[P.n_prb + q] = 0.f;
+    }
     Xchg X;
     xchg_setup(X, P, g, smem, tile, &abort_flag);
 
@@ -741,6 +770,7 @@ __global__ void __launch_bounds__(fwd_max_threads(M), 1) seq_fwd_fused_kernel(Fu
         }
     }
     if (st.pc > 0) flush_probes(P, g, pr, st.pb, chunk0, st.pc);
+    write_probe_sums(P, g, pr);
     cluster_sync_all();
 }
 
@@ -794,8 +824,12 @@ __global__ void __launch_bounds__(fwd_max_threads(M), 1) seq_fwd_nl_kernel(Fused
     ProbeRing pr;
     pr.buf = smem + 2 * tile + 2 * xchg_words(P.NCP);
     pr.own = reinterpret_cast<int*>(pr.buf + 2 * P.n_prb * P.PB);
+    pr.ksum = reinterpret_cast<float*>(pr.own + P.n_prb);
     zero_smem(smem, 2 * tile);
-    for (int q = threadIdx.x; q < P.n_prb; q += blockDim.x) pr.own[q] = 0;
+    for (int q = threadIdx.x; q < P.n_prb; q += blockDim.x) {
+        pr.own[q] = 0;
+        pr.ksum[q] = pr.ksum[P.n_prb + q] = 0.f;
+    }
     Xchg X;
     xchg_setup(X, P, g, smem, tile, &abort_flag);
 
@@ -839,6 +873,7 @@ __global__ void __launch_bounds__(fwd_max_threads(M), 1) seq_fwd_nl_kernel(Fused
         }
     }
     if (st.pc > 0) flush_probes(P, g, pr, st.pb, chunk0, st.pc);
+    write_probe_sums(P, g, pr);
     cluster_sync_all();
 }
 
@@ -880,7 +915,8 @@ WT_DEV void stage_seeds(const FusedParams& P, const Geo& g, float* seeds, int c)
         float sd = 0.f;
         if (t >= 0) {
             const size_t oi = ((size_t)g.inst * P.steps + t) * P.n_prb + q;
-            const float gv = __ldg(P.grad_out + oi);
+            const float gv = P.grad_w ? __ldg(P.grad_w + (size_t)g.inst * P.n_prb + q)
+                                      : __ldg(P.grad_out + oi);
             sd = __ldg(P.prb_kind_col + q) ? fmul(gv, fmul(2.0f, __ldg(P.amp + oi))) : gv;
         }
         dst[q * P.PB + k] = sd;
@@ -1443,7 +1479,7 @@ int wt_fused_plan(int nx, int ny, int steps, int n_prb, int cluster_req, int seg
     const size_t SMEM_MAX = 227 * 1024 - 64;   // dynamic smem per CTA (static: 28 B)
     const int PB = n_prb > 0 ? std::max(1, std::min(32, 2048 / n_prb)) : 32;
     auto r16 = [](size_t v) { return (v + 15) / 16 * 16; };
-    const size_t aux_fwd = r16((size_t)(2 * n_prb * PB + n_prb) * 4);
+    const size_t aux_fwd = r16((size_t)(2 * n_prb * PB + 3 * n_prb) * 4);   // ring, owners, sums
     const size_t aux_bwd = r16((size_t)(2 * n_prb * PB) * 4);
     for (int ci = 0; ci < 5; ++ci) {
         int C = Cs[ci];
@@ -1541,6 +1577,54 @@ static int ensure_attributes(void (*kern)(wt::FusedParams), size_t smem, bool no
         v.second = true;
     }
     return WT_OK;
+}
+
+// The reference's training loss on the time-summed probe outputs
+// (wavetorch/train.py:61-62, utils.py:35-36), and its gradient:
+//   p = I / sum_q I,  loss = mean_b CE(p_b, label_b) = mean_b (lse(p_b) - p_b[label])
+//   dL/dp = (softmax(p) - onehot) / B,  dL/dI_k = (dL/dp_k - sum_j dL/dp_j p_j) / sum_q I
+// One block; thread b handles instance b, the batch mean is a shared sum.
+__global__ void loss_ce_np_kernel(int batch, int n_prb, const float* __restrict__ sum,
+                                  const int64_t* __restrict__ labels, float* __restrict__ loss,
+                                  float* __restrict__ grad_sum) {
+    __shared__ float part[256];
+    float acc = 0.f;
+    for (int bi = threadIdx.x; bi < batch; bi += blockDim.x) {
+        const float* I = sum + (size_t)bi * n_prb;
+        float* gI = grad_sum + (size_t)bi * n_prb;
+        float S = 0.f;
+        for (int q = 0; q < n_prb; ++q) S = fadd(S, I[q]);
+        float m = -INFINITY;
+        for (int q = 0; q < n_prb; ++q) m = fmaxf(m, fdiv(I[q], S));
+        float se = 0.f;
+        for (int q = 0; q < n_prb; ++q) se = fadd(se, expf(fsub(fdiv(I[q], S), m)));
+        const float lse = fadd(m, logf(se));
+        const int lab = (int)labels[bi];
+        const float pl = (lab >= 0 && lab < n_prb) ? fdiv(I[lab], S) : 0.f;
+        acc = fadd(acc, fsub(lse, pl));
+        float dot = 0.f;
+        for (int q = 0; q < n_prb; ++q) {      // dL/dp into grad_sum first
+            const float p = fdiv(I[q], S);
+            const float dp = fdiv(fsub(fdiv(expf(fsub(p, m)), se), q == lab ? 1.f : 0.f), (float)batch);
+            gI[q] = dp;
+            dot = fadd(dot, fmul(dp, p));
+        }
+        for (int q = 0; q < n_prb; ++q) gI[q] = fdiv(fsub(gI[q], dot), S);
+    }
+    part[threadIdx.x] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        float t = 0.f;
+        for (int i = 0; i < (int)blockDim.x; ++i) t = fadd(t, part[i]);
+        *loss = fdiv(t, (float)batch);
+    }
+}
+
+int wt_launch_loss_ce_np(int batch, int n_prb, const float* sum, const int64_t* labels,
+                         float* loss, float* grad_sum, cudaStream_t st) {
+    loss_ce_np_kernel<<<1, 256, 0, st>>>(batch, n_prb, sum, labels, loss, grad_sum);
+    wt_count_launches(1);
+    return wt_cuda_status(cudaGetLastError());
 }
 
 static int launch_kernel(void (*kern)(wt::FusedParams), const wt::FusedParams& P, int C,
