@@ -51,12 +51,6 @@ WT_DEV float lap5(float u, float l, float c, float r, float d, float w, float w4
     }
 }
 
-// Runtime-dispatched form for kernels that are not templated on the order.
-WT_DEV float lap5_rt(int order, float u, float l, float c, float r, float d, float w, float w4) {
-    return order == WT_LAP_SEQ ? lap5<WT_LAP_SEQ>(u, l, c, r, d, w, w4)
-                               : lap5<WT_LAP_PAIRED>(u, l, c, r, d, w, w4);
-}
-
 // Leapfrog update in the reference's order (wavetorch/cell.py:13-16):
 //   A * ( (two_over*y1 - Bc*y2) + c2*L )
 WT_DEV float leapfrog(float A, float Bc, float c2, float two_over, float y1, float y2, float L) {
@@ -108,11 +102,6 @@ WT_DEV uint32_t cluster_ctarank() {
     asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
     return r;
 }
-WT_DEV uint32_t cluster_nctarank() {
-    uint32_t r;
-    asm volatile("mov.u32 %0, %%cluster_nctarank;" : "=r"(r));
-    return r;
-}
 // Map a local shared-memory address to the same offset in CTA `rank` of the
 // cluster (a 32-bit shared::cluster address).
 WT_DEV uint32_t map_shared_rank(const void* local_smem, uint32_t rank) {
@@ -120,9 +109,6 @@ WT_DEV uint32_t map_shared_rank(const void* local_smem, uint32_t rank) {
     uint32_t r;
     asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(a), "r"(rank));
     return r;
-}
-WT_DEV void st_cluster_f32(uint32_t addr, float v) {
-    asm volatile("st.shared::cluster.f32 [%0], %1;" ::"r"(addr), "f"(v) : "memory");
 }
 WT_DEV void cluster_arrive_release() {
     asm volatile("barrier.cluster.arrive.release.aligned;" ::: "memory");

@@ -88,21 +88,8 @@ WT_DEV void sts_col(float* p, const float (&s)[M]) {
 template <int M>
 constexpr int chunk_width() { return M % 4 == 0 ? 4 : M % 2 == 0 ? 2 : 1; }
 
-template <int M>
-WT_DEV void st_chunks(float* base, int NT, int tid, const float (&s)[M]) {
-    constexpr int V = chunk_width<M>();
-#pragma unroll
-    for (int j = 0; j < M / V; ++j) {
-        float* p = base + ((size_t)j * NT + tid) * V;
-        if constexpr (V == 4)
-            *reinterpret_cast<float4*>(p) = make_float4(s[4 * j], s[4 * j + 1], s[4 * j + 2], s[4 * j + 3]);
-        else if constexpr (V == 2)
-            *reinterpret_cast<float2*>(p) = make_float2(s[2 * j], s[2 * j + 1]);
-        else
-            *p = s[j];
-    }
-}
-// st_chunks from the thread's own chunk-0 address p (stride: floats between chunks).
+// Chunk-major store from the thread's own chunk-0 address p (stride: floats
+// between chunks).
 template <int M>
 WT_DEV void st_chunks_at(float* p, int stride, const float (&s)[M]) {
     constexpr int V = chunk_width<M>();
@@ -1105,7 +1092,7 @@ __global__ void __launch_bounds__(bwd_max_threads(M), 1) seq_bwd_fused_kernel(Fu
 // Adjoint in tape mode: the forward stored Lap(h_{t-1}) of every cell and
 // step, so the adjoint runs its T steps in one sweep with no recompute.  The
 // tape is laid out [step][instance][cta][chunk][thread] (chunk-major, see
-// st_chunks): both kernels use the same strips, so a CTA's values of one
+// chunk_width): both kernels use the same strips, so a CTA's values of one
 // step are one contiguous slice, written with coalesced vector stores and
 // read back from shared memory without bank conflicts.  Slices
 // arrive by bulk copy into a ring of `nbuf` shared-memory slots, issued by
