@@ -52,7 +52,7 @@ def parse():
     p.add_argument("--T", type=int, default=WORKLOAD["steps"])
     p.add_argument("--kernels-only", action="store_true",
                    help="run only the sequence kernels (forward + adjoint) -- the profiling case")
-    p.add_argument("--workload", choices=["batched", "ragged", "nonlinear"], default="batched",
+    p.add_argument("--workload", choices=["batched", "ragged", "nonlinear", "lens"], default="batched",
                    help="ragged: many models of different grid sizes / step counts in one graph; "
                         "nonlinear: B=64, 120x120, T=5000 with saturable damping and Kerr term")
     p.add_argument("--instances", type=int, default=256, help="models in the ragged workload")
@@ -651,8 +651,67 @@ def run_nonlinear(args):
         print(json.dumps(line), flush=True)
 
 
+def run_lens(args):
+    """Large-grid lens design: 1024x1024 (PML 40), one instance, line source
+    along x=60 from y=200 to 824 driven by sin(2 pi 0.02 t), T=8000, loss
+    -sum_t I(900, 512), gradient w.r.t. a full-grid rho ~ U(0,1).  Grids this
+    large run in the plain per-step form (every field kept: 33.5 GB)."""
+    import numpy as np
+    import torch
+    import wavetorch_gb300 as wt
+    from wavetorch_gb300.data import sinusoid
+    world, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    N, T = 1024, args.T if args.T != WORKLOAD["steps"] else 8000
+    geom = wt.WaveGeometryFreeForm((N, N), 1.0, c0=1.0, c1=0.5, abs_N=40, abs_sig=3.0, abs_p=2,
+                                   rho=torch.rand(N, N, generator=torch.Generator().manual_seed(3)))
+    model = wt.WaveRNN(wt.WaveCell(0.707, geom), wt.WaveLineSource(60, 200, 60, 824),
+                       [wt.WaveIntensityProbe(900, 512)]).to(dev)
+    x = torch.from_numpy(sinusoid(T, 0.02)).to(dev)          # [1, T]
+
+    def step():
+        model.cell.geom.rho.grad = None
+        y = model(x)
+        loss = -y.sum()
+        loss.backward()
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize(dev)
+    stream = torch.cuda.current_stream(dev)
+    ts = []
+    with ClockSampler(local) as clk:
+        for _ in range(args.steps):
+            e = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+            e[0].record(stream)
+            step()
+            e[1].record(stream)
+            torch.cuda.synchronize(dev)
+            ts.append(e[0].elapsed_time(e[1]) / 1e3)
+    t = statistics.mean(ts)
+    fwd_bytes = 12 * N * N * T          # the per-step form's algorithmic HBM bytes
+    line = {
+        "metric": "cell-steps/s fwd+adjoint, 1024x1024 lens design (plain per-step form)",
+        "value": N * N * T / t, "unit": "cell-steps/s", "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": t * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "fp32",
+        "data": "synthetic (sinusoidal line source, random-init rho)",
+        "config": {"workload": f"lens: 1024x1024 (PML 40), line source x=60 y=200..824, T={T}, "
+                               "objective -sum_t I(900,512), fwd + adjoint to dL/drho",
+                   "form": "plain (grids above 256x256 do not fit the fused form)"},
+        "algorithmic_GBps": (fwd_bytes + 20 * N * N * T) / t / 1e9,
+        "clocks": clk.summary(),
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
+    if args.workload == "lens" and args.impl == "ours":
+        run_lens(args)
+        return
     if args.workload == "ragged" and args.impl == "ours":
         run_ragged(args)
         return
