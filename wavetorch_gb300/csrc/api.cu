@@ -104,6 +104,8 @@ struct SeqPlan {
     size_t o_prbmap, o_prbnext, o_prbkind;          // entry index == output column
     size_t o_fcell, o_fkind, o_fcol;                // probes, descending reference order
     size_t o_err;
+    size_t o_tileflag;                              // plain: tiles of the vector kernels
+    int tiles_x, tiles_y;
     size_t tables_end;
     // float areas
     size_t o_amp;
@@ -152,6 +154,9 @@ int make_plan(const wt_seq_desc* d, SeqPlan* p, bool nl = false) {
     P.o_fkind = o; o = up(o + (P.np + 1) * I);
     P.o_fcol = o; o = up(o + (P.np + 1) * I);
     P.o_err = o; o = up(o + I);
+    P.tiles_x = (P.nx + wt::STEP4_TX - 1) / wt::STEP4_TX;
+    P.tiles_y = (P.ny + wt::STEP4_TY - 1) / wt::STEP4_TY;
+    P.o_tileflag = o; o = up(o + (size_t)P.tiles_x * P.tiles_y * I);
     P.tables_end = o;
     const size_t bp = (size_t)P.B * P.plane;
     P.o_amp = o; o = up(o + (size_t)P.B * P.T * (P.np + 1) * F);
@@ -257,15 +262,22 @@ int upload_tables(const wt_seq_desc* d, const SeqPlan& P, void* ws, cudaStream_t
         H(P.o_fcol)[j] = i;
     }
     H(P.o_err)[0] = 0;
+    // tiles of the vector per-step kernels that hold a source or probe cell
+    auto flag = [&](int cell) {
+        const int cx = cell / P.ny, cy = cell % P.ny;
+        H(P.o_tileflag)[(size_t)(cx / wt::STEP4_TX) * P.tiles_y + cy / wt::STEP4_TY] = 1;
+    };
+    for (int i = 0; i < P.ns; ++i) flag(d->sources_host[i].cell);
+    for (int i = 0; i < P.np; ++i) flag(d->probes_host[i].cell);
     // Small tables go to the device inside a kernel's parameters, so the host
     // does not wait: the per-cell maps (plain form only) are filled with -1
     // and every other entry is written explicitly.
     static thread_local wt::IntScatter sc;
     sc.n = 0;
-    auto put = [&](size_t off_bytes, size_t count, bool skip_minus1) {
+    auto put = [&](size_t off_bytes, size_t count, bool skip_fill, int fill = -1) {
         const int* src = H(off_bytes);
         for (size_t i = 0; i < count; ++i) {
-            if (skip_minus1 && src[i] == -1) continue;
+            if (skip_fill && src[i] == fill) continue;
             if (sc.n == wt::INT_SCATTER_CAP) return false;
             sc.idx[sc.n] = (int)(off_bytes / sizeof(int) + i);
             sc.val[sc.n++] = src[i];
@@ -273,7 +285,9 @@ int upload_tables(const wt_seq_desc* d, const SeqPlan& P, void* ws, cudaStream_t
         return true;
     };
     const bool plain = P.form == WT_FORM_PLAIN;
-    bool fits = (!plain || (put(P.o_srcmap, P.plane, true) && put(P.o_prbmap, P.plane, true))) &&
+    const size_t ntiles = (size_t)P.tiles_x * P.tiles_y;
+    bool fits = (!plain || (put(P.o_srcmap, P.plane, true) && put(P.o_prbmap, P.plane, true) &&
+                            put(P.o_tileflag, ntiles, true, 0))) &&
                 put(P.o_srcnext, P.ns, false) && put(P.o_srcrow, P.ns, false) &&
                 put(P.o_srccell, P.ns, false) && put(P.o_prbnext, P.np, false) &&
                 put(P.o_prbkind, P.np, false) && put(P.o_fcell, P.np, false) &&
@@ -284,6 +298,7 @@ int upload_tables(const wt_seq_desc* d, const SeqPlan& P, void* ws, cudaStream_t
         if (plain) {
             if ((rc = wt_launch_fill_int(base + P.o_srcmap / sizeof(int), P.plane, -1, st))) return rc;
             if ((rc = wt_launch_fill_int(base + P.o_prbmap / sizeof(int), P.plane, -1, st))) return rc;
+            if ((rc = wt_launch_fill_int(base + P.o_tileflag / sizeof(int), ntiles, 0, st))) return rc;
         }
         return wt_launch_scatter_ints(base, sc, st);
     }
@@ -366,6 +381,8 @@ extern "C" int wt_seq_fwd(const wt_scalars* s, const wt_seq_desc* d, const float
         e.out = out;
         e.amp = at<float>(workspace, P.o_amp);
         e.n_probe = P.np;
+        e.tileflag = at<int>(workspace, P.o_tileflag);
+        e.tiles_y = P.tiles_y;
         const size_t hbs = (size_t)P.T * plane;   // history is [B][T][nx][ny]
         for (int t = 0; t < P.T; ++t) {
             e.t = t;
@@ -428,6 +445,8 @@ extern "C" int wt_seq_bwd(const wt_scalars* s, const wt_seq_desc* d, const float
         e.src_next = at<int>(workspace, P.o_srcnext);
         e.src_row = at<int>(workspace, P.o_srcrow);
         e.grad_x = grad_x;
+        e.tileflag = at<int>(workspace, P.o_tileflag);
+        e.tiles_y = P.tiles_y;
         const size_t hbs = (size_t)P.T * plane;
         for (int t = P.T - 1; t >= 0; --t) {
             e.t = t;

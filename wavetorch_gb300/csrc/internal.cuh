@@ -19,7 +19,15 @@ struct SeqEpilogue {
     float* out;               // [batch][steps][n_probe]
     float* amp;               // [batch][steps][n_probe] raw amplitudes (adjoint seeds)
     int n_probe;
+    // per tile of the vector kernels (STEP4_TX x STEP4_TY cells): nonzero when
+    // a source or probe lies in it; null = look up the maps at every cell
+    const int* tileflag;
+    int tiles_y;
 };
+
+// Tile of the vector (float4) per-step kernels: rows x columns.
+constexpr int STEP4_TX = 8;
+constexpr int STEP4_TY = 128;
 
 // Per-step epilogue of the plain sequence adjoint.
 struct AdjEpilogue {
@@ -33,6 +41,8 @@ struct AdjEpilogue {
     const int* src_next;
     const int* src_row;
     float* grad_x;                 // [batch][steps] or null
+    const int* tileflag;           // as SeqEpilogue::tileflag
+    int tiles_y;
 };
 
 // Parameters of the fused persistent kernels.

@@ -6,6 +6,8 @@
 // Layout: fields [batch][nx][ny] float32.  A CTA of 32x8 threads covers an
 // 8-row x 32-column tile; the tile plus a one-cell halo is staged in shared
 // memory with coalesced loads, so each input cell is read from L2/HBM once.
+#include <initializer_list>
+
 #include "internal.cuh"
 
 namespace wt {
@@ -248,6 +250,191 @@ seq_adj_step_kernel(StepScalars k, int nx, int ny, const float* __restrict__ b,
     }
 }
 
+// ---------------------------------------------------------------------------
+// Vector (float4) per-step kernels, for rows of a multiple of 4 cells with
+// 16-byte aligned fields: a CTA of 8 x 32 threads covers an 8-row x
+// 128-column tile, each thread 4 consecutive cells of one row.  The tile and
+// its halo are staged with coalesced float4 loads (rows x0-1 .. x0+8, columns
+// y0-4 .. y0+131, whole 4-cell chunks, zero outside the grid); a thread reads
+// its centre, upper and lower rows as float4 and its left / right neighbours
+// from the adjacent lanes.  The arithmetic per cell is the scalar kernels'.
+constexpr int S4W = STEP4_TY + 8;      // staged columns per row (y0-4 .. y0+131)
+
+WT_DEV void stage_tile4(float (*s)[S4W], const float* __restrict__ f, int nx, int ny, int x0,
+                        int y0) {
+    const int tid = threadIdx.y * 32 + threadIdx.x;
+    constexpr int CH = S4W / 4;        // float4 chunks per staged row
+    for (int i = tid; i < (STEP4_TX + 2) * CH; i += STEP4_TX * 32) {
+        const int rr = i / CH, j = i - rr * CH;
+        const int gx = x0 - 1 + rr, gy = y0 - 4 + 4 * j;
+        float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (gx >= 0 && gx < nx && gy >= 0 && gy < ny)
+            v = __ldg(reinterpret_cast<const float4*>(f + (size_t)gx * ny + gy));
+        *reinterpret_cast<float4*>(&s[rr][4 * j]) = v;
+    }
+}
+
+// The thread's 4 cells of row r (columns q0 .. q0+3 of the staged tile):
+// centre, up, down and the left / right neighbours of each.
+struct Quad {
+    float c[4], u[4], d[4], l[4], r[4];
+};
+WT_DEV void load_quad(Quad& Q, float (*s)[S4W], int r, int q0) {
+    float4 C = *reinterpret_cast<const float4*>(&s[r][q0]);
+    float4 U = *reinterpret_cast<const float4*>(&s[r - 1][q0]);
+    float4 D = *reinterpret_cast<const float4*>(&s[r + 1][q0]);
+    Q.c[0] = C.x; Q.c[1] = C.y; Q.c[2] = C.z; Q.c[3] = C.w;
+    Q.u[0] = U.x; Q.u[1] = U.y; Q.u[2] = U.z; Q.u[3] = U.w;
+    Q.d[0] = D.x; Q.d[1] = D.y; Q.d[2] = D.z; Q.d[3] = D.w;
+    float left = __shfl_up_sync(0xffffffffu, C.w, 1);
+    float right = __shfl_down_sync(0xffffffffu, C.x, 1);
+    if (threadIdx.x == 0) left = s[r][q0 - 1];
+    if (threadIdx.x == 31) right = s[r][q0 + 4];
+    Q.l[0] = left; Q.l[1] = C.x; Q.l[2] = C.y; Q.l[3] = C.z;
+    Q.r[0] = C.y; Q.r[1] = C.z; Q.r[2] = C.w; Q.r[3] = right;
+}
+
+template <int ORDER, bool EPI>
+__global__ void __launch_bounds__(STEP4_TX * 32)
+step_fwd4_kernel(StepScalars k, int nx, int ny, int coef_batched, const float* __restrict__ b,
+                 const float* __restrict__ c, const float* __restrict__ y1, size_t bs1,
+                 const float* __restrict__ y2, size_t bs2, float* __restrict__ y, size_t bs,
+                 SeqEpilogue e) {
+    __shared__ __align__(16) float s[STEP4_TX + 2][S4W];
+    const int inst = blockIdx.z;
+    const int x0 = blockIdx.y * STEP4_TX, y0 = blockIdx.x * STEP4_TY;
+    const size_t plane = (size_t)nx * ny;
+    stage_tile4(s, y1 + inst * bs1, nx, ny, x0, y0);
+    __syncthreads();
+    const int gx = x0 + threadIdx.y, gy = y0 + 4 * threadIdx.x;
+    Quad Q;
+    load_quad(Q, s, threadIdx.y + 1, 4 + 4 * threadIdx.x);   // all lanes: the shuffles need them
+    if (gx >= nx || gy >= ny) return;
+    const size_t cell = (size_t)gx * ny + gy;
+    const size_t ci = coef_batched ? inst * plane + cell : cell;
+    const float4 b4 = __ldg(reinterpret_cast<const float4*>(b + ci));
+    const float4 c4 = __ldg(reinterpret_cast<const float4*>(c + ci));
+    const float4 p4 = __ldg(reinterpret_cast<const float4*>(y2 + inst * bs2 + cell));
+    const float bb[4] = {b4.x, b4.y, b4.z, b4.w}, cc[4] = {c4.x, c4.y, c4.z, c4.w};
+    const float pp[4] = {p4.x, p4.y, p4.z, p4.w};
+    float v[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        const FwdCoef f = fwd_coef(bb[j], cc[j], k);
+        const float L = lap5<ORDER>(Q.u[j], Q.l[j], Q.c[j], Q.r[j], Q.d[j], k.lap_w, k.lap_w4);
+        v[j] = leapfrog(f.A, f.Bc, f.c2, k.two_over, Q.c[j], pp[j], L);
+    }
+    if (EPI && (!e.tileflag || __ldg(e.tileflag + blockIdx.y * e.tiles_y + blockIdx.x))) {
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            for (int en = __ldg(e.srcmap + cell + j); en >= 0; en = __ldg(e.src_next + en)) {
+                int row = __ldg(e.src_row + en);
+                row = row < 0 ? inst : row;
+                v[j] = fadd(v[j], __ldg(e.x + (size_t)row * e.steps + e.t));
+            }
+            for (int en = __ldg(e.probemap + cell + j); en >= 0; en = __ldg(e.probe_next + en)) {
+                size_t o = ((size_t)inst * e.steps + e.t) * e.n_probe + en;
+                e.out[o] = __ldg(e.probe_kind + en) ? fmul(v[j], v[j]) : v[j];
+                if (e.amp) e.amp[o] = v[j];
+            }
+        }
+    }
+    *reinterpret_cast<float4*>(y + inst * bs + cell) = make_float4(v[0], v[1], v[2], v[3]);
+}
+
+// The adjoint's staged field Kg * lam_{t+1} (coefficients of the cell).
+WT_DEV void stage_c2g4(float (*s)[S4W], const float* __restrict__ lam, const float* __restrict__ b,
+                       const float* __restrict__ c, const StepScalars& k, int nx, int ny, int x0,
+                       int y0) {
+    const int tid = threadIdx.y * 32 + threadIdx.x;
+    constexpr int CH = S4W / 4;
+    for (int i = tid; i < (STEP4_TX + 2) * CH; i += STEP4_TX * 32) {
+        const int rr = i / CH, j = i - rr * CH;
+        const int gx = x0 - 1 + rr, gy = y0 - 4 + 4 * j;
+        float o[4] = {0.f, 0.f, 0.f, 0.f};
+        if (lam && gx >= 0 && gx < nx && gy >= 0 && gy < ny) {
+            const size_t hc = (size_t)gx * ny + gy;
+            const float4 l4 = __ldg(reinterpret_cast<const float4*>(lam + hc));
+            const float4 b4 = __ldg(reinterpret_cast<const float4*>(b + hc));
+            const float4 c4 = __ldg(reinterpret_cast<const float4*>(c + hc));
+            const float ll[4] = {l4.x, l4.y, l4.z, l4.w}, bb[4] = {b4.x, b4.y, b4.z, b4.w};
+            const float cv[4] = {c4.x, c4.y, c4.z, c4.w};
+#pragma unroll
+            for (int m = 0; m < 4; ++m) o[m] = fmul(bwd_coef(bb[m], cv[m], k).Kg, ll[m]);
+        }
+        *reinterpret_cast<float4*>(&s[rr][4 * j]) = make_float4(o[0], o[1], o[2], o[3]);
+    }
+}
+
+template <int ORDER>
+__global__ void __launch_bounds__(STEP4_TX * 32)
+seq_adj_step4_kernel(StepScalars k, int nx, int ny, const float* __restrict__ b,
+                     const float* __restrict__ c, const float* __restrict__ lam1,
+                     const float* __restrict__ lam2, const float* __restrict__ hprev, size_t hbs,
+                     float* __restrict__ lam_out, float* __restrict__ gc, AdjEpilogue e) {
+    __shared__ __align__(16) float sg[STEP4_TX + 2][S4W];
+    __shared__ __align__(16) float sy[STEP4_TX + 2][S4W];
+    const int inst = blockIdx.z;
+    const int x0 = blockIdx.y * STEP4_TX, y0 = blockIdx.x * STEP4_TY;
+    const size_t plane = (size_t)nx * ny;
+    stage_c2g4(sg, lam1 ? lam1 + inst * plane : nullptr, b, c, k, nx, ny, x0, y0);
+    if (hprev) stage_tile4(sy, hprev + inst * hbs, nx, ny, x0, y0);
+    __syncthreads();
+    const int gx = x0 + threadIdx.y, gy = y0 + 4 * threadIdx.x;
+    const int r = threadIdx.y + 1, q0 = 4 + 4 * threadIdx.x;
+    Quad G, Y;
+    load_quad(G, sg, r, q0);
+    if (hprev) load_quad(Y, sy, r, q0);
+    if (gx >= nx || gy >= ny) return;
+    const size_t cell = (size_t)gx * ny + gy;
+    const size_t ic = inst * plane + cell;
+    const float4 b4 = __ldg(reinterpret_cast<const float4*>(b + cell));
+    const float4 c4 = __ldg(reinterpret_cast<const float4*>(c + cell));
+    const float bb[4] = {b4.x, b4.y, b4.z, b4.w}, cv[4] = {c4.x, c4.y, c4.z, c4.w};
+    float l1[4] = {0.f, 0.f, 0.f, 0.f}, l2[4] = {0.f, 0.f, 0.f, 0.f};
+    if (lam1) {
+        const float4 v = __ldg(reinterpret_cast<const float4*>(lam1 + ic));
+        l1[0] = v.x; l1[1] = v.y; l1[2] = v.z; l1[3] = v.w;
+    }
+    if (lam2) {
+        const float4 v = __ldg(reinterpret_cast<const float4*>(lam2 + ic));
+        l2[0] = v.x; l2[1] = v.y; l2[2] = v.z; l2[3] = v.w;
+    }
+    const bool taps = !e.tileflag || __ldg(e.tileflag + blockIdx.y * e.tiles_y + blockIdx.x);
+    float lam[4], g4[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        const BwdCoef kb = bwd_coef(bb[j], cv[j], k);
+        // gradient arriving at h_t: first gy2 from step t+2, then gy1 from t+1
+        float lv = 0.f;
+        if (lam2) lv = fmul(kb.Ky2, l2[j]);
+        if (lam1) {
+            const float lg = lap5<ORDER>(G.u[j], G.l[j], G.c[j], G.r[j], G.d[j], k.lap_w, k.lap_w4);
+            const float gy1 = fadd(fmul(k.dt2, lg), fmul(fmul(2.0f, l1[j]), kb.X1));
+            lv = lam2 ? fadd(lv, gy1) : gy1;
+        }
+        if (taps) {
+            // probe seeds, highest probe index first (descending chains)
+            for (int en = __ldg(e.probemap + cell + j); en >= 0; en = __ldg(e.probe_next + en)) {
+                size_t o = ((size_t)inst * e.steps + e.t) * e.n_probe + en;
+                float gv = __ldg(e.grad_out + o);
+                float sd = __ldg(e.probe_kind + en) ? fmul(gv, fmul(2.0f, __ldg(e.amp + o))) : gv;
+                lv = fadd(lv, sd);
+            }
+        }
+        lam[j] = lv;
+        const float L = hprev ? lap5<ORDER>(Y.u[j], Y.l[j], Y.c[j], Y.r[j], Y.d[j], k.lap_w, k.lap_w4)
+                              : 0.0f;
+        g4[j] = fmul(fmul(kb.X1, fmul(kb.Kc, L)), lv);
+        if (e.grad_x && taps) {
+            for (int en = __ldg(e.srcmap + cell + j); en >= 0; en = __ldg(e.src_next + en))
+                if (__ldg(e.src_row + en) < 0) e.grad_x[(size_t)inst * e.steps + e.t] = lv;
+        }
+    }
+    *reinterpret_cast<float4*>(lam_out + ic) = make_float4(lam[0], lam[1], lam[2], lam[3]);
+    if (gc) *reinterpret_cast<float4*>(gc + ic) = make_float4(g4[0], g4[1], g4[2], g4[3]);
+}
+
 // Phase 2: G_c += chunked batch sum of gc (wavetorch autograd: sum-to-shape of
 // each step's [batch,nx,ny] grad_c, then accumulation over steps).
 __global__ void seq_adj_reduce_kernel(int batch, size_t plane, const float* __restrict__ gc,
@@ -274,10 +461,38 @@ __global__ void fill_zero_kernel(float* p, size_t n) {
 
 // ---------------------------------------------------------------------------
 // Launch helpers used by api.cu
+// The vector kernels need rows of a multiple of 4 cells and 16-byte aligned
+// fields and strides.
+static bool vec4_ok(int ny, std::initializer_list<const void*> ptrs,
+                    std::initializer_list<size_t> strides) {
+    if (ny % 4) return false;
+    for (const void* p : ptrs)
+        if (p && (reinterpret_cast<uintptr_t>(p) & 15)) return false;
+    for (size_t s : strides)
+        if (s % 4) return false;
+    return true;
+}
+
 int wt_launch_step_fwd(const StepScalars& k, int batch, int nx, int ny, int coef_batched,
                        const float* b, const float* c, const float* y1, size_t bs1,
                        const float* y2, size_t bs2, float* y, size_t bs,
                        const wt::SeqEpilogue* epi, cudaStream_t st) {
+    if (vec4_ok(ny, {b, c, y1, y2, y}, {bs1, bs2, bs})) {
+        dim3 blk(32, wt::STEP4_TX);
+        dim3 grd((ny + wt::STEP4_TY - 1) / wt::STEP4_TY, (nx + wt::STEP4_TX - 1) / wt::STEP4_TX, batch);
+        wt::SeqEpilogue e{};
+        if (epi) e = *epi;
+        const bool ep = epi != nullptr;
+        if (k.lap_order == WT_LAP_SEQ) {
+            if (ep) wt::step_fwd4_kernel<WT_LAP_SEQ, true><<<grd, blk, 0, st>>>(k, nx, ny, coef_batched, b, c, y1, bs1, y2, bs2, y, bs, e);
+            else    wt::step_fwd4_kernel<WT_LAP_SEQ, false><<<grd, blk, 0, st>>>(k, nx, ny, coef_batched, b, c, y1, bs1, y2, bs2, y, bs, e);
+        } else {
+            if (ep) wt::step_fwd4_kernel<WT_LAP_PAIRED, true><<<grd, blk, 0, st>>>(k, nx, ny, coef_batched, b, c, y1, bs1, y2, bs2, y, bs, e);
+            else    wt::step_fwd4_kernel<WT_LAP_PAIRED, false><<<grd, blk, 0, st>>>(k, nx, ny, coef_batched, b, c, y1, bs1, y2, bs2, y, bs, e);
+        }
+        wt_count_launches(1);
+        return wt_cuda_status(cudaGetLastError());
+    }
     dim3 blk(wt::TY, wt::TX);
     dim3 grd((ny + wt::TY - 1) / wt::TY, (nx + wt::TX - 1) / wt::TX, batch);
     if (epi) {
@@ -315,6 +530,16 @@ int wt_launch_seq_adj_step(const StepScalars& k, int batch, int nx, int ny, cons
                            const float* c, const float* lam1, const float* lam2,
                            const float* hprev, size_t hbs, float* lam_out, float* gc,
                            const wt::AdjEpilogue& e, cudaStream_t st) {
+    if (vec4_ok(ny, {b, c, lam1, lam2, hprev, lam_out, gc}, {hbs, (size_t)nx * ny})) {
+        dim3 blk(32, wt::STEP4_TX);
+        dim3 grd((ny + wt::STEP4_TY - 1) / wt::STEP4_TY, (nx + wt::STEP4_TX - 1) / wt::STEP4_TX, batch);
+        if (k.lap_order == WT_LAP_SEQ)
+            wt::seq_adj_step4_kernel<WT_LAP_SEQ><<<grd, blk, 0, st>>>(k, nx, ny, b, c, lam1, lam2, hprev, hbs, lam_out, gc, e);
+        else
+            wt::seq_adj_step4_kernel<WT_LAP_PAIRED><<<grd, blk, 0, st>>>(k, nx, ny, b, c, lam1, lam2, hprev, hbs, lam_out, gc, e);
+        wt_count_launches(1);
+        return wt_cuda_status(cudaGetLastError());
+    }
     dim3 blk(wt::TY, wt::TX);
     dim3 grd((ny + wt::TY - 1) / wt::TY, (nx + wt::TX - 1) / wt::TX, batch);
     if (k.lap_order == WT_LAP_SEQ)
