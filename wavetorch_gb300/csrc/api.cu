@@ -369,7 +369,7 @@ extern "C" int wt_seq_fwd(const wt_scalars* s, const wt_seq_desc* d, const float
         float* hist = at<float>(workspace, P.o_hist);
         float* zero = at<float>(workspace, P.o_zero);
         if ((st = wt_launch_fill_zero(zero, plane, cs))) return st;
-        wt::SeqEpilogue e;
+        wt::SeqEpilogue e{};
         e.srcmap = at<int>(workspace, P.o_srcmap);
         e.src_next = at<int>(workspace, P.o_srcnext);
         e.src_row = at<int>(workspace, P.o_srcrow);
@@ -433,7 +433,7 @@ extern "C" int wt_seq_bwd(const wt_scalars* s, const wt_seq_desc* d, const float
         float* hist = at<float>(workspace, P.o_hist);
         float* lam = at<float>(workspace, P.o_lam);
         float* gc = at<float>(workspace, P.o_gc);
-        wt::AdjEpilogue e;
+        wt::AdjEpilogue e{};
         e.probemap = at<int>(workspace, P.o_prbmap);
         e.probe_next = at<int>(workspace, P.o_prbnext);
         e.probe_kind = at<int>(workspace, P.o_prbkind);
@@ -453,11 +453,15 @@ extern "C" int wt_seq_bwd(const wt_scalars* s, const wt_seq_desc* d, const float
             const float* l1 = t + 1 < P.T ? lam + (size_t)((t + 1) % 3) * bp : nullptr;
             const float* l2 = t + 2 < P.T ? lam + (size_t)((t + 2) % 3) * bp : nullptr;
             const float* hp = t >= 1 ? hist + (size_t)(t - 1) * plane : nullptr;
+            if (P.B == 1) {       // one instance: the step accumulates dL/dc itself
+                e.G = grad_c;
+                e.first = t == P.T - 1;
+            }
             st = wt_launch_seq_adj_step(k, P.B, P.nx, P.ny, b, c, l1, l2, hp, hbs,
                                         lam + (size_t)(t % 3) * bp, gc, e, cs);
             if (st) return st;
-            st = wt_launch_seq_adj_reduce(P.B, plane, gc, grad_c, t == P.T - 1, cs);
-            if (st) return st;
+            if (P.B > 1 && (st = wt_launch_seq_adj_reduce(P.B, plane, gc, grad_c, t == P.T - 1, cs)))
+                return st;
         }
         return WT_OK;
     }

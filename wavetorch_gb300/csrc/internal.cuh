@@ -43,6 +43,10 @@ struct AdjEpilogue {
     float* grad_x;                 // [batch][steps] or null
     const int* tileflag;           // as SeqEpilogue::tileflag
     int tiles_y;
+    // batch of one: accumulate dL/dc here directly (the batch reduction's
+    // arithmetic for one instance) instead of writing the step's term
+    float* G;
+    int first;
 };
 
 // Parameters of the fused persistent kernels.

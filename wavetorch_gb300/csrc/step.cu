@@ -236,9 +236,15 @@ seq_adj_step_kernel(StepScalars k, int nx, int ny, const float* __restrict__ b,
         }
     }
     lam_out[ic] = lam;
-    if (gc) {
+    if (gc || e.G) {
         float L = hprev ? tile_lap<ORDER>(sy, r, q, k) : 0.0f;
-        gc[ic] = fmul(fmul(kb.X1, fmul(kb.Kc, L)), lam);
+        const float t = fmul(fmul(kb.X1, fmul(kb.Kc, L)), lam);
+        if (e.G) {
+            const float acc = fadd(0.f, t);
+            e.G[cell] = e.first ? acc : fadd(e.G[cell], acc);
+        } else {
+            gc[ic] = t;
+        }
     }
     if (e.grad_x) {
         for (int en = __ldg(e.srcmap + cell); en >= 0; en = __ldg(e.src_next + en)) {
@@ -432,7 +438,20 @@ seq_adj_step4_kernel(StepScalars k, int nx, int ny, const float* __restrict__ b,
         }
     }
     *reinterpret_cast<float4*>(lam_out + ic) = make_float4(lam[0], lam[1], lam[2], lam[3]);
-    if (gc) *reinterpret_cast<float4*>(gc + ic) = make_float4(g4[0], g4[1], g4[2], g4[3]);
+    if (e.G) {
+        float4* gp = reinterpret_cast<float4*>(e.G + cell);
+        float acc[4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) acc[j] = fadd(0.f, g4[j]);
+        if (!e.first) {
+            const float4 o = *gp;
+            acc[0] = fadd(o.x, acc[0]); acc[1] = fadd(o.y, acc[1]);
+            acc[2] = fadd(o.z, acc[2]); acc[3] = fadd(o.w, acc[3]);
+        }
+        *gp = make_float4(acc[0], acc[1], acc[2], acc[3]);
+    } else if (gc) {
+        *reinterpret_cast<float4*>(gc + ic) = make_float4(g4[0], g4[1], g4[2], g4[3]);
+    }
 }
 
 // Phase 2: G_c += chunked batch sum of gc (wavetorch autograd: sum-to-shape of
@@ -530,7 +549,7 @@ int wt_launch_seq_adj_step(const StepScalars& k, int batch, int nx, int ny, cons
                            const float* c, const float* lam1, const float* lam2,
                            const float* hprev, size_t hbs, float* lam_out, float* gc,
                            const wt::AdjEpilogue& e, cudaStream_t st) {
-    if (vec4_ok(ny, {b, c, lam1, lam2, hprev, lam_out, gc}, {hbs, (size_t)nx * ny})) {
+    if (vec4_ok(ny, {b, c, lam1, lam2, hprev, lam_out, gc, e.G}, {hbs, (size_t)nx * ny})) {
         dim3 blk(32, wt::STEP4_TX);
         dim3 grd((ny + wt::STEP4_TY - 1) / wt::STEP4_TY, (nx + wt::STEP4_TX - 1) / wt::STEP4_TX, batch);
         if (k.lap_order == WT_LAP_SEQ)
