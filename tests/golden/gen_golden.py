@@ -260,6 +260,21 @@ def case_geom(wt, N, seed):
             "grad_c": _np(gc), "grad_rho": _np(gr), "b": _np(geom.b)}
 
 
+def case_holey(wt):
+    """WaveGeometryHoley (wavetorch/geom.py:88-132): rho and c of three
+    exponential holes on a 64x48 grid, and the gradient of a random linear
+    functional of c with respect to the holes' x, y, r."""
+    g = torch.Generator().manual_seed(16)
+    geom = wt.WaveGeometryHoley((64, 48), 1.0, c0=1.0, c1=0.5, abs_N=10, abs_sig=3.0, abs_p=2,
+                                x=[20.3, 35.5, 44.0], y=[12.0, 30.0, 24.5], r=[3.0, 5.5, 2.5])
+    c = geom.c
+    w = torch.randn(64, 48, generator=g)
+    gx, gy, gr = torch.autograd.grad((c * w).sum(), [geom.x, geom.y, geom.r])
+    return {"rho": _np(geom.rho), "c": _np(c), "w": _np(w), "grad_x": _np(gx), "grad_y": _np(gy),
+            "grad_r": _np(gr), "x": np.array([20.3, 35.5, 44.0], np.float32),
+            "y": np.array([12.0, 30.0, 24.5], np.float32), "r": np.array([3.0, 5.5, 2.5], np.float32)}
+
+
 def state_keys(wt):
     """state_dict keys, shapes and dtypes of a reference model (drop-in check)."""
     geom = wt.WaveGeometryFreeForm((50, 50), 1.0, c0=1.0, c1=0.5, abs_N=10, abs_sig=3.0, abs_p=2,
@@ -293,6 +308,7 @@ def main():
         "step_b20_h1": lambda: case_step(wt, 20, 10, 0.707, 1.0, 7),
         "geom_n100": lambda: case_geom(wt, 100, 8),
         "geom_n160": lambda: case_geom(wt, 160, 9),
+        "holey": lambda: case_holey(wt),
     }
     only = set(sys.argv[1:])
     if not only or "state_keys" in only:

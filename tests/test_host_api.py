@@ -135,3 +135,24 @@ def test_synthetic_vowels_shape_and_norm():
     assert x.shape == (8, 3500) and x.dtype == np.float32
     assert np.allclose(np.abs(x).max(axis=1), 1.0)
     assert set(np.unique(y)) <= {0, 1, 2}
+
+
+def _holey(d, dev="cpu"):
+    import wavetorch_gb300 as wt
+    return wt.WaveGeometryHoley((64, 48), 1.0, c0=1.0, c1=0.5, abs_N=10, abs_sig=3.0, abs_p=2,
+                                x=d["x"].tolist(), y=d["y"].tolist(), r=d["r"].tolist()).to(dev)
+
+
+def test_holey_geometry_matches_reference_on_cpu():
+    """WaveGeometryHoley runs the reference's torch operations
+    (wavetorch/geom.py:88-132): on the CPU rho, c and the gradients with
+    respect to the holes' centres and radii are the reference's."""
+    import torch
+    d = golden("holey")
+    geom = _holey(d)
+    c = geom.c
+    gx, gy, gr = torch.autograd.grad((c * torch.from_numpy(d["w"])).sum(), [geom.x, geom.y, geom.r])
+    assert np.array_equal(geom.rho.detach().numpy(), d["rho"])
+    assert np.array_equal(c.detach().numpy(), d["c"])
+    for got, key in ((gx, "grad_x"), (gy, "grad_y"), (gr, "grad_r")):
+        assert np.allclose(got.numpy(), d[key], rtol=1e-6, atol=0), key
