@@ -272,6 +272,39 @@ int wt_rho_to_c_work_bytes(const wt_geom_desc* g, size_t* bytes);
 int wt_rho_to_c_fwd_noalloc(const wt_geom_desc* g, const float* rho, const float* blur_kernel,
                             float* c, wt_stream_t stream);
 
+/* ======================================================================== *
+ * 4. Hole geometry (WaveGeometryHoley, wavetorch/geom.py:88-132).           *
+ * ======================================================================== */
+
+typedef struct wt_holey_desc {
+    int32_t nx, ny;
+    int32_t n_holes;          /* holes used: the shortest of x, y, r         */
+    float eta, beta;          /* projection parameters                       */
+    float c0, c1;             /* float32 values of the c0/c1 buffers         */
+} wt_holey_desc;
+
+/* rho = P(s), s[i][j] = sum_k exp(-sqrt((i - x_k)^2 + (j - y_k)^2) / r_k)
+ * (holes summed in index order), c = c0 + (c1 - c0) * rho, P as for the
+ * free-form geometry.  Replaces WaveGeometryHoley._rho / .rho / .c
+ * (wavetorch/geom.py:109-132).  x, y, r: n_holes device floats.  rho and c
+ * ([nx, ny]) may each be NULL.  work: wt_holey_work_bytes bytes, caller-
+ * owned; the forward writes the tanh values the backward reads.            */
+int wt_holey_fwd(const wt_holey_desc* d, const float* x, const float* y, const float* r,
+                 float* rho, float* c, float* work, wt_stream_t stream);
+
+/* grad_x/y/r[k] = sum over cells of d(rho, c)/d(x_k, y_k, r_k) applied to
+ * grad_rho and grad_c (either may be NULL), using `work` from the matching
+ * forward.  Cell contributions are formed in float32 in the order of the
+ * reference's autograd chain and summed in double, in a fixed order.  A hole
+ * centred exactly on a cell gives NaN gradients, as in the reference (the
+ * derivative of the distance at 0).                                        */
+int wt_holey_bwd(const wt_holey_desc* d, const float* x, const float* y, const float* r,
+                 const float* grad_rho, const float* grad_c, float* grad_x, float* grad_y,
+                 float* grad_r, float* work, wt_stream_t stream);
+
+/* Bytes of `work` the two calls above need. */
+int wt_holey_work_bytes(const wt_holey_desc* d, size_t* bytes);
+
 #ifdef __cplusplus
 }
 #endif

@@ -3,7 +3,7 @@
 numpy/ctypes front end of ``wave_oracle.c``, the plain-C float32 restatement
 of fancompute/wavetorch v0.2.1's time-stepping path (wavetorch/cell.py:12-44,
 wavetorch/operators.py:5-11, wavetorch/rnn.py:36-72, wavetorch/geom.py:63-85,
-207-233).  Pinned against golden vectors produced by running the reference
+109-132, 207-233).  Pinned against golden vectors produced by running the reference
 (tests/golden/).  Nothing in the product imports this module.
 """
 from __future__ import annotations
@@ -148,6 +148,33 @@ def rho_to_c_bwd(th, kernel, blur_n, eta, beta, c0, c1, grad_c):
     load().or_rho_to_c_bwd(nx, ny, rad, blur_n, C.c_float(eta), C.c_float(beta), C.c_float(c0),
                            C.c_float(c1), _p(k), _p(th), _p(g), _p(gr))
     return gr
+
+
+def holey(nx, ny, x, y, r, eta, beta, c0, c1):
+    """Hole geometry (wavetorch/geom.py:109-132): returns (rho, c, tanh values)
+    for holes at (x_k, y_k) of radius r_k (the shortest of the three sets)."""
+    x, y, r = _f(x).ravel(), _f(y).ravel(), _f(r).ravel()
+    nh = min(len(x), len(y), len(r))
+    rho = np.empty((nx, ny), np.float32)
+    c = np.empty_like(rho)
+    th = np.empty_like(rho)
+    load().or_holey(nx, ny, nh, C.c_float(eta), C.c_float(beta), C.c_float(c0), C.c_float(c1),
+                    _p(x), _p(y), _p(r), _p(rho), _p(c), _p(th))
+    return rho, c, th
+
+
+def holey_bwd(x, y, r, th, eta, beta, c0, c1, grad_rho=None, grad_c=None):
+    """Gradients (x, y, r) of <grad_rho, rho> + <grad_c, c> for the holes."""
+    x, y, r, th = _f(x).ravel(), _f(y).ravel(), _f(r).ravel(), _f(th)
+    nh = min(len(x), len(y), len(r))
+    nx, ny = th.shape
+    grho = None if grad_rho is None else _f(grad_rho)
+    gc = None if grad_c is None else _f(grad_c)
+    gx, gy, gr = (np.zeros(nh, np.float32) for _ in range(3))
+    load().or_holey_bwd(nx, ny, nh, C.c_float(eta), C.c_float(beta), C.c_float(c0),
+                        C.c_float(c1), _p(x), _p(y), _p(r), _p(th), _p(grho), _p(gc), _p(gx),
+                        _p(gy), _p(gr))
+    return gx, gy, gr
 
 
 def num_threads() -> int:

@@ -413,6 +413,72 @@ void or_rho_to_c_bwd(int nx, int ny, int rad, int blur_n, float eta, float beta,
     free(a); free(t);
 }
 
+/* ---- hole geometry (wavetorch/geom.py:109-132) ----------------------------
+ * s[i][j] = sum_k exp(-sqrt((i - x_k)^2 + (j - y_k)^2) / r_k), the holes added
+ * in index order to a zero field (geom.py:119-123); rho = P(s) and
+ * c = c0 + (c1 - c0) rho (geom.py:125-132).  exp and tanh are evaluated in
+ * double and rounded once to float.  rho, c, th nullable. */
+static float hole_exp(float fi, float fj, float xk, float yk, float rk, float* dist, float* dx,
+                      float* dy) {
+    float a = fi - xk, b = fj - yk;
+    float d = sqrtf(a * a + b * b);
+    *dist = d; *dx = a; *dy = b;
+    return (float)exp((double)(-d / rk));
+}
+
+void or_holey(int nx, int ny, int nh, float eta, float beta, float c0, float c1, const float* x,
+              const float* y, const float* r, float* rho, float* c, float* th) {
+    double be = (double)beta * (double)eta, b1 = (double)beta * (1.0 - (double)eta);
+    float tbe = (float)tanh(be);
+    float den = (float)(tanh(be) + tanh(b1));
+    float dc = (float)((double)c1 - (double)c0);
+    for (int i = 0; i < nx; ++i)
+        for (int j = 0; j < ny; ++j) {
+            float s = 0.0f, d, a, b;
+            for (int k = 0; k < nh; ++k) s = s + hole_exp((float)i, (float)j, x[k], y[k], r[k], &d, &a, &b);
+            float tz = (float)tanh((double)(beta * (s - eta)));
+            float P = (tz + tbe) / den;
+            size_t q = (size_t)i * ny + j;
+            if (th) th[q] = tz;
+            if (rho) rho[q] = P;
+            if (c) c[q] = c0 + dc * P;
+        }
+}
+
+/* Gradients with respect to the holes' centres and radii, the reference's
+ * autograd chain per cell (MulBackward, DivBackward, TanhBackward,
+ * ExpBackward, DivBackward for both operands, NegBackward, SqrtBackward,
+ * PowBackward, SubBackward) in float32; the sum over cells in double.  grho
+ * and gc nullable (zero). */
+void or_holey_bwd(int nx, int ny, int nh, float eta, float beta, float c0, float c1,
+                  const float* x, const float* y, const float* r, const float* th,
+                  const float* grho, const float* gc, float* gx, float* gy, float* gr) {
+    double be = (double)beta * (double)eta, b1 = (double)beta * (1.0 - (double)eta);
+    float den = (float)(tanh(be) + tanh(b1));
+    float dc = (float)((double)c1 - (double)c0);
+    for (int k = 0; k < nh; ++k) {
+        double ax = 0.0, ay = 0.0, ar = 0.0;
+        for (int i = 0; i < nx; ++i)
+            for (int j = 0; j < ny; ++j) {
+                size_t q = (size_t)i * ny + j;
+                float gp = (grho ? grho[q] : 0.0f) + (gc ? gc[q] * dc : 0.0f);
+                float gs = ((gp / den) * (1.0f - th[q] * th[q])) * beta;
+                float d, a, b;
+                float e = hole_exp((float)i, (float)j, x[k], y[k], r[k], &d, &a, &b);
+                float ge = gs * e;
+                float gq = ge / r[k];
+                float grk = -ge * ((-d / r[k]) / r[k]);
+                float gd2 = -gq / (2.0f * d);
+                ax += (double)(-(gd2 * (2.0f * a)));
+                ay += (double)(-(gd2 * (2.0f * b)));
+                ar += (double)grk;
+            }
+        gx[k] = (float)ax;
+        gy[k] = (float)ay;
+        gr[k] = (float)ar;
+    }
+}
+
 int or_num_threads(void) {
 #ifdef _OPENMP
     extern int omp_get_max_threads(void);

@@ -96,3 +96,19 @@ def test_fp64_finite_difference_fixtures_match_reference_autograd(name):
     fd, ag = d["fd_grad"], d["grad_rho64"]
     assert fd.shape == (16,)
     assert np.abs(fd - ag).max() <= 1e-7 * np.abs(fd).max()
+
+
+def test_holey_geometry():
+    """The oracle's hole geometry against the reference's (golden `holey`:
+    64x48, three holes, gradients of sum(c * w)).  A one-ulp difference in
+    exp moves the projected density by up to beta/2 ulps, so a few cells
+    differ by a few 1e-6."""
+    d = golden("holey")
+    rho, c, th = o.holey(64, 48, d["x"], d["y"], d["r"], 0.5, 100.0, 1.0, 0.5)
+    assert np.abs(rho - d["rho"]).max() <= 5e-6
+    assert np.abs(c - d["c"]).max() <= 5e-6
+    assert np.count_nonzero(rho != d["rho"]) <= 0.005 * rho.size
+    g = o.holey_bwd(d["x"], d["y"], d["r"], th, 0.5, 100.0, 1.0, 0.5, grad_c=d["w"])
+    for got, key in zip(g, ("grad_x", "grad_y", "grad_r")):
+        ref = d[key]
+        assert np.abs(got - ref).max() <= 2e-5 * np.abs(ref).max(), key

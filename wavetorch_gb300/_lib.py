@@ -32,6 +32,7 @@ EXPORTED = [
     "wt_loss_ce_normalize_power", "wt_seq_bwd_sum",
     "wt_seq_workspace_bytes_nl", "wt_seq_fwd_nl", "wt_seq_bwd_nl",
     "wt_rho_to_c_fwd", "wt_rho_to_c_bwd", "wt_rho_to_c_work_bytes", "wt_rho_to_c_fwd_noalloc",
+    "wt_holey_fwd", "wt_holey_bwd", "wt_holey_work_bytes",
 ]
 
 
@@ -72,6 +73,13 @@ class GeomDesc(C.Structure):
     ]
 
 
+class HoleyDesc(C.Structure):
+    _fields_ = [
+        ("nx", C.c_int32), ("ny", C.c_int32), ("n_holes", C.c_int32),
+        ("eta", C.c_float), ("beta", C.c_float), ("c0", C.c_float), ("c1", C.c_float),
+    ]
+
+
 _VP = C.c_void_p
 _lock = threading.Lock()
 _lib = None
@@ -107,6 +115,9 @@ def _declare(lib):
     lib.wt_rho_to_c_bwd.argtypes = [P(GeomDesc), _VP, _VP, _VP, _VP, _VP, _VP]
     lib.wt_rho_to_c_work_bytes.argtypes = [P(GeomDesc), P(C.c_size_t)]
     lib.wt_rho_to_c_fwd_noalloc.argtypes = [P(GeomDesc), _VP, _VP, _VP, _VP]
+    lib.wt_holey_fwd.argtypes = [P(HoleyDesc), _VP, _VP, _VP, _VP, _VP, _VP, _VP]
+    lib.wt_holey_bwd.argtypes = [P(HoleyDesc)] + [_VP] * 10
+    lib.wt_holey_work_bytes.argtypes = [P(HoleyDesc), P(C.c_size_t)]
     for name in EXPORTED:
         if name not in ("wt_version", "wt_status_string", "wt_last_error", "wt_kernel_launches"):
             getattr(lib, name).restype = C.c_int

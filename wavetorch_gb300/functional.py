@@ -287,6 +287,42 @@ class WaveSeqNLFn(torch.autograd.Function):
 
 
 # ---------------------------------------------------------------------------
+class HoleyFn(torch.autograd.Function):
+    """(rho, c) of the hole geometry (wavetorch/geom.py:109-132) from the
+    holes' centres x, y and radii r; one kernel forward, two backward."""
+
+    @staticmethod
+    def forward(ctx, x, y, r, hdesc: _lib.HoleyDesc):
+        ctx.set_materialize_grads(False)
+        x, y, r = (_require_cuda_f32(n, t).reshape(-1) for n, t in (("x", x), ("y", y), ("r", r)))
+        lib = _lib.load()
+        n = C.c_size_t(0)
+        _lib.check(lib.wt_holey_work_bytes(C.byref(hdesc), C.byref(n)), "wt_holey_work_bytes")
+        work = torch.empty((int(n.value) + 7) // 8, dtype=torch.float64, device=x.device)
+        shape = (hdesc.nx, hdesc.ny)
+        rho = torch.empty(shape, device=x.device)
+        c = torch.empty(shape, device=x.device)
+        _lib.check(lib.wt_holey_fwd(C.byref(hdesc), _ptr(x), _ptr(y), _ptr(r), _ptr(rho),
+                                    _ptr(c), _ptr(work), _stream(x.device)), "wt_holey_fwd")
+        ctx.save_for_backward(x, y, r, work)
+        ctx.hdesc = hdesc
+        return rho, c
+
+    @staticmethod
+    def backward(ctx, grad_rho, grad_c):
+        x, y, r, work = ctx.saved_tensors
+        if grad_rho is None and grad_c is None:
+            return None, None, None, None
+        grho = None if grad_rho is None else _require_cuda_f32("grad_rho", grad_rho)
+        gc = None if grad_c is None else _require_cuda_f32("grad_c", grad_c)
+        gx, gy, gr = torch.zeros_like(x), torch.zeros_like(y), torch.zeros_like(r)
+        work = work.clone()   # the adjoint writes its partial sums into it
+        _lib.check(_lib.load().wt_holey_bwd(C.byref(ctx.hdesc), _ptr(x), _ptr(y), _ptr(r),
+                                            _ptr(grho), _ptr(gc), _ptr(gx), _ptr(gy), _ptr(gr),
+                                            _ptr(work), _stream(x.device)), "wt_holey_bwd")
+        return gx, gy, gr, None
+
+
 class RhoToCFn(torch.autograd.Function):
     """c = c0 + (c1 - c0) * P(blur^n(rho)) (wavetorch/geom.py:207-233)."""
 

@@ -3,7 +3,8 @@
 
 Buffer and parameter names are the reference's, so ``state_dict`` files and
 ``state_reconstruction_args`` round-trip between the two implementations.
-The free-form map rho -> c runs on the GPU (:class:`~wavetorch_gb300.functional.RhoToCFn`).
+The free-form map rho -> c and the hole geometry run on the GPU
+(:class:`~wavetorch_gb300.functional.RhoToCFn`, :class:`~wavetorch_gb300.functional.HoleyFn`).
 """
 from __future__ import annotations
 
@@ -14,7 +15,7 @@ import numpy as np
 import torch
 
 from . import _lib
-from .functional import RhoToCFn, _f32
+from .functional import HoleyFn, RhoToCFn, _f32
 from .utils import host_scalar, to_tensor
 
 
@@ -105,7 +106,12 @@ class WaveGeometry(torch.nn.Module):
 
 
 class WaveGeometryHoley(WaveGeometry):
-    """Density from a sum of exponential holes, projected (wavetorch/geom.py:88-132)."""
+    """Density from a sum of exponential holes, projected (wavetorch/geom.py:88-132).
+
+    With the holes on a CUDA device, rho and c come from one kernel
+    (:class:`~wavetorch_gb300.functional.HoleyFn`, ``wt_holey_fwd``) and their
+    gradients with respect to the holes' centres and radii from its adjoint
+    (``wt_holey_bwd``)."""
 
     def __init__(self, domain_shape: Tuple, h: float, c0: float, c1: float, abs_N: int = 20,
                  abs_sig: float = 11, abs_p: float = 4.0, eta: float = 0.5, beta: float = 100.0,
@@ -123,7 +129,21 @@ class WaveGeometryHoley(WaveGeometry):
                    "r": deepcopy(self.r.detach())}
         return {**super().state_reconstruction_args(), **my_args}
 
+    def holey_desc(self) -> _lib.HoleyDesc:
+        for name in ("x", "y", "r"):
+            if getattr(self, name).dim() != 1:
+                raise TypeError(f"the holes' {name} must be a 1-D tensor (one entry per hole)")
+        n = min(self.x.numel(), self.y.numel(), self.r.numel())   # zip() stops at the shortest
+        return _lib.HoleyDesc(self.domain_shape[0], self.domain_shape[1], n, _f32(self.eta),
+                              _f32(self.beta), _f32(self.c0), _f32(self.c1))
+
+    def _rho_c(self):
+        """(rho, c) on the GPU: one kernel evaluates both."""
+        return HoleyFn.apply(self.x, self.y, self.r, self.holey_desc())
+
     def _rho(self):
+        """The reference's torch operations (wavetorch/geom.py:109-123), for
+        holes held on the CPU."""
         eta, beta = self.eta.item(), self.beta.item()
         dev, dt = self.x.device, self.x.dtype
         xv = torch.arange(0, self.domain_shape[0], dtype=dt, device=dev)
@@ -137,10 +157,14 @@ class WaveGeometryHoley(WaveGeometry):
 
     @property
     def rho(self):
+        if self.x.is_cuda:
+            return self._rho_c()[0]
         return self._rho()
 
     @property
     def c(self):
+        if self.x.is_cuda:
+            return self._rho_c()[1]
         return self.c0.item() + (self.c1.item() - self.c0.item()) * self._rho()
 
 
