@@ -116,7 +116,7 @@ typedef struct wt_probe_entry {
 } wt_probe_entry;
 
 #define WT_FORM_PLAIN  0   /* per-step kernels, every field kept (exact)     */
-#define WT_FORM_FUSED  1   /* persistent cluster kernels, checkpointed       */
+#define WT_FORM_FUSED  1   /* persistent kernels (cluster or band layout)    */
 
 typedef struct wt_seq_desc {
     int32_t batch, nx, ny, steps;
@@ -129,7 +129,18 @@ typedef struct wt_seq_desc {
     int32_t cluster;                       /* CTAs per instance, 0 = auto    */
     int32_t output_fields;                 /* 1: also write every field      */
     int32_t coef_batched;                  /* 1: one geometry per instance   */
+    int32_t sm_count;                      /* SMs for the band layout, 0 = the
+                                              current device's                */
 } wt_seq_desc;
+
+/* The fused form has two layouts.  Instances that fit on one thread-block
+ * cluster (up to 256 columns; up to 256 rows with 16-CTA clusters) run one
+ * cluster per instance with the band boundaries exchanged over distributed
+ * shared memory.  Larger grids (up to 1024 columns) run in bands of rows, one
+ * CTA per band and SM in a cooperative launch, the band boundaries exchanged
+ * through global memory; that layout needs batch x bands <= sm_count, no
+ * output_fields, and runs its adjoint from the tape only (segment 0 or -1).
+ * `cluster` applies to the cluster layout only.                            */
 
 /* `segment` chooses how the fused form's adjoint gets the forward's fields:
  *   -1  tape: the forward stores Lap(h_{t-1}) of every cell and step

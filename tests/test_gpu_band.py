@@ -1,0 +1,114 @@
+"""The fused form's band layout (grids too large for one thread-block cluster:
+bands of rows, one CTA per band, boundaries exchanged through global memory)
+against the oracle, which is pinned bit for bit to the reference.  Probe
+outputs bit-exact; dL/dc within 1e-6 (the cluster layout's arithmetic)."""
+import numpy as np
+import pytest
+import torch
+
+import oracle.oracle as o
+from wavetorch_gb300 import _lib
+from wavetorch_gb300.functional import (SeqSpec, fused_supported, lap_order, scalars,
+                                        seq_backward, seq_device_status, seq_forward)
+from wavetorch_gb300.geom import pml_profile
+
+pytestmark = pytest.mark.gpu
+
+
+def rel(a, b):
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    return np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300)
+
+
+def problem(nx, ny, B, T, seed, abs_N=8, batched=False):
+    rng = np.random.default_rng(seed)
+    b = pml_profile((nx, ny), abs_N, 3.0, 2).numpy()
+    shape = (B, nx, ny) if batched else (nx, ny)
+    if batched:   # one geometry per instance: b and c are both [B, nx, ny]
+        b = np.stack([b * np.float32(1 + 0.5 * k) for k in range(B)]).astype(np.float32)
+    c = (0.5 + 0.5 * rng.random(shape)).astype(np.float32)
+    t = np.arange(T, dtype=np.float32)
+    x = np.stack([np.sin(0.21 * (k + 1) * t) for k in range(B)]).astype(np.float32)
+    return b, c, x
+
+
+def check(cuda, nx, ny, B, T, src, prb, seed=0, sm_count=0, grad_x=False, batched=False):
+    b, c, x = problem(nx, ny, B, T, seed, batched=batched)
+    g = np.random.default_rng(seed + 1).standard_normal((B, T, len(prb))).astype(np.float32)
+    order = lap_order(B, nx, ny, 1.0)
+    spec = SeqSpec(B, nx, ny, T, src, prb, form=_lib.WT_FORM_FUSED, sm_count=sm_count,
+                   coef_batched=batched)
+    assert fused_supported(spec)
+    sc = scalars(0.707, 1.0, order)
+    tb, tc, tx = (torch.from_numpy(v).to(cuda) for v in (b, c, x))
+    out, _, psum, ws = seq_forward(spec, sc, tb, tc, tx, want_sum=True)
+    gc, gx = seq_backward(spec, sc, tb, tc, tx, torch.from_numpy(g).to(cuda), ws, grad_x)
+    torch.cuda.synchronize()
+    assert seq_device_status(spec, ws) == _lib.WT_OK
+    insts = range(B) if batched else [None]
+    for k in insts:
+        S = o.Seq(1 if batched else B, nx, ny, T, 0.707, 1.0, src, prb, order=order)
+        ck = c[k] if batched else c
+        bk = b[k] if batched else b
+        xk = x[k:k + 1] if batched else x
+        gk = g[k:k + 1] if batched else g
+        oout, hist = S.forward(bk, ck, xk)
+        ogc, ogx = S.backward(bk, ck, hist, gk, want_x=grad_x)
+        got_out = out.cpu().numpy()[k:k + 1] if batched else out.cpu().numpy()
+        assert np.array_equal(got_out, oout)
+        got_gc = gc.cpu().numpy()[k] if batched else gc.cpu().numpy()
+        assert rel(got_gc, ogc) <= 1e-6, rel(got_gc, ogc)
+        if grad_x:
+            assert rel(gx.cpu().numpy(), ogx) <= 1e-6
+    # Kahan time sums of the outputs, as the cluster layout forms them
+    s = np.zeros(psum.shape, np.float32)
+    comp = np.zeros_like(s)
+    for t in range(T):
+        y = out.cpu().numpy()[:, t, :] - comp
+        tk = s + y
+        comp = (tk - s) - y
+        s = tk
+    assert np.array_equal(psum.cpu().numpy(), s)
+    return out, gc
+
+
+def test_lens_grid_line_source(cuda):
+    """1024 x 1024 (the lens configuration's grid, 147 bands of 7 rows on
+    152 SMs): a 625-cell line source on row 60, probes on the rows where
+    bands meet (55/56, 62/63) and inside a band."""
+    N, T = 1024, 48
+    src = [(60 * N + y, -1) for y in range(200, 825)]
+    prb = [(62 * N + 512, 1, 0), (63 * N + 500, 1, 1), (55 * N + 530, 0, 2), (70 * N + 512, 1, 3)]
+    check(cuda, N, N, 1, T, src, prb)
+
+
+@pytest.mark.parametrize("nx,ny,B", [(301, 530, 1), (301, 530, 2), (24, 600, 1), (160, 1000, 1)])
+def test_ragged_edges(cuda, nx, ny, B):
+    """Rows not a multiple of the band height (padding rows in the last band),
+    columns not a multiple of 32 (padding threads), batches of two; 24 x 600
+    takes the Laplacian order of torch's small-grid path."""
+    src = [((nx // 3) * ny + ny // 2, -1)]
+    prb = [((nx // 3 + 3) * ny + ny // 2 + 1, 1, 0), ((nx // 3 - 2) * ny + ny // 2, 0, 1),
+           ((nx - 1) * ny + ny - 1, 1, 2)]
+    check(cuda, nx, ny, B, 70, src, prb, seed=nx)
+
+
+def test_several_strips_per_band(cuda):
+    """Fewer SMs than bands of one strip: with 20 SMs a 300 x 300 grid runs
+    19 bands of two 8-row strips (640 threads), exchanging inside a band
+    through the tile and between bands through global memory."""
+    N = 300
+    src = [(40 * N + 150, -1), (40 * N + 151, -1)]
+    prb = [(15 * N + 150, 1, 0), (16 * N + 149, 1, 1), (31 * N + 152, 0, 2), (100 * N + 150, 1, 3)]
+    check(cuda, N, N, 1, 90, src, prb, sm_count=20)
+
+
+def test_input_gradient_and_per_instance_geometry(cuda):
+    """dL/dx at a point source, and one geometry per instance
+    (coef_batched) with per-instance dL/dc."""
+    nx, ny = 280, 400
+    src = [(100 * ny + 200, -1)]
+    prb = [(110 * ny + 200, 1, 0), (95 * ny + 210, 1, 1)]
+    check(cuda, nx, ny, 1, 60, src, prb, grad_x=True)
+    check(cuda, nx, ny, 2, 60, src, prb, batched=True, seed=3)

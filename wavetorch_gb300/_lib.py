@@ -58,7 +58,7 @@ class SeqDesc(C.Structure):
         ("n_sources", C.c_int32), ("sources_host", C.POINTER(SourceEntry)),
         ("n_probes", C.c_int32), ("probes_host", C.POINTER(ProbeEntry)),
         ("form", C.c_int32), ("segment", C.c_int32), ("cluster", C.c_int32),
-        ("output_fields", C.c_int32), ("coef_batched", C.c_int32),
+        ("output_fields", C.c_int32), ("coef_batched", C.c_int32), ("sm_count", C.c_int32),
     ]
 
 

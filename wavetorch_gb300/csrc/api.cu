@@ -111,11 +111,55 @@ struct SeqPlan {
     size_t o_amp;
     size_t o_hist, o_zero, o_lam, o_gc;             // plain
     size_t o_ckpt, o_stash, o_gcpart, o_lap, o_grho; // fused
+    size_t o_halo;                                  // fused, band layout
     size_t total;
     int seg, nseg;
     bool tape;                                      // fused: tape mode
+    bool band;                                      // fused: band layout
     WtFusedLaunch L;
+    WtBandLaunch BL;
 };
+
+// SMs of the band layout: the descriptor's count, else the current device's
+// (0 when there is no device).
+int band_sms(const wt_seq_desc* d) {
+    if (d->sm_count > 0) return d->sm_count;
+    int dev = 0, n = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) {
+        cudaGetLastError();   // leave no sticky error behind
+        return 0;
+    }
+    return n;
+}
+
+// Workspace of the band layout after the shared tables (offset o): the tape
+// (every step's Laplacian, [step][batch][band][M][threads]), the exchange
+// words, the per-instance dL/dc.  Sources and probes: at most two of each per
+// thread.
+int plan_band(const wt_seq_desc* d, SeqPlan& P, size_t o) {
+    const WtBandLaunch& B = P.BL;
+    const size_t F = sizeof(float);
+    P.band = true;
+    P.tape = true;
+    P.seg = P.T;
+    P.nseg = 1;
+    P.o_lap = o; o = up(o + (size_t)P.T * P.B * B.PR * B.threads * B.M * F);
+    P.o_halo = o; o = up(o + wt_band_halo_bytes(P.B, B));
+    P.o_gcpart = o; o = up(o + (size_t)P.B * P.plane * F);
+    std::vector<int> cnt((size_t)B.PR * B.S * B.NCP, 0);
+    auto key = [&](int cell) {
+        const int gx = cell / P.ny, gy = cell % P.ny;
+        return ((size_t)(gx / B.R) * B.S + (gx % B.R) / B.M) * B.NCP + gy;
+    };
+    for (int i = 0; i < P.ns; ++i)
+        if (++cnt[key(d->sources_host[i].cell)] > 2) return WT_ERR_UNSUPPORTED;
+    std::fill(cnt.begin(), cnt.end(), 0);
+    for (int i = 0; i < P.np; ++i)
+        if (++cnt[key(d->probes_host[i].cell)] > 2) return WT_ERR_UNSUPPORTED;
+    P.total = o;
+    return WT_OK;
+}
 
 int make_plan(const wt_seq_desc* d, SeqPlan* p, bool nl = false) {
     if (!d || d->batch <= 0 || d->nx <= 0 || d->ny <= 0 || d->steps <= 0) return WT_ERR_INVALID;
@@ -124,6 +168,7 @@ int make_plan(const wt_seq_desc* d, SeqPlan* p, bool nl = false) {
         return WT_ERR_INVALID;
     if (d->form != WT_FORM_PLAIN && d->form != WT_FORM_FUSED) return WT_ERR_INVALID;
     if (d->coef_batched != 0 && d->coef_batched != 1) return WT_ERR_INVALID;
+    if (d->sm_count < 0) return WT_ERR_INVALID;
     if (d->coef_batched && d->form != WT_FORM_FUSED) return WT_ERR_UNSUPPORTED;
     const long long cells = (long long)d->nx * d->ny;
     if (cells > (1LL << 30)) return WT_ERR_INVALID;
@@ -168,6 +213,13 @@ int make_plan(const wt_seq_desc* d, SeqPlan* p, bool nl = false) {
     } else {
         if (d->segment < -2) return WT_ERR_INVALID;
         int st = wt_fused_plan(P.nx, P.ny, P.T, P.np, d->cluster, d->segment, &P.L);
+        if (st == WT_ERR_UNSUPPORTED && !nl && d->cluster == 0 && !d->output_fields &&
+            (d->segment == 0 || d->segment == -1)) {
+            // too large for one cluster: bands of rows, one CTA per band
+            const int sms = band_sms(d);
+            if (sms > 0 && wt_band_plan(P.B, P.nx, P.ny, P.np, sms, &P.BL) == WT_OK)
+                return plan_band(d, P, o);
+        }
         if (st) return st;
         const size_t tape_bytes = (size_t)(nl ? 2 : 1) * P.T * P.B * P.L.C * P.L.threads * P.L.M * F;
         if (nl) {
@@ -335,6 +387,7 @@ wt::FusedParams fused_params(const wt_scalars* s, const SeqPlan& P, const float*
     F.nbuf = P.L.nbuf;
     F.gc_part = at<float>(ws, P.o_gcpart);
     F.err = at<int>(ws, P.o_err);
+    F.halo = P.band ? at<unsigned long long>(ws, P.o_halo) : nullptr;
     return F;
 }
 
@@ -402,7 +455,7 @@ extern "C" int wt_seq_fwd(const wt_scalars* s, const wt_seq_desc* d, const float
         F.out = out;
         F.fields = d->output_fields ? fields : nullptr;
         F.psum = P.np > 0 ? probe_sum : nullptr;   // summed in the probe flushes
-        return wt_launch_fused(true, F, P.L, cs);
+        return P.band ? wt_launch_band(true, F, P.BL, cs) : wt_launch_fused(true, F, P.L, cs);
     }
     if (probe_sum && P.np > 0)
         return wt_launch_probe_sum(P.B, P.T, P.np, out, probe_sum, cs);
@@ -469,7 +522,8 @@ extern "C" int wt_seq_bwd(const wt_scalars* s, const wt_seq_desc* d, const float
     F.grad_out = grad_out;
     F.grad_x = grad_x;
     if (P.coef_batched) F.gc_part = grad_c;   // per-instance dL/dc is the result
-    if ((st = wt_launch_fused(false, F, P.L, cs))) return st;
+    st = P.band ? wt_launch_band(false, F, P.BL, cs) : wt_launch_fused(false, F, P.L, cs);
+    if (st) return st;
     if (P.coef_batched) return WT_OK;
     return wt_launch_seq_adj_reduce(P.B, plane, F.gc_part, grad_c, 1, cs);
 }

@@ -95,6 +95,10 @@ struct FusedParams {
     float b0, uth, cnl;     // satdamp_b0, satdamp_uth, c_nl (float32 values)
     float* grho_part;       // [batch][nx][ny] per-instance direct dL/drho
     int* err;
+    // band form (grids too large for one cluster): C is the number of bands
+    // per instance; the bands' boundary rows travel through global memory
+    unsigned long long* halo;   // [batch][band][from above | from below][2][NCP] tagged words
+    int* abort_g;               // launch-wide abort word (a wait gave up)
 };
 
 // Up to INT_SCATTER_CAP int writes base[idx[i]] = val[i], passed by value as
@@ -126,6 +130,22 @@ struct WtFusedLaunch {
     size_t smem_bwd_base;   // adjoint shared memory before the tape ring
     int nbuf_nl;            // ring slices of the nonlinear adjoint (two-part slices)
 };
+
+// Launch shape of the band kernels (see seq_band.cu).
+struct WtBandLaunch {
+    int PR;                 // bands per instance (CTAs per instance)
+    int M, S, R;            // cells per thread, strips per band, rows per band (S * M)
+    int NCP;                // threads per strip row (ny rounded up to 32)
+    int LD;                 // tile column stride (floats)
+    int threads;            // S * NCP
+    int PB;                 // probe chunk length
+    size_t smem_fwd, smem_bwd;
+};
+
+int wt_band_plan(int batch, int nx, int ny, int n_prb, int n_sm, WtBandLaunch* L);
+// Bytes of the band form's halo area (words and the abort word) for a plan.
+size_t wt_band_halo_bytes(int batch, const WtBandLaunch& L);
+int wt_launch_band(bool fwd, const wt::FusedParams& P, const WtBandLaunch& L, cudaStream_t st);
 
 int wt_launch_step_fwd(const StepScalars& k, int batch, int nx, int ny, int coef_batched,
                        const float* b, const float* c, const float* y1, size_t bs1,

@@ -1,0 +1,627 @@
+// Band-decomposed persistent sequence kernels: the fused form for grids too
+// large for one thread-block cluster (more than 256 columns, or more rows than
+// 16 CTAs hold).  Same arithmetic, in the same order, as the cluster kernels
+// (the time loop of wavetorch/rnn.py:50-70 and the adjoint of its T TimeStep
+// nodes, wavetorch/cell.py:26-44).
+//
+// Decomposition.  Instance i's nx x ny grid is cut into PR bands of R rows;
+// band p runs on CTA i*PR + p.  The launch is cooperative: every CTA of the
+// grid is resident at once (one per SM), which the waits below rely on.
+// Inside a band the layout is the cluster kernels': thread (col, strip) owns
+// the M cells (strip*M .. strip*M + M-1, col) and keeps their fields (forward)
+// or adjoint state (adjoint) in registers; its neighbours' columns come from a
+// double-buffered column-major tile in shared memory, one __syncthreads per
+// step.  The per-cell update coefficients are in shared memory, laid out
+// [coefficient][cell i][thread] (a warp reads 32 consecutive words).
+//
+// Exchange between bands.  A band's first and last rows travel through
+// global memory as 64-bit words {float bits, tag = exchange index + 1},
+// written with st.relaxed.gpu into the neighbouring band's halo array
+// [2 parities][NCP]; the one thread that needs a value polls its word with
+// ld.relaxed.gpu until the tag matches (an aligned 8-byte access is single-copy
+// atomic: the value is valid whenever the tag is).  Double buffering by parity
+// is enough: a band writes parity p for exchange k+2 only after it received
+// exchange k+1 from its neighbour, whose same thread sent that after reading
+// exchange k.  Each step computes the cells that need no halo value first, so
+// the halo's trip through L2 overlaps them.
+//
+// Waits are bounded (2 s, %globaltimer).  A wait that gives up records
+// WT_DEVERR_TIMEOUT and raises a launch-wide abort word, which every waiting
+// thread also polls; each CTA leaves its loop at the end of that step.
+//
+// Adjoint: tape mode only.  The forward stores Lap(h_{t-1}) of every cell and
+// step, [step][batch][band][cell i][thread]; the adjoint reads its step's
+// values once.  Its state per cell is lambda (the next step's adjoint field,
+// formed as soon as both of its terms are known), the pending grad_y2 term
+// and the running dL/dc: the sums are the cluster kernels', operand for
+// operand.
+#include <algorithm>
+#include <map>
+#include <mutex>
+
+#include "internal.cuh"
+
+namespace wt {
+namespace band {
+
+constexpr int OFF = 1;       // first own row in a tile column (row 0: the zero row above)
+constexpr int SRCMAX = 2;    // source entries one thread may own
+constexpr int PRBMAX = 2;    // probe entries one thread may own
+constexpr uint64_t WAIT_LIMIT_NS = 2000000000ull;
+constexpr int MAX_THREADS = 1024;
+
+WT_DEV void st_gpu_u64(unsigned long long* p, unsigned long long v) {
+    asm volatile("st.relaxed.gpu.global.b64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+WT_DEV unsigned long long ld_gpu_u64(const unsigned long long* p) {
+    unsigned long long v;
+    asm volatile("ld.relaxed.gpu.global.b64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return v;
+}
+WT_DEV int ld_gpu_s32(const int* p) {
+    int v;
+    asm volatile("ld.relaxed.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+WT_DEV void st_gpu_s32(int* p, int v) {
+    asm volatile("st.relaxed.gpu.global.b32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+// Thread geometry.  top / bot: the thread's strip is its band's first / last
+// and a band lies above / below it (its end cell then borders another CTA).
+struct Geo {
+    int inst, band, col, strip, gx0;
+    bool colv, top, bot;
+};
+
+WT_DEV Geo make_geo(const FusedParams& P, int M) {
+    Geo g;
+    g.inst = blockIdx.x / P.C;
+    g.band = blockIdx.x - g.inst * P.C;
+    g.col = threadIdx.x % P.NCP;
+    g.strip = threadIdx.x / P.NCP;
+    g.gx0 = g.band * P.R + g.strip * M;
+    g.colv = g.col < P.ny;
+    g.top = g.strip == 0 && g.band > 0;
+    g.bot = g.strip == P.R / M - 1 && g.band + 1 < P.C;
+    return g;
+}
+
+// Per-thread addresses: its column of tile slot 0 (slot 1 is `tile` floats
+// further), its coefficient words, and its column's word in its band's halo
+// array (parity 0, "from above"; a band's array is [from above | from
+// below][2][NCP], and the bands of an instance are consecutive).  Its words:
+//   received from above:  me + par*NCP          (when top)
+//   received from below:  me + (2 + par)*NCP    (when bot)
+//   sent to the band above (its "from below"):  me - 2*NCP + par*NCP
+//   sent to the band below (its "from above"):  me + 4*NCP + par*NCP
+struct Lane {
+    float* col0;
+    const float* coef;
+    unsigned long long* me;
+    int tile, NT;
+};
+
+WT_DEV Lane make_lane(const FusedParams& P, const Geo& g, float* tiles, const float* coef) {
+    Lane l;
+    l.col0 = tiles + (g.col + 1) * P.LD + OFF + (g.gx0 - g.band * P.R);
+    l.coef = coef + threadIdx.x;
+    l.tile = (P.ny + 2) * P.LD;
+    l.NT = blockDim.x;
+    l.me = P.halo + ((size_t)g.inst * P.C + g.band) * 4 * P.NCP + g.col;
+    return l;
+}
+
+// Bounded wait for exchange word w to carry `tag`; its value, or 0 with
+// gave_up set (and the launch's abort word raised if this wait timed out).
+// The CTA leaves its loop at the next __syncthreads_or of gave_up.
+WT_DEV float recv(const FusedParams& P, const unsigned long long* w, uint32_t tag, bool& gave_up) {
+    unsigned long long v = ld_gpu_u64(w);
+    if ((uint32_t)(v >> 32) == tag) return __uint_as_float((uint32_t)v);
+    const uint64_t t0 = global_ns();
+    for (uint32_t it = 1;; ++it) {
+        v = ld_gpu_u64(w);
+        if ((uint32_t)(v >> 32) == tag) return __uint_as_float((uint32_t)v);
+        if ((it & 255u) == 0) {
+            if (ld_gpu_s32(P.abort_g)) break;
+            if (global_ns() - t0 > WAIT_LIMIT_NS) {
+                atomicExch(P.err, WT_DEVERR_TIMEOUT);
+                st_gpu_s32(P.abort_g, 1);
+                break;
+            }
+        }
+    }
+    gave_up = true;
+    return 0.f;
+}
+
+WT_DEV void send(unsigned long long* w, uint32_t tag, float v) {
+    st_gpu_u64(w, ((unsigned long long)tag << 32) | __float_as_uint(v));
+}
+
+// 4-byte asynchronous copy global -> this thread's own shared word (the
+// adjoint's tape staging), and waiting for all of this thread's copies.
+WT_DEV void cp_async4(float* dst, const float* src) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(smem_addr(dst)), "l"(src)
+                 : "memory");
+}
+WT_DEV void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+WT_DEV void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
+
+// Per-thread sources (table order) and probes (descending reference order),
+// packed: source e = (input row << 5) | cell index i; probe e = (column << 6) |
+// (kind << 5) | i.
+struct Taps {
+    int ns, np;
+    int s0, s1, p0, p1;
+    WT_DEV int s(int e) const { return e == 0 ? s0 : s1; }
+    WT_DEV int p(int e) const { return e == 0 ? p0 : p1; }
+    WT_DEV int src_i(int e) const { return s(e) & 31; }
+    WT_DEV int src_row(int e) const { return s(e) >> 5; }
+    WT_DEV int prb_i(int e) const { return p(e) & 31; }
+    WT_DEV int prb_col(int e) const { return p(e) >> 6; }
+    WT_DEV bool prb_intensity(int e) const { return (p(e) & 32) != 0; }
+};
+
+template <int M>
+WT_DEV void build_taps(const FusedParams& P, const Geo& g, Taps& tp) {
+    int ns = 0, np = 0, s0 = 0, s1 = 0, p0 = 0, p1 = 0;
+    if (g.colv) {
+        for (int e = 0; e < P.n_src; ++e) {
+            const int cell = __ldg(P.src_cell + e);
+            const int cx = cell / P.ny, cy = cell - cx * P.ny, i = cx - g.gx0;
+            if (cy == g.col && i >= 0 && i < M) {
+                const int row = __ldg(P.src_row + e);
+                const int v = ((row < 0 ? g.inst : row) << 5) | i;
+                if (ns == 0) s0 = v; else if (ns == 1) s1 = v; else atomicExch(P.err, WT_DEVERR_BOUNDS);
+                ++ns;
+            }
+        }
+        for (int e = 0; e < P.n_prb; ++e) {
+            const int cell = __ldg(P.prb_cell + e);
+            const int cx = cell / P.ny, cy = cell - cx * P.ny, i = cx - g.gx0;
+            if (cy == g.col && i >= 0 && i < M) {
+                const int v = (__ldg(P.prb_col + e) << 6) | (__ldg(P.prb_kind + e) << 5) | i;
+                if (np == 0) p0 = v; else if (np == 1) p1 = v; else atomicExch(P.err, WT_DEVERR_BOUNDS);
+                ++np;
+            }
+        }
+    }
+    tp.ns = min(ns, SRCMAX);
+    tp.np = min(np, PRBMAX);
+    tp.s0 = s0; tp.s1 = s1; tp.p0 = p0; tp.p1 = p1;
+}
+
+WT_DEV void zero_smem(float* s, int n) {
+    for (int i = threadIdx.x; i < n; i += blockDim.x) s[i] = 0.f;
+}
+
+// ---- probes (forward) and adjoint seeds: the cluster kernels' scheme ------
+// Forward: shared ring buffers [2][n_prb][PB] of raw amplitudes; a probe's
+// owner stores one value per step, and every PB steps the CTA writes the
+// finished chunk of the probes it owns (plus their Kahan time sums).
+struct ProbeRing {
+    float* buf;
+    int* own;       // 0: not owned here; 1 amplitude; 2 intensity
+    float* ksum;    // [2][n_prb]: running sum and compensation
+};
+
+WT_DEV void flush_probes(const FusedParams& P, const Geo& g, const ProbeRing& pr, int b, int t0,
+                         int n) {
+    const int tot = P.n_prb * P.PB;
+    for (int idx = threadIdx.x; idx < tot; idx += blockDim.x) {
+        const int q = idx / P.PB, tt = idx - q * P.PB;
+        if (tt >= n || !pr.own[q]) continue;
+        const float v = pr.buf[(b * P.n_prb + q) * P.PB + tt];
+        const size_t oi = ((size_t)g.inst * P.steps + t0 + tt) * P.n_prb + q;
+        P.out[oi] = (pr.own[q] == 2) ? fmul(v, v) : v;
+        P.amp[oi] = v;
+    }
+    if (!P.psum) return;
+    for (int q = threadIdx.x; q < P.n_prb; q += blockDim.x) {
+        if (!pr.own[q]) continue;
+        float s = pr.ksum[q], comp = pr.ksum[P.n_prb + q];
+        const float* vb = pr.buf + (size_t)(b * P.n_prb + q) * P.PB;
+        for (int tt = 0; tt < n; ++tt) {
+            const float v = vb[tt];
+            const float y = fsub((pr.own[q] == 2) ? fmul(v, v) : v, comp);
+            const float tk = fadd(s, y);
+            comp = fsub(fsub(tk, s), y);
+            s = tk;
+        }
+        pr.ksum[q] = s;
+        pr.ksum[P.n_prb + q] = comp;
+    }
+}
+
+// Adjoint: seeds of chunk c (adjoint steps u = c*PB .. c*PB + PB-1, t =
+// T-1-u) of every probe column into ring buffer c & 1: intensity g * (2 y)
+// (autograd's PowBackward), amplitude g.
+WT_DEV void stage_seeds(const FusedParams& P, const Geo& g, float* seeds, int c) {
+    float* dst = seeds + (size_t)(c & 1) * P.n_prb * P.PB;
+    const int tot = P.n_prb * P.PB;
+    for (int idx = threadIdx.x; idx < tot; idx += blockDim.x) {
+        const int q = idx / P.PB, k = idx - q * P.PB;
+        const int t = P.steps - 1 - (c * P.PB + k);
+        float sd = 0.f;
+        if (t >= 0) {
+            const size_t oi = ((size_t)g.inst * P.steps + t) * P.n_prb + q;
+            const float gv = P.grad_w ? __ldg(P.grad_w + (size_t)g.inst * P.n_prb + q)
+                                      : __ldg(P.grad_out + oi);
+            sd = __ldg(P.prb_kind_col + q) ? fmul(gv, fmul(2.0f, __ldg(P.amp + oi))) : gv;
+        }
+        dst[q * P.PB + k] = sd;
+    }
+}
+
+// ============================================================================
+// Forward.  Step t computes h_t from h_{t-1} (cur) and h_{t-2} (inout, which
+// it overwrites); tile slot RS = t & 1 holds h_{t-1}, slot RS ^ 1 receives
+// h_t.  Exchange t carries h_t's band rows with tag t + 1 in parity RS.
+template <int M, int ORDER, int RS>
+WT_DEV void fwd_step(const FusedParams& P, const Geo& g, const Lane& ln, const Taps& tp,
+                     const ProbeRing& pr, int t, int pb, int pc, float* tape, float (&xv)[SRCMAX],
+                     const float (&cur)[M], float (&inout)[M], bool& gave_up) {
+    const float* rcol = ln.col0 + RS * ln.tile;
+    float* wcol = ln.col0 + (RS ^ 1) * ln.tile;
+    const int LD = P.LD, NT = ln.NT;
+    const float w = P.k.lap_w, w4 = P.k.lap_w4;
+    auto update = [&](int i, float up, float dn) {
+        const float L = lap5<ORDER>(up, rcol[i - LD], cur[i], rcol[i + LD], dn, w, w4);
+        const float A = ln.coef[(0 * M + i) * NT], Bc = ln.coef[(1 * M + i) * NT],
+                    C2 = ln.coef[(2 * M + i) * NT];
+        inout[i] = leapfrog(A, Bc, C2, P.k.two_over, cur[i], inout[i], L);
+        __stcs(tape + (size_t)i * NT, L);
+    };
+    // cells whose neighbours are all in this CTA, while the halo travels
+#pragma unroll
+    for (int i = 1; i < M - 1; ++i) update(i, cur[i - 1], cur[i + 1]);
+    float up = rcol[-1], dn = rcol[M];
+    if (t > 0) {
+        if (g.top) up = recv(P, ln.me + (RS ^ 1) * P.NCP, (uint32_t)t, gave_up);
+        if (g.bot) dn = recv(P, ln.me + (2 + (RS ^ 1)) * P.NCP, (uint32_t)t, gave_up);
+    }
+    update(0, up, cur[1]);
+    update(M - 1, cur[M - 2], dn);
+#pragma unroll
+    for (int i = 0; i < M; ++i) wcol[i] = inout[i];
+    if (tp.ns) {   // sources in table order, through the column (no register indexing)
+#pragma unroll
+        for (int e = 0; e < SRCMAX; ++e)
+            if (e < tp.ns) wcol[tp.src_i(e)] = fadd(wcol[tp.src_i(e)], xv[e]);
+#pragma unroll
+        for (int i = 0; i < M; ++i) inout[i] = wcol[i];
+        if (t + 1 < P.steps) {
+#pragma unroll
+            for (int e = 0; e < SRCMAX; ++e)
+                if (e < tp.ns) xv[e] = __ldg(P.x + (size_t)tp.src_row(e) * P.steps + t + 1);
+        }
+    }
+    if (t + 1 < P.steps) {
+        if (g.top) send(ln.me + (RS - 2) * P.NCP, (uint32_t)(t + 1), inout[0]);
+        if (g.bot) send(ln.me + (4 + RS) * P.NCP, (uint32_t)(t + 1), inout[M - 1]);
+    }
+    if (tp.np) {
+        float* row = pr.buf + (size_t)pb * P.n_prb * P.PB + pc;
+#pragma unroll
+        for (int e = 0; e < PRBMAX; ++e)
+            if (e < tp.np) row[tp.prb_col(e) * P.PB] = wcol[tp.prb_i(e)];
+    }
+}
+
+template <int M, int ORDER>
+__global__ void __launch_bounds__(MAX_THREADS, 1) seq_fwd_band_kernel(FusedParams P) {
+    extern __shared__ __align__(16) float smem[];
+    const int NT = blockDim.x;
+    const Geo g = make_geo(P, M);
+    const int tile = (P.ny + 2) * P.LD;
+    float* coef = smem + 2 * tile;
+    ProbeRing pr;
+    pr.buf = coef + 3 * M * NT;
+    pr.own = reinterpret_cast<int*>(pr.buf + 2 * P.n_prb * P.PB);
+    pr.ksum = reinterpret_cast<float*>(pr.own + P.n_prb);
+    zero_smem(smem, 2 * tile);
+    for (int q = threadIdx.x; q < P.n_prb; q += NT) {
+        pr.own[q] = 0;
+        pr.ksum[q] = pr.ksum[P.n_prb + q] = 0.f;
+    }
+#pragma unroll
+    for (int i = 0; i < M; ++i) {
+        float A = 0.f, Bc = 0.f, C2 = 0.f;
+        const int gx = g.gx0 + i;
+        if (g.colv && gx < P.nx) {
+            const size_t cell = P.coef_stride * g.inst + (size_t)gx * P.ny + g.col;
+            const FwdCoef f = fwd_coef(__ldg(P.b + cell), __ldg(P.c + cell), P.k);
+            A = f.A; Bc = f.Bc; C2 = f.c2;
+        }
+        coef[(0 * M + i) * NT + threadIdx.x] = A;
+        coef[(1 * M + i) * NT + threadIdx.x] = Bc;
+        coef[(2 * M + i) * NT + threadIdx.x] = C2;
+    }
+    const Lane ln = make_lane(P, g, smem, coef);
+    Taps tp;
+    build_taps<M>(P, g, tp);
+    float xv[SRCMAX];
+#pragma unroll
+    for (int e = 0; e < SRCMAX; ++e)
+        xv[e] = e < tp.ns ? __ldg(P.x + (size_t)tp.src_row(e) * P.steps) : 0.f;
+    __syncthreads();      // ownership flags cleared before the owners mark theirs
+    if (g.colv) {
+#pragma unroll
+        for (int e = 0; e < PRBMAX; ++e)
+            if (e < tp.np) pr.own[tp.prb_col(e)] = tp.prb_intensity(e) ? 2 : 1;
+    }
+    __syncthreads();      // tiles, coefficients and flags in place
+
+    float ya[M], yb[M];   // ya: h_{t-1} at even t, yb at odd t
+#pragma unroll
+    for (int i = 0; i < M; ++i) ya[i] = yb[i] = 0.f;
+    float* tape = P.lap + ((size_t)g.inst * P.C + g.band) * NT * M + threadIdx.x;
+    const size_t tape_step = (size_t)P.batch * P.C * NT * M;
+    int pb = 0, pc = 0, chunk0 = 0;
+    bool gave_up = false, aborted = false;
+    for (int t = 0; t < P.steps; ++t) {
+        if (g.colv) {
+            if (t & 1) fwd_step<M, ORDER, 1>(P, g, ln, tp, pr, t, pb, pc, tape, xv, yb, ya, gave_up);
+            else       fwd_step<M, ORDER, 0>(P, g, ln, tp, pr, t, pb, pc, tape, xv, ya, yb, gave_up);
+        }
+        tape += tape_step;
+        if ((aborted = __syncthreads_or(gave_up))) break;
+        if (++pc == P.PB) {
+            flush_probes(P, g, pr, pb, chunk0, P.PB);
+            pc = 0;
+            pb ^= 1;
+            chunk0 = t + 1;
+        }
+    }
+    if (aborted) return;
+    if (pc > 0) flush_probes(P, g, pr, pb, chunk0, pc);
+    __syncthreads();
+    if (P.psum)
+        for (int q = threadIdx.x; q < P.n_prb; q += NT)
+            if (pr.own[q]) P.psum[(size_t)g.inst * P.n_prb + q] = pr.ksum[q];
+}
+
+// ============================================================================
+// Adjoint.  Adjoint step u handles t = T-1-u.  On entry lam holds lambda_t
+// without its probe seeds (grad_y1 from step t+1 plus grad_y2 from step t+2,
+// in that sum's order), pend the grad_y2 term of step t+1.  Exchange u
+// carries Kg * lambda_t (autograd's c^2 g / (1 + b dt)) in parity u & 1.
+// Each thread's M tape values of step t arrive by cp.async in its own words
+// of a shared staging area [M][threads], issued as soon as it has used the
+// previous step's (a whole step ahead of use).
+template <int M, int ORDER>
+__global__ void __launch_bounds__(MAX_THREADS, 1) seq_bwd_band_kernel(FusedParams P) {
+    extern __shared__ __align__(16) float smem[];
+    const int NT = blockDim.x;
+    const Geo g = make_geo(P, M);
+    const int tile = (P.ny + 2) * P.LD;
+    float* coef = smem + 2 * tile;
+    float* lys = coef + 4 * M * NT + threadIdx.x;    // this thread's staged tape words
+    float* seeds = coef + 5 * M * NT;
+    zero_smem(smem, 2 * tile);
+#pragma unroll
+    for (int i = 0; i < M; ++i) {
+        BwdCoef k{0.f, 0.f, 0.f, 0.f};
+        const int gx = g.gx0 + i;
+        if (g.colv && gx < P.nx) {
+            const size_t cell = P.coef_stride * g.inst + (size_t)gx * P.ny + g.col;
+            k = bwd_coef(__ldg(P.b + cell), __ldg(P.c + cell), P.k);
+        }
+        coef[(0 * M + i) * NT + threadIdx.x] = k.X1;
+        coef[(1 * M + i) * NT + threadIdx.x] = k.Kc;
+        coef[(2 * M + i) * NT + threadIdx.x] = k.Kg;
+        coef[(3 * M + i) * NT + threadIdx.x] = k.Ky2;
+    }
+    const Lane ln = make_lane(P, g, smem, coef);
+    Taps tp;
+    build_taps<M>(P, g, tp);
+    stage_seeds(P, g, seeds, 0);
+    __syncthreads();
+
+    float lam[M], pend[M], acc[M];
+#pragma unroll
+    for (int i = 0; i < M; ++i) lam[i] = pend[i] = acc[i] = 0.f;
+    const size_t tape_step = (size_t)P.batch * P.C * NT * M;
+    const float* tape = P.lap + (size_t)(P.steps - 1) * tape_step +
+                        ((size_t)g.inst * P.C + g.band) * NT * M + threadIdx.x;
+    if (g.colv) {
+#pragma unroll
+        for (int i = 0; i < M; ++i) cp_async4(lys + i * NT, tape + (size_t)i * NT);
+        cp_async_commit();
+    }
+    const int LD = P.LD;
+    const float w = P.k.lap_w, w4 = P.k.lap_w4, dt2 = P.k.dt2;
+    int pk = 0, pcn = 0;
+    bool gave_up = false, aborted = false;
+    for (int u = 0; u < P.steps; ++u) {
+        const int t = P.steps - 1 - u;
+        float* col = ln.col0 + (u & 1) * ln.tile;
+        float c2g[M];
+        if (pk == 0 && u + P.PB < P.steps)   // next chunk, a barrier ahead of use
+            stage_seeds(P, g, seeds, pcn + 1);
+        if (g.colv) {
+            if (tp.np || (P.grad_x && tp.ns)) {
+                // seeds at their cells and dL/dx at the source, through the
+                // thread's column of the slot it is about to publish into
+#pragma unroll
+                for (int i = 0; i < M; ++i) col[i] = lam[i];
+                const float* sr = seeds + (size_t)(pcn & 1) * P.n_prb * P.PB + pk;
+#pragma unroll
+                for (int e = 0; e < PRBMAX; ++e)
+                    if (e < tp.np) col[tp.prb_i(e)] = fadd(col[tp.prb_i(e)], sr[tp.prb_col(e) * P.PB]);
+                if (P.grad_x) {
+#pragma unroll
+                    for (int e = 0; e < SRCMAX; ++e)
+                        if (e < tp.ns && tp.src_row(e) == g.inst)
+                            P.grad_x[(size_t)g.inst * P.steps + t] = col[tp.src_i(e)];
+                }
+#pragma unroll
+                for (int i = 0; i < M; ++i) lam[i] = col[i];
+            }
+#pragma unroll
+            for (int i = 0; i < M; ++i) {
+                c2g[i] = fmul(ln.coef[(2 * M + i) * NT], lam[i]);
+                col[i] = c2g[i];
+            }
+            if (g.top) send(ln.me + ((u & 1) - 2) * P.NCP, (uint32_t)(u + 1), c2g[0]);
+            if (g.bot) send(ln.me + (4 + (u & 1)) * P.NCP, (uint32_t)(u + 1), c2g[M - 1]);
+        }
+        if ((aborted = __syncthreads_or(gave_up))) break;
+        if (g.colv) {
+            auto update = [&](int i, float up, float dn) {
+                const float lg = lap5<ORDER>(up, col[i - LD], c2g[i], col[i + LD], dn, w, w4);
+                const float X1 = ln.coef[(0 * M + i) * NT], Kc = ln.coef[(1 * M + i) * NT],
+                            Ky2 = ln.coef[(3 * M + i) * NT];
+                acc[i] = fadd(acc[i], fmul(fmul(X1, fmul(Kc, lys[i * NT])), lam[i]));
+                const float gy1 = fadd(fmul(dt2, lg), fmul(fmul(2.0f, lam[i]), X1));
+                const float g2 = fmul(Ky2, lam[i]);
+                lam[i] = fadd(pend[i], gy1);
+                pend[i] = g2;
+            };
+            cp_async_wait_all();
+#pragma unroll
+            for (int i = 1; i < M - 1; ++i) update(i, c2g[i - 1], c2g[i + 1]);
+            float up = col[-1], dn = col[M];
+            if (g.top) up = recv(P, ln.me + (u & 1) * P.NCP, (uint32_t)(u + 1), gave_up);
+            if (g.bot) dn = recv(P, ln.me + (2 + (u & 1)) * P.NCP, (uint32_t)(u + 1), gave_up);
+            update(0, up, c2g[1]);
+            update(M - 1, c2g[M - 2], dn);
+        }
+        tape -= tape_step;
+        if (g.colv && u + 1 < P.steps) {   // the staged words were all read above
+#pragma unroll
+            for (int i = 0; i < M; ++i) cp_async4(lys + i * NT, tape + (size_t)i * NT);
+            cp_async_commit();
+        }
+        if (++pk == P.PB) { pk = 0; ++pcn; }
+    }
+    cp_async_wait_all();   // no copy outlives the kernel's shared memory
+    if (!aborted) aborted = __syncthreads_or(gave_up);
+    if (aborted || !g.colv) return;
+    float* o = P.gc_part + (size_t)g.inst * P.nx * P.ny;
+#pragma unroll
+    for (int i = 0; i < M; ++i) {
+        const int gx = g.gx0 + i;
+        if (gx < P.nx) o[(size_t)gx * P.ny + g.col] = acc[i];
+    }
+}
+
+}  // namespace band
+}  // namespace wt
+
+// ---------------------------------------------------------------------------
+// Host side
+
+// Tile column stride: a zero row, R own rows, a zero row; odd, so that a
+// warp's accesses to one row of 32 consecutive columns hit 32 banks.
+static int band_ld(int R) {
+    int ld = R + 2;
+    return ld | 1;
+}
+
+// Bands of R = S * M rows with the fewest cells per CTA (the per-step work of
+// one SM), such that batch * bands CTAs fit on n_sm SMs (one each) and S * NCP
+// threads in one CTA; ties: the larger M (fewer threads, fewer barrier
+// arrivals per cell).
+int wt_band_plan(int batch, int nx, int ny, int n_prb, int n_sm, WtBandLaunch* L) {
+    if (batch <= 0 || nx <= 0 || ny <= 0 || n_sm <= 0 || !L) return WT_ERR_INVALID;
+    const int NCP = ((ny + 31) / 32) * 32;
+    if (NCP > wt::band::MAX_THREADS) return WT_ERR_UNSUPPORTED;
+    const size_t SMEM_MAX = 227 * 1024 - 64;
+    const int PB = n_prb > 0 ? std::max(1, std::min(32, 2048 / n_prb)) : 32;
+    auto r16 = [](size_t v) { return (v + 15) / 16 * 16; };
+    const size_t aux_fwd = r16((size_t)(2 * n_prb * PB + 3 * n_prb) * 4);
+    const size_t aux_bwd = r16((size_t)(2 * n_prb * PB) * 4);
+    long best_cost = -1;
+    for (int S = 1; S * NCP <= wt::band::MAX_THREADS; ++S) {
+        for (int M = 8; M >= 2; --M) {
+            const int R = S * M;
+            const long PR = (nx + R - 1) / R;
+            if ((long)batch * PR > n_sm) continue;
+            const int threads = S * NCP;
+            const int LD = band_ld(R);
+            const size_t tiles = 2 * (size_t)(ny + 2) * LD * sizeof(float);
+            const size_t fwd = tiles + (size_t)3 * M * threads * sizeof(float) + aux_fwd;
+            const size_t bwd = tiles + (size_t)5 * M * threads * sizeof(float) + aux_bwd;
+            if (fwd > SMEM_MAX || bwd > SMEM_MAX) continue;
+            const long cost = (long)R * NCP;
+            if (best_cost >= 0 && cost >= best_cost) continue;
+            best_cost = cost;
+            L->PR = (int)PR; L->M = M; L->S = S; L->R = R; L->NCP = NCP; L->LD = LD;
+            L->threads = threads; L->PB = PB; L->smem_fwd = fwd; L->smem_bwd = bwd;
+        }
+    }
+    return best_cost < 0 ? WT_ERR_UNSUPPORTED : WT_OK;
+}
+
+size_t wt_band_halo_bytes(int batch, const WtBandLaunch& L) {
+    // the words, then the abort word (its own 256-byte line)
+    return (size_t)batch * L.PR * 4 * L.NCP * sizeof(unsigned long long) + 256;
+}
+
+static int band_attributes(void (*kern)(wt::FusedParams), size_t smem) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return wt_cuda_status(e);
+    static std::mutex mu;
+    static std::map<std::pair<int, const void*>, size_t> done;
+    std::lock_guard<std::mutex> lock(mu);
+    size_t& v = done[{dev, reinterpret_cast<const void*>(kern)}];
+    if (v < smem) {
+        e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return wt_cuda_status(e);
+        v = smem;
+    }
+    return WT_OK;
+}
+
+template <int M, int ORDER>
+static int launch_band_m(bool fwd, const wt::FusedParams& P, const WtBandLaunch& L,
+                         cudaStream_t st) {
+    void (*kern)(wt::FusedParams) = fwd ? wt::band::seq_fwd_band_kernel<M, ORDER>
+                                        : wt::band::seq_bwd_band_kernel<M, ORDER>;
+    const size_t smem = fwd ? L.smem_fwd : L.smem_bwd;
+    int rc = band_attributes(kern, smem);
+    if (rc) return rc;
+    // fresh exchange words (tag 0: nothing sent yet) and abort word
+    cudaError_t e = cudaMemsetAsync(P.halo, 0, wt_band_halo_bytes(P.batch, L), st);
+    if (e != cudaSuccess) return wt_cuda_status(e);
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(P.batch * L.PR, 1, 1);
+    cfg.blockDim = dim3(L.threads, 1, 1);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;   // all bands resident at once
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    e = cudaLaunchKernelEx(&cfg, kern, P);
+    wt_count_launches(1);
+    return wt_cuda_status(e);
+}
+
+template <int ORDER>
+static int launch_band_order(bool fwd, const wt::FusedParams& P, const WtBandLaunch& L,
+                             cudaStream_t st) {
+    switch (L.M) {
+        case 2: return launch_band_m<2, ORDER>(fwd, P, L, st);
+        case 3: return launch_band_m<3, ORDER>(fwd, P, L, st);
+        case 4: return launch_band_m<4, ORDER>(fwd, P, L, st);
+        case 5: return launch_band_m<5, ORDER>(fwd, P, L, st);
+        case 6: return launch_band_m<6, ORDER>(fwd, P, L, st);
+        case 7: return launch_band_m<7, ORDER>(fwd, P, L, st);
+        case 8: return launch_band_m<8, ORDER>(fwd, P, L, st);
+        default: return WT_ERR_UNSUPPORTED;
+    }
+}
+
+int wt_launch_band(bool fwd, const wt::FusedParams& P0, const WtBandLaunch& L, cudaStream_t st) {
+    if (!P0.lap || !P0.halo) return WT_ERR_INVALID;
+    wt::FusedParams P = P0;
+    P.C = L.PR; P.R = L.R; P.NCP = L.NCP; P.LD = L.LD; P.PB = L.PB;
+    P.abort_g = reinterpret_cast<int*>(P.halo + (size_t)P.batch * L.PR * 4 * L.NCP);
+    return P.k.lap_order == WT_LAP_SEQ ? launch_band_order<WT_LAP_SEQ>(fwd, P, L, st)
+                                       : launch_band_order<WT_LAP_PAIRED>(fwd, P, L, st);
+}

@@ -130,6 +130,7 @@ class SeqSpec:
     cluster: int = 0
     output_fields: bool = False
     coef_batched: bool = False      # one geometry (b, c) per instance
+    sm_count: int = 0               # SMs the band layout may use (0: the device's)
 
     def desc(self):
         ns, np_ = len(self.sources), len(self.probes)
@@ -138,7 +139,8 @@ class SeqSpec:
         d = _lib.SeqDesc(self.batch, self.nx, self.ny, self.steps, ns,
                          C.cast(src, C.POINTER(_lib.SourceEntry)), np_,
                          C.cast(prb, C.POINTER(_lib.ProbeEntry)), self.form, self.segment,
-                         self.cluster, int(self.output_fields), int(self.coef_batched))
+                         self.cluster, int(self.output_fields), int(self.coef_batched),
+                         int(self.sm_count))
         return d, (src, prb)   # keep the arrays alive with the descriptor
 
 
@@ -150,10 +152,10 @@ def seq_workspace_bytes(spec: SeqSpec) -> int:
 
 
 def fused_supported(spec: SeqSpec) -> bool:
-    """Whether the fused form can plan this sequence: the whole instance must
-    fit on one thread-block cluster (square grids up to 256x256 cells, with
-    16-CTA clusters above 160x160).  Any
-    other error is left for the real call to report."""
+    """Whether the fused form can plan this sequence: on one thread-block
+    cluster per instance (grids up to 256x256 cells), or in bands of rows, one
+    CTA per band and SM (up to 1024 columns, batch x bands within the SM
+    count).  Any other error is left for the real call to report."""
     d, keep = dataclasses.replace(spec, form=_lib.WT_FORM_FUSED).desc()
     n = C.c_size_t(0)
     return _lib.load().wt_seq_workspace_bytes(C.byref(d), C.byref(n)) != _lib.WT_ERR_UNSUPPORTED
