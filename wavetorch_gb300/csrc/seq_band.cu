@@ -38,6 +38,7 @@
 #include <algorithm>
 #include <map>
 #include <mutex>
+#include <type_traits>
 
 #include "internal.cuh"
 
@@ -100,15 +101,17 @@ struct Lane {
     const float* coef;
     unsigned long long* me;
     int tile, NT;
+    float a0;       // the forward's A where b = 0: (dt^-2 + 0 * dt^-1)^-1
 };
 
 WT_DEV Lane make_lane(const FusedParams& P, const Geo& g, float* tiles, const float* coef) {
     Lane l;
     l.col0 = tiles + (g.col + 1) * P.LD + OFF + (g.gx0 - g.band * P.R);
-    l.coef = coef + threadIdx.x;
+    l.coef = coef;   // the thread's own words (the kernel passes its base)
     l.tile = (P.ny + 2) * P.LD;
     l.NT = blockDim.x;
     l.me = P.halo + ((size_t)g.inst * P.C + g.band) * 4 * P.NCP + g.col;
+    l.a0 = fwd_coef(0.f, 0.f, P.k).A;
     return l;
 }
 
@@ -120,6 +123,7 @@ WT_DEV float recv(const FusedParams& P, const unsigned long long* w, uint32_t ta
     if ((uint32_t)(v >> 32) == tag) return __uint_as_float((uint32_t)v);
     const uint64_t t0 = global_ns();
     for (uint32_t it = 1;; ++it) {
+        __nanosleep(32);   // leave the issue slots to the warps still computing
         v = ld_gpu_u64(w);
         if ((uint32_t)(v >> 32) == tag) return __uint_as_float((uint32_t)v);
         if ((it & 255u) == 0) {
@@ -149,13 +153,18 @@ WT_DEV void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memor
 WT_DEV void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
 
 // Per-thread sources (table order) and probes (descending reference order),
-// packed: source e = (input row << 5) | cell index i; probe e = (column << 6) |
-// (kind << 5) | i.
+// two of each at most, packed into three words so they stay in registers:
+//   source e (16 bits):  (input row << 5) | cell index i
+//   probe e (16 bits):   (column << 6) | (kind << 5) | i
+//   meta:                ns | np << 2 | src_edge << 4
+// (input rows < 2048 and columns < 1024, which the host checks).
 struct Taps {
-    int ns, np;
-    int s0, s1, p0, p1;
-    WT_DEV int s(int e) const { return e == 0 ? s0 : s1; }
-    WT_DEV int p(int e) const { return e == 0 ? p0 : p1; }
+    int src, prb, meta;
+    WT_DEV int ns() const { return meta & 3; }
+    WT_DEV int np() const { return (meta >> 2) & 3; }
+    WT_DEV bool src_edge() const { return (meta >> 4) & 1; }   // a source on a sent cell
+    WT_DEV int s(int e) const { return (src >> (16 * e)) & 0xffff; }
+    WT_DEV int p(int e) const { return (prb >> (16 * e)) & 0xffff; }
     WT_DEV int src_i(int e) const { return s(e) & 31; }
     WT_DEV int src_row(int e) const { return s(e) >> 5; }
     WT_DEV int prb_i(int e) const { return p(e) & 31; }
@@ -165,32 +174,45 @@ struct Taps {
 
 template <int M>
 WT_DEV void build_taps(const FusedParams& P, const Geo& g, Taps& tp) {
-    int ns = 0, np = 0, s0 = 0, s1 = 0, p0 = 0, p1 = 0;
+    int ns = 0, np = 0, src = 0, prb = 0, edge = 0;
+    // the thread's cells lie in [lo, hi) of the row-major cell index
+    const int lo = g.gx0 * P.ny + g.col, hi = (g.gx0 + M - 1) * P.ny + g.col + 1;
     if (g.colv) {
         for (int e = 0; e < P.n_src; ++e) {
             const int cell = __ldg(P.src_cell + e);
+            if (cell < lo || cell >= hi) continue;
             const int cx = cell / P.ny, cy = cell - cx * P.ny, i = cx - g.gx0;
             if (cy == g.col && i >= 0 && i < M) {
                 const int row = __ldg(P.src_row + e);
                 const int v = ((row < 0 ? g.inst : row) << 5) | i;
-                if (ns == 0) s0 = v; else if (ns == 1) s1 = v; else atomicExch(P.err, WT_DEVERR_BOUNDS);
+                if (ns < SRCMAX) src |= v << (16 * ns);
+                else atomicExch(P.err, WT_DEVERR_BOUNDS);
+                if ((i == 0 && g.top) || (i == M - 1 && g.bot)) edge = 1;
                 ++ns;
             }
         }
         for (int e = 0; e < P.n_prb; ++e) {
             const int cell = __ldg(P.prb_cell + e);
+            if (cell < lo || cell >= hi) continue;
             const int cx = cell / P.ny, cy = cell - cx * P.ny, i = cx - g.gx0;
             if (cy == g.col && i >= 0 && i < M) {
                 const int v = (__ldg(P.prb_col + e) << 6) | (__ldg(P.prb_kind + e) << 5) | i;
-                if (np == 0) p0 = v; else if (np == 1) p1 = v; else atomicExch(P.err, WT_DEVERR_BOUNDS);
+                if (np < PRBMAX) prb |= v << (16 * np);
+                else atomicExch(P.err, WT_DEVERR_BOUNDS);
                 ++np;
             }
         }
     }
-    tp.ns = min(ns, SRCMAX);
-    tp.np = min(np, PRBMAX);
-    tp.s0 = s0; tp.s1 = s1; tp.p0 = p0; tp.p1 = p1;
+    tp.src = src;
+    tp.prb = prb;
+    tp.meta = min(ns, SRCMAX) | (min(np, PRBMAX) << 2) | (edge << 4);
 }
+
+// Per-thread coefficient words: thread tid's K words per cell at
+// coef + tid * stride + k * M + i, the stride K * M rounded up to odd (a warp's
+// access to one word hits 32 banks; offsets are compile-time constants).
+template <int M, int K>
+__host__ __device__ constexpr int coef_stride() { return (K * M) | 1; }
 
 WT_DEV void zero_smem(float* s, int n) {
     for (int i = threadIdx.x; i < n; i += blockDim.x) s[i] = 0.f;
@@ -258,7 +280,10 @@ WT_DEV void stage_seeds(const FusedParams& P, const Geo& g, float* seeds, int c)
 // Forward.  Step t computes h_t from h_{t-1} (cur) and h_{t-2} (inout, which
 // it overwrites); tile slot RS = t & 1 holds h_{t-1}, slot RS ^ 1 receives
 // h_t.  Exchange t carries h_t's band rows with tag t + 1 in parity RS.
-template <int M, int ORDER, int RS>
+// INNER: every cell of the thread has b = 0, where the reference's
+// coefficients are A = (dt^-2)^-1 and Bc = dt^-2 for every cell (only c^2
+// is read from shared memory).
+template <int M, int ORDER, int RS, bool INNER>
 WT_DEV void fwd_step(const FusedParams& P, const Geo& g, const Lane& ln, const Taps& tp,
                      const ProbeRing& pr, int t, int pb, int pc, float* tape, float (&xv)[SRCMAX],
                      const float (&cur)[M], float (&inout)[M], bool& gave_up) {
@@ -268,14 +293,14 @@ WT_DEV void fwd_step(const FusedParams& P, const Geo& g, const Lane& ln, const T
     const float w = P.k.lap_w, w4 = P.k.lap_w4;
     auto update = [&](int i, float up, float dn) {
         const float L = lap5<ORDER>(up, rcol[i - LD], cur[i], rcol[i + LD], dn, w, w4);
-        const float A = ln.coef[(0 * M + i) * NT], Bc = ln.coef[(1 * M + i) * NT],
-                    C2 = ln.coef[(2 * M + i) * NT];
-        inout[i] = leapfrog(A, Bc, C2, P.k.two_over, cur[i], inout[i], L);
+        const float A = INNER ? ln.a0 : ln.coef[i];
+        const float Bc = INNER ? P.k.inv_dt2 : ln.coef[M + i];
+        inout[i] = leapfrog(A, Bc, ln.coef[2 * M + i], P.k.two_over, cur[i], inout[i], L);
         __stcs(tape + (size_t)i * NT, L);
     };
-    // cells whose neighbours are all in this CTA, while the halo travels
-#pragma unroll
-    for (int i = 1; i < M - 1; ++i) update(i, cur[i - 1], cur[i + 1]);
+    // the end cells first: their halo values were sent early in the
+    // neighbours' previous step, and this step's go out while the interior
+    // cells are computed
     float up = rcol[-1], dn = rcol[M];
     if (t > 0) {
         if (g.top) up = recv(P, ln.me + (RS ^ 1) * P.NCP, (uint32_t)t, gave_up);
@@ -283,29 +308,36 @@ WT_DEV void fwd_step(const FusedParams& P, const Geo& g, const Lane& ln, const T
     }
     update(0, up, cur[1]);
     update(M - 1, cur[M - 2], dn);
-#pragma unroll
-    for (int i = 0; i < M; ++i) wcol[i] = inout[i];
-    if (tp.ns) {   // sources in table order, through the column (no register indexing)
-#pragma unroll
-        for (int e = 0; e < SRCMAX; ++e)
-            if (e < tp.ns) wcol[tp.src_i(e)] = fadd(wcol[tp.src_i(e)], xv[e]);
-#pragma unroll
-        for (int i = 0; i < M; ++i) inout[i] = wcol[i];
-        if (t + 1 < P.steps) {
-#pragma unroll
-            for (int e = 0; e < SRCMAX; ++e)
-                if (e < tp.ns) xv[e] = __ldg(P.x + (size_t)tp.src_row(e) * P.steps + t + 1);
-        }
-    }
-    if (t + 1 < P.steps) {
+    const bool more = t + 1 < P.steps;
+    if (more && !tp.src_edge()) {
         if (g.top) send(ln.me + (RS - 2) * P.NCP, (uint32_t)(t + 1), inout[0]);
         if (g.bot) send(ln.me + (4 + RS) * P.NCP, (uint32_t)(t + 1), inout[M - 1]);
     }
-    if (tp.np) {
+#pragma unroll
+    for (int i = 1; i < M - 1; ++i) update(i, cur[i - 1], cur[i + 1]);
+#pragma unroll
+    for (int i = 0; i < M; ++i) wcol[i] = inout[i];
+    if (tp.ns()) {   // sources in table order, through the column (no register indexing)
+#pragma unroll
+        for (int e = 0; e < SRCMAX; ++e)
+            if (e < tp.ns()) wcol[tp.src_i(e)] = fadd(wcol[tp.src_i(e)], xv[e]);
+#pragma unroll
+        for (int i = 0; i < M; ++i) inout[i] = wcol[i];
+        if (more) {
+#pragma unroll
+            for (int e = 0; e < SRCMAX; ++e)
+                if (e < tp.ns()) xv[e] = __ldg(P.x + (size_t)tp.src_row(e) * P.steps + t + 1);
+            if (tp.src_edge()) {
+                if (g.top) send(ln.me + (RS - 2) * P.NCP, (uint32_t)(t + 1), inout[0]);
+                if (g.bot) send(ln.me + (4 + RS) * P.NCP, (uint32_t)(t + 1), inout[M - 1]);
+            }
+        }
+    }
+    if (tp.np()) {
         float* row = pr.buf + (size_t)pb * P.n_prb * P.PB + pc;
 #pragma unroll
         for (int e = 0; e < PRBMAX; ++e)
-            if (e < tp.np) row[tp.prb_col(e) * P.PB] = wcol[tp.prb_i(e)];
+            if (e < tp.np()) row[tp.prb_col(e) * P.PB] = wcol[tp.prb_i(e)];
     }
 }
 
@@ -315,9 +347,10 @@ __global__ void __launch_bounds__(MAX_THREADS, 1) seq_fwd_band_kernel(FusedParam
     const int NT = blockDim.x;
     const Geo g = make_geo(P, M);
     const int tile = (P.ny + 2) * P.LD;
+    constexpr int CS = coef_stride<M, 3>();
     float* coef = smem + 2 * tile;
     ProbeRing pr;
-    pr.buf = coef + 3 * M * NT;
+    pr.buf = coef + CS * NT;
     pr.own = reinterpret_cast<int*>(pr.buf + 2 * P.n_prb * P.PB);
     pr.ksum = reinterpret_cast<float*>(pr.own + P.n_prb);
     zero_smem(smem, 2 * tile);
@@ -325,31 +358,37 @@ __global__ void __launch_bounds__(MAX_THREADS, 1) seq_fwd_band_kernel(FusedParam
         pr.own[q] = 0;
         pr.ksum[q] = pr.ksum[P.n_prb + q] = 0.f;
     }
+    bool inner = g.colv;   // every cell real and undamped
 #pragma unroll
     for (int i = 0; i < M; ++i) {
         float A = 0.f, Bc = 0.f, C2 = 0.f;
         const int gx = g.gx0 + i;
         if (g.colv && gx < P.nx) {
             const size_t cell = P.coef_stride * g.inst + (size_t)gx * P.ny + g.col;
-            const FwdCoef f = fwd_coef(__ldg(P.b + cell), __ldg(P.c + cell), P.k);
+            const float bv = __ldg(P.b + cell);
+            const FwdCoef f = fwd_coef(bv, __ldg(P.c + cell), P.k);
             A = f.A; Bc = f.Bc; C2 = f.c2;
+            inner = inner && bv == 0.f;
+        } else {
+            inner = false;
         }
-        coef[(0 * M + i) * NT + threadIdx.x] = A;
-        coef[(1 * M + i) * NT + threadIdx.x] = Bc;
-        coef[(2 * M + i) * NT + threadIdx.x] = C2;
+        coef[threadIdx.x * CS + i] = A;
+        coef[threadIdx.x * CS + M + i] = Bc;
+        coef[threadIdx.x * CS + 2 * M + i] = C2;
     }
-    const Lane ln = make_lane(P, g, smem, coef);
+    inner = __all_sync(0xffffffffu, inner);   // one path per warp
+    const Lane ln = make_lane(P, g, smem, coef + threadIdx.x * CS);
     Taps tp;
     build_taps<M>(P, g, tp);
     float xv[SRCMAX];
 #pragma unroll
     for (int e = 0; e < SRCMAX; ++e)
-        xv[e] = e < tp.ns ? __ldg(P.x + (size_t)tp.src_row(e) * P.steps) : 0.f;
+        xv[e] = e < tp.ns() ? __ldg(P.x + (size_t)tp.src_row(e) * P.steps) : 0.f;
     __syncthreads();      // ownership flags cleared before the owners mark theirs
     if (g.colv) {
 #pragma unroll
         for (int e = 0; e < PRBMAX; ++e)
-            if (e < tp.np) pr.own[tp.prb_col(e)] = tp.prb_intensity(e) ? 2 : 1;
+            if (e < tp.np()) pr.own[tp.prb_col(e)] = tp.prb_intensity(e) ? 2 : 1;
     }
     __syncthreads();      // tiles, coefficients and flags in place
 
@@ -362,8 +401,13 @@ __global__ void __launch_bounds__(MAX_THREADS, 1) seq_fwd_band_kernel(FusedParam
     bool gave_up = false, aborted = false;
     for (int t = 0; t < P.steps; ++t) {
         if (g.colv) {
-            if (t & 1) fwd_step<M, ORDER, 1>(P, g, ln, tp, pr, t, pb, pc, tape, xv, yb, ya, gave_up);
-            else       fwd_step<M, ORDER, 0>(P, g, ln, tp, pr, t, pb, pc, tape, xv, ya, yb, gave_up);
+            if (inner) {
+                if (t & 1) fwd_step<M, ORDER, 1, true>(P, g, ln, tp, pr, t, pb, pc, tape, xv, yb, ya, gave_up);
+                else       fwd_step<M, ORDER, 0, true>(P, g, ln, tp, pr, t, pb, pc, tape, xv, ya, yb, gave_up);
+            } else {
+                if (t & 1) fwd_step<M, ORDER, 1, false>(P, g, ln, tp, pr, t, pb, pc, tape, xv, yb, ya, gave_up);
+                else       fwd_step<M, ORDER, 0, false>(P, g, ln, tp, pr, t, pb, pc, tape, xv, ya, yb, gave_up);
+            }
         }
         tape += tape_step;
         if ((aborted = __syncthreads_or(gave_up))) break;
@@ -396,26 +440,37 @@ __global__ void __launch_bounds__(MAX_THREADS, 1) seq_bwd_band_kernel(FusedParam
     const int NT = blockDim.x;
     const Geo g = make_geo(P, M);
     const int tile = (P.ny + 2) * P.LD;
+    constexpr int CS = coef_stride<M, 4>();
     float* coef = smem + 2 * tile;
-    float* lys = coef + 4 * M * NT + threadIdx.x;    // this thread's staged tape words
-    float* seeds = coef + 5 * M * NT;
+    float* lys = coef + CS * NT + threadIdx.x;       // this thread's staged tape words
+    float* seeds = coef + (CS + M) * NT;
     zero_smem(smem, 2 * tile);
+    // every cell real and undamped: X1 = (0 dt + 1)^-1 = 1, Ky2 = (0 dt - 1) X1 = -1
+    bool inner = g.colv;
 #pragma unroll
     for (int i = 0; i < M; ++i) {
         BwdCoef k{0.f, 0.f, 0.f, 0.f};
         const int gx = g.gx0 + i;
         if (g.colv && gx < P.nx) {
             const size_t cell = P.coef_stride * g.inst + (size_t)gx * P.ny + g.col;
-            k = bwd_coef(__ldg(P.b + cell), __ldg(P.c + cell), P.k);
+            const float bv = __ldg(P.b + cell);
+            k = bwd_coef(bv, __ldg(P.c + cell), P.k);
+            inner = inner && bv == 0.f;
+        } else {
+            inner = false;
         }
-        coef[(0 * M + i) * NT + threadIdx.x] = k.X1;
-        coef[(1 * M + i) * NT + threadIdx.x] = k.Kc;
-        coef[(2 * M + i) * NT + threadIdx.x] = k.Kg;
-        coef[(3 * M + i) * NT + threadIdx.x] = k.Ky2;
+        coef[threadIdx.x * CS + i] = k.X1;
+        coef[threadIdx.x * CS + M + i] = k.Kc;
+        coef[threadIdx.x * CS + 2 * M + i] = k.Kg;
+        coef[threadIdx.x * CS + 3 * M + i] = k.Ky2;
     }
-    const Lane ln = make_lane(P, g, smem, coef);
+    inner = __all_sync(0xffffffffu, inner);   // one path per warp
+    const Lane ln = make_lane(P, g, smem, coef + threadIdx.x * CS);
     Taps tp;
     build_taps<M>(P, g, tp);
+    // threads without a probe cell send their end cells' exchange at the end
+    // of the previous step (no seed can change them in between)
+    const bool early = tp.np() == 0;
     stage_seeds(P, g, seeds, 0);
     __syncthreads();
 
@@ -437,11 +492,10 @@ __global__ void __launch_bounds__(MAX_THREADS, 1) seq_bwd_band_kernel(FusedParam
     for (int u = 0; u < P.steps; ++u) {
         const int t = P.steps - 1 - u;
         float* col = ln.col0 + (u & 1) * ln.tile;
-        float c2g[M];
         if (pk == 0 && u + P.PB < P.steps)   // next chunk, a barrier ahead of use
             stage_seeds(P, g, seeds, pcn + 1);
         if (g.colv) {
-            if (tp.np || (P.grad_x && tp.ns)) {
+            if (tp.np() || (P.grad_x && tp.ns())) {
                 // seeds at their cells and dL/dx at the source, through the
                 // thread's column of the slot it is about to publish into
 #pragma unroll
@@ -449,30 +503,32 @@ __global__ void __launch_bounds__(MAX_THREADS, 1) seq_bwd_band_kernel(FusedParam
                 const float* sr = seeds + (size_t)(pcn & 1) * P.n_prb * P.PB + pk;
 #pragma unroll
                 for (int e = 0; e < PRBMAX; ++e)
-                    if (e < tp.np) col[tp.prb_i(e)] = fadd(col[tp.prb_i(e)], sr[tp.prb_col(e) * P.PB]);
+                    if (e < tp.np()) col[tp.prb_i(e)] = fadd(col[tp.prb_i(e)], sr[tp.prb_col(e) * P.PB]);
                 if (P.grad_x) {
 #pragma unroll
                     for (int e = 0; e < SRCMAX; ++e)
-                        if (e < tp.ns && tp.src_row(e) == g.inst)
+                        if (e < tp.ns() && tp.src_row(e) == g.inst)
                             P.grad_x[(size_t)g.inst * P.steps + t] = col[tp.src_i(e)];
                 }
 #pragma unroll
                 for (int i = 0; i < M; ++i) lam[i] = col[i];
             }
+            // Kg * lambda into the column (read back after the barrier, by
+            // this thread for its own cells and by its neighbours)
 #pragma unroll
-            for (int i = 0; i < M; ++i) {
-                c2g[i] = fmul(ln.coef[(2 * M + i) * NT], lam[i]);
-                col[i] = c2g[i];
+            for (int i = 0; i < M; ++i) col[i] = fmul(ln.coef[2 * M + i], lam[i]);
+            if (!early || u == 0) {
+                if (g.top) send(ln.me + ((u & 1) - 2) * P.NCP, (uint32_t)(u + 1), col[0]);
+                if (g.bot) send(ln.me + (4 + (u & 1)) * P.NCP, (uint32_t)(u + 1), col[M - 1]);
             }
-            if (g.top) send(ln.me + ((u & 1) - 2) * P.NCP, (uint32_t)(u + 1), c2g[0]);
-            if (g.bot) send(ln.me + (4 + (u & 1)) * P.NCP, (uint32_t)(u + 1), c2g[M - 1]);
         }
         if ((aborted = __syncthreads_or(gave_up))) break;
-        if (g.colv) {
+        auto phase2 = [&](auto inner_tag) {
+            constexpr bool IN = decltype(inner_tag)::value;
             auto update = [&](int i, float up, float dn) {
-                const float lg = lap5<ORDER>(up, col[i - LD], c2g[i], col[i + LD], dn, w, w4);
-                const float X1 = ln.coef[(0 * M + i) * NT], Kc = ln.coef[(1 * M + i) * NT],
-                            Ky2 = ln.coef[(3 * M + i) * NT];
+                const float lg = lap5<ORDER>(up, col[i - LD], col[i], col[i + LD], dn, w, w4);
+                const float X1 = IN ? 1.0f : ln.coef[i], Ky2 = IN ? -1.0f : ln.coef[3 * M + i];
+                const float Kc = ln.coef[M + i];
                 acc[i] = fadd(acc[i], fmul(fmul(X1, fmul(Kc, lys[i * NT])), lam[i]));
                 const float gy1 = fadd(fmul(dt2, lg), fmul(fmul(2.0f, lam[i]), X1));
                 const float g2 = fmul(Ky2, lam[i]);
@@ -480,13 +536,27 @@ __global__ void __launch_bounds__(MAX_THREADS, 1) seq_bwd_band_kernel(FusedParam
                 pend[i] = g2;
             };
             cp_async_wait_all();
-#pragma unroll
-            for (int i = 1; i < M - 1; ++i) update(i, c2g[i - 1], c2g[i + 1]);
+            // the end cells first (their halo values were sent at the end of
+            // the neighbours' previous step), then this thread's next
+            // exchange, then the interior
             float up = col[-1], dn = col[M];
             if (g.top) up = recv(P, ln.me + (u & 1) * P.NCP, (uint32_t)(u + 1), gave_up);
             if (g.bot) dn = recv(P, ln.me + (2 + (u & 1)) * P.NCP, (uint32_t)(u + 1), gave_up);
-            update(0, up, c2g[1]);
-            update(M - 1, c2g[M - 2], dn);
+            update(0, up, col[1]);
+            update(M - 1, col[M - 2], dn);
+            if (early && u + 1 < P.steps) {
+                // the end cells' next lambda is final (no seed on this thread)
+                const int q = (u + 1) & 1;
+                if (g.top) send(ln.me + (q - 2) * P.NCP, (uint32_t)(u + 2), fmul(ln.coef[2 * M], lam[0]));
+                if (g.bot)
+                    send(ln.me + (4 + q) * P.NCP, (uint32_t)(u + 2), fmul(ln.coef[3 * M - 1], lam[M - 1]));
+            }
+#pragma unroll
+            for (int i = 1; i < M - 1; ++i) update(i, col[i - 1], col[i + 1]);
+        };
+        if (g.colv) {
+            if (inner) phase2(std::true_type{});
+            else       phase2(std::false_type{});
         }
         tape -= tape_step;
         if (g.colv && u + 1 < P.steps) {   // the staged words were all read above
@@ -542,8 +612,8 @@ int wt_band_plan(int batch, int nx, int ny, int n_prb, int n_sm, WtBandLaunch* L
             const int threads = S * NCP;
             const int LD = band_ld(R);
             const size_t tiles = 2 * (size_t)(ny + 2) * LD * sizeof(float);
-            const size_t fwd = tiles + (size_t)3 * M * threads * sizeof(float) + aux_fwd;
-            const size_t bwd = tiles + (size_t)5 * M * threads * sizeof(float) + aux_bwd;
+            const size_t fwd = tiles + (size_t)((3 * M) | 1) * threads * sizeof(float) + aux_fwd;
+            const size_t bwd = tiles + (size_t)(((4 * M) | 1) + M) * threads * sizeof(float) + aux_bwd;
             if (fwd > SMEM_MAX || bwd > SMEM_MAX) continue;
             const long cost = (long)R * NCP;
             if (best_cost >= 0 && cost >= best_cost) continue;
