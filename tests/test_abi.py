@@ -52,7 +52,7 @@ def _desc(B=2, N=32, T=10, sources=((5 * 32 + 16, -1),), probes=((20 * 32 + 16, 
     src = (_lib.SourceEntry * max(1, len(sources)))(*[_lib.SourceEntry(*s) for s in sources])
     prb = (_lib.ProbeEntry * max(1, len(probes)))(*[_lib.ProbeEntry(*p) for p in probes])
     d = _lib.SeqDesc(B, N, N, T, len(sources), C.cast(src, C.POINTER(_lib.SourceEntry)),
-                     len(probes), C.cast(prb, C.POINTER(_lib.ProbeEntry)), form, 0, cluster, 0)
+                     len(probes), C.cast(prb, C.POINTER(_lib.ProbeEntry)), form, 0, cluster, 0, 0, 0)
     return d, (src, prb)
 
 
@@ -97,19 +97,60 @@ def test_fused_tap_capacity(lib):
 
 
 def test_fused_plan_size_limit(lib):
-    """The fused form plans instances that fit one cluster (up to 256x256,
-    with 16-CTA clusters above 160); WaveRNN sends larger grids to the plain
-    form."""
+    """The cluster layout plans instances that fit one cluster (up to
+    256x256, with 16-CTA clusters above 160); larger grids need the band
+    layout, which needs the SMs for batch x bands CTAs (with one SM, none)."""
     from wavetorch_gb300.functional import SeqSpec, fused_supported
     for n in (160, 161, 200, 256):
-        assert fused_supported(SeqSpec(2, n, n, 100, [(5, -1)], [(7, 1, 0)])), n
-    assert not fused_supported(SeqSpec(2, 257, 257, 100, [(5, -1)], [(7, 1, 0)]))
-    assert not fused_supported(SeqSpec(1, 1024, 1024, 100, [(5, -1)], [(7, 1, 0)]))
+        assert fused_supported(SeqSpec(2, n, n, 100, [(5, -1)], [(7, 1, 0)], sm_count=1)), n
+    assert not fused_supported(SeqSpec(2, 257, 257, 100, [(5, -1)], [(7, 1, 0)], sm_count=1))
+    assert not fused_supported(SeqSpec(1, 1024, 1024, 100, [(5, -1)], [(7, 1, 0)], sm_count=1))
     # the plain form takes any grid
     spec = SeqSpec(1, 1024, 1024, 100, [(5, -1)], [(7, 1, 0)], form=0)
     d, keep = spec.desc()
     n = C.c_size_t(0)
     assert lib.wt_seq_workspace_bytes(C.byref(d), C.byref(n)) == 0
+
+
+def test_band_layout_plan(lib):
+    """Grids no cluster holds run in bands of rows, one CTA per band and SM:
+    1024x1024 on 152 SMs takes 147 bands of 7 rows (1024 threads), and its
+    workspace is the tape (T x 147 x 1024 x 7 floats), the exchange words,
+    dL/dc and the tables.  Refused (the caller uses the plain form): more
+    bands than SMs, more than 1024 columns, field outputs, checkpoint modes,
+    an explicit cluster size, more than two sources on one thread's cells."""
+    from wavetorch_gb300 import _lib
+    from wavetorch_gb300.functional import SeqSpec, fused_supported, seq_workspace_bytes
+    N, T = 1024, 100
+    src = [(60 * N + y, -1) for y in range(200, 825)]
+    prb = [(900 * N + 512, 1, 0)]
+    spec = SeqSpec(1, N, N, T, src, prb, sm_count=152)
+    assert fused_supported(spec)
+    tape = T * 147 * 1024 * 7 * 4
+    halo = 147 * 4 * 1024 * 8
+    ws = seq_workspace_bytes(spec)
+    assert tape + halo + N * N * 4 < ws < tape + halo + N * N * 4 + 16 * 2**20
+    assert seq_workspace_bytes(SeqSpec(1, N, N, T, src, prb, sm_count=152, segment=-1)) == ws
+
+    def status(**kw):
+        args = dict(batch=1, nx=N, ny=N, steps=T, sources=src, probes=prb, sm_count=152)
+        args.update(kw)
+        d, keep = SeqSpec(**args).desc()
+        n = C.c_size_t(0)
+        return lib.wt_seq_workspace_bytes(C.byref(d), C.byref(n))
+
+    U = _lib.WT_ERR_UNSUPPORTED
+    assert status(batch=2) == U                      # 2 x 147 bands > 152 SMs
+    assert status(ny=1056, sources=[(61, -1)], probes=[(70, 1, 0)]) == U   # > 1024 columns
+    assert status(output_fields=True, probes=[]) == U
+    assert status(segment=50) == U
+    assert status(segment=-2) == U
+    assert status(cluster=4) == U
+    assert status(sources=[(60 * N + 5, -1), (61 * N + 5, -1), (62 * N + 5, -1)]) == U
+    assert status(sources=[(60 * N + 5, -1), (61 * N + 5, -1)]) == _lib.WT_OK
+    assert status(sm_count=-1) == _lib.WT_ERR_INVALID
+    # several strips per band when bands of one strip would need too many SMs
+    assert status(nx=300, ny=300, sources=[(61, -1)], probes=[(70, 1, 0)], sm_count=20) == _lib.WT_OK
 
 
 def test_fused_adjoint_modes(lib):
