@@ -351,11 +351,45 @@ def run_ours(args):
         t_plain = max_over_ranks(statistics.mean(pe), world, dev)
         g_rel = float(torch.linalg.norm((grad_fused - grad_plain).double()) /
                       torch.linalg.norm(grad_plain.double()))
+        # the plain form's kernels without their launch cost: its forward and
+        # adjoint sequences (3 launches per time step) replayed from a CUDA graph
+        pspec = SeqSpec(B, N, N, T, src, prb, form=_lib.WT_FORM_PLAIN)
+        side = torch.cuda.Stream(device=dev)
+        side.wait_stream(stream)
+        with torch.cuda.stream(side):
+            _, _, _, pws = seq_forward(pspec, sc, b, c, x)
+            seq_backward(pspec, sc, b, c, x, gout, pws, False)
+            del pws
+        stream.wait_stream(side)
+        torch.cuda.synchronize(dev)
+        graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(graph):
+            _, _, _, pws = seq_forward(pspec, sc, b, c, x)
+            seq_backward(pspec, sc, b, c, x, gout, pws, False)
+        graph.replay()
+        torch.cuda.synchronize(dev)
+        pg = []
+        for k in range(2):
+            flush.zero_()
+            a, z = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            graph.replay()
+            z.record(stream)
+            torch.cuda.synchronize(dev)
+            pg.append(a.elapsed_time(z) / 1e3)
+        del graph, pws
+        torch.cuda.empty_cache()
+        t_pgraph = max_over_ranks(statistics.mean(pg), world, dev)
         plain = {"value": world * cell_steps / t_plain, "ms_per_step": t_plain * 1e3,
                  "fused_over_plain": t_plain / t_step,
                  "grad_rel_err_fused_vs_plain": g_rel,
+                 "kernels_graph_ms": t_pgraph * 1e3,
+                 "fused_kernels_over_plain_kernels_graph": t_pgraph / (t_f + t_b),
                  "note": "plain = one kernel per step, every field kept; bit-exact with the "
-                         "reference's float32 CPU path"}
+                         "reference's float32 CPU path. Run as a user runs it, it is partly "
+                         "bound by the host's launch rate (3 launches per time step); "
+                         "kernels_graph_ms is its forward + adjoint kernels replayed from a "
+                         "CUDA graph, compared with the fused kernels' own time"}
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
