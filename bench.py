@@ -521,6 +521,16 @@ def run_kernels_only(args):
                       "cell_steps_per_s": B * N * N * T / ((f + bw) / 1e3)}))
 
 
+def layout_counts(rb):
+    """How many groups of a ragged batch run in each fused layout."""
+    counts = {}
+    for g in rb.groups:
+        c = g.spec.cluster
+        key = f"cluster {c}" if c > 0 else f"bands <= {g.spec.sm_count // len(g.idx)} per model"
+        counts[key] = counts.get(key, 0) + 1
+    return counts
+
+
 def run_ragged(args):
     """Ragged workload: `instances` single-instance models, grid side
     U{64..256} (PML 20), step count U{500..4000}, the vowel-like generator
@@ -602,6 +612,7 @@ def run_ragged(args):
         "config": {"workload": f"ragged: {n} models, N ~ U{{64..256}} (PML 20), T ~ U{{500..4000}}, "
                                "fwd + adjoint to dL/drho per model",
                    "instances": n, "groups": len(rb.groups), "cell_steps": cell_steps,
+                   "layouts": layout_counts(rb),
                    "l2": "flushed (512 MiB write) before every timed step",
                    "setup_s": t_setup},
         "per_model_loop": {"plain_cell_steps_per_s": loops["plain"],

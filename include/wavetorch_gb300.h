@@ -126,7 +126,8 @@ typedef struct wt_seq_desc {
     const wt_probe_entry* probes_host;     /* host array, n_probes entries   */
     int32_t form;                          /* WT_FORM_PLAIN / WT_FORM_FUSED  */
     int32_t segment;                       /* fused adjoint mode, see below  */
-    int32_t cluster;                       /* CTAs per instance, 0 = auto    */
+    int32_t cluster;                       /* CTAs per instance, 0 = auto,
+                                              -1 = the band layout            */
     int32_t output_fields;                 /* 1: also write every field      */
     int32_t coef_batched;                  /* 1: one geometry per instance   */
     int32_t sm_count;                      /* SMs for the band layout, 0 = the
@@ -140,7 +141,9 @@ typedef struct wt_seq_desc {
  * CTA per band and SM in a cooperative launch, the band boundaries exchanged
  * through global memory; that layout needs batch x bands <= sm_count, no
  * output_fields, and runs its adjoint from the tape only (segment 0 or -1).
- * `cluster` applies to the cluster layout only.                            */
+ * `cluster` > 0 fixes the cluster size; -1 asks for the band layout even
+ * where a cluster would hold the instance (its CTAs need not share a GPC,
+ * as a cluster's must).                                                     */
 
 /* `segment` chooses how the fused form's adjoint gets the forward's fields:
  *   -1  tape: the forward stores Lap(h_{t-1}) of every cell and step

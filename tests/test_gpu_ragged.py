@@ -27,8 +27,7 @@ def make(N, seed, dev):
                       [wt.WaveIntensityProbe(N - 20, N // 2 + d) for d in (-15, 0, 15)]).to(dev)
 
 
-@pytest.mark.parametrize("graph", [False, True])
-def test_ragged_step_matches_models_run_alone(cuda, graph):
+def _ragged_case(cuda):
     # enough steps for the wave to reach the probes (N - 40 cells away at
     # about 0.7 cells per step), else every intensity is 0 and the loss 0/0
     sizes = [64, 64, 100, 150, 200, 256]
@@ -39,7 +38,10 @@ def test_ragged_step_matches_models_run_alone(cuda, graph):
         x, lab = vowel_like(1, T, seed=200 + i)
         inputs.append(torch.from_numpy(x[0]).to(cuda))
         labels.append(int(lab[0]))
-    rb = RaggedBatch(models, inputs, labels, graph=graph)
+    return models, inputs, labels
+
+
+def _check_against_alone(cuda, rb, models, inputs, labels):
     for _ in range(2):                       # replays are repeatable
         losses = rb.step().clone()
     torch.cuda.synchronize()
@@ -52,3 +54,24 @@ def test_ragged_step_matches_models_run_alone(cuda, graph):
         loss.backward()
         assert abs(losses[i].item() - loss.item()) <= 1e-5 * abs(loss.item()), i
         assert rel(grads[i].cpu().numpy(), m.cell.geom.rho.grad.cpu().numpy()) <= 1e-5, i
+
+
+@pytest.mark.parametrize("graph", [False, True])
+def test_ragged_step_matches_models_run_alone(cuda, graph):
+    models, inputs, labels = _ragged_case(cuda)
+    rb = RaggedBatch(models, inputs, labels, graph=graph)
+    _check_against_alone(cuda, rb, models, inputs, labels)
+
+
+def test_ragged_groups_in_band_layout(cuda):
+    """Groups of the larger grids run in the band layout (at most 12 CTAs
+    per instance): same losses and gradients as the models run alone."""
+    models, inputs, labels = _ragged_case(cuda)
+    rb = RaggedBatch(models, inputs, labels, graph=False, autotune=False)
+    banded = 0
+    for grp in rb.groups:
+        if grp.N >= 200:
+            grp.spec.cluster, grp.spec.sm_count = -1, 12 * len(grp.idx)
+            banded += 1
+    assert banded == 2
+    _check_against_alone(cuda, rb, models, inputs, labels)

@@ -156,3 +156,17 @@ def test_holey_geometry_matches_reference_on_cpu():
     assert np.array_equal(c.detach().numpy(), d["c"])
     for got, key in ((gx, "grad_x"), (gy, "grad_y"), (gr, "grad_r")):
         assert np.allclose(got.numpy(), d[key], rtol=1e-6, atol=0), key
+
+
+def test_ragged_cluster_choice():
+    """The ragged autotuner's choice from measured times: the size of least
+    SM-time per group (groups share the SMs), unless a group alone would
+    then outlast the whole batch; a group of G instances takes G x size SMs."""
+    from wavetorch_gb300.ragged import pick_cluster_sizes
+    small = {1: 1.8, 2: 1.1, 4: 0.8, 8: 0.6}          # seconds per size
+    # many groups: the cheapest size (1 SM x 1.8) everywhere
+    assert pick_cluster_sizes([(small, 1.0, 1)] * 200 + [({16: 1.0}, 1.0, 1)], 152) == [1] * 200 + [16]
+    # one long group on an idle machine: alone it would set the step -> faster sizes
+    assert pick_cluster_sizes([(small, 10.0, 1), ({16: 0.5}, 1.0, 1)], 152) == [8, 16]
+    # a group of 40 instances at size 2 already fills the machine's SM-time bound
+    assert pick_cluster_sizes([(small, 1.0, 40)], 80) == [2]

@@ -211,9 +211,12 @@ int make_plan(const wt_seq_desc* d, SeqPlan* p, bool nl = false) {
         P.o_lam = o; o = up(o + 3 * bp * F);
         P.o_gc = o; o = up(o + bp * F);
     } else {
-        if (d->segment < -2) return WT_ERR_INVALID;
-        int st = wt_fused_plan(P.nx, P.ny, P.T, P.np, d->cluster, d->segment, &P.L);
-        if (st == WT_ERR_UNSUPPORTED && !nl && d->cluster == 0 && !d->output_fields &&
+        if (d->segment < -2 || d->cluster < -1) return WT_ERR_INVALID;
+        // cluster -1 asks for the band layout; 0 takes a cluster when one
+        // holds the instance, else bands
+        int st = d->cluster == -1 ? (int)WT_ERR_UNSUPPORTED
+                                  : wt_fused_plan(P.nx, P.ny, P.T, P.np, d->cluster, d->segment, &P.L);
+        if (st == WT_ERR_UNSUPPORTED && !nl && d->cluster <= 0 && !d->output_fields &&
             (d->segment == 0 || d->segment == -1)) {
             // too large for one cluster: bands of rows, one CTA per band
             const int sms = band_sms(d);

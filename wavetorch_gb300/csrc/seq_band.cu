@@ -139,6 +139,14 @@ WT_DEV float recv(const FusedParams& P, const unsigned long long* w, uint32_t ta
     return 0.f;
 }
 
+// recv with the word's first load already done (v, issued before the
+// barrier that precedes the use, so its trip to L2 overlaps the barrier).
+WT_DEV float recv_pre(const FusedParams& P, unsigned long long v, const unsigned long long* w,
+                      uint32_t tag, bool& gave_up) {
+    if ((uint32_t)(v >> 32) == tag) return __uint_as_float((uint32_t)v);
+    return recv(P, w, tag, gave_up);
+}
+
 WT_DEV void send(unsigned long long* w, uint32_t tag, float v) {
     st_gpu_u64(w, ((unsigned long long)tag << 32) | __float_as_uint(v));
 }
@@ -286,7 +294,8 @@ WT_DEV void stage_seeds(const FusedParams& P, const Geo& g, float* seeds, int c)
 template <int M, int ORDER, int RS, bool INNER>
 WT_DEV void fwd_step(const FusedParams& P, const Geo& g, const Lane& ln, const Taps& tp,
                      const ProbeRing& pr, int t, int pb, int pc, float* tape, float (&xv)[SRCMAX],
-                     const float (&cur)[M], float (&inout)[M], bool& gave_up) {
+                     const float (&cur)[M], float (&inout)[M], unsigned long long& hu,
+                     unsigned long long& hd, bool& gave_up) {
     const float* rcol = ln.col0 + RS * ln.tile;
     float* wcol = ln.col0 + (RS ^ 1) * ln.tile;
     const int LD = P.LD, NT = ln.NT;
@@ -303,8 +312,8 @@ WT_DEV void fwd_step(const FusedParams& P, const Geo& g, const Lane& ln, const T
     // cells are computed
     float up = rcol[-1], dn = rcol[M];
     if (t > 0) {
-        if (g.top) up = recv(P, ln.me + (RS ^ 1) * P.NCP, (uint32_t)t, gave_up);
-        if (g.bot) dn = recv(P, ln.me + (2 + (RS ^ 1)) * P.NCP, (uint32_t)t, gave_up);
+        if (g.top) up = recv_pre(P, hu, ln.me + (RS ^ 1) * P.NCP, (uint32_t)t, gave_up);
+        if (g.bot) dn = recv_pre(P, hd, ln.me + (2 + (RS ^ 1)) * P.NCP, (uint32_t)t, gave_up);
     }
     update(0, up, cur[1]);
     update(M - 1, cur[M - 2], dn);
@@ -338,6 +347,10 @@ WT_DEV void fwd_step(const FusedParams& P, const Geo& g, const Lane& ln, const T
 #pragma unroll
         for (int e = 0; e < PRBMAX; ++e)
             if (e < tp.np()) row[tp.prb_col(e) * P.PB] = wcol[tp.prb_i(e)];
+    }
+    if (more) {   // first look at the next step's halo words (exchange t)
+        if (g.top) hu = ld_gpu_u64(ln.me + RS * P.NCP);
+        if (g.bot) hd = ld_gpu_u64(ln.me + (2 + RS) * P.NCP);
     }
 }
 
@@ -399,14 +412,15 @@ __global__ void __launch_bounds__(MAX_THREADS, 1) seq_fwd_band_kernel(FusedParam
     const size_t tape_step = (size_t)P.batch * P.C * NT * M;
     int pb = 0, pc = 0, chunk0 = 0;
     bool gave_up = false, aborted = false;
+    unsigned long long hu = 0, hd = 0;
     for (int t = 0; t < P.steps; ++t) {
         if (g.colv) {
             if (inner) {
-                if (t & 1) fwd_step<M, ORDER, 1, true>(P, g, ln, tp, pr, t, pb, pc, tape, xv, yb, ya, gave_up);
-                else       fwd_step<M, ORDER, 0, true>(P, g, ln, tp, pr, t, pb, pc, tape, xv, ya, yb, gave_up);
+                if (t & 1) fwd_step<M, ORDER, 1, true>(P, g, ln, tp, pr, t, pb, pc, tape, xv, yb, ya, hu, hd, gave_up);
+                else       fwd_step<M, ORDER, 0, true>(P, g, ln, tp, pr, t, pb, pc, tape, xv, ya, yb, hu, hd, gave_up);
             } else {
-                if (t & 1) fwd_step<M, ORDER, 1, false>(P, g, ln, tp, pr, t, pb, pc, tape, xv, yb, ya, gave_up);
-                else       fwd_step<M, ORDER, 0, false>(P, g, ln, tp, pr, t, pb, pc, tape, xv, ya, yb, gave_up);
+                if (t & 1) fwd_step<M, ORDER, 1, false>(P, g, ln, tp, pr, t, pb, pc, tape, xv, yb, ya, hu, hd, gave_up);
+                else       fwd_step<M, ORDER, 0, false>(P, g, ln, tp, pr, t, pb, pc, tape, xv, ya, yb, hu, hd, gave_up);
             }
         }
         tape += tape_step;
@@ -489,6 +503,7 @@ __global__ void __launch_bounds__(MAX_THREADS, 1) seq_bwd_band_kernel(FusedParam
     const float w = P.k.lap_w, w4 = P.k.lap_w4, dt2 = P.k.dt2;
     int pk = 0, pcn = 0;
     bool gave_up = false, aborted = false;
+    unsigned long long hu = 0, hd = 0;
     for (int u = 0; u < P.steps; ++u) {
         const int t = P.steps - 1 - u;
         float* col = ln.col0 + (u & 1) * ln.tile;
@@ -521,6 +536,9 @@ __global__ void __launch_bounds__(MAX_THREADS, 1) seq_bwd_band_kernel(FusedParam
                 if (g.top) send(ln.me + ((u & 1) - 2) * P.NCP, (uint32_t)(u + 1), col[0]);
                 if (g.bot) send(ln.me + (4 + (u & 1)) * P.NCP, (uint32_t)(u + 1), col[M - 1]);
             }
+            // first look at this step's halo words, across the barrier
+            if (g.top) hu = ld_gpu_u64(ln.me + (u & 1) * P.NCP);
+            if (g.bot) hd = ld_gpu_u64(ln.me + (2 + (u & 1)) * P.NCP);
         }
         if ((aborted = __syncthreads_or(gave_up))) break;
         auto phase2 = [&](auto inner_tag) {
@@ -540,8 +558,8 @@ __global__ void __launch_bounds__(MAX_THREADS, 1) seq_bwd_band_kernel(FusedParam
             // the neighbours' previous step), then this thread's next
             // exchange, then the interior
             float up = col[-1], dn = col[M];
-            if (g.top) up = recv(P, ln.me + (u & 1) * P.NCP, (uint32_t)(u + 1), gave_up);
-            if (g.bot) dn = recv(P, ln.me + (2 + (u & 1)) * P.NCP, (uint32_t)(u + 1), gave_up);
+            if (g.top) up = recv_pre(P, hu, ln.me + (u & 1) * P.NCP, (uint32_t)(u + 1), gave_up);
+            if (g.bot) dn = recv_pre(P, hd, ln.me + (2 + (u & 1)) * P.NCP, (uint32_t)(u + 1), gave_up);
             update(0, up, col[1]);
             update(M - 1, col[M - 2], dn);
             if (early && u + 1 < P.steps) {

@@ -10,8 +10,10 @@ loss masked to each instance's own steps, so its forward fields, losses and
 gradients are those of the instance run alone.  Every group runs on its own
 stream; one training step (rho -> c for every instance, the fused forwards,
 the losses and their gradients, the fused adjoints, c -> rho) is captured
-once into a CUDA graph and replayed.  A small autotuner times the cluster
-sizes each group's grid admits and keeps the fastest.
+once into a CUDA graph and replayed.  A small autotuner times the layouts
+each group's grid admits (clusters of 1-16 CTAs per instance, or bands of
+rows) and keeps, per group, the one of least SM-time unless that group alone
+would then set the step time.
 
 Loss per instance: ``CrossEntropy(normalize_power(sum_t I), label)``, the
 reference's training loss (wavetorch/train.py:61-62, utils.py:35-36); its
@@ -33,8 +35,8 @@ from .geom import WaveGeometryFreeForm
 from .probe import WaveProbe
 from .source import WaveSource
 
-# cluster size chosen per (grid, source/probe layout) by the autotuner
-_TUNED: Dict[tuple, int] = {}
+# measured seconds per layout option, per (grid, source/probe layout)
+_TUNED: Dict[tuple, Dict[tuple, float]] = {}
 
 
 @dataclass
@@ -53,6 +55,52 @@ class _Group:
     onehot: torch.Tensor            # [G, P]
     work: List[torch.Tensor] = field(default_factory=list)   # rho -> c scratch per instance
     stream: Optional[torch.cuda.Stream] = None
+
+
+def _option_spec(opt: tuple, G: int) -> tuple:
+    """(cluster, sm_count) of a layout option for a group of G instances:
+    (c, 0) a cluster of c CTAs per instance; (-1, p) bands, at most p CTAs
+    per instance."""
+    cl, per = opt
+    return (cl, 0) if cl > 0 else (-1, per * G)
+
+
+def _option_sms(opt) -> int:
+    """SMs one instance occupies under a layout option (a cluster size, or
+    a (cluster, bands) pair as `_option_spec` takes)."""
+    if isinstance(opt, tuple):
+        return opt[0] if opt[0] > 0 else opt[1]
+    return opt
+
+
+def pick_cluster_sizes(timings: Sequence[tuple], n_sm: int) -> List:
+    """Layout option per group from measured times.
+
+    timings: per group (times, scale, G): times maps a layout option (a
+    cluster size, or a (cluster, bands) pair) -> seconds of the group's
+    measured run (its G instances side by side), scale the factor to the
+    group's full step count.  An option using c SMs per instance occupies
+    G x c SMs for the group's time t(c).  Start from the size with the
+    least SM-time (c x t(c)); the step then takes at least max(total SM-time /
+    n_sm, the longest group's time).  While the longest group's time is above
+    the SM-time bound, move it to a faster size (the one of least SM-time
+    among the faster ones): the groups run concurrently, so only the longest
+    one can set the step time."""
+    S = _option_sms
+    groups = []
+    for times, scale, G in timings:
+        opts = sorted(times, key=lambda o: (S(o), str(o)))
+        groups.append((opts, {o: times[o] * scale for o in opts}, G))
+    pick = [min(opts, key=lambda o: (S(o) * t[o], S(o))) for opts, t, _ in groups]
+    for _ in range(4 * len(groups) + 1):
+        bound = sum(G * S(o) * t[o] for o, (_, t, G) in zip(pick, groups)) / max(n_sm, 1)
+        k = max(range(len(groups)), key=lambda j: groups[j][1][pick[j]])
+        opts, t, _ = groups[k]
+        faster = [o for o in opts if t[o] < t[pick[k]]]
+        if t[pick[k]] <= bound or not faster:
+            break
+        pick[k] = min(faster, key=lambda o: (S(o) * t[o], -t[o]))
+    return pick
 
 
 def _check_model(m) -> None:
@@ -142,14 +190,16 @@ class RaggedBatch:
         if graph:
             self._capture()
 
-    def _fit_memory(self, share: float = 0.3) -> None:
+    def _fit_memory(self, share: float = 0.6) -> None:
         """Groups whose tapes would take the workspaces past `share` of the
-        device's memory (largest first) use checkpoints instead (segment -2)."""
-        total_mem = torch.cuda.get_device_properties(self.device).total_memory
+        device memory free now (largest first) use checkpoints instead
+        (segment -2).  The graph keeps one workspace per group for its whole
+        life, so the budget is what is free when the batch is built."""
+        free, _ = torch.cuda.mem_get_info(self.device)
         sizes = [seq_workspace_bytes(g.spec) for g in self.groups]
         total = sum(sizes)
         for k in sorted(range(len(self.groups)), key=lambda k: -sizes[k]):
-            if total <= share * total_mem:
+            if total <= share * free:
                 break
             g = self.groups[k]
             g.spec.segment = -2
@@ -225,39 +275,59 @@ class RaggedBatch:
 
     # -- autotuner ----------------------------------------------------------
     def _autotune(self, steps: int = 96) -> None:
-        """Pick each group's cluster size by timing a short forward + adjoint
-        of its instances for every size its grid admits (cached per layout)."""
+        """Pick each group's layout: a cluster of 1, 2, 4 or 8 CTAs per
+        instance, or bands of rows (at most 8 or 12 CTAs per instance, any
+        SMs); a 16-CTA cluster only where no band layout plans (clusters that
+        large must each fit within one GPC, which limits how many run at
+        once).  Every option is timed on a short forward + adjoint (cached per
+        layout); the groups share the GPU's SMs, so the choice minimises
+        SM-time (CTAs x time), except where a group alone would then outlast
+        the whole batch."""
         for grp in self.groups:
-            if grp.key in _TUNED:
-                grp.spec.cluster = _TUNED[grp.key]
+            if grp.key not in _TUNED:
+                _TUNED[grp.key] = self._time_options(grp, min(grp.T, steps))
+        n_sm = torch.cuda.get_device_properties(self.device).multi_processor_count
+        choice = pick_cluster_sizes(
+            [(_TUNED[g.key], g.T / min(g.T, steps), len(g.idx)) for g in self.groups], n_sm)
+        for grp, opt in zip(self.groups, choice):
+            grp.spec.cluster, grp.spec.sm_count = _option_spec(opt, len(grp.idx))
+
+    def _time_options(self, grp: _Group, T: int) -> Dict[tuple, float]:
+        """Seconds of a T-step forward + adjoint of the group's instances per
+        layout option (see `_option_spec`)."""
+        out: Dict[tuple, float] = {}
+        x = grp.x[:, :T].contiguous()
+        g = torch.ones(len(grp.idx), T, len(grp.spec.probes), device=self.device)
+        c = torch.ones_like(grp.c) * 0.75
+        G = len(grp.idx)
+        options = [(1, 0), (2, 0), (4, 0), (8, 0)]
+        if grp.spec.segment in (0, -1):
+            options += [(-1, 8), (-1, 12)]
+        for opt in options + [(16, 0)]:
+            if opt == (16, 0) and any(o[0] == -1 for o in out):
                 continue
-            T = min(grp.T, steps)
-            best, best_t = 0, float("inf")
-            x = grp.x[:, :T].contiguous()
-            g = torch.ones(len(grp.idx), T, len(grp.spec.probes), device=self.device)
-            c = torch.ones_like(grp.c) * 0.75
-            for cl in (1, 2, 4, 8, 16):
-                spec = SeqSpec(len(grp.idx), grp.N, grp.N, T, grp.spec.sources, grp.spec.probes,
-                               form=_lib.WT_FORM_FUSED, segment=grp.spec.segment, cluster=cl,
-                               coef_batched=True)
-                if not fused_supported(spec):
-                    continue
-                try:
-                    ts = []
-                    for r in range(3):
-                        torch.cuda.synchronize(self.device)
-                        t0 = time.perf_counter()
-                        _, _, _, ws = seq_forward(spec, grp.sc, grp.b, c, x)
-                        seq_backward(spec, grp.sc, grp.b, c, x, g, ws, False)
-                        torch.cuda.synchronize(self.device)
-                        if r:
-                            ts.append(time.perf_counter() - t0)
-                except _lib.WaveKernelError:
-                    continue
-                if min(ts) < best_t:
-                    best, best_t = cl, min(ts)
-            _TUNED[grp.key] = best
-            grp.spec.cluster = best
+            cl, per = _option_spec(opt, G)
+            spec = SeqSpec(G, grp.N, grp.N, T, grp.spec.sources, grp.spec.probes,
+                           form=_lib.WT_FORM_FUSED, segment=grp.spec.segment, cluster=cl,
+                           coef_batched=True, sm_count=per)
+            if not fused_supported(spec):
+                continue
+            try:
+                ts = []
+                for r in range(3):
+                    torch.cuda.synchronize(self.device)
+                    t0 = time.perf_counter()
+                    _, _, _, ws = seq_forward(spec, grp.sc, grp.b, c, x)
+                    seq_backward(spec, grp.sc, grp.b, c, x, g, ws, False)
+                    torch.cuda.synchronize(self.device)
+                    if r:
+                        ts.append(time.perf_counter() - t0)
+            except _lib.WaveKernelError:
+                continue
+            out[opt] = min(ts)
+        if not out:
+            raise ValueError(f"no fused layout serves a {grp.N}x{grp.N} grid")
+        return out
 
     def cell_steps(self) -> int:
         """Cell-steps of one training step (each model's N^2 x T_i)."""
