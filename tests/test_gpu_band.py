@@ -112,3 +112,39 @@ def test_input_gradient_and_per_instance_geometry(cuda):
     prb = [(110 * ny + 200, 1, 0), (95 * ny + 210, 1, 1)]
     check(cuda, nx, ny, 1, 60, src, prb, grad_x=True)
     check(cuda, nx, ny, 2, 60, src, prb, batched=True, seed=3)
+
+
+def test_missing_arrival_times_out_and_the_context_survives(cuda):
+    """A host-forced missing arrival: one band never sends its boundary rows
+    (the test hook wt_test_band_missing_arrival).  Its neighbours' bounded
+    waits give up after about 2 s, the launch's abort word stops every band,
+    the status word reads WT_ERR_TIMEOUT, and the next sequence on the same
+    context is correct."""
+    import ctypes as C
+    import time
+    from wavetorch_gb300.functional import _ptr, _stream, seq_workspace_bytes
+    nx, ny, B, T = 300, 400, 1, 40
+    src = [(100 * ny + 200, -1)]
+    prb = [(110 * ny + 200, 1, 0)]
+    b, c, x = problem(nx, ny, B, T, 7)
+    spec = SeqSpec(B, nx, ny, T, src, prb, form=_lib.WT_FORM_FUSED)
+    sc = scalars(0.707, 1.0, lap_order(B, nx, ny, 1.0))
+    d, keep = spec.desc()
+    n = seq_workspace_bytes(spec)
+    ws = torch.empty(n, dtype=torch.uint8, device=cuda)
+    out = torch.empty(B, T, 1, device=cuda)
+    tb, tc, tx = (torch.from_numpy(v).to(cuda) for v in (b, c, x))
+    lib = _lib.load()
+    fn = lib.wt_test_band_missing_arrival
+    fn.argtypes = [C.POINTER(_lib.Scalars), C.POINTER(_lib.SeqDesc)] + [C.c_void_p] * 5 + \
+                  [C.c_size_t, C.c_int32, C.c_void_p]
+    fn.restype = C.c_int
+    torch.cuda.synchronize()
+    t0 = time.time()
+    assert fn(C.byref(sc), C.byref(d), _ptr(tb), _ptr(tc), _ptr(tx), _ptr(out), _ptr(ws), n, 2,
+              _stream(cuda)) == _lib.WT_OK
+    torch.cuda.synchronize()
+    elapsed = time.time() - t0
+    assert seq_device_status(spec, ws) == _lib.WT_ERR_TIMEOUT
+    assert 1.5 < elapsed < 60, elapsed
+    check(cuda, nx, ny, B, T, src, prb, seed=7)

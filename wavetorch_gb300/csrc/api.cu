@@ -7,6 +7,7 @@
 #include <vector>
 
 #include "internal.cuh"
+#include "../../include/wavetorch_gb300_testing.h"
 
 // ---------------------------------------------------------------------------
 static thread_local char g_last_err[256] = "";
@@ -545,6 +546,26 @@ extern "C" int wt_seq_device_status(const wt_seq_desc* d, const void* workspace,
     if (h == WT_DEVERR_BOUNDS) return WT_ERR_INVALID;
     if (h == WT_DEVERR_TIMEOUT) return WT_ERR_TIMEOUT;
     return WT_OK;
+}
+
+extern "C" int wt_test_band_missing_arrival(const wt_scalars* s, const wt_seq_desc* d,
+                                            const float* b, const float* c, const float* x,
+                                            float* out, void* workspace, size_t workspace_bytes,
+                                            int32_t band, wt_stream_t stream) {
+    if (!scalars_ok(s)) return WT_ERR_INVALID;
+    SeqPlan P;
+    int st = make_plan(d, &P);
+    if (st) return st;
+    if (!P.band) return WT_ERR_UNSUPPORTED;
+    if (band < 0 || band >= P.BL.PR) return WT_ERR_INVALID;
+    if (!b || !c || !workspace || workspace_bytes < P.total) return WT_ERR_INVALID;
+    if ((P.ns > 0 && !x) || (P.np > 0 && !out)) return WT_ERR_INVALID;
+    cudaStream_t cs = (cudaStream_t)stream;
+    if ((st = upload_tables(d, P, workspace, cs))) return st;
+    wt::FusedParams F = fused_params(s, P, b, c, x, workspace);
+    F.out = out;
+    F.mute_band1 = band + 1;
+    return wt_launch_band(true, F, P.BL, cs);
 }
 
 // ---------------------------------------------------------------------------

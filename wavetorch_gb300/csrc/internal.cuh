@@ -99,6 +99,7 @@ struct FusedParams {
     // per instance; the bands' boundary rows travel through global memory
     unsigned long long* halo;   // [batch][band][from above | from below][2][NCP] tagged words
     int* abort_g;               // launch-wide abort word (a wait gave up)
+    int mute_band1;             // test hook: band index + 1 whose forward never sends; 0: none
 };
 
 // Up to INT_SCATTER_CAP int writes base[idx[i]] = val[i], passed by value as

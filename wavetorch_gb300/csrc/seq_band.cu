@@ -318,7 +318,9 @@ WT_DEV void fwd_step(const FusedParams& P, const Geo& g, const Lane& ln, const T
     update(0, up, cur[1]);
     update(M - 1, cur[M - 2], dn);
     const bool more = t + 1 < P.steps;
-    if (more && !tp.src_edge()) {
+    // (a band muted by the missing-arrival test hook never sends)
+    const bool sends = more && g.band + 1 != P.mute_band1;
+    if (sends && !tp.src_edge()) {
         if (g.top) send(ln.me + (RS - 2) * P.NCP, (uint32_t)(t + 1), inout[0]);
         if (g.bot) send(ln.me + (4 + RS) * P.NCP, (uint32_t)(t + 1), inout[M - 1]);
     }
@@ -336,7 +338,7 @@ WT_DEV void fwd_step(const FusedParams& P, const Geo& g, const Lane& ln, const T
 #pragma unroll
             for (int e = 0; e < SRCMAX; ++e)
                 if (e < tp.ns()) xv[e] = __ldg(P.x + (size_t)tp.src_row(e) * P.steps + t + 1);
-            if (tp.src_edge()) {
+            if (sends && tp.src_edge()) {
                 if (g.top) send(ln.me + (RS - 2) * P.NCP, (uint32_t)(t + 1), inout[0]);
                 if (g.bot) send(ln.me + (4 + RS) * P.NCP, (uint32_t)(t + 1), inout[M - 1]);
             }
