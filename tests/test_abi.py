@@ -41,6 +41,16 @@ def test_every_declared_symbol_is_exported(lib):
         assert hasattr(lib, n), n
 
 
+def test_test_hooks_are_exported(lib):
+    """The test hooks' header (outside the drop-in ABI) is exported too."""
+    text = open(os.path.join(ROOT, "include", "wavetorch_gb300_testing.h")).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    names = sorted(set(re.findall(r"\b(wt_[a-z0-9_]+)\s*\(", text)))
+    assert names == ["wt_test_band_missing_arrival"]
+    for n in names:
+        assert hasattr(lib, n), n
+
+
 def test_version_and_status_strings(lib):
     assert b"sm_103a" in lib.wt_version()
     assert lib.wt_status_string(1) == b"invalid argument"
