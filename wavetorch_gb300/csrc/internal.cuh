@@ -130,6 +130,7 @@ struct WtFusedLaunch {
     size_t smem_fwd_tape;   // forward shared memory in tape mode
     size_t smem_bwd_base;   // adjoint shared memory before the tape ring
     int nbuf_nl;            // ring slices of the nonlinear adjoint (two-part slices)
+    size_t smem_nl_coef;    // the nonlinear adjoint's per-thread coefficient words
 };
 
 // Launch shape of the band kernels (see seq_band.cu).

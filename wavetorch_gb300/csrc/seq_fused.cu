@@ -686,6 +686,8 @@ constexpr int fwd_max_threads(int M) {
     return M <= 5 ? 768 : M == 6 ? 640 : M == 8 ? 512 : M <= 10 ? 384 : 256;
 }
 constexpr int bwd_max_threads(int M) { return M >= 10 ? 384 : 512; }
+// Per-thread coefficient words of the nonlinear adjoint (b_pml, c_lin, rho).
+__host__ __device__ constexpr int nl_coef_stride(int M) { return (3 * M) | 1; }
 
 // ============================================================================
 // Forward
@@ -1245,20 +1247,21 @@ __global__ void __launch_bounds__(bwd_max_threads(M), 1) seq_bwd_tape_kernel(Fus
 // Nonlinear cell, adjoint (tape mode).  Per step s, with g = lam_s and the
 // tape's Lap(h1), h1 = h_{s-1} (slot s) and h2 = h_{s-2} (part 1 of slot
 // s-1), TimeStep's backward (wavetorch/cell.py:33-42) at the step's own b, c,
-// then autograd's chain through b(h1, rho) and c(h1, rho):
+// then autograd's chain through b(h1, rho) and c(h1, rho).  lam enters as
+// this step's (seeded) lambda and leaves as the next step's, pend carries
+// the grad_y2 term one step:
 //   dL/dh1  += grad_b * rho * dsat/dh1 + grad_c * (rho c_nl) * 2 h1
 //   dL/drho += grad_b * sat + grad_c * h1^2 * c_nl      (direct; accr)
 //   dL/dc_lin += grad_c                                  (accc)
-WT_DEV void adj_cell_nl(const FusedParams& P, float lg, float lam, float Ly, float h1, float h2,
-                        float bp, float cl, float rh, float& accc, float& accr, float& gy1,
-                        float& g2) {
+WT_DEV void adj_cell_nl(const FusedParams& P, float lg, float& lam, float Ly, float h1, float h2,
+                        float bp, float cl, float rh, float& accc, float& accr, float& pend) {
     const NLCoef n = nl_coef(P, bp, cl, rh, h1);
     const float dt = P.k.dt, dt2 = P.k.dt2;
     const float v = fadd(fmul(n.b, dt), 1.0f);                          // b*dt + 1
     const float X1 = fdiv(1.0f, v);
     const float gc = fmul(fmul(X1, fmul(fmul(fmul(2.0f, n.c), dt2), Ly)), lam);
     float gh = fadd(fmul(dt2, lg), fmul(fmul(2.0f, lam), X1));            // grad_y1
-    g2 = fmul(fmul(fsub(fmul(n.b, dt), 1.0f), X1), lam);                  // grad_y2
+    const float g2 = fmul(fmul(fsub(fmul(n.b, dt), 1.0f), X1), lam);      // grad_y2
     accc = fadd(accc, gc);
     float dr = 0.f;
     if (P.b0 > 0.f) {
@@ -1280,7 +1283,11 @@ WT_DEV void adj_cell_nl(const FusedParams& P, float lg, float lam, float Ly, flo
         gh = fadd(gh, fmul(fmul(gc, fmul(rh, P.cnl)), fmul(2.0f, h1)));
     }
     accr = fadd(accr, dr);
-    gy1 = gh;
+    // the next step's lambda: its grad_y2 term (from the step after this one)
+    // plus this step's grad_y1 term, in autograd's order; this step's grad_y2
+    // term waits one step
+    lam = fadd(pend, gh);
+    pend = g2;
 }
 
 template <int M, int ORDER>
@@ -1297,20 +1304,35 @@ __global__ void __launch_bounds__(bwd_max_threads(M), 1) seq_bwd_nl_kernel(Fused
 
     const size_t plane = (size_t)P.nx * P.ny;
     float* seeds = smem + 2 * tile + 2 * xchg_words(P.NCP);
+    // b_pml, c_lin and rho of the thread's cells: per-thread shared words at
+    // constant offsets (stride 3M rounded up to odd: conflict-free), then the
+    // tape ring (16-byte aligned)
+    constexpr int CS = nl_coef_stride(M);
+    float* coefs = seeds + ((2 * P.n_prb * P.PB + 3) & ~3);
+    float* cw = coefs + threadIdx.x * CS;
     TapeRing ring;
-    ring.buf = seeds + ((2 * P.n_prb * P.PB + 3) & ~3);
+    ring.buf = coefs + ((CS * (int)blockDim.x + 3) & ~3);
     ring.slice = 2 * (int)blockDim.x * M;             // two parts: Lap(h1), h1
     ring.full = reinterpret_cast<unsigned long long*>(ring.buf + (size_t)P.nbuf * ring.slice);
     if (threadIdx.x == 0) {
         for (int s = 0; s < P.nbuf; ++s) mbar_init(smem_addr(ring.full + s), 1);
         fence_mbarrier_init_cluster();
     }
-
-    float bp[M], cl[M], rh[M];
-    load_nl_coef<M>(P, g, bp, cl, rh);
-    float gy1[M], gy2a[M], gy2b[M], accc[M], accr[M];
+    {
+        float bp[M], cl[M], rh[M];
+        load_nl_coef<M>(P, g, bp, cl, rh);
 #pragma unroll
-    for (int i = 0; i < M; ++i) gy1[i] = gy2a[i] = gy2b[i] = accc[i] = accr[i] = 0.f;
+        for (int i = 0; i < M; ++i) {
+            cw[i] = bp[i];
+            cw[M + i] = cl[i];
+            cw[2 * M + i] = rh[i];
+        }
+    }
+    // adjoint state: lam (this step's lambda before its seeds), pend (the
+    // grad_y2 term of the previous step), the two accumulators
+    float lam[M], pend[M], accc[M], accr[M];
+#pragma unroll
+    for (int i = 0; i < M; ++i) lam[i] = pend[i] = accc[i] = accr[i] = 0.f;
     stage_seeds(P, g, seeds, 0);
     cluster_sync_all();
 
@@ -1329,37 +1351,25 @@ __global__ void __launch_bounds__(bwd_max_threads(M), 1) seq_bwd_nl_kernel(Fused
     uint32_t phase = 0;
     int pk = 0, pc = 0;
     bool ok = true;
-    auto step = [&](auto par, int u, float (&g2)[M]) -> bool {
+    auto step = [&](auto par, int u) -> bool {
         constexpr int PAR = decltype(par)::value;
         const int t = P.steps - 1 - u;
         float* col = ln.col0 + PAR * ln.tile;
         const int prev = slot == 0 ? P.nbuf - 1 : slot - 1;     // slot of step t-1
-        // the step's fields come first: c2g needs b and c at h1
-        float h1[M], h2[M], lam[M], c2g[M];
-        if (g.colv) {
-            tape_wait(P, X, ring, slot, (phase >> slot) & 1u);
-            ld_chunks_at<M>(h1, ring.buf + (size_t)slot * ring.slice + part + lane_off, stride);
-            if (t > 0) {
-                tape_wait(P, X, ring, prev, (phase >> prev) & 1u);
-                ld_chunks_at<M>(h2, ring.buf + (size_t)prev * ring.slice + part + lane_off, stride);
-            } else {
-#pragma unroll
-                for (int i = 0; i < M; ++i) h2[i] = 0.f;
-            }
-        }
-#pragma unroll
-        for (int i = 0; i < M; ++i) {
-            lam[i] = fadd(g2[i], gy1[i]);
-            c2g[i] = 0.f;
-        }
+        const float* sl = ring.buf + (size_t)slot * ring.slice;
         if (pk == 0 && u + P.PB < P.steps)
             stage_seeds(P, g, seeds, pc + 1);
         if (g.colv) {
+            // c2g needs b and c at h1: the step's field first
+            tape_wait(P, X, ring, slot, (phase >> slot) & 1u);
+            float h1[M];
+            ld_chunks_at<M>(h1, sl + part + lane_off, stride);
             if (tp.np || (P.grad_x && tp.ns))
                 seed_and_read<M>(P, g, X, tp, PAR, t, lam, seeds + (size_t)(pc & 1) * P.n_prb * P.PB + pk);
+            float c2g[M];
 #pragma unroll
             for (int i = 0; i < M; ++i) {
-                const NLCoef n = nl_coef(P, bp[i], cl[i], rh[i], h1[i]);
+                const NLCoef n = nl_coef(P, cw[i], cw[M + i], cw[2 * M + i], h1[i]);
                 const float X1 = fdiv(1.0f, fadd(fmul(n.b, P.k.dt), 1.0f));
                 c2g[i] = fmul(fmul(X1, fmul(n.c, n.c)), lam[i]);   // (b*dt+1)^-1 * c^2 * g
             }
@@ -1375,33 +1385,44 @@ __global__ void __launch_bounds__(bwd_max_threads(M), 1) seq_bwd_nl_kernel(Fused
             tape_issue(P, g, ring, lo, slot + 1 == P.nbuf ? 0 : slot + 1);
         }
         if (g.colv) {
+            // Kg*lambda of the thread's own cells and its neighbours' from
+            // the tile; the step's tape values from the ring again
             Column<M> c;
             lds_col<M>(c.lf, col - P.LD);
             lds_col<M>(c.rt, col + P.LD);
             c.up = col[-1];
             c.dn = col[M];
-            float Ly[M];
-            ld_chunks_at<M>(Ly, ring.buf + (size_t)slot * ring.slice + lane_off, stride);
+            float c2g[M], h1[M], h2[M], Ly[M];
+            lds_col<M>(c2g, col);
+            ld_chunks_at<M>(h1, sl + part + lane_off, stride);
+            ld_chunks_at<M>(Ly, sl + lane_off, stride);
+            if (t > 0) {
+                tape_wait(P, X, ring, prev, (phase >> prev) & 1u);
+                ld_chunks_at<M>(h2, ring.buf + (size_t)prev * ring.slice + part + lane_off, stride);
+            } else {
+#pragma unroll
+                for (int i = 0; i < M; ++i) h2[i] = 0.f;
+            }
             phase ^= 1u << slot;
 #pragma unroll
             for (int i = 1; i < M - 1; ++i)
-                adj_cell_nl(P, lap_cell<M, ORDER>(P, c, c2g, i), lam[i], Ly[i], h1[i], h2[i], bp[i],
-                            cl[i], rh[i], accc[i], accr[i], gy1[i], g2[i]);
+                adj_cell_nl(P, lap_cell<M, ORDER>(P, c, c2g, i), lam[i], Ly[i], h1[i], h2[i], cw[i],
+                            cw[M + i], cw[2 * M + i], accc[i], accr[i], pend[i]);
             if (ln.rup) c.up = recv_at(P, X, ln.rup + PAR * ln.pstride, u);
             if (ln.rdn) c.dn = recv_at(P, X, ln.rdn + PAR * ln.pstride, u);
-            adj_cell_nl(P, lap_cell<M, ORDER>(P, c, c2g, 0), lam[0], Ly[0], h1[0], h2[0], bp[0],
-                        cl[0], rh[0], accc[0], accr[0], gy1[0], g2[0]);
+            adj_cell_nl(P, lap_cell<M, ORDER>(P, c, c2g, 0), lam[0], Ly[0], h1[0], h2[0], cw[0],
+                        cw[M], cw[2 * M], accc[0], accr[0], pend[0]);
             adj_cell_nl(P, lap_cell<M, ORDER>(P, c, c2g, M - 1), lam[M - 1], Ly[M - 1], h1[M - 1],
-                        h2[M - 1], bp[M - 1], cl[M - 1], rh[M - 1], accc[M - 1], accr[M - 1],
-                        gy1[M - 1], g2[M - 1]);
+                        h2[M - 1], cw[M - 1], cw[2 * M - 1], cw[3 * M - 1], accc[M - 1],
+                        accr[M - 1], pend[M - 1]);
         }
         slot = prev;
         if (++pk == P.PB) { pk = 0; ++pc; }
         return true;
     };
     for (int u = 0; u < P.steps && ok; ++u)
-        ok = (u & 1) ? step(std::integral_constant<int, 1>{}, u, gy2a)
-                     : step(std::integral_constant<int, 0>{}, u, gy2b);
+        ok = (u & 1) ? step(std::integral_constant<int, 1>{}, u)
+                     : step(std::integral_constant<int, 0>{}, u);
     if (!ok && threadIdx.x == 0) {
         for (int s = lo; s < lo + P.nbuf && s < P.steps; ++s)
             tape_wait(P, X, ring, s % P.nbuf, (uint32_t)(((P.steps - 1 - s) / P.nbuf) & 1));
@@ -1506,7 +1527,12 @@ int wt_fused_plan(int nx, int ny, int steps, int n_prb, int cluster_req, int seg
         L->smem_tape = tiles + aux_bwd + (size_t)L->nbuf * (slice + 8);
         L->smem_fwd_tape = tiles + aux_fwd;
         L->smem_bwd_base = tiles + aux_bwd;
-        const int nfit = 2 * slice < (1u << 20) ? (int)((SMEM_MAX - tiles - aux_bwd) / (2 * slice + 8)) : 0;
+        // the nonlinear adjoint keeps its cells' b_pml, c_lin, rho in shared
+        // memory before the ring
+        L->smem_nl_coef = r16((size_t)wt::nl_coef_stride(M) * L->threads * sizeof(float));
+        const size_t nl_room = SMEM_MAX - tiles - aux_bwd;
+        const int nfit = 2 * slice < (1u << 20) && nl_room > L->smem_nl_coef
+                             ? (int)((nl_room - L->smem_nl_coef) / (2 * slice + 8)) : 0;
         L->nbuf_nl = std::min(8, nfit);
         if (L->smem_fwd_tape > SMEM_MAX || L->threads > wt::fwd_max_threads(M)) L->nbuf = 0;
         return 0;
@@ -1684,7 +1710,8 @@ static int launch_nl(bool fwd, const wt::FusedParams& P0, const WtFusedLaunch& L
     P.R = L.R;
     P.LD = L.LD;
     if (fwd) return launch_kernel(wt::seq_fwd_nl_kernel<M, ORDER>, P, L.C, L.threads, L.smem_fwd_tape, st);
-    const size_t smem = L.smem_bwd_base + (size_t)P.nbuf * (2 * (size_t)L.threads * M * sizeof(float) + 8);
+    const size_t smem = L.smem_bwd_base + L.smem_nl_coef +
+                        (size_t)P.nbuf * (2 * (size_t)L.threads * M * sizeof(float) + 8);
     return launch_kernel(wt::seq_bwd_nl_kernel<M, ORDER>, P, L.C, L.threads, smem, st);
 }
 
