@@ -956,6 +956,20 @@ WT_DEV void adj_cell_pp(float lg, float lam, float Ly, float X1, float Kc, float
     g2 = fmul(Ky2, lam);
 }
 
+// adj_cell with lambda formed one step ahead: lam enters as this step's
+// (seeded) lambda and leaves as the next step's, fadd(grad_y2 term of the
+// step after this one, this step's grad_y1 term) in autograd's order; pend
+// carries this step's grad_y2 term one step.  Same operations as adj_cell_pp
+// followed by the next step's sum.
+WT_DEV void adj_cell_lp(float lg, float& lam, float Ly, float X1, float Kc, float Ky2, float dt2,
+                        float& acc, float& pend) {
+    acc = fadd(acc, fmul(fmul(X1, fmul(Kc, Ly)), lam));
+    const float gy1 = fadd(fmul(dt2, lg), fmul(fmul(2.0f, lam), X1));
+    const float g2 = fmul(Ky2, lam);
+    lam = fadd(pend, gy1);
+    pend = g2;
+}
+
 template <int M, int ORDER>
 __global__ void __launch_bounds__(bwd_max_threads(M), 1) seq_bwd_fused_kernel(FusedParams P) {
     extern __shared__ __align__(16) float smem[];
@@ -1154,9 +1168,11 @@ __global__ void __launch_bounds__(bwd_max_threads(M), 1) seq_bwd_tape_kernel(Fus
 
     float X1[M], Kc[M], Kg[M], Ky2[M];
     load_bwd_coef<M>(P, g, X1, Kc, Kg, Ky2);
-    float gy1[M], gy2a[M], gy2b[M], acc[M];
+    // adjoint state: lam (this step's lambda before its seeds), pend (the
+    // grad_y2 term of the previous step), the running dL/dc
+    float lam[M], pend[M], acc[M];
 #pragma unroll
-    for (int i = 0; i < M; ++i) gy1[i] = gy2a[i] = gy2b[i] = acc[i] = 0.f;
+    for (int i = 0; i < M; ++i) lam[i] = pend[i] = acc[i] = 0.f;
     stage_seeds(P, g, seeds, 0);
     cluster_sync_all();   // zeroed tiles, ring and halo words; barriers initialised
 
@@ -1174,25 +1190,26 @@ __global__ void __launch_bounds__(bwd_max_threads(M), 1) seq_bwd_tape_kernel(Fus
     uint32_t phase = 0;
     int pk = 0, pc = 0;
     bool ok = true;
-    // One adjoint step; g2 holds the grad_y2 term written two steps ago and
-    // receives this step's (the two arrays alternate, so nothing is copied).
-    auto step = [&](int u, float (&g2)[M]) -> bool {
+    const Lane ln = make_lane(P, g, X);
+    // One adjoint step on the precomputed addresses; exchange u uses tile
+    // slot and word parity PAR = u & 1.
+    auto step = [&](auto par, int u) -> bool {
+        constexpr int PAR = decltype(par)::value;
         const int t = P.steps - 1 - u;
-        float lam[M], c2g[M];
-#pragma unroll
-        for (int i = 0; i < M; ++i) {
-            lam[i] = fadd(g2[i], gy1[i]);
-            c2g[i] = 0.f;
-        }
+        float* col = ln.col0 + PAR * ln.tile;
+        float c2g[M];
         if (pk == 0 && u + P.PB < P.steps)   // next chunk, a barrier ahead of use
             stage_seeds(P, g, seeds, pc + 1);
         if (g.colv) {
             if (tp.np || (P.grad_x && tp.ns))
-                seed_and_read<M>(P, g, X, tp, u & 1, t, lam,
+                seed_and_read<M>(P, g, X, tp, PAR, t, lam,
                                  seeds + (size_t)(pc & 1) * P.n_prb * P.PB + pk);
 #pragma unroll
             for (int i = 0; i < M; ++i) c2g[i] = fmul(Kg[i], lam[i]);
-            publish<M>(P, g, X, u & 1, u, c2g);
+            const unsigned long long tag = (unsigned long long)(uint32_t)(u + 1) << 32;
+            if (ln.sup) st_cluster_u64(ln.sup + PAR * ln.pstride, tag | __float_as_uint(c2g[0]));
+            if (ln.sdn) st_cluster_u64(ln.sdn + PAR * ln.pstride, tag | __float_as_uint(c2g[M - 1]));
+            sts_col<M>(col, c2g);
         }
         if (!exchange_end(X, u)) return false;
         // step t+1's slice was read before this barrier: refill its slot
@@ -1203,28 +1220,32 @@ __global__ void __launch_bounds__(bwd_max_threads(M), 1) seq_bwd_tape_kernel(Fus
         }
         if (g.colv) {
             Column<M> c;
-            load_sides<M>(c, P, g, X, u & 1, -1);   // interior first; halo words below
+            lds_col<M>(c.lf, col - P.LD);
+            lds_col<M>(c.rt, col + P.LD);
+            c.up = col[-1];
+            c.dn = col[M];
             tape_wait(P, X, ring, slot, (phase >> slot) & 1u);
             phase ^= 1u << slot;
             float Ly[M];
             ld_chunks<M>(Ly, ring.buf + (size_t)slot * ring.slice, blockDim.x, threadIdx.x);
 #pragma unroll
             for (int i = 1; i < M - 1; ++i)
-                adj_cell_pp(lap_cell<M, ORDER>(P, c, c2g, i), lam[i], Ly[i], X1[i], Kc[i], Ky2[i],
-                            P.k.dt2, acc[i], gy1[i], g2[i]);
-            if (g.strip == 0 && g.has_up) c.up = recv_word(P, X, X.hup + (u & 1) * X.NCP + g.col, u);
-            if (g.strip == g.S - 1 && g.has_dn)
-                c.dn = recv_word(P, X, X.hdn + (u & 1) * X.NCP + g.col, u);
-            adj_cell_pp(lap_cell<M, ORDER>(P, c, c2g, 0), lam[0], Ly[0], X1[0], Kc[0], Ky2[0],
-                        P.k.dt2, acc[0], gy1[0], g2[0]);
-            adj_cell_pp(lap_cell<M, ORDER>(P, c, c2g, M - 1), lam[M - 1], Ly[M - 1], X1[M - 1],
-                        Kc[M - 1], Ky2[M - 1], P.k.dt2, acc[M - 1], gy1[M - 1], g2[M - 1]);
+                adj_cell_lp(lap_cell<M, ORDER>(P, c, c2g, i), lam[i], Ly[i], X1[i], Kc[i], Ky2[i],
+                            P.k.dt2, acc[i], pend[i]);
+            if (ln.rup) c.up = recv_at(P, X, ln.rup + PAR * ln.pstride, u);
+            if (ln.rdn) c.dn = recv_at(P, X, ln.rdn + PAR * ln.pstride, u);
+            adj_cell_lp(lap_cell<M, ORDER>(P, c, c2g, 0), lam[0], Ly[0], X1[0], Kc[0], Ky2[0],
+                        P.k.dt2, acc[0], pend[0]);
+            adj_cell_lp(lap_cell<M, ORDER>(P, c, c2g, M - 1), lam[M - 1], Ly[M - 1], X1[M - 1],
+                        Kc[M - 1], Ky2[M - 1], P.k.dt2, acc[M - 1], pend[M - 1]);
         }
         slot = slot == 0 ? P.nbuf - 1 : slot - 1;
         if (++pk == P.PB) { pk = 0; ++pc; }
         return true;
     };
-    for (int u = 0; u < P.steps && ok; ++u) ok = (u & 1) ? step(u, gy2a) : step(u, gy2b);
+    for (int u = 0; u < P.steps && ok; ++u)
+        ok = (u & 1) ? step(std::integral_constant<int, 1>{}, u)
+                     : step(std::integral_constant<int, 0>{}, u);
     if (!ok && threadIdx.x == 0) {
         // leaving early: let the copies still in flight land first (the last
         // nbuf issued steps hold one copy per slot, step s in slot s % nbuf
