@@ -394,6 +394,7 @@ def run_ours(args):
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
         cpu = cpu_baseline(sample_T=WORKLOAD["steps"])
+    parity = parity_vs_reference(dev) if rank == 0 else None
 
     if rank == 0:
         line = {
@@ -421,6 +422,7 @@ def run_ours(args):
             "cpu_baseline": cpu,
             "plain_form": plain,
             "fused_loss": fused_loss,
+            "parity": parity,
             "clocks": clk.summary(),
             "gpu_launches": int(launches),
         }
@@ -430,6 +432,55 @@ def run_ours(args):
 
 
 # ---------------------------------------------------------------------------
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "tests", "golden")
+
+
+def parity_vs_reference(dev):
+    """Rel. L2 of our probe outputs, loss and dL/drho against the reference's
+    own results on the committed fixtures (made by running the reference in
+    float32 and, for the configuration-0 case, float64): configuration-0
+    physics (B=1, 100x100, T=200) and configuration-1 physics at a reduced
+    size (B=4, 120x120, T=150), fused and plain forms."""
+    import numpy as np
+    import torch
+    import wavetorch_gb300 as wt
+
+    def rel(a, b):
+        a, b = np.asarray(a, np.float64), np.asarray(b, np.float64)
+        return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+
+    res = {}
+    for name in ("cfg0_small", "cfg1_small"):
+        path = os.path.join(GOLDEN, name + ".npz")
+        if not os.path.exists(path):
+            continue
+        d = np.load(path)
+        N = int(d["N"])
+        for form in ("fused", "plain"):
+            geom = wt.WaveGeometryFreeForm((N, N), 1.0, c0=1.0, c1=0.5, abs_N=int(d["abs_N"]),
+                                           abs_sig=3.0, abs_p=2, rho=torch.from_numpy(d["rho"]))
+            srcs = [wt.WaveSource(int(cc) // N, int(cc) % N) for cc, _ in d["sources"]]
+            prbs = [(wt.WaveIntensityProbe if k else wt.WaveProbe)(int(cc) // N, int(cc) % N)
+                    for cc, k, _ in d["probes"]]
+            m = wt.WaveRNN(wt.WaveCell(0.707, geom), srcs, prbs, form=form).to(dev)
+            y = m(torch.from_numpy(d["x"]).to(dev))
+            loss = torch.nn.CrossEntropyLoss()(wt.utils.normalize_power(y.sum(dim=1)),
+                                               torch.from_numpy(d["labels"]).to(dev))
+            loss.backward()
+            out = y.detach().cpu().numpy()
+            g = m.cell.geom.rho.grad.cpu().numpy()
+            r = {"out_vs_ref_fp32": rel(out, d["out"]),
+                 "loss_vs_ref_fp32": rel(loss.item(), float(d["loss"])),
+                 "grad_rho_vs_ref_fp32": rel(g, d["grad_rho"])}
+            if "out64" in d.files:
+                r["out_vs_ref_fp64"] = rel(out, d["out64"])
+                r["grad_rho_vs_ref_fp64"] = rel(g, d["grad_rho64"])
+                r["ref_fp32_out_vs_ref_fp64"] = rel(d["out"], d["out64"])
+                r["ref_fp32_grad_rho_vs_ref_fp64"] = rel(d["grad_rho"], d["grad_rho64"])
+            res[f"{name}/{form}"] = r
+    return res
+
+
 def cpu_baseline(sample_T: int, batch: int = WORKLOAD["batch"]):
     """The oracle port (plain C, OpenMP over all host threads) on a bounded
     sample of the workload: the full batch and grid, the first sample_T steps."""
