@@ -161,6 +161,14 @@ def test_band_layout_plan(lib):
     assert status(sm_count=-1) == _lib.WT_ERR_INVALID
     # several strips per band when bands of one strip would need too many SMs
     assert status(nx=300, ny=300, sources=[(61, -1)], probes=[(70, 1, 0)], sm_count=20) == _lib.WT_OK
+    # cluster -1 asks for bands where a cluster would hold the grid; below -1 invalid
+    small = dict(nx=120, ny=120, sources=[(20 * 120 + 60, -1)], probes=[(80 * 120 + 50, 1, 0)])
+    assert status(cluster=-1, sm_count=16, **small) == _lib.WT_OK
+    assert status(cluster=-1, sm_count=16, segment=-2, **small) == U
+    assert status(cluster=-2, **small) == _lib.WT_ERR_INVALID
+    sz = lambda **kw: seq_workspace_bytes(SeqSpec(1, 120, 120, T, [(20 * 120 + 60, -1)],
+                                                  [(80 * 120 + 50, 1, 0)], **kw))
+    assert sz(cluster=-1, sm_count=16) != sz(sm_count=16)   # a different layout
 
 
 def test_fused_adjoint_modes(lib):

@@ -33,12 +33,13 @@ def problem(nx, ny, B, T, seed, abs_N=8, batched=False):
     return b, c, x
 
 
-def check(cuda, nx, ny, B, T, src, prb, seed=0, sm_count=0, grad_x=False, batched=False):
+def check(cuda, nx, ny, B, T, src, prb, seed=0, sm_count=0, grad_x=False, batched=False,
+          cluster=0):
     b, c, x = problem(nx, ny, B, T, seed, batched=batched)
     g = np.random.default_rng(seed + 1).standard_normal((B, T, len(prb))).astype(np.float32)
     order = lap_order(B, nx, ny, 1.0)
     spec = SeqSpec(B, nx, ny, T, src, prb, form=_lib.WT_FORM_FUSED, sm_count=sm_count,
-                   coef_batched=batched)
+                   coef_batched=batched, cluster=cluster)
     assert fused_supported(spec)
     sc = scalars(0.707, 1.0, order)
     tb, tc, tx = (torch.from_numpy(v).to(cuda) for v in (b, c, x))
@@ -102,6 +103,15 @@ def test_several_strips_per_band(cuda):
     src = [(40 * N + 150, -1), (40 * N + 151, -1)]
     prb = [(15 * N + 150, 1, 0), (16 * N + 149, 1, 1), (31 * N + 152, 0, 2), (100 * N + 150, 1, 3)]
     check(cuda, N, N, 1, 90, src, prb, sm_count=20)
+
+
+def test_bands_requested_for_a_cluster_sized_grid(cuda):
+    """cluster = -1 runs a grid one cluster would hold in bands (here 120 x 120,
+    two instances on 16 SMs: bands of several strips), with the same results."""
+    N = 120
+    src = [(20 * N + 60, -1)]
+    prb = [(80 * N + y, 1, k) for k, y in enumerate((35, 50, 65))]
+    check(cuda, N, N, 2, 150, src, prb, sm_count=16, cluster=-1)
 
 
 def test_input_gradient_and_per_instance_geometry(cuda):
