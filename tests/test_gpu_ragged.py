@@ -7,6 +7,7 @@ import pytest
 import torch
 
 import wavetorch_gb300 as wt
+from wavetorch_gb300 import _lib
 from wavetorch_gb300.data import vowel_like
 from wavetorch_gb300.ragged import RaggedBatch
 
@@ -45,6 +46,7 @@ def _check_against_alone(cuda, rb, models, inputs, labels):
     for _ in range(2):                       # replays are repeatable
         losses = rb.step().clone()
     torch.cuda.synchronize()
+    assert rb.device_status() == _lib.WT_OK
     grads = [m.cell.geom.rho.grad.clone() for m in models]
     for i, m in enumerate(models):
         m.cell.geom.rho.grad = None
@@ -63,9 +65,11 @@ def test_ragged_step_matches_models_run_alone(cuda, graph):
     _check_against_alone(cuda, rb, models, inputs, labels)
 
 
-def test_ragged_groups_in_band_layout(cuda):
+@pytest.mark.parametrize("graph", [False, True])
+def test_ragged_groups_in_band_layout(cuda, graph):
     """Groups of the larger grids run in the band layout (at most 12 CTAs
-    per instance): same losses and gradients as the models run alone."""
+    per instance, cooperative launches, captured in the step's CUDA graph
+    too): same losses and gradients as the models run alone."""
     models, inputs, labels = _ragged_case(cuda)
     rb = RaggedBatch(models, inputs, labels, graph=False, autotune=False)
     banded = 0
@@ -74,4 +78,6 @@ def test_ragged_groups_in_band_layout(cuda):
             grp.spec.cluster, grp.spec.sm_count = -1, 12 * len(grp.idx)
             banded += 1
     assert banded == 2
+    if graph:
+        rb._capture()
     _check_against_alone(cuda, rb, models, inputs, labels)

@@ -55,6 +55,7 @@ class _Group:
     onehot: torch.Tensor            # [G, P]
     work: List[torch.Tensor] = field(default_factory=list)   # rho -> c scratch per instance
     stream: Optional[torch.cuda.Stream] = None
+    ws: Optional[torch.Tensor] = None   # the sequence workspace of the last step
 
 
 def _option_spec(opt: tuple, G: int) -> tuple:
@@ -228,6 +229,7 @@ class RaggedBatch:
                                                    _ptr(geom.blur_kernel[0, 0]), _ptr(grp.c[j]),
                                                    _ptr(grp.work[j]), st), "wt_rho_to_c_fwd")
                 out, _, _, ws = seq_forward(grp.spec, grp.sc, grp.b, grp.c, grp.x)
+                grp.ws = ws
                 # loss = CE(normalize_power(sum over the instance's own steps))
                 I = (out * grp.mask).sum(dim=1)                     # [G, P]
                 S = I.sum(dim=1, keepdim=True)
@@ -265,6 +267,17 @@ class RaggedBatch:
         self.graph = torch.cuda.CUDAGraph()
         with torch.cuda.graph(self.graph):
             self.losses = self._run()
+
+    def device_status(self) -> int:
+        """The sequence kernels' status words of the last step (synchronises):
+        WT_OK, or WT_ERR_TIMEOUT when a bounded wait gave up."""
+        from .functional import seq_device_status
+        worst = _lib.WT_OK
+        for grp in self.groups:
+            if grp.ws is not None:
+                st = seq_device_status(grp.spec, grp.ws)
+                worst = st if st != _lib.WT_OK else worst
+        return worst
 
     def step(self) -> torch.Tensor:
         """One training step of every model; returns the losses [n_models]."""
