@@ -165,7 +165,7 @@ class RaggedBatch:
             spec = SeqSpec(G, N, N, T, src, prb, form=_lib.WT_FORM_FUSED, segment=segment,
                            coef_batched=True)
             if not fused_supported(spec):
-                raise ValueError(f"a {N}x{N} grid is too large for the fused form")
+                raise ValueError(f"the fused form does not plan a {N}x{N} grid")
             # each model is an instance of its own: the Laplacian order of a batch of one
             sc = scalars(dt, h, lap_order(1, N, N, h))
             lab = torch.as_tensor([int(labels[i]) for i in idx], device=dev)

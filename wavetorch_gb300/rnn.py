@@ -3,9 +3,11 @@
 For the reference's own source and probe types and a linear cell, the whole
 loop is one :class:`~wavetorch_gb300.functional.WaveSeqFn` call:
 
-* ``form='fused'`` (default): persistent cluster kernels, sqrt(T)-style
-  checkpoints and segment recompute in the adjoint; grids too large for one
-  thread-block cluster run in the plain form instead;
+* ``form='fused'`` (default): persistent kernels -- one thread-block cluster
+  per instance (grids up to 256x256), the adjoint from a Laplacian tape or
+  from checkpoints with segment recompute; larger grids (up to 1024 columns)
+  in bands of rows, one CTA per band and SM; shapes neither layout plans run
+  in the plain form instead.  ``cluster`` fixes the cluster size (-1: bands);
 * ``form='plain'``: one forward kernel per step with every field kept, and one
   adjoint kernel per step -- the reference's dataflow, bit-exact with it;
 * ``form='step'``: the reference's Python loop structure, each step a
@@ -139,7 +141,7 @@ class WaveRNN(torch.nn.Module):
                        form=_FORMS[form if form in _FORMS else "fused"], segment=self.segment,
                        cluster=self.cluster, output_fields=fields_out)
         if spec.form == _lib.WT_FORM_FUSED and not fused_supported(spec):
-            spec.form = _lib.WT_FORM_PLAIN   # instance too large for one cluster
+            spec.form = _lib.WT_FORM_PLAIN   # neither fused layout plans this shape
         b = geom.b
         out = WaveSeqFn.apply(c, b, x.contiguous(), spec, sc)
         if fields_out:
