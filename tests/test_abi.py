@@ -159,6 +159,8 @@ def test_band_layout_plan(lib):
     assert status(sources=[(60 * N + 5, -1), (61 * N + 5, -1), (62 * N + 5, -1)]) == U
     assert status(sources=[(60 * N + 5, -1), (61 * N + 5, -1)]) == _lib.WT_OK
     assert status(sm_count=-1) == _lib.WT_ERR_INVALID
+    many = [((900 + k // 1000) * N + k % 1000, 1, k) for k in range(1024)]
+    assert status(probes=many) == U                  # probe columns beyond the tap words
     # several strips per band when bands of one strip would need too many SMs
     assert status(nx=300, ny=300, sources=[(61, -1)], probes=[(70, 1, 0)], sm_count=20) == _lib.WT_OK
     # cluster -1 asks for bands where a cluster would hold the grid; below -1 invalid

@@ -618,6 +618,7 @@ int wt_band_plan(int batch, int nx, int ny, int n_prb, int n_sm, WtBandLaunch* L
     if (batch <= 0 || nx <= 0 || ny <= 0 || n_sm <= 0 || !L) return WT_ERR_INVALID;
     const int NCP = ((ny + 31) / 32) * 32;
     if (NCP > wt::band::MAX_THREADS) return WT_ERR_UNSUPPORTED;
+    if (n_prb >= 1024) return WT_ERR_UNSUPPORTED;   // probe columns beyond the tap words
     const size_t SMEM_MAX = 227 * 1024 - 64;
     const int PB = n_prb > 0 ? std::max(1, std::min(32, 2048 / n_prb)) : 32;
     auto r16 = [](size_t v) { return (v + 15) / 16 * 16; };
