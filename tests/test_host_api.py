@@ -170,3 +170,14 @@ def test_ragged_cluster_choice():
     assert pick_cluster_sizes([(small, 10.0, 1), ({16: 0.5}, 1.0, 1)], 152) == [8, 16]
     # a group of 40 instances at size 2 already fills the machine's SM-time bound
     assert pick_cluster_sizes([(small, 1.0, 40)], 80) == [2]
+
+
+def test_ragged_layout_choice_with_band_options():
+    """Options may be (cluster, bands) pairs: a band option with at most p
+    CTAs per model counts p SMs per model; the least SM-time wins."""
+    from wavetorch_gb300.ragged import _option_spec, pick_cluster_sizes
+    big = {(16, 0): 2.0, (-1, 8): 2.9, (-1, 12): 2.2}      # SM-times 32, 23.2, 26.4
+    assert pick_cluster_sizes([(big, 1.0, 1)] * 100, 152) == [(-1, 8)] * 100
+    # alone on the machine it would set the step: the fastest option instead
+    assert pick_cluster_sizes([(big, 1.0, 1)], 152) == [(16, 0)]
+    assert _option_spec((-1, 8), 3) == (-1, 24) and _option_spec((4, 0), 3) == (4, 0)
