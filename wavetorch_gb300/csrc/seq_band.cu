@@ -222,6 +222,14 @@ WT_DEV void build_taps(const FusedParams& P, const Geo& g, Taps& tp) {
 template <int M, int K>
 __host__ __device__ constexpr int coef_stride() { return (K * M) | 1; }
 
+// v added to cell i of y, where i is a per-thread value: one select per cell
+// (neither a runtime register index nor a round trip through shared memory
+// on the owning warp, which would pace its band).
+template <int M>
+WT_DEV void add_at(float (&y)[M], int i, float v) {
+#pragma unroll
+    for (int k = 0; k < M; ++k) y[k] = (k == i) ? fadd(y[k], v) : y[k];
+}
 WT_DEV void zero_smem(float* s, int n) {
     for (int i = threadIdx.x; i < n; i += blockDim.x) s[i] = 0.f;
 }
@@ -326,14 +334,10 @@ WT_DEV void fwd_step(const FusedParams& P, const Geo& g, const Lane& ln, const T
     }
 #pragma unroll
     for (int i = 1; i < M - 1; ++i) update(i, cur[i - 1], cur[i + 1]);
-#pragma unroll
-    for (int i = 0; i < M; ++i) wcol[i] = inout[i];
-    if (tp.ns()) {   // sources in table order, through the column (no register indexing)
+    if (tp.ns()) {   // sources in table order
 #pragma unroll
         for (int e = 0; e < SRCMAX; ++e)
-            if (e < tp.ns()) wcol[tp.src_i(e)] = fadd(wcol[tp.src_i(e)], xv[e]);
-#pragma unroll
-        for (int i = 0; i < M; ++i) inout[i] = wcol[i];
+            if (e < tp.ns()) add_at<M>(inout, tp.src_i(e), xv[e]);
         if (more) {
 #pragma unroll
             for (int e = 0; e < SRCMAX; ++e)
@@ -344,6 +348,8 @@ WT_DEV void fwd_step(const FusedParams& P, const Geo& g, const Lane& ln, const T
             }
         }
     }
+#pragma unroll
+    for (int i = 0; i < M; ++i) wcol[i] = inout[i];
     if (tp.np()) {
         float* row = pr.buf + (size_t)pb * P.n_prb * P.PB + pc;
 #pragma unroll
@@ -514,7 +520,9 @@ __global__ void __launch_bounds__(MAX_THREADS, 1) seq_bwd_band_kernel(FusedParam
         if (g.colv) {
             if (tp.np() || (P.grad_x && tp.ns())) {
                 // seeds at their cells and dL/dx at the source, through the
-                // thread's column of the slot it is about to publish into
+                // thread's column of the slot it is about to publish into (a
+                // select per cell would hold more registers than this kernel
+                // has to spare)
 #pragma unroll
                 for (int i = 0; i < M; ++i) col[i] = lam[i];
                 const float* sr = seeds + (size_t)(pcn & 1) * P.n_prb * P.PB + pk;

@@ -417,25 +417,30 @@ WT_DEV void load_bwd_coef(const FusedParams& P, const Geo& g, float (&X1)[M], fl
 }
 
 
-// The thread's own column of tile slot `slot` (its M cells).
+
+// v added to cell i of y, where i is a per-thread value: one select per cell
+// (a runtime register index costs a jump per step on the owning warp, and a
+// round trip through shared memory made that warp pace its whole cluster).
 template <int M>
-WT_DEV float* own_column(const FusedParams& P, const Geo& g, const Xchg& X, int slot) {
-    return X.tiles + slot * X.tile + (g.col + 1) * P.LD + OFF + g.xl0;
+WT_DEV void add_at(float (&y)[M], int i, float v) {
+#pragma unroll
+    for (int k = 0; k < M; ++k) y[k] = (k == i) ? fadd(y[k], v) : y[k];
+}
+template <int M>
+WT_DEV float value_at(const float (&y)[M], int i) {
+    float v = 0.f;
+#pragma unroll
+    for (int k = 0; k < M; ++k) v = (k == i) ? y[k] : v;
+    return v;
 }
 
-// Sources (in table order) with the inputs prefetched one step ahead.  A
-// source's cell index varies by thread, and indexing registers by a runtime
-// value costs a jump per step on the warp that owns the source; so the
-// injection goes through the thread's column of the tile (already stored):
-// add there, then reload the column into registers.
+// Sources (in table order) with the inputs prefetched one step ahead.
 template <int M>
-WT_DEV void apply_sources(const FusedParams& P, const Geo& g, const Xchg& X, const Taps& tp,
-                          int slot, float (&y)[M], float (&xv)[SRCMAX], int tnext) {
-    float* colp = own_column<M>(P, g, X, slot);
+WT_DEV void apply_sources(const FusedParams& P, const Taps& tp, float (&y)[M], float (&xv)[SRCMAX],
+                          int tnext) {
 #pragma unroll
     for (int e = 0; e < SRCMAX; ++e)
-        if (e < tp.ns) colp[tp.src_i(e)] = fadd(colp[tp.src_i(e)], xv[e]);
-    lds_col<M>(y, colp);
+        if (e < tp.ns) add_at<M>(y, tp.src_i(e), xv[e]);
     if (tnext >= 0 && tnext < P.steps) {
 #pragma unroll
         for (int e = 0; e < SRCMAX; ++e)
@@ -469,11 +474,11 @@ WT_DEV void fwd_update(const FusedParams& P, const Geo& g, const Xchg& X, const 
         L[i] = lap_cell<M, ORDER>(P, c, cur, i);
         inout[i] = leapfrog(A[i], Bc[i], C2[i], P.k.two_over, cur[i], inout[i], L[i]);
     }
-    store_column<M>(P, g, X, ws, inout);
     if (tp.ns) {
-        apply_sources<M>(P, g, X, tp, ws, inout, xv, tnext);
+        apply_sources<M>(P, tp, inout, xv, tnext);
         if (ks >= 0 && tp.src_edge) send_halo(g, X, ks, inout[0], inout[M - 1]);
     }
+    store_column<M>(P, g, X, ws, inout);
 }
 
 // Field-dependent coefficients of the nonlinear cell, in the reference's
@@ -544,14 +549,14 @@ WT_DEV void fwd_update_lane(const FusedParams& P, const Geo& g, const Xchg& X, c
     }
 #pragma unroll
     for (int i = 1; i < M - 1; ++i) update(i);
-    sts_col<M>(wcol, inout);
     if (tp.ns) {
-        apply_sources<M>(P, g, X, tp, RS ^ 1, inout, xv, t + 1);
+        apply_sources<M>(P, tp, inout, xv, t + 1);
         if (send && tp.src_edge) {
             if (ln.sup) st_cluster_u64(ln.sup + RS * ln.pstride, tag | __float_as_uint(inout[0]));
             if (ln.sdn) st_cluster_u64(ln.sdn + RS * ln.pstride, tag | __float_as_uint(inout[M - 1]));
         }
     }
+    sts_col<M>(wcol, inout);
 }
 
 struct FwdState {
@@ -913,27 +918,18 @@ WT_DEV void stage_seeds(const FusedParams& P, const Geo& g, float* seeds, int c)
 }
 
 // Probe seeds into lam (descending reference order) and dL/dx at the
-// source, for the few threads that own such cells.  The cells' indices vary by
-// thread, so instead of indexing registers by a runtime value the thread
-// passes lam through its own column of the tile slot it is about to publish
-// into (that column has no readers until the publish): store, add the seeds
-// at their cells, read dL/dx, reload.
+// source, for the few threads that own such cells, in registers (add_at).
 template <int M>
-WT_DEV void seed_and_read(const FusedParams& P, const Geo& g, const Xchg& X, const Taps& tp,
-                          int slot, int t, float (&lam)[M], const float* sr) {
-    float* colp = own_column<M>(P, g, X, slot);
-    sts_col<M>(colp, lam);
-    if (tp.np) {
+WT_DEV void seed_and_read(const FusedParams& P, const Geo& g, const Taps& tp, int t,
+                          float (&lam)[M], const float* sr) {
 #pragma unroll
-        for (int e = 0; e < PRBMAX; ++e)
-            if (e < tp.np) colp[tp.prb_i(e)] = fadd(colp[tp.prb_i(e)], sr[tp.prb_col(e) * P.PB]);
-        lds_col<M>(lam, colp);
-    }
+    for (int e = 0; e < PRBMAX; ++e)
+        if (e < tp.np) add_at<M>(lam, tp.prb_i(e), sr[tp.prb_col(e) * P.PB]);
     if (P.grad_x && tp.ns) {
 #pragma unroll
         for (int e = 0; e < SRCMAX; ++e)
             if (e < tp.ns && tp.src_row(e) == g.inst)
-                P.grad_x[(size_t)g.inst * P.steps + t] = colp[tp.src_i(e)];
+                P.grad_x[(size_t)g.inst * P.steps + t] = value_at<M>(lam, tp.src_i(e));
     }
 }
 
@@ -1063,7 +1059,7 @@ __global__ void __launch_bounds__(bwd_max_threads(M), 1) seq_bwd_fused_kernel(Fu
                 stage_seeds(P, g, seeds, u / P.PB + 1);
             if (g.colv) {
                 if (tp.np || (P.grad_x && tp.ns))
-                    seed_and_read<M>(P, g, X, tp, kx & 1, t, lam,
+                    seed_and_read<M>(P, g, tp, t, lam,
                                      seeds + (size_t)((u / P.PB) & 1) * P.n_prb * P.PB + u % P.PB);
 #pragma unroll
                 for (int i = 0; i < M; ++i) c2g[i] = fmul(Kg[i], lam[i]);
@@ -1202,8 +1198,7 @@ __global__ void __launch_bounds__(bwd_max_threads(M), 1) seq_bwd_tape_kernel(Fus
             stage_seeds(P, g, seeds, pc + 1);
         if (g.colv) {
             if (tp.np || (P.grad_x && tp.ns))
-                seed_and_read<M>(P, g, X, tp, PAR, t, lam,
-                                 seeds + (size_t)(pc & 1) * P.n_prb * P.PB + pk);
+                seed_and_read<M>(P, g, tp, t, lam, seeds + (size_t)(pc & 1) * P.n_prb * P.PB + pk);
 #pragma unroll
             for (int i = 0; i < M; ++i) c2g[i] = fmul(Kg[i], lam[i]);
             const unsigned long long tag = (unsigned long long)(uint32_t)(u + 1) << 32;
@@ -1386,7 +1381,7 @@ __global__ void __launch_bounds__(bwd_max_threads(M), 1) seq_bwd_nl_kernel(Fused
             float h1[M];
             ld_chunks_at<M>(h1, sl + part + lane_off, stride);
             if (tp.np || (P.grad_x && tp.ns))
-                seed_and_read<M>(P, g, X, tp, PAR, t, lam, seeds + (size_t)(pc & 1) * P.n_prb * P.PB + pk);
+                seed_and_read<M>(P, g, tp, t, lam, seeds + (size_t)(pc & 1) * P.n_prb * P.PB + pk);
             float c2g[M];
 #pragma unroll
             for (int i = 0; i < M; ++i) {
