@@ -11,8 +11,10 @@
 // the M cells (strip*M .. strip*M + M-1, col) and keeps their fields (forward)
 // or adjoint state (adjoint) in registers; its neighbours' columns come from a
 // double-buffered column-major tile in shared memory, one __syncthreads per
-// step.  The per-cell update coefficients are in shared memory, laid out
-// [coefficient][cell i][thread] (a warp reads 32 consecutive words).
+// step.  The per-cell update coefficients are in shared memory, each
+// thread's words at constant offsets (stride rounded up to odd: a warp's
+// access to one word hits 32 banks); warps whose cells all have b = 0 use the
+// reference's b = 0 values as constants instead.
 //
 // Exchange between bands.  A band's first and last rows travel through
 // global memory as 64-bit words {float bits, tag = exchange index + 1},
@@ -22,8 +24,8 @@
 // atomic: the value is valid whenever the tag is).  Double buffering by parity
 // is enough: a band writes parity p for exchange k+2 only after it received
 // exchange k+1 from its neighbour, whose same thread sent that after reading
-// exchange k.  Each step computes the cells that need no halo value first, so
-// the halo's trip through L2 overlaps them.
+// exchange k.  Each step computes and sends a strip's end cells first and
+// its interior after, so the halo's trip through L2 overlaps the interior.
 //
 // Waits are bounded (2 s, %globaltimer).  A wait that gives up records
 // WT_DEVERR_TIMEOUT and raises a launch-wide abort word, which every waiting
