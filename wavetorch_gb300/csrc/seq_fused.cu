@@ -943,20 +943,12 @@ WT_DEV void adj_cell(float lg, float lam, float Ly, float X1, float Kc, float Ky
     gy2a = fmul(Ky2, lam);
 }
 
-// adj_cell with the two pending grad_y2 terms in alternating arrays: g2 holds
-// the term of two steps ago on entry and this step's term on exit.
-WT_DEV void adj_cell_pp(float lg, float lam, float Ly, float X1, float Kc, float Ky2, float dt2,
-                        float& acc, float& gy1, float& g2) {
-    acc = fadd(acc, fmul(fmul(X1, fmul(Kc, Ly)), lam));
-    gy1 = fadd(fmul(dt2, lg), fmul(fmul(2.0f, lam), X1));
-    g2 = fmul(Ky2, lam);
-}
-
 // adj_cell with lambda formed one step ahead: lam enters as this step's
 // (seeded) lambda and leaves as the next step's, fadd(grad_y2 term of the
 // step after this one, this step's grad_y1 term) in autograd's order; pend
-// carries this step's grad_y2 term one step.  Same operations as adj_cell_pp
-// followed by the next step's sum.
+// carries this step's grad_y2 term one step.  Same operations as adj_cell
+// followed by the next step's sum (which the checkpoint kernel forms at the
+// start of that step).
 WT_DEV void adj_cell_lp(float lg, float& lam, float Ly, float X1, float Kc, float Ky2, float dt2,
                         float& acc, float& pend) {
     acc = fadd(acc, fmul(fmul(X1, fmul(Kc, Ly)), lam));
