@@ -181,3 +181,20 @@ def test_ragged_layout_choice_with_band_options():
     # alone on the machine it would set the step: the fastest option instead
     assert pick_cluster_sizes([(big, 1.0, 1)], 152) == [(16, 0)]
     assert _option_spec((-1, 8), 3) == (-1, 24) and _option_spec((4, 0), 3) == (4, 0)
+
+
+def test_save_load_roundtrip_hole_geometry(tmp_path):
+    """A model on a hole geometry round-trips through the model file: the
+    geometry class is rebuilt by name from its reconstruction arguments
+    (holes' centres and radii, eta, beta), as in the reference's io."""
+    geom = wt.WaveGeometryHoley((48, 40), 1.0, c0=1.0, c1=0.5, abs_N=8, abs_sig=3.0, abs_p=2,
+                                x=[20.5, 30.25], y=[10.5, 25.75], r=[3.0, 4.5])
+    m = wt.WaveRNN(wt.WaveCell(0.707, geom), wt.WaveSource(10, 20),
+                   [wt.WaveIntensityProbe(38, 20)])
+    wt.io.save_model(m, "h", savedir=str(tmp_path) + "/", cfg={"dtype": "float32"}, verbose=False)
+    m2, _, _, _ = wt.io.load_model(str(tmp_path / "h.pt"))
+    g2 = m2.cell.geom
+    assert isinstance(g2, wt.WaveGeometryHoley)
+    for name in ("x", "y", "r"):
+        assert torch.equal(getattr(g2, name), getattr(geom, name)), name
+    assert torch.equal(g2.rho, geom.rho) and torch.equal(g2.c, geom.c)
