@@ -319,6 +319,38 @@ int wt_holey_bwd(const wt_holey_desc* d, const float* x, const float* y, const f
 /* Bytes of `work` the two calls above need. */
 int wt_holey_work_bytes(const wt_holey_desc* d, size_t* bytes);
 
+/* ======================================================================== *
+ * 5. Ragged batches: the layout of each group of a batch of models.         *
+ *    No counterpart in the reference, which trains one model at a time.     *
+ * ======================================================================== */
+
+/* One layout option of a group, with its measured time.                    */
+typedef struct wt_ragged_option {
+    int32_t cluster;    /* wt_seq_desc.cluster of the option (> 0, or -1: bands) */
+    int32_t ctas;       /* SMs one instance occupies (the cluster size, or the
+                           band layout's limit per instance)                 */
+    double seconds;     /* the group's measured run with this option         */
+} wt_ragged_option;
+
+/* One group of a ragged batch: `instances` models of one grid, run side by
+ * side in one launch.                                                       */
+typedef struct wt_ragged_group {
+    int32_t instances;
+    double scale;                       /* measured run -> full step count  */
+    int32_t n_options;
+    const wt_ragged_option* options;    /* host array                       */
+} wt_ragged_group;
+
+/* Pick one option per group (choice[g]: an index into group g's options).
+ * The groups run concurrently and share the GPU's n_sm SMs, so the choice
+ * minimises SM-time (instances x ctas x seconds x scale; ties: fewer CTAs,
+ * then the earlier option); the step then takes at least max(total SM-time /
+ * n_sm, the longest group's time).  While the longest group's time is above
+ * that SM-time bound, it moves to a faster option (of those, the least
+ * SM-time; ties: the slower).  Host only; deterministic.                   */
+int wt_ragged_plan(const wt_ragged_group* groups, int32_t n_groups, int32_t n_sm,
+                   int32_t* choice);
+
 #ifdef __cplusplus
 }
 #endif

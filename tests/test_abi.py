@@ -223,3 +223,20 @@ def test_geom_work_bytes(lib):
     n = C.c_size_t(0)
     assert lib.wt_rho_to_c_work_bytes(C.byref(g), C.byref(n)) == 0
     assert n.value == 2 * 10 * 12 * 4
+
+
+def test_ragged_plan_validates_arguments(lib):
+    """wt_ragged_plan: no SMs, a group without options or instances, or a
+    negative time is an invalid argument; an empty batch is fine."""
+    from wavetorch_gb300 import _lib
+    opt = (_lib.RaggedOption * 1)(_lib.RaggedOption(4, 4, 1.0))
+    grp = (_lib.RaggedGroup * 1)(_lib.RaggedGroup(1, 1.0, 1, C.cast(opt, C.POINTER(_lib.RaggedOption))))
+    out = (C.c_int32 * 1)()
+    assert lib.wt_ragged_plan(grp, 1, 152, out) == _lib.WT_OK and out[0] == 0
+    assert lib.wt_ragged_plan(grp, 1, 0, out) == _lib.WT_ERR_INVALID
+    assert lib.wt_ragged_plan(grp, 0, 152, out) == _lib.WT_OK
+    bad = (_lib.RaggedGroup * 1)(_lib.RaggedGroup(0, 1.0, 1, C.cast(opt, C.POINTER(_lib.RaggedOption))))
+    assert lib.wt_ragged_plan(bad, 1, 152, out) == _lib.WT_ERR_INVALID
+    neg = (_lib.RaggedOption * 1)(_lib.RaggedOption(4, 4, -1.0))
+    grp2 = (_lib.RaggedGroup * 1)(_lib.RaggedGroup(1, 1.0, 1, C.cast(neg, C.POINTER(_lib.RaggedOption))))
+    assert lib.wt_ragged_plan(grp2, 1, 152, out) == _lib.WT_ERR_INVALID

@@ -33,6 +33,7 @@ EXPORTED = [
     "wt_seq_workspace_bytes_nl", "wt_seq_fwd_nl", "wt_seq_bwd_nl",
     "wt_rho_to_c_fwd", "wt_rho_to_c_bwd", "wt_rho_to_c_work_bytes", "wt_rho_to_c_fwd_noalloc",
     "wt_holey_fwd", "wt_holey_bwd", "wt_holey_work_bytes",
+    "wt_ragged_plan",
 ]
 
 
@@ -80,6 +81,15 @@ class HoleyDesc(C.Structure):
     ]
 
 
+class RaggedOption(C.Structure):
+    _fields_ = [("cluster", C.c_int32), ("ctas", C.c_int32), ("seconds", C.c_double)]
+
+
+class RaggedGroup(C.Structure):
+    _fields_ = [("instances", C.c_int32), ("scale", C.c_double), ("n_options", C.c_int32),
+                ("options", C.POINTER(RaggedOption))]
+
+
 _VP = C.c_void_p
 _lock = threading.Lock()
 _lib = None
@@ -118,6 +128,7 @@ def _declare(lib):
     lib.wt_holey_fwd.argtypes = [P(HoleyDesc), _VP, _VP, _VP, _VP, _VP, _VP, _VP]
     lib.wt_holey_bwd.argtypes = [P(HoleyDesc)] + [_VP] * 10
     lib.wt_holey_work_bytes.argtypes = [P(HoleyDesc), P(C.c_size_t)]
+    lib.wt_ragged_plan.argtypes = [P(RaggedGroup), C.c_int32, C.c_int32, P(C.c_int32)]
     for name in EXPORTED:
         if name not in ("wt_version", "wt_status_string", "wt_last_error", "wt_kernel_launches"):
             getattr(lib, name).restype = C.c_int

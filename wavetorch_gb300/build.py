@@ -18,7 +18,7 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB_NAME = "libwavetorch_gb300.so"
 LIB_PATH = os.path.join(HERE, LIB_NAME)
-SOURCES = ["api.cu", "step.cu", "seq_fused.cu", "seq_band.cu", "geom.cu", "holey.cu"]
+SOURCES = ["api.cu", "step.cu", "seq_fused.cu", "seq_band.cu", "geom.cu", "holey.cu", "ragged.cu"]
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = [

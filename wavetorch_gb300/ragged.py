@@ -75,33 +75,30 @@ def _option_sms(opt) -> int:
 
 
 def pick_cluster_sizes(timings: Sequence[tuple], n_sm: int) -> List:
-    """Layout option per group from measured times.
+    """Layout option per group from measured times (the library's
+    wt_ragged_plan).
 
     timings: per group (times, scale, G): times maps a layout option (a
     cluster size, or a (cluster, bands) pair) -> seconds of the group's
     measured run (its G instances side by side), scale the factor to the
     group's full step count.  An option using c SMs per instance occupies
-    G x c SMs for the group's time t(c).  Start from the size with the
-    least SM-time (c x t(c)); the step then takes at least max(total SM-time /
-    n_sm, the longest group's time).  While the longest group's time is above
-    the SM-time bound, move it to a faster size (the one of least SM-time
-    among the faster ones): the groups run concurrently, so only the longest
-    one can set the step time."""
-    S = _option_sms
-    groups = []
+    G x c SMs for the group's time.  The choice minimises SM-time unless the
+    group alone would outlast the batch (see wt_ragged_plan)."""
+    keep, groups, order = [], [], []
     for times, scale, G in timings:
-        opts = sorted(times, key=lambda o: (S(o), str(o)))
-        groups.append((opts, {o: times[o] * scale for o in opts}, G))
-    pick = [min(opts, key=lambda o: (S(o) * t[o], S(o))) for opts, t, _ in groups]
-    for _ in range(4 * len(groups) + 1):
-        bound = sum(G * S(o) * t[o] for o, (_, t, G) in zip(pick, groups)) / max(n_sm, 1)
-        k = max(range(len(groups)), key=lambda j: groups[j][1][pick[j]])
-        opts, t, _ = groups[k]
-        faster = [o for o in opts if t[o] < t[pick[k]]]
-        if t[pick[k]] <= bound or not faster:
-            break
-        pick[k] = min(faster, key=lambda o: (S(o) * t[o], -t[o]))
-    return pick
+        opts = sorted(times, key=lambda o: (_option_sms(o), str(o)))
+        arr = (_lib.RaggedOption * len(opts))(*[
+            _lib.RaggedOption(o[0] if isinstance(o, tuple) else int(o), _option_sms(o),
+                              float(times[o])) for o in opts])
+        keep.append(arr)
+        order.append(opts)
+        groups.append(_lib.RaggedGroup(int(G), float(scale), len(opts),
+                                       C.cast(arr, C.POINTER(_lib.RaggedOption))))
+    n = len(groups)
+    garr = (_lib.RaggedGroup * max(n, 1))(*groups)
+    choice = (C.c_int32 * max(n, 1))()
+    _lib.check(_lib.load().wt_ragged_plan(garr, n, int(n_sm), choice), "wt_ragged_plan")
+    return [order[g][choice[g]] for g in range(n)]
 
 
 def _check_model(m) -> None:
