@@ -84,6 +84,18 @@ def test_lens_grid_line_source(cuda):
     check(cuda, N, N, 1, T, src, prb)
 
 
+def test_sources_and_probes_on_strip_and_band_edges(cuda):
+    """1024 x 512, two instances on 152 SMs: 74 bands of 14 rows, each two
+    strips of 7 rows (1024 threads).  Sources on row 63 (a band's second
+    strip, first row), 69 (the band's last row) and 70 (the next band's first
+    row): those strips pass their edge values on after the injection.  Probes
+    on the rows where strips and bands meet."""
+    N, W, T = 1024, 512, 40
+    src = [(63 * W + 200, -1), (69 * W + 201, -1), (70 * W + 300, 1)]
+    prb = [(56 * W + 200, 1, 0), (62 * W + 201, 1, 1), (70 * W + 301, 0, 2), (84 * W + 300, 1, 3)]
+    check(cuda, N, W, 2, T, src, prb, sm_count=152)
+
+
 @pytest.mark.parametrize("nx,ny,B", [(301, 530, 1), (301, 530, 2), (24, 600, 1), (160, 1000, 1)])
 def test_ragged_edges(cuda, nx, ny, B):
     """Rows not a multiple of the band height (padding rows in the last band),
