@@ -88,23 +88,88 @@ def barrier(world: int, device=None):
 
 
 class ClockSampler:
-    """nvidia-smi clock / throttle samples taken while the timed region runs."""
+    """SM clock and clock-event (throttle) reasons sampled while the timed
+    region runs: every 2 ms through NVML (the driver's libnvidia-ml, read-only
+    queries), else from nvidia-smi at 100 ms.  The sampler is running before
+    __enter__ returns, so the samples cover the region even when it lasts only
+    a few tens of milliseconds."""
     Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
          "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
          "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+    # nvmlClocksEventReasons bits reported (the rest: idle, application or
+    # display clock settings, sync boost)
+    NVML_REASONS = {0x4: "sw_power_cap", 0x8: "hw_slowdown", 0x20: "sw_thermal_slowdown",
+                    0x40: "hw_thermal_slowdown", 0x80: "hw_power_brake_slowdown"}
+    PERIOD_S = 0.002
 
     def __init__(self, index: int):
         self.index = index
         self.proc = None
         self.lines = []
+        self.samples = []        # NVML: (sm MHz, reason bits)
+        self.max_mhz = None
+        self.source = None
+        self._stop = threading.Event()
+        self._thread = None
+
+    def _nvml_handle(self):
+        import ctypes
+        nv = ctypes.CDLL("libnvidia-ml.so.1")
+        if nv.nvmlInit_v2() != 0:
+            raise OSError("nvmlInit failed")
+        h = ctypes.c_void_p()
+        ok = False
+        try:
+            import torch
+            uuid = str(torch.cuda.get_device_properties(self.index).uuid)
+            ok = nv.nvmlDeviceGetHandleByUUID(("GPU-" + uuid).encode(), ctypes.byref(h)) == 0
+        except Exception:
+            ok = False
+        if not ok:
+            vis = os.environ.get("CUDA_VISIBLE_DEVICES", "").split(",")
+            idx = int(vis[self.index]) if vis[0].strip().isdigit() else self.index
+            if nv.nvmlDeviceGetHandleByIndex_v2(idx, ctypes.byref(h)) != 0:
+                raise OSError("no NVML handle for the device")
+        get_reasons = getattr(nv, "nvmlDeviceGetCurrentClocksEventReasons", None) or \
+            nv.nvmlDeviceGetCurrentClocksThrottleReasons
+        mx = ctypes.c_uint()
+        if nv.nvmlDeviceGetMaxClockInfo(h, 1, ctypes.byref(mx)) == 0:   # NVML_CLOCK_SM
+            self.max_mhz = float(mx.value)
+        return nv, h, get_reasons
+
+    def _nvml_loop(self, nv, h, get_reasons):
+        import ctypes
+        clk, rs = ctypes.c_uint(), ctypes.c_ulonglong()
+        while True:
+            if nv.nvmlDeviceGetClockInfo(h, 1, ctypes.byref(clk)) == 0 and \
+                    get_reasons(h, ctypes.byref(rs)) == 0:
+                self.samples.append((float(clk.value), int(rs.value)))
+            if self._stop.wait(self.PERIOD_S):
+                return
 
     def __enter__(self):
         try:
+            nv, h, get_reasons = self._nvml_handle()
+            self.source = "nvml"
+            self._thread = threading.Thread(target=self._nvml_loop, args=(nv, h, get_reasons),
+                                            daemon=True)
+            self._thread.start()
+            t0 = time.perf_counter()
+            while not self.samples and time.perf_counter() - t0 < 1.0:
+                time.sleep(self.PERIOD_S)
+            return self
+        except (OSError, AttributeError, ValueError, IndexError):
+            self.source = None
+        try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
-                 "--format=csv,noheader,nounits", "-lms", "200"],
+                 "--format=csv,noheader,nounits", "-lms", "100"],
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.source = "nvidia-smi"
             threading.Thread(target=self._read, daemon=True).start()
+            t0 = time.perf_counter()
+            while not self.lines and time.perf_counter() - t0 < 3.0:
+                time.sleep(0.01)
         except (OSError, FileNotFoundError):
             self.proc = None
         return self
@@ -114,6 +179,9 @@ class ClockSampler:
             self.lines.append(line.strip())
 
     def __exit__(self, *a):
+        if self._thread is not None:
+            self._stop.set()
+            self._thread.join(timeout=5)
         if self.proc is not None:
             self.proc.terminate()
             try:
@@ -122,6 +190,14 @@ class ClockSampler:
                 self.proc.kill()
 
     def summary(self):
+        if self.samples:
+            sm = [c for c, _ in self.samples]
+            bits = 0
+            for _, r in self.samples:
+                bits |= r
+            reasons = sorted(n for b, n in self.NVML_REASONS.items() if bits & b)
+            return {"sm_mhz": statistics.median(sm), "sm_max_mhz": self.max_mhz or max(sm),
+                    "reasons": reasons, "samples": len(sm), "source": "nvml, every 2 ms"}
         if not self.lines:
             return None
         sm, mx, reasons = [], [], set()
@@ -141,7 +217,7 @@ class ClockSampler:
         if not sm:
             return None
         return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
-                "samples": len(sm)}
+                "samples": len(sm), "source": "nvidia-smi, every 100 ms"}
 
 
 def measured_peaks():
