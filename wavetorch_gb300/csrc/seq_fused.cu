@@ -1179,6 +1179,14 @@ __global__ void __launch_bounds__(bwd_max_threads(M), 1) seq_bwd_tape_kernel(Fus
     int pk = 0, pc = 0;
     bool ok = true;
     const Lane ln = make_lane(P, g, X);
+    const bool issuer = threadIdx.x == 0;
+    const bool taps_here = tp.np || (P.grad_x && tp.ns);   // seeds to add / dL/dx to read
+    // this thread's chunk 0 in the slot of the current step (kept
+    // incrementally), and the chunk stride of a slice
+    constexpr int V = chunk_width<M>();
+    const int cstride = (int)blockDim.x * V;
+    const float* ly_top = ring.buf + (size_t)(P.nbuf - 1) * ring.slice + (size_t)threadIdx.x * V;
+    const float* ly = ly_top - (size_t)(P.nbuf - 1 - slot) * ring.slice;
     // One adjoint step on the precomputed addresses; exchange u uses tile
     // slot and word parity PAR = u & 1.
     auto step = [&](auto par, int u) -> bool {
@@ -1189,7 +1197,7 @@ __global__ void __launch_bounds__(bwd_max_threads(M), 1) seq_bwd_tape_kernel(Fus
         if (pk == 0 && u + P.PB < P.steps)   // next chunk, a barrier ahead of use
             stage_seeds(P, g, seeds, pc + 1);
         if (g.colv) {
-            if (tp.np || (P.grad_x && tp.ns))
+            if (taps_here)
                 seed_and_read<M>(P, g, tp, t, lam, seeds + (size_t)(pc & 1) * P.n_prb * P.PB + pk);
 #pragma unroll
             for (int i = 0; i < M; ++i) c2g[i] = fmul(Kg[i], lam[i]);
@@ -1200,7 +1208,7 @@ __global__ void __launch_bounds__(bwd_max_threads(M), 1) seq_bwd_tape_kernel(Fus
         }
         if (!exchange_end(X, u)) return false;
         // step t+1's slice was read before this barrier: refill its slot
-        if (threadIdx.x == 0 && u > 0 && t + 1 - P.nbuf >= 0) {
+        if (issuer && u > 0 && t + 1 - P.nbuf >= 0) {
             fence_proxy_async_smem();
             lo = t + 1 - P.nbuf;
             tape_issue(P, g, ring, lo, slot + 1 == P.nbuf ? 0 : slot + 1);
@@ -1214,7 +1222,7 @@ __global__ void __launch_bounds__(bwd_max_threads(M), 1) seq_bwd_tape_kernel(Fus
             tape_wait(P, X, ring, slot, (phase >> slot) & 1u);
             phase ^= 1u << slot;
             float Ly[M];
-            ld_chunks<M>(Ly, ring.buf + (size_t)slot * ring.slice, blockDim.x, threadIdx.x);
+            ld_chunks_at<M>(Ly, ly, cstride);
 #pragma unroll
             for (int i = 1; i < M - 1; ++i)
                 adj_cell_lp(lap_cell<M, ORDER>(P, c, c2g, i), lam[i], Ly[i], X1[i], Kc[i], Ky2[i],
@@ -1226,13 +1234,16 @@ __global__ void __launch_bounds__(bwd_max_threads(M), 1) seq_bwd_tape_kernel(Fus
             adj_cell_lp(lap_cell<M, ORDER>(P, c, c2g, M - 1), lam[M - 1], Ly[M - 1], X1[M - 1],
                         Kc[M - 1], Ky2[M - 1], P.k.dt2, acc[M - 1], pend[M - 1]);
         }
-        slot = slot == 0 ? P.nbuf - 1 : slot - 1;
+        if (slot == 0) { slot = P.nbuf - 1; ly = ly_top; }
+        else           { --slot; ly -= ring.slice; }
         if (++pk == P.PB) { pk = 0; ++pc; }
         return true;
     };
-    for (int u = 0; u < P.steps && ok; ++u)
-        ok = (u & 1) ? step(std::integral_constant<int, 1>{}, u)
-                     : step(std::integral_constant<int, 0>{}, u);
+    // two steps per iteration: the exchange parity is fixed in each
+    for (int u = 0; u < P.steps && ok; u += 2) {
+        ok = step(std::integral_constant<int, 0>{}, u);
+        if (ok && u + 1 < P.steps) ok = step(std::integral_constant<int, 1>{}, u + 1);
+    }
     if (!ok && threadIdx.x == 0) {
         // leaving early: let the copies still in flight land first (the last
         // nbuf issued steps hold one copy per slot, step s in slot s % nbuf
