@@ -512,7 +512,7 @@ GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "tests", "gold
 
 
 def parity_vs_reference(dev):
-    """Rel. L2 of our probe outputs, loss and dL/drho against the reference's
+    """Rel. L2 of our probe outputs, fields, loss and dL/drho against the reference's
     own results on the committed fixtures (made by running the reference in
     float32 and, for the configuration-0 case, float64): configuration-0
     physics (B=1, 100x100, T=200) and configuration-1 physics at a reduced
@@ -545,13 +545,24 @@ def parity_vs_reference(dev):
             loss.backward()
             out = y.detach().cpu().numpy()
             g = m.cell.geom.rho.grad.cpu().numpy()
+            # field snapshots the fixture holds (steps named field_<t>)
+            snaps = sorted(int(k.split("_")[1]) for k in d.files if k.startswith("field_"))
+            with torch.no_grad():
+                f = m(torch.from_numpy(d["x"]).to(dev), output_fields=True)
+            f = np.stack([f[:, t].cpu().numpy() for t in snaps])
+            f32 = np.stack([d[f"field_{t}"] for t in snaps])
             r = {"out_vs_ref_fp32": rel(out, d["out"]),
+                 "fields_vs_ref_fp32": rel(f, f32),
                  "loss_vs_ref_fp32": rel(loss.item(), float(d["loss"])),
-                 "grad_rho_vs_ref_fp32": rel(g, d["grad_rho"])}
+                 "grad_rho_vs_ref_fp32": rel(g, d["grad_rho"]),
+                 "field_steps": snaps}
             if "out64" in d.files:
+                f64 = np.stack([d[f"field64_{t}"] for t in snaps])
                 r["out_vs_ref_fp64"] = rel(out, d["out64"])
+                r["fields_vs_ref_fp64"] = rel(f, f64)
                 r["grad_rho_vs_ref_fp64"] = rel(g, d["grad_rho64"])
                 r["ref_fp32_out_vs_ref_fp64"] = rel(d["out"], d["out64"])
+                r["ref_fp32_fields_vs_ref_fp64"] = rel(f32, f64)
                 r["ref_fp32_grad_rho_vs_ref_fp64"] = rel(d["grad_rho"], d["grad_rho64"])
             res[f"{name}/{form}"] = r
     return res

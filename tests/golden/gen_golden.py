@@ -89,12 +89,13 @@ def case_cfg0(wt):
     r32 = run_model(wt, field_steps=(0, 99, T - 1), **kw)
     wt.utils.set_dtype('float64')
     try:
-        r64 = run_model(wt, dtype=torch.float64, **kw)
+        r64 = run_model(wt, dtype=torch.float64, field_steps=(0, 99, T - 1), **kw)
     finally:
         wt.utils.set_dtype('float32')
     res = dict(r32)
     res.update({"x": x, "labels": labels, "out64": r64["out"], "grad_c64": r64["grad_c"],
                 "grad_rho64": r64["grad_rho"], "c64": r64["c"]})
+    res.update({f"field64_{t}": r64[f"field_{t}"] for t in (0, 99, T - 1)})
     res.update(meta(N=N, T=T, B=1, abs_N=20, sources=[(20 * N + 50, -1)],
                     probes=[(80 * N + y, 1, i) for i, y in enumerate((35, 50, 65))]))
     return as32(res)

@@ -86,6 +86,9 @@ def test_fp32_vs_fp64_floor():
     d = golden("cfg0_small")
     assert rel(d["out"], d["out64"]) < 1e-4
     assert rel(d["grad_rho"], d["grad_rho64"]) < 1e-4
+    for t in (99, 199):
+        assert rel(d[f"field_{t}"], d[f"field64_{t}"]) < 1e-4
+    assert not d["field64_0"].any()       # x_0 = sin(0): nothing injected yet
 
 
 @pytest.mark.parametrize("name", ["fd64_linear", "fd64_nonlinear"])
