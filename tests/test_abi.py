@@ -217,6 +217,45 @@ def test_step_entry_points_validate_before_touching_the_device(lib):
     assert lib.wt_step_fwd(C.byref(sc), 1, 8, 8, 0, p, p, p, p, p, None) == _lib.WT_ERR_INVALID  # y aliases y1
 
 
+def test_other_entry_points_validate_before_touching_the_device(lib):
+    """Every compute entry point refuses missing buffers, a too-small
+    workspace or bad descriptors with WT_ERR_INVALID before any device work
+    (all buffer arguments here are NULL, so nothing can reach a device)."""
+    from wavetorch_gb300 import _lib
+    INV = _lib.WT_ERR_INVALID
+    sc = _lib.Scalars(0.707, 1.0, 0)
+    for form in (0, 1):
+        d, keep = _desc(form=form)
+        assert lib.wt_seq_fwd(C.byref(sc), C.byref(d), *([None] * 7), 0, None) == INV
+        assert lib.wt_seq_bwd(C.byref(sc), C.byref(d), *([None] * 7), 0, None) == INV
+        assert lib.wt_seq_device_status(C.byref(d), None, 0, None) == INV
+    bad = _lib.Scalars(0.0, 1.0, 0)
+    d, keep = _desc(form=1)
+    assert lib.wt_seq_fwd(C.byref(bad), C.byref(d), *([None] * 7), 0, None) == INV
+    assert lib.wt_seq_bwd_sum(C.byref(sc), C.byref(d), *([None] * 6), 0, None) == INV
+    d0, keep0 = _desc(form=0)    # the probe-sum adjoint exists only in the fused form
+    assert lib.wt_seq_bwd_sum(C.byref(sc), C.byref(d0), *([None] * 6), 0, None) == \
+        _lib.WT_ERR_UNSUPPORTED
+    nl = _lib.NonLinear(0.05, 0.3, 0.1)
+    assert lib.wt_seq_fwd_nl(C.byref(sc), C.byref(d), C.byref(nl), *([None] * 7), 0, None) == INV
+    assert lib.wt_seq_bwd_nl(C.byref(sc), C.byref(d), C.byref(nl), *([None] * 9), 0, None) == INV
+    assert lib.wt_loss_ce_normalize_power(0, 3, None, None, None, None, None) == INV
+    assert lib.wt_loss_ce_normalize_power(2, 3, None, None, None, None, None) == INV
+    g = _lib.GeomDesc(10, 12, 1, 1, 0.5, 100.0, 1.0, 0.5)
+    assert lib.wt_rho_to_c_fwd(C.byref(g), None, None, None, None, None) == INV
+    assert lib.wt_rho_to_c_bwd(C.byref(g), None, None, None, None, None, None) == INV
+    assert lib.wt_rho_to_c_fwd_noalloc(C.byref(g), None, None, None, None) == INV
+    gbad = _lib.GeomDesc(0, 12, 1, 1, 0.5, 100.0, 1.0, 0.5)
+    n = C.c_size_t(0)
+    assert lib.wt_rho_to_c_work_bytes(C.byref(gbad), C.byref(n)) == INV
+    h = _lib.HoleyDesc(64, 48, 3, 0.5, 100.0, 1.0, 0.5)
+    assert lib.wt_holey_fwd(C.byref(h), *([None] * 7)) == INV
+    assert lib.wt_holey_bwd(C.byref(h), *([None] * 10)) == INV
+    assert lib.wt_holey_work_bytes(C.byref(h), None) == INV
+    hbad = _lib.HoleyDesc(64, 0, 3, 0.5, 100.0, 1.0, 0.5)
+    assert lib.wt_holey_work_bytes(C.byref(hbad), C.byref(n)) == INV
+
+
 def test_geom_work_bytes(lib):
     from wavetorch_gb300 import _lib
     g = _lib.GeomDesc(10, 12, 1, 1, 0.5, 100.0, 1.0, 0.5)
