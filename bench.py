@@ -52,9 +52,12 @@ def parse():
     p.add_argument("--T", type=int, default=WORKLOAD["steps"])
     p.add_argument("--kernels-only", action="store_true",
                    help="run only the sequence kernels (forward + adjoint) -- the profiling case")
-    p.add_argument("--workload", choices=["batched", "ragged", "nonlinear", "lens"], default="batched",
+    p.add_argument("--workload", choices=["batched", "ragged", "nonlinear", "lens", "fields"],
+                   default="batched",
                    help="ragged: many models of different grid sizes / step counts in one graph; "
-                        "nonlinear: B=64, 120x120, T=5000 with saturable damping and Kerr term")
+                        "nonlinear: B=64, 120x120, T=5000 with saturable damping and Kerr term; "
+                        "lens: 1024x1024, T=8000; fields: the benchmark's forward with every "
+                        "field written")
     p.add_argument("--instances", type=int, default=256, help="models in the ragged workload")
     return p.parse_args()
 
@@ -908,8 +911,72 @@ def run_lens(args):
         print(json.dumps(line), flush=True)
 
 
+def run_fields(args):
+    """Field streaming (WaveRNN.forward(x, output_fields=True), the reference's
+    rnn.py:59-67): the benchmark's model and inputs (B=32, 120x120, T=3500),
+    forward only, every field [B, T, 120, 120] written to HBM (6.45 GB).  The
+    fused kernel writes each step's fields straight from registers; the plain
+    form computes its field history and copies it out.  Both results are
+    compared bit for bit."""
+    import torch
+    world, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    B, T, N = args.batch, args.T, WORKLOAD["nx"]
+    field_bytes = 4 * B * T * N * N
+    peak, peak_src = measured_peaks()
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
+
+    def timed(form, steps, warmup):
+        model, x_np, _ = build_model(dev, B, T, seed=1234, form=form)
+        x = torch.from_numpy(x_np).to(dev)
+        stream = torch.cuda.current_stream(dev)
+        with torch.no_grad():
+            for _ in range(warmup):
+                model(x, output_fields=True)
+            torch.cuda.synchronize(dev)
+            ts = []
+            for _ in range(steps):
+                flush.zero_()
+                e = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+                e[0].record(stream)
+                f = model(x, output_fields=True)
+                e[1].record(stream)
+                torch.cuda.synchronize(dev)
+                ts.append(e[0].elapsed_time(e[1]) / 1e3)
+        return statistics.mean(ts), f
+
+    with ClockSampler(local) as clk:
+        t, f_fused = timed("fused", args.steps, args.warmup)
+    line = {
+        "metric": "cell-steps/s forward with every field written (output_fields), fused form",
+        "value": B * N * N * T / t, "unit": "cell-steps/s", "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": t * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "fp32",
+        "data": "synthetic (seeded vowel-like waveforms, random-init rho)",
+        "config": {"workload": f"field streaming: B={B}, {N}x{N} (PML 20), T={T}, forward only, "
+                               "fields [B, T, N, N] written to HBM",
+                   "l2": "flushed (512 MiB write) before every timed step; output 6.45 GB"},
+        "fields_GBps": field_bytes / t / 1e9,
+        "fields_frac_of_hbm_peak": field_bytes / t / 1e9 / peak,
+        "peak_source": f"hbm_gbs of {peak_src}",
+        "clocks": clk.summary(),
+    }
+    if not args.no_plain:
+        t_plain, f_plain = timed("plain", 1, 1)
+        line["plain_form"] = {"ms_per_step": t_plain * 1e3,
+                              "cell_steps_per_s": B * N * N * T / t_plain,
+                              "fused_over_plain": t_plain / t,
+                              "fields_bit_identical": bool(torch.equal(f_fused, f_plain))}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
+    if args.workload == "fields" and args.impl == "ours":
+        run_fields(args)
+        return
     if args.workload == "lens" and args.impl == "ours":
         run_lens(args)
         return

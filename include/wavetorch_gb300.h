@@ -152,8 +152,9 @@ typedef struct wt_seq_desc {
  *       recompute.
  *   >0  checkpoints every `segment` steps; the adjoint recomputes each
  *       segment's forward (workspace ~ 2 fields per segment).
- *    0  automatic: the tape when it takes at most 16 GiB, else checkpoints at
- *       the largest interval whose recompute stash fits in shared memory.
+ *    0  automatic: the tape when it takes at most 16 GiB and output_fields
+ *       is 0, else checkpoints at the largest interval whose recompute stash
+ *       fits in shared memory.
  *   -2  checkpoints at that automatic interval (never the tape).
  * Both modes give identical results.  The plain form ignores it.            */
 

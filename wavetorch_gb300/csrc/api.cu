@@ -234,8 +234,11 @@ int make_plan(const wt_seq_desc* d, SeqPlan* p, bool nl = false) {
             P.L.nbuf = P.L.nbuf_nl;
             P.tape = true;
         } else {
+            // automatic mode: no tape next to field outputs (the caller
+            // already receives every field; checkpoints cost 2/seg of them)
             P.tape = P.L.nbuf >= 2 &&
-                     (d->segment == -1 || (d->segment == 0 && tape_bytes <= WT_TAPE_AUTO_MAX_BYTES));
+                     (d->segment == -1 || (d->segment == 0 && !d->output_fields &&
+                                           tape_bytes <= WT_TAPE_AUTO_MAX_BYTES));
         }
         if (d->segment == -1 && !P.tape) return WT_ERR_UNSUPPORTED;
         if (P.tape) {
