@@ -19,6 +19,7 @@ Prints ONE JSON line (rank 0).
 from __future__ import annotations
 
 import argparse
+import contextlib
 import json
 import os
 import statistics
@@ -52,12 +53,12 @@ def parse():
     p.add_argument("--T", type=int, default=WORKLOAD["steps"])
     p.add_argument("--kernels-only", action="store_true",
                    help="run only the sequence kernels (forward + adjoint) -- the profiling case")
-    p.add_argument("--workload", choices=["batched", "ragged", "nonlinear", "lens", "fields"],
+    p.add_argument("--workload", choices=["batched", "ragged", "nonlinear", "lens", "fields", "holey"],
                    default="batched",
                    help="ragged: many models of different grid sizes / step counts in one graph; "
                         "nonlinear: B=64, 120x120, T=5000 with saturable damping and Kerr term; "
                         "lens: 1024x1024, T=8000; fields: the benchmark's forward with every "
-                        "field written")
+                        "field written; holey: the benchmark's step through 16 holes")
     p.add_argument("--instances", type=int, default=256, help="models in the ragged workload")
     return p.parse_args()
 
@@ -797,7 +798,7 @@ def run_nonlinear(args):
         x, lab = vowel_like(B, steps, seed=7 + rank)
         return m, torch.from_numpy(x * np.float32(0.2)).to(dev), torch.from_numpy(lab).to(dev)
 
-    def timed(form, steps, reps, warm):
+    def timed(form, steps, reps, warm, clk=None):
         m, x, lab = make(form, steps)
         flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
         stream = torch.cuda.current_stream(dev)
@@ -805,18 +806,19 @@ def run_nonlinear(args):
             train_step(m, x, lab)
         torch.cuda.synchronize(dev)
         ts = []
-        for _ in range(reps):
-            flush.zero_()
-            e = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
-            e[0].record(stream)
-            train_step(m, x, lab)
-            e[1].record(stream)
-            torch.cuda.synchronize(dev)
-            ts.append(e[0].elapsed_time(e[1]) / 1e3)
+        with clk or contextlib.nullcontext():
+            for _ in range(reps):
+                flush.zero_()
+                e = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+                e[0].record(stream)
+                train_step(m, x, lab)
+                e[1].record(stream)
+                torch.cuda.synchronize(dev)
+                ts.append(e[0].elapsed_time(e[1]) / 1e3)
         return statistics.mean(ts)
 
-    with ClockSampler(local) as clk:
-        t_fused = timed("fused", T, args.steps, args.warmup)
+    clk = ClockSampler(local)
+    t_fused = timed("fused", T, args.steps, args.warmup, clk)
     t_step = timed("step", 200, 2, 1)
     value = B * N * N * T / t_fused
     step_rate = B * N * N * 200 / t_step
@@ -871,18 +873,19 @@ def run_lens(args):
         torch.cuda.synchronize(dev)
         stream = torch.cuda.current_stream(dev)
         ts = []
-        for _ in range(steps):
-            e = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
-            e[0].record(stream)
-            step()
-            e[1].record(stream)
-            torch.cuda.synchronize(dev)
-            ts.append(e[0].elapsed_time(e[1]) / 1e3)
+        with clk or contextlib.nullcontext():
+            for _ in range(steps):
+                e = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+                e[0].record(stream)
+                step()
+                e[1].record(stream)
+                torch.cuda.synchronize(dev)
+                ts.append(e[0].elapsed_time(e[1]) / 1e3)
         return statistics.mean(ts), model.cell.geom.rho.grad.clone()
 
     fused = make("fused")
-    with ClockSampler(local) as clk:
-        t, g_fused = timed(fused, args.steps, args.warmup)
+    clk = ClockSampler(local)
+    t, g_fused = timed(fused, args.steps, args.warmup, clk)
     del fused
     torch.cuda.empty_cache()
     t_plain, g_plain = timed(make("plain"), 1, 1) if not args.no_plain else (None, None)
@@ -927,7 +930,7 @@ def run_fields(args):
     peak, peak_src = measured_peaks()
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
 
-    def timed(form, steps, warmup):
+    def timed(form, steps, warmup, clk=None):
         model, x_np, _ = build_model(dev, B, T, seed=1234, form=form)
         x = torch.from_numpy(x_np).to(dev)
         stream = torch.cuda.current_stream(dev)
@@ -936,18 +939,19 @@ def run_fields(args):
                 model(x, output_fields=True)
             torch.cuda.synchronize(dev)
             ts = []
-            for _ in range(steps):
-                flush.zero_()
-                e = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
-                e[0].record(stream)
-                f = model(x, output_fields=True)
-                e[1].record(stream)
-                torch.cuda.synchronize(dev)
-                ts.append(e[0].elapsed_time(e[1]) / 1e3)
+            with clk or contextlib.nullcontext():
+                for _ in range(steps):
+                    flush.zero_()
+                    e = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+                    e[0].record(stream)
+                    f = model(x, output_fields=True)
+                    e[1].record(stream)
+                    torch.cuda.synchronize(dev)
+                    ts.append(e[0].elapsed_time(e[1]) / 1e3)
         return statistics.mean(ts), f
 
-    with ClockSampler(local) as clk:
-        t, f_fused = timed("fused", args.steps, args.warmup)
+    clk = ClockSampler(local)
+    t, f_fused = timed("fused", args.steps, args.warmup, clk)
     line = {
         "metric": "cell-steps/s forward with every field written (output_fields), fused form",
         "value": B * N * N * T / t, "unit": "cell-steps/s", "n_gpus": 1, "steps": args.steps,
@@ -972,8 +976,95 @@ def run_fields(args):
         print(json.dumps(line), flush=True)
 
 
+def run_holey(args):
+    """Training step through the hole geometry (wavetorch/geom.py:88-132): the
+    benchmark's model and inputs (B=32, 120x120, T=3500) with c from 16 holes
+    (seeded centres in the design region, radii 2..6) instead of the
+    free-form density; the gradients reach the holes' centres and radii.
+    Also times the geometry alone: rho and c from the holes and the adjoint
+    back to (x, y, r)."""
+    import numpy as np
+    import torch
+    import wavetorch_gb300 as wt
+    from wavetorch_gb300.data import vowel_like
+    world, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    B, T, N, nh = args.batch, args.T, WORKLOAD["nx"], 16
+    rng = np.random.default_rng(7)
+    hx, hy = (30.0 + 60.0 * rng.random(nh)).tolist(), (30.0 + 60.0 * rng.random(nh)).tolist()
+    hr = (2.0 + 4.0 * rng.random(nh)).tolist()
+    geom = wt.WaveGeometryHoley((N, N), 1.0, c0=1.0, c1=0.5, abs_N=WORKLOAD["abs_N"], abs_sig=3.0,
+                                abs_p=2, x=hx, y=hy, r=hr)
+    model = wt.WaveRNN(wt.WaveCell(0.707, geom), wt.WaveSource(20, 60),
+                       [wt.WaveIntensityProbe(80, y) for y in (35, 50, 65)]).to(dev)
+    x_np, lab = vowel_like(B, T, seed=1234)
+    x = torch.from_numpy(np.ascontiguousarray(x_np)).to(dev)
+    labels = torch.from_numpy(lab).to(dev)
+    holes = [model.cell.geom.x, model.cell.geom.y, model.cell.geom.r]
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
+    stream = torch.cuda.current_stream(dev)
+
+    def train():
+        for p in holes:
+            p.grad = None
+        y = model(x)
+        loss = torch.nn.CrossEntropyLoss()(wt.utils.normalize_power(y.sum(dim=1)), labels)
+        loss.backward()
+
+    w = torch.randn(N, N, generator=torch.Generator().manual_seed(8)).to(dev)
+
+    def geometry():
+        for p in holes:
+            p.grad = None
+        (model.cell.geom.c * w).sum().backward()
+
+    def timed(fn, steps, warmup, flush_l2, clk=None):
+        for _ in range(warmup):
+            fn()
+        torch.cuda.synchronize(dev)
+        ts = []
+        with clk or contextlib.nullcontext():
+            for _ in range(steps):
+                if flush_l2:
+                    flush.zero_()
+                e = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+                e[0].record(stream)
+                fn()
+                e[1].record(stream)
+                torch.cuda.synchronize(dev)
+                ts.append(e[0].elapsed_time(e[1]) / 1e3)
+        return statistics.mean(ts)
+
+    clk = ClockSampler(local)
+    t = timed(train, args.steps, args.warmup, True, clk)
+    grads_finite = all(bool(torch.isfinite(p.grad).all()) for p in holes)
+    t_geo = timed(geometry, 50, 5, False)
+    line = {
+        "metric": "cell-steps/s fwd+adjoint, hole geometry (16 holes), fused form",
+        "value": B * N * N * T / t, "unit": "cell-steps/s", "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": t * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "fp32",
+        "data": "synthetic (seeded vowel-like waveforms, 16 seeded holes)",
+        "config": {"workload": f"training step through the hole geometry: B={B}, {N}x{N} "
+                               f"(PML 20), T={T}, 16 holes, fwd + adjoint to dL/d(x, y, r)",
+                   "l2": "flushed (512 MiB write) before every timed step"},
+        "geometry_ms": t_geo * 1e3,
+        "geometry_note": "rho and c from the holes plus the adjoint to (x, y, r) through "
+                         "autograd, one call at a time (50 calls, warm); at 120x120 its kernels "
+                         "are short, so this includes the host's launch time",
+        "hole_grads_finite": grads_finite,
+        "clocks": clk.summary(),
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
+    if args.workload == "holey" and args.impl == "ours":
+        run_holey(args)
+        return
     if args.workload == "fields" and args.impl == "ours":
         run_fields(args)
         return
