@@ -1,0 +1,42 @@
+"""Host-side pieces of bench.py that need no GPU: the clock record's
+summary (from NVML samples or nvidia-smi lines) and the committed
+per-launch DRAM traffic it reports beside the roofline."""
+import bench
+
+
+def test_nvml_samples_summary():
+    c = bench.ClockSampler(0)
+    c.max_mhz = 2070.0
+    # idle (0x1) and application-clock (0x2) bits are not throttling; power
+    # cap (0x4) in one sample; hardware slowdown with its thermal cause in another
+    c.samples = [(2070.0, 0x0), (2055.0, 0x1 | 0x2), (1980.0, 0x4), (2070.0, 0x8 | 0x40)]
+    s = c.summary()
+    assert s["sm_mhz"] == 2062.5
+    assert s["sm_max_mhz"] == 2070.0
+    assert s["reasons"] == ["hw_slowdown", "hw_thermal_slowdown", "sw_power_cap"]
+    assert s["samples"] == 4 and s["source"].startswith("nvml")
+
+
+def test_nvidia_smi_lines_summary():
+    c = bench.ClockSampler(0)
+    c.lines = ["0, 2070, 2070, 812.3, 0x0000000000000000, Not Active, Not Active, Not Active, "
+               "Not Active",
+               "0, 1965, 2070, 1390.1, 0x0000000000000004, Not Active, Not Active, Not Active, "
+               "Active",
+               "garbled"]
+    s = c.summary()
+    assert s["sm_mhz"] == (2070 + 1965) / 2
+    assert s["sm_max_mhz"] == 2070.0
+    assert s["reasons"] == ["sw_power_cap"]
+    assert s["samples"] == 2 and s["source"].startswith("nvidia-smi")
+
+
+def test_no_samples_gives_no_record():
+    assert bench.ClockSampler(0).summary() is None
+
+
+def test_committed_traffic_of_the_fused_kernels():
+    # the T=200 capture scaled to T=3500, as profiles/traffic.txt states
+    assert bench.committed_traffic("seq_bwd_tape_kernel") == 6941428480
+    assert bench.committed_traffic("seq_bwd_fused_kernel") == 1040063360
+    assert bench.committed_traffic("no_such_kernel") is None
