@@ -1,9 +1,9 @@
 """ORACLE -- test infrastructure only (tests, smoke check, CPU baseline).
 
 numpy/ctypes front end of ``wave_oracle.c``, the plain-C float32 restatement
-of fancompute/wavetorch v0.2.1's time-stepping path (wavetorch/cell.py:12-44,
-wavetorch/operators.py:5-11, wavetorch/rnn.py:36-72, wavetorch/geom.py:63-85,
-109-132, 207-233).  Pinned against golden vectors produced by running the reference
+of fancompute/wavetorch v0.2.1's time-stepping path (wavetorch/cell.py:8-44,
+:79-107, wavetorch/operators.py:5-11, wavetorch/rnn.py:36-72,
+wavetorch/geom.py:63-85, 109-132, 207-233).  Pinned against golden vectors produced by running the reference
 (tests/golden/).  Nothing in the product imports this module.
 """
 from __future__ import annotations
@@ -126,6 +126,33 @@ class Seq:
         d = self.desc()
         load().or_seq_bwd(C.byref(d), _p(b), _p(c), _p(hist), _p(g), _p(gc), _p(gx))
         return gc, gx
+
+
+class NL(C.Structure):
+    _fields_ = [("b0", C.c_float), ("uth", C.c_float), ("cnl", C.c_float)]
+
+
+def seq_forward_nl(S, b, c_lin, rho, x, b0, uth, cnl):
+    """Nonlinear cell (wavetorch/cell.py:8-9, :79-107) over the sequence S:
+    returns (out [B,T,Q], hist [B,T,nx,ny])."""
+    b, c_lin, rho, x = _f(b), _f(c_lin), _f(rho), _f(x)
+    out = np.empty((S.batch, S.steps, S.np), np.float32)
+    hist = np.empty((S.batch, S.steps, S.nx, S.ny), np.float32)
+    d, n = S.desc(), NL(b0, uth, cnl)
+    load().or_seq_fwd_nl(C.byref(d), C.byref(n), _p(b), _p(c_lin), _p(rho), _p(x), _p(out),
+                         _p(hist))
+    return out, hist
+
+
+def seq_backward_nl(S, b, c_lin, rho, hist, grad_out, b0, uth, cnl):
+    """Returns (dL/dc_lin, the direct dL/drho of the nonlinear terms)."""
+    b, c_lin, rho, hist, g = _f(b), _f(c_lin), _f(rho), _f(hist), _f(grad_out)
+    gc = np.empty((S.nx, S.ny), np.float32)
+    gr = np.empty((S.nx, S.ny), np.float32)
+    d, n = S.desc(), NL(b0, uth, cnl)
+    load().or_seq_bwd_nl(C.byref(d), C.byref(n), _p(b), _p(c_lin), _p(rho), _p(hist), _p(g),
+                         _p(gc), _p(gr))
+    return gc, gr
 
 
 def rho_to_c(rho, kernel, blur_n, eta, beta, c0, c1):

@@ -10,7 +10,8 @@
  *                 row-major fused multiply-add chain when batch > 1 or the grid
  *                 has > 20480 cells (ORD_SEQ), else the im2col+GEMM pairing
  *                 (u + l) + (-4c + (r + d)) (ORD_PAIRED, h == 1).
- *   update        wavetorch/cell.py:12-17, left to right.
+ *   update        wavetorch/cell.py:12-17, left to right; the nonlinear
+ *                 cell's b and c (cell.py:8-9, :93-101) per cell and step.
  *   adjoint       wavetorch/cell.py:26-44, plus autograd's accumulation order:
  *                 the gradient reaching h_t is (grad_y2 from step t+2 +
  *                 grad_y1 from step t+1), then the probe terms in descending
@@ -330,6 +331,206 @@ void or_seq_bwd(const or_desc* d, const float* b, const float* c, const float* h
         }
     }
     free(X1); free(Kc); free(Kg); free(Ky2); free(lam); free(gct); free(pidx);
+}
+
+/* ---- nonlinear cell, wavetorch/cell.py:8-9, :79-107 ---------------------
+ * Per step, from h1 = h_{t-1} (the post-source field):
+ *   b = b_pml + rho * (b0 / (1 + |h1 / uth|^2))      (when b0 > 0)
+ *   c = c_lin + (rho * c_nl) * h1^2                  (when c_nl != 0)
+ * then TimeStep with these per-instance b, c.  rho is the raw density
+ * parameter (wavetorch/rnn.py:47, geom.py:185-205), c_lin its projected
+ * speed. */
+typedef struct or_nl {
+    float b0, uth, cnl;
+} or_nl;
+
+typedef struct nl_cell {
+    float b, c, sat, q, a, D;    /* b, c of the step; sat, |h1/uth| pieces */
+} nl_cell;
+
+static inline nl_cell nl_bc(const or_nl* n, float bp, float cl, float rho, float h1) {
+    nl_cell r;
+    r.b = bp; r.c = cl; r.sat = 0.0f; r.q = 0.0f; r.a = 0.0f; r.D = 1.0f;
+    if (n->b0 > 0.0f) {
+        r.q = h1 / n->uth;
+        r.a = fabsf(r.q);
+        r.D = 1.0f + r.a * r.a;
+        r.sat = n->b0 / r.D;
+        r.b = bp + rho * r.sat;
+    }
+    if (n->cnl != 0.0f) r.c = cl + (rho * n->cnl) * (h1 * h1);
+    return r;
+}
+
+/* forward: as or_seq_fwd with b, c formed per cell and step */
+void or_seq_fwd_nl(const or_desc* d, const or_nl* n, const float* bp, const float* cl,
+                   const float* rho, const float* x, float* out, float* hist) {
+    const int B = d->batch, nx = d->nx, ny = d->ny, T = d->steps;
+    scal s = make_scal(d->dt, d->h);
+    const size_t plane = (size_t)nx * ny;
+    const size_t hb = (size_t)T * plane;
+    float* zero = (float*)calloc(plane, sizeof(float));
+    for (int t = 0; t < T; ++t) {
+#pragma omp parallel for schedule(static)
+        for (int k = 0; k < B; ++k) {
+            const float* y1 = t >= 1 ? hist + k * hb + (size_t)(t - 1) * plane : zero;
+            const float* y2 = t >= 2 ? hist + k * hb + (size_t)(t - 2) * plane : zero;
+            float* y = hist + k * hb + (size_t)t * plane;
+            for (int i = 0; i < nx; ++i)
+                for (int j = 0; j < ny; ++j) {
+                    size_t q = (size_t)i * ny + j;
+                    nl_cell m = nl_bc(n, bp[q], cl[q], rho[q], y1[q]);
+                    float L = lap_at(y1, nx, ny, i, j, &s, d->order);
+                    y[q] = update(m.b, m.c, y1[q], y2[q], L, &s);
+                }
+            for (int e = 0; e < d->n_src; ++e) {
+                int row = d->src_row[e] < 0 ? k : d->src_row[e];
+                y[d->src_cell[e]] = y[d->src_cell[e]] + x[(size_t)row * T + t];
+            }
+            for (int q = 0; q < d->n_prb; ++q) {
+                float v = y[d->prb_cell[q]];
+                out[((size_t)k * T + t) * d->n_prb + q] = d->prb_kind[q] ? v * v : v;
+            }
+        }
+    }
+    free(zero);
+}
+
+/* Adjoint of or_seq_fwd_nl in the order autograd runs the reference's graph
+ * (highest sequence number first).  Step s's nodes run after those of every
+ * later step: TimeStep_s, then the Kerr branch (AddBackward, MulBackward,
+ * PowBackward(h1, 2), MulBackward(rho, c_nl)), then the damping branch
+ * (AddBackward, MulBackward(rho, sat), DivBackward(b0, D), AddBackward,
+ * PowBackward(a, 2), AbsBackward, DivBackward(h1, uth)), then the probes of
+ * step s-1.  So the gradient of h_{s-1} is
+ *   (((grad_y2 of step s+1 + grad_y1 of step s) + Kerr term) + damping term)
+ * plus the probe terms in descending probe order; the density's gradient
+ * takes, per step from the last, the Kerr term then the damping term (each
+ * summed over the batch first, as sum_to does), and c_lin's the batch sum of
+ * grad_c.  Formulas: TimeStep.backward (cell.py:26-44); torch's derivatives
+ * of mul, div (other: -grad * ((self / other) / other)), pow (grad * (2 x)),
+ * abs (grad * sgn).  Outputs: grad_c (dL/dc_lin) and grad_rho (the direct
+ * part; the projection's part is added by the caller, last, as autograd
+ * does). */
+void or_seq_bwd_nl(const or_desc* d, const or_nl* n, const float* bp, const float* cl,
+                   const float* rho, const float* hist, const float* grad_out, float* grad_c,
+                   float* grad_rho) {
+    const int B = d->batch, nx = d->nx, ny = d->ny, T = d->steps;
+    scal s = make_scal(d->dt, d->h);
+    const float dt = s.dt;
+    const size_t plane = (size_t)nx * ny, bp_ = (size_t)B * plane, hb = (size_t)T * plane;
+    float* lam = (float*)malloc(sizeof(float) * 3 * bp_);     /* lambda_t, ring of 3 */
+    int set[3] = {0, 0, 0};                                     /* a gradient has arrived */
+    float* Kg = (float*)malloc(sizeof(float) * bp_);            /* X1 c^2 of the step */
+    float* gcs = (float*)malloc(sizeof(float) * bp_);           /* grad_c of the step */
+    float* gkr = (float*)malloc(sizeof(float) * bp_);           /* grad_c * h1^2 */
+    float* gbs = (float*)malloc(sizeof(float) * bp_);           /* grad_b * sat */
+    float* zero = (float*)calloc(plane, sizeof(float));
+    int* pidx = (int*)malloc(sizeof(int) * (d->n_prb + 1));
+    for (int q = 0; q < d->n_prb; ++q) pidx[q] = q;
+    for (int a = 1; a < d->n_prb; ++a) {
+        int v = pidx[a], j = a - 1;
+        while (j >= 0 && d->prb_order[pidx[j]] < d->prb_order[v]) { pidx[j + 1] = pidx[j]; --j; }
+        pidx[j + 1] = v;
+    }
+    int first_rho = 1;
+    for (int t = T - 1; t >= 0; --t) {
+        float* L0 = lam + (size_t)(t % 3) * bp_;
+        /* probe terms of step t into lambda_t */
+        if (!set[t % 3]) memset(L0, 0, sizeof(float) * bp_);
+        for (int k = 0; k < B; ++k)
+            for (int a = 0; a < d->n_prb; ++a) {
+                int q = pidx[a];
+                size_t o = ((size_t)k * T + t) * d->n_prb + q;
+                float gv = grad_out[o];
+                float amp = hist[k * hb + (size_t)t * plane + d->prb_cell[q]];
+                float sd = d->prb_kind[q] ? gv * (2.0f * amp) : gv;
+                float* cell = L0 + k * plane + d->prb_cell[q];
+                *cell = *cell + sd;   /* IndexBackward: zeros with the value added */
+            }
+        if (d->n_prb > 0) set[t % 3] = 1;
+        /* step t's nodes: coefficients from h1 = h_{t-1}, h2 = h_{t-2} */
+        float* L1 = lam + (size_t)((t + 2) % 3) * bp_;   /* lambda_{t-1} */
+        float* L2 = lam + (size_t)((t + 1) % 3) * bp_;   /* lambda_{t-2} */
+        const int has1 = t >= 1, has2 = t >= 2;
+#pragma omp parallel for schedule(static)
+        for (int k = 0; k < B; ++k) {
+            const float* h1 = has1 ? hist + k * hb + (size_t)(t - 1) * plane : zero;
+            const float* h2 = has2 ? hist + k * hb + (size_t)(t - 2) * plane : zero;
+            const float* g = L0 + k * plane;
+            for (size_t q = 0; q < plane; ++q) {
+                nl_cell m = nl_bc(n, bp[q], cl[q], rho[q], h1[q]);
+                float X1 = 1.0f / (m.b * dt + 1.0f);
+                Kg[k * plane + q] = X1 * (m.c * m.c);
+            }
+            for (int i = 0; i < nx; ++i)
+                for (int j = 0; j < ny; ++j) {
+                    size_t q = (size_t)i * ny + j, ic = k * plane + q;
+                    nl_cell m = nl_bc(n, bp[q], cl[q], rho[q], h1[q]);
+                    float gv = set[t % 3] ? g[q] : 0.0f;
+                    float bdt = m.b * dt;
+                    float X1 = 1.0f / (bdt + 1.0f);
+                    float L = lap_at(h1, nx, ny, i, j, &s, d->order);
+                    float gc = (2.0f * m.c) * s.dt2;                  /* grad_c */
+                    gc = gc * L;
+                    gc = X1 * gc;
+                    gc = gc * gv;
+                    gcs[ic] = gc;
+                    float gb = 0.0f;                                  /* grad_b */
+                    if (n->b0 > 0.0f) {
+                        float v = dt * m.b + 1.0f;
+                        float kb = -(1.0f / (v * v));
+                        kb = kb * dt;
+                        float in = ((m.c * m.c) * s.dt2) * L;
+                        in = in + 2.0f * h1[q];
+                        in = in - 2.0f * h2[q];
+                        gb = (kb * in) * gv;
+                    }
+                    gkr[ic] = gc * (h1[q] * h1[q]);
+                    gbs[ic] = gb * m.sat;
+                    if (has1) {
+                        float lg = lap_scaled(Kg + k * plane, g, nx, ny, i, j, &s, d->order);
+                        float v = s.dt2 * lg + (2.0f * gv) * X1;       /* grad_y1 */
+                        float* l1 = L1 + ic;
+                        v = set[(t + 2) % 3] ? *l1 + v : v;
+                        if (n->cnl != 0.0f)                            /* Kerr term */
+                            v = v + (gc * (rho[q] * n->cnl)) * (2.0f * h1[q]);
+                        if (n->b0 > 0.0f) {                            /* damping term */
+                            float gsat = gb * rho[q];
+                            float gD = -gsat * ((n->b0 / m.D) / m.D);
+                            float ga = gD * (2.0f * m.a);
+                            float sg = m.q > 0.0f ? 1.0f : (m.q < 0.0f ? -1.0f : 0.0f);
+                            v = v + (ga * sg) / n->uth;
+                        }
+                        *l1 = v;
+                    }
+                    if (has2) L2[ic] = ((bdt - 1.0f) * X1) * gv;     /* grad_y2, first arrival */
+                }
+        }
+        if (has1) set[(t + 2) % 3] = 1;
+        if (has2) set[(t + 1) % 3] = 1;
+        set[t % 3] = 0;   /* the ring slot is lambda_{t-3} from here on */
+#pragma omp parallel for schedule(static)
+        for (long q = 0; q < (long)plane; ++q) {
+            float sc = batch_sum(gcs + q, plane, B);
+            grad_c[q] = (t == T - 1) ? sc : grad_c[q] + sc;
+            float r = first_rho ? 0.0f : grad_rho[q];
+            int have = !first_rho;
+            if (n->cnl != 0.0f) {
+                float v = batch_sum(gkr + q, plane, B) * n->cnl;
+                r = have ? r + v : v;
+                have = 1;
+            }
+            if (n->b0 > 0.0f) {
+                float v = batch_sum(gbs + q, plane, B);
+                r = have ? r + v : v;
+                have = 1;
+            }
+            grad_rho[q] = have ? r : 0.0f;
+        }
+        if (n->cnl != 0.0f || n->b0 > 0.0f) first_rho = 0;
+    }
+    free(lam); free(Kg); free(gcs); free(gkr); free(gbs); free(zero); free(pidx);
 }
 
 /* ---- free-form geometry, wavetorch/geom.py:207-233 ---------------------- */

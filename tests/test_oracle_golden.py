@@ -1,7 +1,8 @@
 """Pin the CPU oracle against golden vectors produced by the reference itself.
 
 Expected agreement (see oracle/wave_oracle.c):
-  * sequence forward outputs and fields, and dL/dc: bit-exact;
+  * sequence forward outputs and fields, and dL/dc: bit-exact (linear and
+    nonlinear cells);
   * one-step backward: bit-exact except a few cells where torch's own
     kernels take a tail path (the last plane%16 cells of a batch sum over
     more than 16 instances; im2col+GEMM tail cells of single-instance grids);
@@ -78,6 +79,24 @@ def test_rho_to_c(name):
     assert rel(c, d["c"]) < 3e-7
     gr = o.rho_to_c_bwd(th, d["blur_kernel"], 1, 0.5, 100.0, 1.0, 0.5, d["grad_c"])
     assert rel(gr, d["grad_rho"]) < 5e-6
+
+
+def test_nonlinear_cell():
+    """The nonlinear cell (saturable damping and Kerr term, wavetorch/cell.py:
+    8-9, :79-107; golden `nonlinear`: B=2, 40x40, T=60): probe outputs and
+    dL/dc_lin bit-exact (the adjoint replays autograd's node order); dL/drho,
+    the direct part plus the projection's, within 5e-6 (ulps of tanh in the
+    projection, as in test_rho_to_c)."""
+    d = golden("nonlinear")
+    S = seq_of(d)
+    nl = (float(d["satdamp_b0"]), float(d["satdamp_uth"]), float(d["c_nl"]))
+    out, hist = o.seq_forward_nl(S, d["b"], d["c"], d["rho"], d["x"], *nl)
+    assert np.array_equal(out, d["out"])
+    gc, gr = o.seq_backward_nl(S, d["b"], d["c"], d["rho"], hist, d["grad_out"], *nl)
+    assert np.array_equal(gc, d["grad_c"])
+    _, th = o.rho_to_c(d["rho"], d["blur_kernel"], 1, 0.5, 100.0, 1.0, 0.5)
+    total = gr + o.rho_to_c_bwd(th, d["blur_kernel"], 1, 0.5, 100.0, 1.0, 0.5, gc)
+    assert rel(total, d["grad_rho"]) < 5e-6
 
 
 def test_fp32_vs_fp64_floor():
