@@ -120,6 +120,42 @@ def test_fp64_finite_difference_fixtures_match_reference_autograd(name):
     assert np.abs(fd - ag).max() <= 1e-7 * np.abs(fd).max()
 
 
+@pytest.mark.parametrize("name", ["fd64_linear", "fd64_nonlinear"])
+def test_oracle_gradient_against_fp64_central_differences(name):
+    """The oracle's whole adjoint (sequence, nonlinear terms, projection) at
+    16 design cells against central differences of the reference run in
+    float64: within 1e-5 of the largest derivative (measured 2.6e-6 linear,
+    1.2e-6 nonlinear).  This pins the adjoint's algebra independently of
+    autograd's order."""
+    import torch
+    from wavetorch_gb300.geom import pml_profile
+    from wavetorch_gb300.utils import normalize_power
+    d = golden(name)
+    B, N, T, abs_N = int(d["B"]), int(d["N"]), int(d["T"]), int(d["abs_N"])
+    b = pml_profile((N, N), abs_N, 3.0, 2).numpy()
+    kern = np.full((3, 3), np.float32(1.0) / np.float32(9.0), np.float32)
+    rho = d["rho"]
+    c, th = o.rho_to_c(rho, kern, 1, 0.5, 100.0, 1.0, 0.5)
+    S = seq_of(d)
+    nl = (float(d["satdamp_b0"]), float(d["satdamp_uth"]), float(d["c_nl"]))
+    nonlinear = nl[0] > 0 or nl[2] != 0
+    if nonlinear:
+        out, hist = o.seq_forward_nl(S, b, c, rho, d["x"], *nl)
+    else:
+        out, hist = S.forward(b, c, d["x"])
+    y = torch.from_numpy(out).requires_grad_()
+    loss = torch.nn.CrossEntropyLoss()(normalize_power(y.sum(dim=1)), torch.from_numpy(d["labels"]))
+    (g,) = torch.autograd.grad(loss, [y])
+    if nonlinear:
+        gc, direct = o.seq_backward_nl(S, b, c, rho, hist, g.numpy(), *nl)
+    else:
+        (gc, _), direct = S.backward(b, c, hist, g.numpy()), 0.0
+    total = direct + o.rho_to_c_bwd(th, kern, 1, 0.5, 100.0, 1.0, 0.5, gc)
+    ours = total.reshape(-1).astype(np.float64)[d["fd_index"]]
+    fd = d["fd_grad"]
+    assert np.abs(ours - fd).max() <= 1e-5 * np.abs(fd).max()
+
+
 def test_holey_geometry():
     """The oracle's hole geometry against the reference's (golden `holey`:
     64x48, three holes, gradients of sum(c * w)).  A one-ulp difference in
