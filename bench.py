@@ -93,8 +93,8 @@ def barrier(world: int, device=None):
 
 class ClockSampler:
     """SM clock and clock-event (throttle) reasons sampled while the timed
-    region runs: every 2 ms through NVML (the driver's libnvidia-ml, read-only
-    queries), else from nvidia-smi at 100 ms.  The sampler is running before
+    region runs: every 2 ms through NVML (libnvidia-ml, which comes with the
+    NVIDIA display driver; read-only queries), else from nvidia-smi at 100 ms.  The sampler is running before
     __enter__ returns, so the samples cover the region even when it lasts only
     a few tens of milliseconds."""
     Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
