@@ -40,3 +40,26 @@ def test_committed_traffic_of_the_fused_kernels():
     assert bench.committed_traffic("seq_bwd_tape_kernel") == 6941428480
     assert bench.committed_traffic("seq_bwd_fused_kernel") == 1040063360
     assert bench.committed_traffic("no_such_kernel") is None
+
+
+def test_reference_arm_prints_the_contract_line():
+    """`bench.py --impl reference` (the reference's CPU path restated, on the
+    host cores) prints one JSON line with the keys the benchmark contract
+    asks of that arm; a batch of 2 keeps the run to a few seconds."""
+    import json
+    import os
+    import subprocess
+    import sys
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    r = subprocess.run([sys.executable, os.path.join(root, "bench.py"), "--impl", "reference",
+                        "--steps", "1", "--warmup", "0", "--batch", "2"],
+                       capture_output=True, text=True, timeout=600, cwd=root)
+    assert r.returncode == 0, r.stderr[-2000:]
+    lines = [ln for ln in r.stdout.splitlines() if ln.startswith("{")]
+    assert len(lines) == 1
+    d = json.loads(lines[0])
+    assert d["impl"] == "reference" and d["unit"] == "cell-steps/s" and d["value"] > 0
+    assert d["higher_is_better"] is True and d["n_gpus"] == 1
+    assert d["cpu_baseline"]["kind"] == "port" and d["cpu_baseline"]["cores"] >= 1
+    assert d["e2e"] == {"value": d["value"], "unit": "cell-steps/s", "h2d_bytes_per_step": 0,
+                        "d2h_bytes_per_step": 0}
