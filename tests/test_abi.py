@@ -5,6 +5,7 @@ import os
 import re
 import shutil
 
+import numpy as np
 import pytest
 
 from conftest import ROOT
@@ -92,6 +93,42 @@ def test_invalid_descriptors_rejected(lib, bad):
     d, keep = _desc(**bad)
     n = C.c_size_t(0)
     assert lib.wt_seq_workspace_bytes(C.byref(d), C.byref(n)) == _lib.WT_ERR_INVALID
+
+
+def test_planner_on_random_valid_descriptors(lib):
+    """The workspace planner (host code; it launches nothing) on 600 random
+    valid descriptors,
+    from 1x1 grids to 2048x2048, T up to 1e5, every form, adjoint mode,
+    cluster request and flag: it answers OK or UNSUPPORTED, never INVALID,
+    and an OK plan holds at least the probe amplitudes (and, for the plain
+    form, every field)."""
+    from wavetorch_gb300 import _lib
+    rng = np.random.default_rng(0)
+    sizes = [1, 2, 7, 16, 33, 64, 120, 160, 200, 256, 257, 300, 512, 1024, 2048]
+    for _ in range(600):
+        B = int(rng.choice([1, 2, 3, 32, 64, 200]))
+        nx, ny = int(rng.choice(sizes)), int(rng.choice(sizes))
+        T = int(rng.choice([1, 2, 3, 50, 3500, 100000]))
+        srcs = tuple((int(rng.integers(0, nx * ny)), int(rng.choice([-1, 0, B - 1])))
+                     for _ in range(int(rng.integers(0, 4))))
+        prbs = tuple((int(rng.integers(0, nx * ny)), int(rng.integers(0, 2)), i)
+                     for i in range(int(rng.integers(0, 5))))
+        src = (_lib.SourceEntry * max(1, len(srcs)))(*[_lib.SourceEntry(*v) for v in srcs])
+        prb = (_lib.ProbeEntry * max(1, len(prbs)))(*[_lib.ProbeEntry(*v) for v in prbs])
+        form = int(rng.integers(0, 2))
+        d = _lib.SeqDesc(B, nx, ny, T, len(srcs), C.cast(src, C.POINTER(_lib.SourceEntry)),
+                         len(prbs), C.cast(prb, C.POINTER(_lib.ProbeEntry)), form,
+                         int(rng.choice([-2, -1, 0, 1, 7, T])), int(rng.choice([-1, 0, 1, 2, 4, 16])),
+                         int(rng.integers(0, 2)), int(rng.integers(0, 2)), 0)
+        n = C.c_size_t(0)
+        st = lib.wt_seq_workspace_bytes(C.byref(d), C.byref(n))
+        assert st in (_lib.WT_OK, _lib.WT_ERR_UNSUPPORTED), (B, nx, ny, T, form)
+        if st == _lib.WT_OK:
+            assert n.value >= B * T * len(prbs) * 4
+            if form == 0:
+                assert n.value >= B * T * nx * ny * 4
+        st = lib.wt_seq_workspace_bytes_nl(C.byref(d), C.byref(n))
+        assert st in (_lib.WT_OK, _lib.WT_ERR_UNSUPPORTED)
 
 
 def test_fused_tap_capacity(lib):
