@@ -316,3 +316,66 @@ def test_ragged_plan_validates_arguments(lib):
     neg = (_lib.RaggedOption * 1)(_lib.RaggedOption(4, 4, -1.0))
     grp2 = (_lib.RaggedGroup * 1)(_lib.RaggedGroup(1, 1.0, 1, C.cast(neg, C.POINTER(_lib.RaggedOption))))
     assert lib.wt_ragged_plan(grp2, 1, 152, out) == _lib.WT_ERR_INVALID
+
+
+def _ragged_plan_restated(groups, n_sm):
+    """wt_ragged_plan's rule as its header states it, in double precision:
+    least SM-time per group (ties: fewer CTAs, then the earlier option); then,
+    while the longest group outlasts total SM-time / n_sm, move it to the
+    faster option of least SM-time (ties: the slower)."""
+    t = lambda g, k: groups[g][2][k][1] * groups[g][1]          # noqa: E731
+    sms = lambda g, k: float(groups[g][2][k][0])                # noqa: E731
+    pick = []
+    for g in range(len(groups)):
+        best = 0
+        for k in range(1, len(groups[g][2])):
+            if (sms(g, k) * t(g, k), sms(g, k)) < (sms(g, best) * t(g, best), sms(g, best)):
+                best = k
+        pick.append(best)
+    for _ in range(4 * len(groups) + 1):
+        if not groups:
+            break
+        bound = 0.0
+        for g in range(len(groups)):
+            bound += groups[g][0] * sms(g, pick[g]) * t(g, pick[g])
+        bound /= n_sm
+        kg = 0
+        for g in range(1, len(groups)):
+            if t(g, pick[g]) > t(kg, pick[kg]):
+                kg = g
+        tk = t(kg, pick[kg])
+        if tk <= bound:
+            break
+        cand = [k for k in range(len(groups[kg][2])) if t(kg, k) < tk]
+        if not cand:
+            break
+        best = cand[0]
+        for k in cand[1:]:
+            if (sms(kg, k) * t(kg, k), -t(kg, k)) < (sms(kg, best) * t(kg, best), -t(kg, best)):
+                best = k
+        pick[kg] = best
+    return pick
+
+
+def test_ragged_plan_matches_its_stated_rule(lib):
+    """wt_ragged_plan against a restatement of its documented rule on 400
+    random batches (1-20 groups, 1-6 options, tied times included)."""
+    from wavetorch_gb300 import _lib
+    rng = np.random.default_rng(3)
+    for _ in range(400):
+        groups = []
+        for _ in range(int(rng.integers(1, 21))):
+            opts = [(int(rng.choice([1, 2, 4, 8, 12, 16])),
+                     float(rng.choice([0.5, 1.0, 2.0])) if rng.random() < 0.3
+                     else float(rng.uniform(0.01, 3.0)))
+                    for _ in range(int(rng.integers(1, 7)))]
+            groups.append((int(rng.integers(1, 31)), float(rng.uniform(0.5, 8.0)), opts))
+        n_sm = int(rng.choice([8, 152]))
+        arrs = [(_lib.RaggedOption * len(o))(*[_lib.RaggedOption(c, c, s) for c, s in o])
+                for _, _, o in groups]
+        grp = (_lib.RaggedGroup * len(groups))(*[
+            _lib.RaggedGroup(n, sc, len(o), C.cast(a, C.POINTER(_lib.RaggedOption)))
+            for (n, sc, o), a in zip(groups, arrs)])
+        out = (C.c_int32 * len(groups))()
+        assert lib.wt_ragged_plan(grp, len(groups), n_sm, out) == _lib.WT_OK
+        assert list(out) == _ragged_plan_restated(groups, n_sm)
