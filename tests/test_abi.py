@@ -27,6 +27,34 @@ def lib():
     return _lib.load()
 
 
+def declared_arity():
+    """{function: number of parameters} from the header's prototypes."""
+    text = open(HEADER).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    out = {}
+    for name, params in re.findall(r"\b(wt_[a-z0-9_]+)\s*\(([^)]*)\)\s*;", text):
+        params = params.strip()
+        out[name] = 0 if params in ("", "void") else params.count(",") + 1
+    return out
+
+
+def test_ctypes_binding_matches_the_header(lib):
+    """Every function the Python binding declares argument types for takes
+    as many arguments as its prototype in the header (a mismatch would pass
+    pointers in the wrong slots)."""
+    from wavetorch_gb300 import _lib
+    arity = declared_arity()
+    checked = 0
+    for name in _lib.EXPORTED:
+        argtypes = getattr(lib, name).argtypes
+        if argtypes is None:
+            continue
+        assert name in arity, name
+        assert len(argtypes) == arity[name], (name, len(argtypes), arity[name])
+        checked += 1
+    assert checked >= 20
+
+
 def test_header_declares_the_api():
     names = declared_functions()
     for n in ["wt_step_fwd", "wt_step_bwd", "wt_seq_fwd", "wt_seq_bwd", "wt_seq_workspace_bytes",
