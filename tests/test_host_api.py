@@ -198,3 +198,21 @@ def test_save_load_roundtrip_hole_geometry(tmp_path):
     for name in ("x", "y", "r"):
         assert torch.equal(getattr(g2, name), getattr(geom, name)), name
     assert torch.equal(g2.rho, geom.rho) and torch.equal(g2.c, geom.c)
+
+
+def test_utils_match_the_reference_formulas():
+    """wavetorch/utils.py:23-36: the centred window (int() truncation of
+    len/2 -/+ w/2), the argmax accuracy, and the row normalisation of
+    time-summed intensities that feeds the loss."""
+    from wavetorch_gb300 import utils
+    x = np.arange(11)
+    assert list(utils.window_data(x, 4)) == [3, 4, 5, 6]         # [int(3.5):int(7.5)]
+    assert list(utils.window_data(x, 5)) == [3, 4, 5, 6, 7]      # [int(3.0):int(8.0)]
+    assert list(utils.window_data(np.arange(10), 3)) == [3, 4, 5]
+    pred = torch.tensor([[0.1, 0.7, 0.2], [0.5, 0.3, 0.2], [0.2, 0.2, 0.6], [0.9, 0.05, 0.05]])
+    assert utils.accuracy_onehot(pred, torch.tensor([1, 0, 1, 0])) == 0.75
+    X = torch.tensor([[1.0, 3.0], [2.0, 2.0]])
+    P = utils.normalize_power(X)
+    assert torch.equal(P, torch.tensor([[0.25, 0.75], [0.5, 0.5]]))
+    with pytest.raises(ValueError):
+        utils.set_dtype("float16")
