@@ -273,8 +273,11 @@ int wt_rho_to_c_work_bytes(const wt_geom_desc* g, size_t* bytes);
  * x 2 floats (8 MiB) in the library's own static device memory.
  *   - Grids of more than WT_RHO_TO_C_NOALLOC_MAX_CELLS cells are refused with
  *     WT_ERR_UNSUPPORTED before anything runs; use wt_rho_to_c_fwd for them.
- *   - The first call on each device looks up that device's copy of the array
- *     (with the device current); make it before any stream capture begins.
+ *   - Each call looks up the current device's copy of the array (with that
+ *     device current; the lookup allocates nothing), so a device reset
+ *     between calls leaves no stale address behind.  The first call on a
+ *     device also loads the library's device code there: make it before
+ *     any stream capture begins.
  *   - Every call on a device shares that one array.  No part of it has to
  *     start at zero (each call writes every element it reads), but calls
  *     whose executions overlap (different streams, or host threads, without

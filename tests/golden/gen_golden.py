@@ -276,6 +276,26 @@ def case_holey(wt):
             "y": np.array([12.0, 30.0, 24.5], np.float32), "r": np.array([3.0, 5.5, 2.5], np.float32)}
 
 
+def ref_model_file(wt):
+    """A model file written by the reference's own ``io.save_model``
+    (wavetorch/io.py:13-40): free-form geometry 40x40 (PML 8) with a seeded
+    density, two point sources, three intensity probes; plus the model's
+    float32 outputs on a short seeded input, for a load-and-run check."""
+    N, T, B = 40, 50, 2
+    g = torch.Generator().manual_seed(17)
+    geom = wt.WaveGeometryFreeForm((N, N), 1.0, c0=1.0, c1=0.5, abs_N=8, abs_sig=3.0, abs_p=2,
+                                   rho=torch.rand(N, N, generator=g))
+    cell = wt.WaveCell(0.707, geom)
+    model = wt.WaveRNN(cell, [wt.WaveSource(10, 20), wt.WaveSource(12, 14)],
+                       [wt.WaveIntensityProbe(30, y) for y in (12, 20, 28)])
+    wt.io.save_model(model, "ref_model", savedir=HERE + "/", cfg={"dtype": "float32"},
+                     verbose=False)
+    x, _ = vowel_like(B, T, seed=17)
+    with torch.no_grad():
+        out = model(torch.from_numpy(x))
+    return {"x": x, "out": _np(out), "c": _np(geom.c), "b": _np(geom.b), "rho": _np(geom.rho)}
+
+
 def state_keys(wt):
     """state_dict keys, shapes and dtypes of a reference model (drop-in check)."""
     geom = wt.WaveGeometryFreeForm((50, 50), 1.0, c0=1.0, c1=0.5, abs_N=10, abs_sig=3.0, abs_p=2,
@@ -310,6 +330,7 @@ def main():
         "geom_n100": lambda: case_geom(wt, 100, 8),
         "geom_n160": lambda: case_geom(wt, 160, 9),
         "holey": lambda: case_holey(wt),
+        "ref_model": lambda: ref_model_file(wt),
     }
     only = set(sys.argv[1:])
     if not only or "state_keys" in only:

@@ -23,7 +23,7 @@ import types
 
 import numpy as np
 
-REFERENCE_ROOT = os.environ.get("WAVETORCH_REFERENCE", "/root/reference")
+REFERENCE_ROOT = os.environ.get("WAVETORCH_REFERENCE", "")
 
 
 def _stub(name, **attrs):
@@ -81,7 +81,12 @@ def _line(r0, c0, r1, c1):
 
 
 def import_reference():
-    """Return the reference ``wavetorch`` package, imported unmodified."""
+    """Return the reference ``wavetorch`` package, imported unmodified from
+    the directory named by the WAVETORCH_REFERENCE environment variable (the
+    directory that holds the ``wavetorch`` package)."""
+    if not REFERENCE_ROOT or not os.path.isdir(os.path.join(REFERENCE_ROOT, "wavetorch")):
+        raise RuntimeError("set WAVETORCH_REFERENCE to the directory holding the reference's "
+                           "wavetorch package")
     if "wavetorch" in sys.modules and getattr(sys.modules["wavetorch"], "__file__", "").startswith(REFERENCE_ROOT):
         return sys.modules["wavetorch"]
     for name in ["librosa", "pandas", "seaborn", "matplotlib", "matplotlib.pyplot",

@@ -264,3 +264,21 @@ def test_kahan_probe_sums(cuda, name):
     assert np.array_equal(sums["plain"], sums["fused"])
     ref = d["out"].astype(np.float64).sum(axis=1)
     assert np.abs(sums["fused"] - ref).max() <= 1e-6 * np.abs(ref).max()
+
+
+@pytest.mark.parametrize("form", ["plain", "fused"])
+def test_model_file_from_the_reference_runs_like_the_reference(cuda, form):
+    """A model file written by the reference's io.save_model, loaded with
+    wavetorch_gb300.io.load_model and run on the GPU: its probe outputs on
+    the stored input match the reference's float32 outputs within 1e-5
+    (rel. L2; c differs from the reference's by ulps of tanh)."""
+    import os
+    from conftest import GOLDEN
+    d = golden("ref_model")
+    m, _, _, _ = wt.io.load_model(os.path.join(GOLDEN, "ref_model.pt"))
+    m.form = form
+    m = m.to(cuda)
+    with torch.no_grad():
+        out = m(T(d["x"], cuda))
+    torch.cuda.synchronize()
+    assert rel(out.cpu().numpy(), d["out"]) <= 1e-5

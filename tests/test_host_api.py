@@ -129,6 +129,43 @@ def test_save_load_roundtrip(tmp_path):
         assert k == k2 and torch.equal(v, v2)
 
 
+def test_load_model_file_written_by_the_reference():
+    """tests/golden/ref_model.pt was written by the reference's own
+    io.save_model (wavetorch/io.py:13-40).  load_model rebuilds the same
+    geometry (density, PML, class), the two sources and three probes in
+    module order, and dt; probes come back as intensity probes, the
+    reference loader's rule for files without probe kinds."""
+    d = golden("ref_model")
+    m, hist, geo_hist, cfg = wt.io.load_model(os.path.join(GOLDEN, "ref_model.pt"))
+    assert cfg == {"dtype": "float32"} and hist is None and len(geo_hist) == 1
+    g = m.cell.geom
+    assert isinstance(g, wt.WaveGeometryFreeForm)
+    assert np.array_equal(g.rho.detach().numpy(), d["rho"])
+    assert np.array_equal(g.b.numpy(), d["b"])
+    assert [s.cells() for s in m.sources] == [[(10, 20)], [(12, 14)]]
+    assert [p.cells() for p in m.probes] == [[(30, 12)], [(30, 20)], [(30, 28)]]
+    assert all(type(p) is wt.WaveIntensityProbe for p in m.probes)
+    assert abs(m.cell.dt.item() - 0.707) < 1e-7
+    ref_keys = set(torch.load(os.path.join(GOLDEN, "ref_model.pt"), weights_only=False)["model_state"])
+    assert set(m.state_dict()) == ref_keys
+
+
+def test_model_file_keeps_probe_kinds_and_line_sources(tmp_path):
+    """Files written here record the probe classes (a key the reference's
+    loader ignores), so amplitude probes stay amplitude probes; a line
+    source comes back as a source over the same cells."""
+    geom = wt.WaveGeometryFreeForm((48, 48), 1.0, c0=1.0, c1=0.5, abs_N=10)
+    m = wt.WaveRNN(wt.WaveCell(0.707, geom), [wt.WaveLineSource(14, 12, 14, 30), wt.WaveSource(20, 20)],
+                   [wt.WaveProbe(30, 20), wt.WaveIntensityProbe(30, 24)])
+    wt.io.save_model(m, "k", savedir=str(tmp_path) + "/", cfg={"dtype": "float32"}, verbose=False)
+    m2, _, _, _ = wt.io.load_model(str(tmp_path / "k.pt"))
+    assert [type(p) for p in m2.probes] == [wt.WaveProbe, wt.WaveIntensityProbe]
+    assert [s.cells() for s in m2.sources] == [s.cells() for s in m.sources]
+    assert m2.source_table(1) == m.source_table(1)
+    for (k, v), (k2, v2) in zip(m.state_dict().items(), m2.state_dict().items()):
+        assert k == k2 and torch.equal(v, v2)
+
+
 def test_synthetic_vowels_shape_and_norm():
     from wavetorch_gb300.data import vowel_like
     x, y = vowel_like(8, 3500, seed=3)
@@ -143,19 +180,15 @@ def _holey(d, dev="cpu"):
                                 x=d["x"].tolist(), y=d["y"].tolist(), r=d["r"].tolist()).to(dev)
 
 
-def test_holey_geometry_matches_reference_on_cpu():
-    """WaveGeometryHoley runs the reference's torch operations
-    (wavetorch/geom.py:88-132): on the CPU rho, c and the gradients with
-    respect to the holes' centres and radii are the reference's."""
-    import torch
+def test_holey_geometry_on_cpu_raises():
+    """Hole geometries have no CPU path: reading rho or c of CPU-held holes
+    raises, as every wave operation on CPU tensors does (the oracle, not the
+    product, evaluates them on the CPU: tests/test_oracle_golden.py)."""
     d = golden("holey")
     geom = _holey(d)
-    c = geom.c
-    gx, gy, gr = torch.autograd.grad((c * torch.from_numpy(d["w"])).sum(), [geom.x, geom.y, geom.r])
-    assert np.array_equal(geom.rho.detach().numpy(), d["rho"])
-    assert np.array_equal(c.detach().numpy(), d["c"])
-    for got, key in ((gx, "grad_x"), (gy, "grad_y"), (gr, "grad_r")):
-        assert np.allclose(got.numpy(), d[key], rtol=1e-6, atol=0), key
+    for name in ("rho", "c"):
+        with pytest.raises((RuntimeError, TypeError, ValueError)):
+            getattr(geom, name)
 
 
 def test_ragged_cluster_choice():
@@ -195,9 +228,8 @@ def test_save_load_roundtrip_hole_geometry(tmp_path):
     m2, _, _, _ = wt.io.load_model(str(tmp_path / "h.pt"))
     g2 = m2.cell.geom
     assert isinstance(g2, wt.WaveGeometryHoley)
-    for name in ("x", "y", "r"):
+    for name in ("x", "y", "r", "eta", "beta", "b"):
         assert torch.equal(getattr(g2, name), getattr(geom, name)), name
-    assert torch.equal(g2.rho, geom.rho) and torch.equal(g2.c, geom.c)
 
 
 def test_utils_match_the_reference_formulas():

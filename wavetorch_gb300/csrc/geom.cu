@@ -173,30 +173,18 @@ extern "C" int wt_rho_to_c_bwd(const wt_geom_desc* d, const float* rho, const fl
 // ---------------------------------------------------------------------------
 // wt_rho_to_c_fwd_noalloc: the same forward with its scratch (tanh values and
 // blurred density, 2 floats per cell) in this file-scope array instead of a
-// caller-owned buffer.  Each device has its own copy; the address of the
-// current device's copy is looked up once and cached.
-#include <mutex>
-
+// caller-owned buffer.  Each device has its own copy.  Its address on the
+// current device is looked up on every call (cudaGetSymbolAddress allocates
+// nothing), so no cached address can outlive a device reset or a re-created
+// primary context.
 static __device__ __align__(256) float g_rho_to_c_scratch[2 * (size_t)WT_RHO_TO_C_NOALLOC_MAX_CELLS];
 
-static constexpr int NOALLOC_MAX_DEVICES = 64;
-static std::mutex g_noalloc_mu;
-static float* g_noalloc_scratch[NOALLOC_MAX_DEVICES] = {};
-
-// Address of the current device's scratch array (looked up on first use).
+// Address of the current device's scratch array.
 static int noalloc_scratch(float** out) {
-    int dev = 0;
-    cudaError_t e = cudaGetDevice(&dev);
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_rho_to_c_scratch);
     if (e != cudaSuccess) return wt_cuda_status(e);
-    if (dev < 0 || dev >= NOALLOC_MAX_DEVICES) return WT_ERR_UNSUPPORTED;
-    std::lock_guard<std::mutex> lock(g_noalloc_mu);
-    if (!g_noalloc_scratch[dev]) {
-        void* p = nullptr;
-        e = cudaGetSymbolAddress(&p, g_rho_to_c_scratch);
-        if (e != cudaSuccess) return wt_cuda_status(e);
-        g_noalloc_scratch[dev] = static_cast<float*>(p);
-    }
-    *out = g_noalloc_scratch[dev];
+    *out = static_cast<float*>(p);
     return WT_OK;
 }
 

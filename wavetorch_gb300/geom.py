@@ -108,10 +108,11 @@ class WaveGeometry(torch.nn.Module):
 class WaveGeometryHoley(WaveGeometry):
     """Density from a sum of exponential holes, projected (wavetorch/geom.py:88-132).
 
-    With the holes on a CUDA device, rho and c come from one kernel
-    (:class:`~wavetorch_gb300.functional.HoleyFn`, ``wt_holey_fwd``) and their
-    gradients with respect to the holes' centres and radii from its adjoint
-    (``wt_holey_bwd``)."""
+    rho and c come from one kernel (:class:`~wavetorch_gb300.functional.HoleyFn`,
+    ``wt_holey_fwd``) and their gradients with respect to the holes' centres
+    and radii from its adjoint (``wt_holey_bwd``).  The holes must be on a
+    CUDA device: like every other operation here, reading ``rho`` or ``c`` of
+    CPU-held holes raises (there is no CPU path)."""
 
     def __init__(self, domain_shape: Tuple, h: float, c0: float, c1: float, abs_N: int = 20,
                  abs_sig: float = 11, abs_p: float = 4.0, eta: float = 0.5, beta: float = 100.0,
@@ -141,31 +142,15 @@ class WaveGeometryHoley(WaveGeometry):
         """(rho, c) on the GPU: one kernel evaluates both."""
         return HoleyFn.apply(self.x, self.y, self.r, self.holey_desc())
 
-    def _rho(self):
-        """The reference's torch operations (wavetorch/geom.py:109-123), for
-        holes held on the CPU."""
-        eta, beta = self.eta.item(), self.beta.item()
-        dev, dt = self.x.device, self.x.dtype
-        xv = torch.arange(0, self.domain_shape[0], dtype=dt, device=dev)
-        yv = torch.arange(0, self.domain_shape[1], dtype=dt, device=dev)
-        gx, gy = torch.meshgrid(xv, yv, indexing='ij')
-        rho = torch.zeros(self.domain_shape, dtype=dt, device=dev)
-        for ri, xi, yi in zip(self.r, self.x, self.y):
-            rho = rho + torch.exp(-torch.sqrt((gx - xi).pow(2) + (gy - yi).pow(2)) / ri)
-        return (np.tanh(beta * eta) + torch.tanh(beta * (rho - eta))) / (
-            np.tanh(beta * eta) + np.tanh(beta * (1 - eta)))
-
     @property
     def rho(self):
-        if self.x.is_cuda:
-            return self._rho_c()[0]
-        return self._rho()
+        """Projected density of the holes (a CUDA tensor; CPU holes raise)."""
+        return self._rho_c()[0]
 
     @property
     def c(self):
-        if self.x.is_cuda:
-            return self._rho_c()[1]
-        return self.c0.item() + (self.c1.item() - self.c0.item()) * self._rho()
+        """Wave speed c = c0 + (c1 - c0) * rho, from the same kernel as rho."""
+        return self._rho_c()[1]
 
 
 class WaveGeometryFreeForm(WaveGeometry):
