@@ -60,6 +60,10 @@ def parse():
                         "lens: 1024x1024, T=8000; fields: the benchmark's forward with every "
                         "field written; holey: the benchmark's step through 16 holes")
     p.add_argument("--instances", type=int, default=256, help="models in the ragged workload")
+    p.add_argument("--cluster", type=int, default=0,
+                   help="--kernels-only: CTAs per instance (0: the planner's choice, -1: bands)")
+    p.add_argument("--segment", type=int, default=0,
+                   help="--kernels-only: adjoint mode (0 auto, -1 tape, >0 checkpoint interval)")
     return p.parse_args()
 
 
@@ -642,7 +646,8 @@ def run_kernels_only(args):
     b = model.cell.geom.b.contiguous()
     prb, _ = model.probe_table()
     spec = SeqSpec(B, N, N, T, model.source_table(B), prb,
-                   form=_lib.WT_FORM_FUSED if args.form == "fused" else _lib.WT_FORM_PLAIN)
+                   form=_lib.WT_FORM_FUSED if args.form == "fused" else _lib.WT_FORM_PLAIN,
+                   cluster=args.cluster, segment=args.segment)
     sc = scalars(0.707, 1.0, lap_order(B, N, N, 1.0))
     g = torch.randn(B, T, len(prb), generator=torch.Generator().manual_seed(3)).to(dev)
     t = []
@@ -659,7 +664,7 @@ def run_kernels_only(args):
     f = sum(a for a, _ in t) / len(t)
     bw = sum(b_ for _, b_ in t) / len(t)
     print(json.dumps({"kernels_only": True, "batch": B, "T": T, "form": args.form,
-                      "ms_fwd": f, "ms_bwd": bw,
+                      "cluster": args.cluster, "segment": args.segment, "ms_fwd": f, "ms_bwd": bw,
                       "cell_steps_per_s": B * N * N * T / ((f + bw) / 1e3)}))
 
 

@@ -42,7 +42,8 @@ typedef struct CUstream_st* wt_stream_t; /* == cudaStream_t */
  *   WT_LAP_SEQ    : ((((w*u + w*l) - 4w*c) + w*r) + w*d)   (fused multiply-adds)
  *   WT_LAP_PAIRED : (u + l) + (-4c + (r + d))              (h == 1 only)
  * u/d are the x-1/x+1 neighbours, l/r the y-1/y+1 neighbours; taps outside the
- * grid are zero (Dirichlet, conv2d padding=1).                              */
+ * grid are zero (Dirichlet, conv2d padding=1).  WT_LAP_PAIRED with an h whose
+ * h**-2 is not exactly 1 is refused with WT_ERR_INVALID.                    */
 #define WT_LAP_SEQ     0
 #define WT_LAP_PAIRED  1
 

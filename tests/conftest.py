@@ -9,6 +9,15 @@ if ROOT not in sys.path:
 
 GOLDEN = os.path.join(ROOT, "tests", "golden")
 
+# Relative L2 tolerance of the fused form's dL/dc against the plain form, the
+# oracle and the reference's autograd (which sum grad_c = (X1 * (Kc * Lap)) * g
+# step by step): the fused kernels sum Lap * g per cell over time with fused
+# multiply-adds, per instance, and apply the time-invariant X1 * Kc once.
+# Both sums round differently by a few ulps per term; over thousands of steps
+# with cancellation the difference stays below this bound (the path's parity
+# bar against the reference is 1e-5).
+FUSED_DC_TOL = 5e-6
+
 
 def pytest_configure(config):
     config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300, sm_103a)")

@@ -4,6 +4,8 @@ plain/fused agreement at full length, and size-independent properties
 (exact linearity under power-of-two input scaling, silence for zero input)."""
 import numpy as np
 import pytest
+
+from conftest import FUSED_DC_TOL
 import torch
 
 import oracle.oracle as o
@@ -47,7 +49,7 @@ def run(spec, sc, b, c, x, g=None):
 
 def test_cfg1_batch_against_oracle_truncated(cuda):
     """B=32, 120x120, first 600 steps: plain form bit-exact with the oracle,
-    fused form forward bit-exact and dL/dc within 1e-6."""
+    fused form forward bit-exact and dL/dc within FUSED_DC_TOL."""
     B, N, steps = 32, 120, 600
     b, c, x, _, src, prb = cfg1_problem(cuda, B, N, 3500)
     x = x[:, :steps].contiguous()
@@ -63,7 +65,7 @@ def test_cfg1_batch_against_oracle_truncated(cuda):
         if form == _lib.WT_FORM_PLAIN:
             assert np.array_equal(gc.cpu().numpy(), ogc)
         else:
-            assert rel(gc.cpu().numpy(), ogc) <= 1e-6
+            assert rel(gc.cpu().numpy(), ogc) <= FUSED_DC_TOL
 
 
 def test_cfg1_full_plain_vs_fused(cuda):
@@ -123,7 +125,7 @@ def test_ragged_segments(cuda):
     for seg in (1, 7, 64, 301, 1000, -1):   # -1: tape mode
         spec = SeqSpec(B, 120, 120, steps, src, prb, form=_lib.WT_FORM_FUSED, segment=seg)
         _, gf = run(spec, sc, b, c, x, g)
-        assert rel(gf.cpu().numpy(), gref.cpu().numpy()) <= 1e-6, seg
+        assert rel(gf.cpu().numpy(), gref.cpu().numpy()) <= FUSED_DC_TOL, seg
 
 
 @pytest.mark.parametrize("cluster", [1, 2, 4, 8])
@@ -143,7 +145,7 @@ def test_cluster_sizes_agree(cuda, cluster):
     f_out, f_gc = run(SeqSpec(2, N, N, 200, src, prb, form=_lib.WT_FORM_FUSED, cluster=cluster),
                       sc, b, c, x, g)
     assert torch.equal(p_out, f_out)
-    assert rel(f_gc.cpu().numpy(), p_gc.cpu().numpy()) <= 1e-6
+    assert rel(f_gc.cpu().numpy(), p_gc.cpu().numpy()) <= FUSED_DC_TOL
 
 
 def test_tape_and_checkpoint_modes_agree_bitwise(cuda):
@@ -167,7 +169,7 @@ def test_tape_and_checkpoint_modes_agree_bitwise(cuda):
 @pytest.mark.parametrize("N", [200, 256])
 def test_large_grids_fused_agree_with_plain(cuda, N):
     """Grids above 160x160 run on 16-CTA clusters: forward identical to the
-    plain form (bit-exact with the reference), dL/dc within 1e-6."""
+    plain form (bit-exact with the reference), dL/dc within FUSED_DC_TOL."""
     geom = wt.WaveGeometryFreeForm((N, N), 1.0, c0=1.0, c1=0.5, abs_N=20, abs_sig=3.0, abs_p=2,
                                    rho=torch.rand(N, N, generator=torch.Generator().manual_seed(N))).to(cuda)
     with torch.no_grad():
@@ -182,14 +184,14 @@ def test_large_grids_fused_agree_with_plain(cuda, N):
     p_out, p_gc = run(SeqSpec(B, N, N, steps, src, prb, form=_lib.WT_FORM_PLAIN), sc, b, c, x, g)
     f_out, f_gc = run(SeqSpec(B, N, N, steps, src, prb, form=_lib.WT_FORM_FUSED), sc, b, c, x, g)
     assert torch.equal(p_out, f_out)
-    assert rel(f_gc.cpu().numpy(), p_gc.cpu().numpy()) <= 1e-6
+    assert rel(f_gc.cpu().numpy(), p_gc.cpu().numpy()) <= FUSED_DC_TOL
 
 
 @pytest.mark.parametrize("N", [64, 150])
 def test_per_instance_geometries(cuda, N):
     """coef_batched: three instances with their own rho (own c) in one fused
     launch agree with three separate single-instance runs of the plain form:
-    outputs bit for bit, per-instance dL/dc within 1e-6."""
+    outputs bit for bit, per-instance dL/dc within FUSED_DC_TOL."""
     B, steps = 3, 250
     cs, bs = [], None
     for i in range(B):
@@ -212,7 +214,7 @@ def test_per_instance_geometries(cuda, N):
         one = SeqSpec(1, N, N, steps, src, prb, form=_lib.WT_FORM_PLAIN)
         o1, g1 = run(one, sc, bs, cs[i], x[i:i + 1].contiguous(), g[i:i + 1].contiguous())
         assert torch.equal(out[i:i + 1], o1), i
-        assert rel(gc[i].cpu().numpy(), g1.cpu().numpy()) <= 1e-6, i
+        assert rel(gc[i].cpu().numpy(), g1.cpu().numpy()) <= FUSED_DC_TOL, i
 
 
 @pytest.mark.parametrize("b0,cnl", [(0.05, 0.1), (0.05, 0.0), (0.0, 0.1)])

@@ -18,7 +18,11 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB_NAME = "libwavetorch_gb300.so"
 LIB_PATH = os.path.join(HERE, LIB_NAME)
-SOURCES = ["api.cu", "step.cu", "seq_fused.cu", "seq_band.cu", "geom.cu", "holey.cu", "ragged.cu"]
+# (source, object name, extra flags): seq_fused.cu builds as four parts (its
+# kernels per Laplacian order) so that they compile in parallel
+SOURCES = [("api.cu", "api", []), ("step.cu", "step", []), ("seq_band.cu", "seq_band", []),
+           ("geom.cu", "geom", []), ("holey.cu", "holey", []), ("ragged.cu", "ragged", [])] + \
+          [("seq_fused.cu", f"seq_fused_{k}", [f"-DWT_FUSED_PART={k}"]) for k in range(4)]
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = [
@@ -38,9 +42,10 @@ def nvcc_path() -> str:
     raise RuntimeError("nvcc not found: the CUDA toolkit is required to build wavetorch_gb300")
 
 
-def _compile(src: str, verbose: bool) -> tuple[str, str]:
-    obj = os.path.join(BUILD, os.path.splitext(src)[0] + ".o")
-    cmd = [nvcc_path(), *ARCH, *NVCC_FLAGS, "-c", os.path.join(CSRC, src), "-o", obj]
+def _compile(unit, verbose: bool) -> tuple[str, str]:
+    src, name, extra = unit
+    obj = os.path.join(BUILD, name + ".o")
+    cmd = [nvcc_path(), *ARCH, *NVCC_FLAGS, *extra, "-c", os.path.join(CSRC, src), "-o", obj]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"nvcc failed for {src}:\n{r.stdout}\n{r.stderr}")

@@ -32,13 +32,17 @@ StepScalars wt_make_scalars(const wt_scalars* s) {
     const float hh = h * h;
     k.lap_w = 1.0f / hh;
     k.lap_w4 = k.lap_w * -4.0f;
-    k.lap_order = s->lap_order;
+    k.lap_order = s->lap_order | (k.lap_w == 1.0f ? WT_LAP_UNIT : 0);
     return k;
 }
 
+// WT_LAP_PAIRED is the order of the reference's im2col path, which it takes
+// for h == 1 only (h**-2 must be exactly 1: the kernels then add the taps
+// without multiplying them).
 static bool scalars_ok(const wt_scalars* s) {
     return s && std::isfinite(s->dt) && s->dt > 0.f && std::isfinite(s->h) && s->h > 0.f &&
-           (s->lap_order == WT_LAP_SEQ || s->lap_order == WT_LAP_PAIRED);
+           (s->lap_order == WT_LAP_SEQ ||
+            (s->lap_order == WT_LAP_PAIRED && 1.0f / (s->h * s->h) == 1.0f));
 }
 
 extern "C" const char* wt_version(void) { return "wavetorch_gb300 0.1.0 sm_103a"; }

@@ -29,14 +29,29 @@ struct StepScalars {
     float dt2;       // dt**2         = dt*dt
     float lap_w;     // h**-2         = 1/(h*h)
     float lap_w4;    // h**-2 * -4
-    int lap_order;   // WT_LAP_SEQ / WT_LAP_PAIRED
+    int lap_order;   // WT_LAP_SEQ / WT_LAP_PAIRED, | WT_LAP_UNIT when lap_w == 1
 };
+
+// Internal Laplacian orders: WT_LAP_SEQ / WT_LAP_PAIRED plus this flag when
+// the tap weight h**-2 is exactly 1 (h == 1).  Then w*v == v exactly and
+// fma(1, v, a) rounds as v + a, so the unit-weight forms drop the
+// multiplications by w and give the same bits with fewer instructions.
+constexpr int WT_LAP_UNIT = 2;
 
 // 5-point Laplacian with the association order of the reference's conv2d.
 // u = (x-1,y), l = (x,y-1), c = (x,y), r = (x,y+1), d = (x+1,y).
 template <int ORDER>
 WT_DEV float lap5(float u, float l, float c, float r, float d, float w, float w4) {
-    if (ORDER == WT_LAP_SEQ) {
+    if constexpr (ORDER == (WT_LAP_SEQ | WT_LAP_UNIT)) {
+        float acc = fadd(u, l);
+        acc = ffma(w4, c, acc);
+        acc = fadd(acc, r);
+        return fadd(acc, d);
+    } else if constexpr (ORDER == (WT_LAP_PAIRED | WT_LAP_UNIT)) {
+        const float ul = fadd(u, l);
+        const float rd = fadd(r, d);
+        return fadd(ul, fadd(fmul(w4, c), rd));
+    } else if constexpr (ORDER == WT_LAP_SEQ) {
         float acc = fmul(w, u);
         acc = ffma(w, l, acc);
         acc = ffma(w4, c, acc);

@@ -173,5 +173,14 @@ int wt_launch_probe_sum(int batch, int steps, int n_prb, const float* out, float
 int wt_launch_loss_ce_np(int batch, int n_prb, const float* sum, const int64_t* labels,
                          float* loss, float* grad_sum, cudaStream_t st);
 int wt_launch_fused(bool fwd, const wt::FusedParams& P, const WtFusedLaunch& L, cudaStream_t st);
+// The same for one Laplacian order each (seq_fused.cu, parts 1 to 3).
+#define WT_FUSED_ORDER_DECL(name)                                                                 \
+    int wt_launch_fused_##name(bool fwd, const wt::FusedParams& P, const WtFusedLaunch& L,        \
+                               cudaStream_t st);                                                  \
+    int wt_launch_fused_nl_##name(bool fwd, const wt::FusedParams& P, const WtFusedLaunch& L,     \
+                                  cudaStream_t st);
+WT_FUSED_ORDER_DECL(seq)
+WT_FUSED_ORDER_DECL(seq_unit)
+WT_FUSED_ORDER_DECL(paired_unit)
 // Nonlinear cell, tape mode: nbuf ring slices of two parts (Lap, field).
 int wt_launch_fused_nl(bool fwd, const wt::FusedParams& P, const WtFusedLaunch& L, cudaStream_t st);

@@ -558,8 +558,7 @@ __global__ void __launch_bounds__(MAX_THREADS, 1) seq_bwd_band_kernel(FusedParam
             auto update = [&](int i, float up, float dn) {
                 const float lg = lap5<ORDER>(up, col[i - LD], col[i], col[i + LD], dn, w, w4);
                 const float X1 = IN ? 1.0f : ln.coef[i], Ky2 = IN ? -1.0f : ln.coef[3 * M + i];
-                const float Kc = ln.coef[M + i];
-                acc[i] = fadd(acc[i], fmul(fmul(X1, fmul(Kc, lys[i * NT])), lam[i]));
+                acc[i] = ffma(lys[i * NT], lam[i], acc[i]);   // sum_t Lap * lam (see below)
                 const float gy1 = fadd(fmul(dt2, lg), fmul(fmul(2.0f, lam[i]), X1));
                 const float g2 = fmul(Ky2, lam[i]);
                 lam[i] = fadd(pend[i], gy1);
@@ -599,11 +598,14 @@ __global__ void __launch_bounds__(MAX_THREADS, 1) seq_bwd_band_kernel(FusedParam
     cp_async_wait_all();   // no copy outlives the kernel's shared memory
     if (!aborted) aborted = __syncthreads_or(gave_up);
     if (aborted || !g.colv) return;
+    // dL/dc = (X1 * Kc) * sum_t Lap(h_{t-1}) * lam_t: grad_c of cell.py:36 with
+    // its time-invariant factor applied once
     float* o = P.gc_part + (size_t)g.inst * P.nx * P.ny;
 #pragma unroll
     for (int i = 0; i < M; ++i) {
         const int gx = g.gx0 + i;
-        if (gx < P.nx) o[(size_t)gx * P.ny + g.col] = acc[i];
+        if (gx < P.nx)
+            o[(size_t)gx * P.ny + g.col] = fmul(fmul(ln.coef[i], ln.coef[M + i]), acc[i]);
     }
 }
 
@@ -723,6 +725,10 @@ int wt_launch_band(bool fwd, const wt::FusedParams& P0, const WtBandLaunch& L, c
     wt::FusedParams P = P0;
     P.C = L.PR; P.R = L.R; P.NCP = L.NCP; P.LD = L.LD; P.PB = L.PB;
     P.abort_g = reinterpret_cast<int*>(P.halo + (size_t)P.batch * L.PR * 4 * L.NCP);
-    return P.k.lap_order == WT_LAP_SEQ ? launch_band_order<WT_LAP_SEQ>(fwd, P, L, st)
-                                       : launch_band_order<WT_LAP_PAIRED>(fwd, P, L, st);
+    switch (P.k.lap_order) {
+        case WT_LAP_SEQ: return launch_band_order<WT_LAP_SEQ>(fwd, P, L, st);
+        case WT_LAP_SEQ | WT_LAP_UNIT: return launch_band_order<WT_LAP_SEQ | WT_LAP_UNIT>(fwd, P, L, st);
+        case WT_LAP_PAIRED | WT_LAP_UNIT: return launch_band_order<WT_LAP_PAIRED | WT_LAP_UNIT>(fwd, P, L, st);
+    }
+    return WT_ERR_INVALID;
 }

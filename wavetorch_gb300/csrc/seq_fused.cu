@@ -402,16 +402,37 @@ WT_DEV void load_fwd_coef(const FusedParams& P, const Geo& g, float (&A)[M], flo
     }
 }
 template <int M>
-WT_DEV void load_bwd_coef(const FusedParams& P, const Geo& g, float (&X1)[M], float (&Kc)[M],
-                          float (&Kg)[M], float (&Ky2)[M]) {
+WT_DEV void load_bwd_coef(const FusedParams& P, const Geo& g, float (&X1)[M], float (&Kg)[M],
+                          float (&Ky2)[M]) {
 #pragma unroll
     for (int i = 0; i < M; ++i) {
-        X1[i] = Kc[i] = Kg[i] = Ky2[i] = 0.f;
+        X1[i] = Kg[i] = Ky2[i] = 0.f;
         int gx = g.gx0 + i;
         if (g.colv && gx < P.nx) {
             size_t cell = P.coef_stride * g.inst + (size_t)gx * P.ny + g.col;
             BwdCoef k = bwd_coef(__ldg(P.b + cell), __ldg(P.c + cell), P.k);
-            X1[i] = k.X1; Kc[i] = k.Kc; Kg[i] = k.Kg; Ky2[i] = k.Ky2;
+            X1[i] = k.X1; Kg[i] = k.Kg; Ky2[i] = k.Ky2;
+        }
+    }
+}
+
+// Per-step factor of a cell's dL/dc (wavetorch/cell.py:36):
+// grad_c = (X1 * (Kc * Lap(h_{t-1}))) * g, so dL/dc = (X1 * Kc) * sum_t Lap * g.
+WT_DEV float dc_scale(const FusedParams& P, size_t cell) {
+    const BwdCoef k = bwd_coef(__ldg(P.b + cell), __ldg(P.c + cell), P.k);
+    return fmul(k.X1, k.Kc);
+}
+
+// Write the thread's per-instance dL/dc: its sums scaled by dc_scale.
+template <int M>
+WT_DEV void store_dc(const FusedParams& P, const Geo& g, const float (&acc)[M]) {
+    float* o = P.gc_part + (size_t)g.inst * P.nx * P.ny;
+#pragma unroll
+    for (int i = 0; i < M; ++i) {
+        int gx = g.gx0 + i;
+        if (gx < P.nx) {
+            const size_t cell = (size_t)gx * P.ny + g.col;
+            o[cell] = fmul(dc_scale(P, P.coef_stride * g.inst + cell), acc[i]);
         }
     }
 }
@@ -933,11 +954,14 @@ WT_DEV void seed_and_read(const FusedParams& P, const Geo& g, const Taps& tp, in
     }
 }
 
-// Adjoint of one cell (wavetorch/cell.py:36-42 with autograd's accumulation):
-// dL/dc += (X1 * (Kc * Lap(h_{t-1}))) * lam; pending grad_y1 / grad_y2 terms.
-WT_DEV void adj_cell(float lg, float lam, float Ly, float X1, float Kc, float Ky2, float dt2,
+// Adjoint of one cell (wavetorch/cell.py:36-42): pending grad_y1 / grad_y2
+// terms in autograd's order, and the running sum acc = sum_t Lap(h_{t-1}) *
+// lam_t of the cell's dL/dc = X1 * Kc * acc (the per-step factor
+// X1 * Kc = (b dt + 1)^-1 * 2 c dt^2 is applied once, when the sum is
+// written: dc_scale).
+WT_DEV void adj_cell(float lg, float lam, float Ly, float X1, float Ky2, float dt2,
                      float& acc, float& gy1, float& gy2a, float& gy2b) {
-    acc = fadd(acc, fmul(fmul(X1, fmul(Kc, Ly)), lam));
+    acc = ffma(Ly, lam, acc);
     gy1 = fadd(fmul(dt2, lg), fmul(fmul(2.0f, lam), X1));
     gy2b = gy2a;
     gy2a = fmul(Ky2, lam);
@@ -949,9 +973,9 @@ WT_DEV void adj_cell(float lg, float lam, float Ly, float X1, float Kc, float Ky
 // carries this step's grad_y2 term one step.  Same operations as adj_cell
 // followed by the next step's sum (which the checkpoint kernel forms at the
 // start of that step).
-WT_DEV void adj_cell_lp(float lg, float& lam, float Ly, float X1, float Kc, float Ky2, float dt2,
+WT_DEV void adj_cell_lp(float lg, float& lam, float Ly, float X1, float Ky2, float dt2,
                         float& acc, float& pend) {
-    acc = fadd(acc, fmul(fmul(X1, fmul(Kc, Ly)), lam));
+    acc = ffma(Ly, lam, acc);
     const float gy1 = fadd(fmul(dt2, lg), fmul(fmul(2.0f, lam), X1));
     const float g2 = fmul(Ky2, lam);
     lam = fadd(pend, gy1);
@@ -1038,8 +1062,8 @@ __global__ void __launch_bounds__(bwd_max_threads(M), 1) seq_bwd_fused_kernel(Fu
         // the last recompute step's stash entries were written by this thread
         // itself, so the adjoint reads them back without a barrier
         // ---- adjoint sweep over the segment ----
-        float X1[M], Kc[M], Kg[M], Ky2[M];
-        load_bwd_coef<M>(P, g, X1, Kc, Kg, Ky2);
+        float X1[M], Kg[M], Ky2[M];
+        load_bwd_coef<M>(P, g, X1, Kg, Ky2);
         for (int t = t1 - 1; t >= t0; --t) {
             float lam[M], c2g[M];
 #pragma unroll
@@ -1066,29 +1090,22 @@ __global__ void __launch_bounds__(bwd_max_threads(M), 1) seq_bwd_fused_kernel(Fu
                 lds_col<M>(Ly, sh.step(t - t0));
 #pragma unroll
                 for (int i = 1; i < M - 1; ++i)
-                    adj_cell(lap_cell<M, ORDER>(P, c, c2g, i), lam[i], Ly[i], X1[i], Kc[i], Ky2[i],
+                    adj_cell(lap_cell<M, ORDER>(P, c, c2g, i), lam[i], Ly[i], X1[i], Ky2[i],
                              P.k.dt2, acc[i], gy1[i], gy2a[i], gy2b[i]);
                 if (g.strip == 0 && g.has_up)
                     c.up = recv_word(P, X, X.hup + (kx & 1) * X.NCP + g.col, kx);
                 if (g.strip == g.S - 1 && g.has_dn)
                     c.dn = recv_word(P, X, X.hdn + (kx & 1) * X.NCP + g.col, kx);
-                adj_cell(lap_cell<M, ORDER>(P, c, c2g, 0), lam[0], Ly[0], X1[0], Kc[0], Ky2[0],
+                adj_cell(lap_cell<M, ORDER>(P, c, c2g, 0), lam[0], Ly[0], X1[0], Ky2[0],
                          P.k.dt2, acc[0], gy1[0], gy2a[0], gy2b[0]);
                 adj_cell(lap_cell<M, ORDER>(P, c, c2g, M - 1), lam[M - 1], Ly[M - 1], X1[M - 1],
-                         Kc[M - 1], Ky2[M - 1], P.k.dt2, acc[M - 1], gy1[M - 1], gy2a[M - 1],
+                         Ky2[M - 1], P.k.dt2, acc[M - 1], gy1[M - 1], gy2a[M - 1],
                          gy2b[M - 1]);
             }
             ++kx;
         }
     }
-    if (g.colv && ok) {
-        float* o = P.gc_part + (size_t)g.inst * plane;
-#pragma unroll
-        for (int i = 0; i < M; ++i) {
-            int gx = g.gx0 + i;
-            if (gx < P.nx) o[(size_t)gx * P.ny + g.col] = acc[i];
-        }
-    }
+    if (g.colv && ok) store_dc<M>(P, g, acc);
     cluster_sync_all();
 }
 
@@ -1143,7 +1160,6 @@ __global__ void __launch_bounds__(bwd_max_threads(M), 1) seq_bwd_tape_kernel(Fus
     Taps tp;
     build_taps<M>(P, g, tp);
 
-    const size_t plane = (size_t)P.nx * P.ny;
     float* seeds = smem + 2 * tile + 2 * xchg_words(P.NCP);
     TapeRing ring;
     ring.buf = seeds + ((2 * P.n_prb * P.PB + 3) & ~3);
@@ -1154,8 +1170,8 @@ __global__ void __launch_bounds__(bwd_max_threads(M), 1) seq_bwd_tape_kernel(Fus
         fence_mbarrier_init_cluster();
     }
 
-    float X1[M], Kc[M], Kg[M], Ky2[M];
-    load_bwd_coef<M>(P, g, X1, Kc, Kg, Ky2);
+    float X1[M], Kg[M], Ky2[M];
+    load_bwd_coef<M>(P, g, X1, Kg, Ky2);
     // adjoint state: lam (this step's lambda before its seeds), pend (the
     // grad_y2 term of the previous step), the running dL/dc
     float lam[M], pend[M], acc[M];
@@ -1225,14 +1241,14 @@ __global__ void __launch_bounds__(bwd_max_threads(M), 1) seq_bwd_tape_kernel(Fus
             ld_chunks_at<M>(Ly, ly, cstride);
 #pragma unroll
             for (int i = 1; i < M - 1; ++i)
-                adj_cell_lp(lap_cell<M, ORDER>(P, c, c2g, i), lam[i], Ly[i], X1[i], Kc[i], Ky2[i],
+                adj_cell_lp(lap_cell<M, ORDER>(P, c, c2g, i), lam[i], Ly[i], X1[i], Ky2[i],
                             P.k.dt2, acc[i], pend[i]);
             if (ln.rup) c.up = recv_at(P, X, ln.rup + PAR * ln.pstride, u);
             if (ln.rdn) c.dn = recv_at(P, X, ln.rdn + PAR * ln.pstride, u);
-            adj_cell_lp(lap_cell<M, ORDER>(P, c, c2g, 0), lam[0], Ly[0], X1[0], Kc[0], Ky2[0],
+            adj_cell_lp(lap_cell<M, ORDER>(P, c, c2g, 0), lam[0], Ly[0], X1[0], Ky2[0],
                         P.k.dt2, acc[0], pend[0]);
             adj_cell_lp(lap_cell<M, ORDER>(P, c, c2g, M - 1), lam[M - 1], Ly[M - 1], X1[M - 1],
-                        Kc[M - 1], Ky2[M - 1], P.k.dt2, acc[M - 1], pend[M - 1]);
+                        Ky2[M - 1], P.k.dt2, acc[M - 1], pend[M - 1]);
         }
         if (slot == 0) { slot = P.nbuf - 1; ly = ly_top; }
         else           { --slot; ly -= ring.slice; }
@@ -1251,14 +1267,7 @@ __global__ void __launch_bounds__(bwd_max_threads(M), 1) seq_bwd_tape_kernel(Fus
         for (int s = lo; s < lo + P.nbuf && s < P.steps; ++s)
             tape_wait(P, X, ring, s % P.nbuf, (uint32_t)(((P.steps - 1 - s) / P.nbuf) & 1));
     }
-    if (g.colv && ok) {
-        float* o = P.gc_part + (size_t)g.inst * plane;
-#pragma unroll
-        for (int i = 0; i < M; ++i) {
-            int gx = g.gx0 + i;
-            if (gx < P.nx) o[(size_t)gx * P.ny + g.col] = acc[i];
-        }
-    }
+    if (g.colv && ok) store_dc<M>(P, g, acc);
     cluster_sync_all();
 }
 
@@ -1464,7 +1473,18 @@ __global__ void __launch_bounds__(bwd_max_threads(M), 1) seq_bwd_nl_kernel(Fused
 }  // namespace wt
 
 // ---------------------------------------------------------------------------
-// Host side: configuration and launch
+// Host side: configuration and launch.
+// The file is compiled as four parts so that the kernels of the three
+// Laplacian orders build in parallel: WT_FUSED_PART 0 holds the planner, the
+// small kernels and the dispatch by order; parts 1, 2 and 3 instantiate the
+// sequence kernels of WT_LAP_SEQ, WT_LAP_SEQ | WT_LAP_UNIT and
+// WT_LAP_PAIRED | WT_LAP_UNIT.  Without WT_FUSED_PART the file holds all.
+#ifndef WT_FUSED_PART
+#define WT_FUSED_PART -1
+#endif
+#define WT_FUSED_HAS(part) (WT_FUSED_PART == -1 || WT_FUSED_PART == (part))
+
+#if WT_FUSED_HAS(0)
 // Column stride of a tile: room for OFF + rows + 1 floats, and conflict-free
 // column accesses of the width the M-cell strips use (float4: LD/4 odd;
 // float2: LD/2 odd; scalar: LD odd).
@@ -1586,31 +1606,6 @@ int wt_launch_probe_sum(int batch, int steps, int n_prb, const float* out, float
     return wt_cuda_status(cudaGetLastError());
 }
 
-// Kernel attributes (dynamic shared memory size, non-portable cluster size)
-// are set once per kernel and device, and raised when a launch needs more:
-// not repeated on every launch, which keeps launches cheap on the host and
-// free of extra runtime calls while a stream is being captured.
-static int ensure_attributes(void (*kern)(wt::FusedParams), size_t smem, bool nonportable) {
-    int dev = 0;
-    cudaError_t e = cudaGetDevice(&dev);
-    if (e != cudaSuccess) return wt_cuda_status(e);
-    static std::mutex mu;
-    static std::map<std::pair<int, const void*>, std::pair<size_t, bool>> done;
-    std::lock_guard<std::mutex> lock(mu);
-    auto& v = done[{dev, reinterpret_cast<const void*>(kern)}];
-    if (v.first < smem) {
-        e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e != cudaSuccess) return wt_cuda_status(e);
-        v.first = smem;
-    }
-    if (nonportable && !v.second) {
-        e = cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
-        if (e != cudaSuccess) return wt_cuda_status(e);
-        v.second = true;
-    }
-    return WT_OK;
-}
-
 // The reference's training loss on the time-summed probe outputs
 // (wavetorch/train.py:61-62, utils.py:35-36), and its gradient:
 //   p = I / sum_q I,  loss = mean_b CE(p_b, label_b) = mean_b (lse(p_b) - p_b[label])
@@ -1657,6 +1652,34 @@ int wt_launch_loss_ce_np(int batch, int n_prb, const float* sum, const int64_t* 
     loss_ce_np_kernel<<<1, 256, 0, st>>>(batch, n_prb, sum, labels, loss, grad_sum);
     wt_count_launches(1);
     return wt_cuda_status(cudaGetLastError());
+}
+
+#endif  // part 0
+
+#if !WT_FUSED_HAS(0) || WT_FUSED_PART == -1
+// Kernel attributes (dynamic shared memory size, non-portable cluster size)
+// are set once per kernel and device, and raised when a launch needs more:
+// not repeated on every launch, which keeps launches cheap on the host and
+// free of extra runtime calls while a stream is being captured.
+static int ensure_attributes(void (*kern)(wt::FusedParams), size_t smem, bool nonportable) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return wt_cuda_status(e);
+    static std::mutex mu;
+    static std::map<std::pair<int, const void*>, std::pair<size_t, bool>> done;
+    std::lock_guard<std::mutex> lock(mu);
+    auto& v = done[{dev, reinterpret_cast<const void*>(kern)}];
+    if (v.first < smem) {
+        e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return wt_cuda_status(e);
+        v.first = smem;
+    }
+    if (nonportable && !v.second) {
+        e = cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+        if (e != cudaSuccess) return wt_cuda_status(e);
+        v.second = true;
+    }
+    return WT_OK;
 }
 
 static int launch_kernel(void (*kern)(wt::FusedParams), const wt::FusedParams& P, int C,
@@ -1744,12 +1767,43 @@ static int launch_nl_order(bool fwd, const wt::FusedParams& P, const WtFusedLaun
     return WT_ERR_UNSUPPORTED;
 }
 
+#endif  // kernel parts
+
+#define WT_FUSED_ORDER_ENTRY(part, name, order)                                                  \
+    int wt_launch_fused_##name(bool fwd, const wt::FusedParams& P, const WtFusedLaunch& L,       \
+                               cudaStream_t st) {                                                \
+        return launch_order<order>(fwd, P, L, st);                                               \
+    }                                                                                            \
+    int wt_launch_fused_nl_##name(bool fwd, const wt::FusedParams& P, const WtFusedLaunch& L,    \
+                                  cudaStream_t st) {                                             \
+        return launch_nl_order<order>(fwd, P, L, st);                                            \
+    }
+#if WT_FUSED_HAS(1)
+WT_FUSED_ORDER_ENTRY(1, seq, WT_LAP_SEQ)
+#endif
+#if WT_FUSED_HAS(2)
+WT_FUSED_ORDER_ENTRY(2, seq_unit, WT_LAP_SEQ | WT_LAP_UNIT)
+#endif
+#if WT_FUSED_HAS(3)
+WT_FUSED_ORDER_ENTRY(3, paired_unit, WT_LAP_PAIRED | WT_LAP_UNIT)
+#endif
+
+#if WT_FUSED_HAS(0)
 int wt_launch_fused_nl(bool fwd, const wt::FusedParams& P, const WtFusedLaunch& L, cudaStream_t st) {
-    return P.k.lap_order == WT_LAP_SEQ ? launch_nl_order<WT_LAP_SEQ>(fwd, P, L, st)
-                                       : launch_nl_order<WT_LAP_PAIRED>(fwd, P, L, st);
+    switch (P.k.lap_order) {
+        case WT_LAP_SEQ: return wt_launch_fused_nl_seq(fwd, P, L, st);
+        case WT_LAP_SEQ | WT_LAP_UNIT: return wt_launch_fused_nl_seq_unit(fwd, P, L, st);
+        case WT_LAP_PAIRED | WT_LAP_UNIT: return wt_launch_fused_nl_paired_unit(fwd, P, L, st);
+    }
+    return WT_ERR_INVALID;
 }
 
 int wt_launch_fused(bool fwd, const wt::FusedParams& P, const WtFusedLaunch& L, cudaStream_t st) {
-    return P.k.lap_order == WT_LAP_SEQ ? launch_order<WT_LAP_SEQ>(fwd, P, L, st)
-                                       : launch_order<WT_LAP_PAIRED>(fwd, P, L, st);
+    switch (P.k.lap_order) {
+        case WT_LAP_SEQ: return wt_launch_fused_seq(fwd, P, L, st);
+        case WT_LAP_SEQ | WT_LAP_UNIT: return wt_launch_fused_seq_unit(fwd, P, L, st);
+        case WT_LAP_PAIRED | WT_LAP_UNIT: return wt_launch_fused_paired_unit(fwd, P, L, st);
+    }
+    return WT_ERR_INVALID;
 }
+#endif

@@ -502,7 +502,7 @@ int wt_launch_step_fwd(const StepScalars& k, int batch, int nx, int ny, int coef
         wt::SeqEpilogue e{};
         if (epi) e = *epi;
         const bool ep = epi != nullptr;
-        if (k.lap_order == WT_LAP_SEQ) {
+        if ((k.lap_order & 1) == WT_LAP_SEQ) {
             if (ep) wt::step_fwd4_kernel<WT_LAP_SEQ, true><<<grd, blk, 0, st>>>(k, nx, ny, coef_batched, b, c, y1, bs1, y2, bs2, y, bs, e);
             else    wt::step_fwd4_kernel<WT_LAP_SEQ, false><<<grd, blk, 0, st>>>(k, nx, ny, coef_batched, b, c, y1, bs1, y2, bs2, y, bs, e);
         } else {
@@ -516,13 +516,13 @@ int wt_launch_step_fwd(const StepScalars& k, int batch, int nx, int ny, int coef
     dim3 grd((ny + wt::TY - 1) / wt::TY, (nx + wt::TX - 1) / wt::TX, batch);
     if (epi) {
         const wt::SeqEpilogue& e = *epi;
-        if (k.lap_order == WT_LAP_SEQ)
+        if ((k.lap_order & 1) == WT_LAP_SEQ)
             wt::step_fwd_kernel<WT_LAP_SEQ, true><<<grd, blk, 0, st>>>(k, nx, ny, coef_batched, b, c, y1, bs1, y2, bs2, y, bs, e);
         else
             wt::step_fwd_kernel<WT_LAP_PAIRED, true><<<grd, blk, 0, st>>>(k, nx, ny, coef_batched, b, c, y1, bs1, y2, bs2, y, bs, e);
     } else {
         wt::SeqEpilogue e{};
-        if (k.lap_order == WT_LAP_SEQ)
+        if ((k.lap_order & 1) == WT_LAP_SEQ)
             wt::step_fwd_kernel<WT_LAP_SEQ, false><<<grd, blk, 0, st>>>(k, nx, ny, coef_batched, b, c, y1, bs1, y2, bs2, y, bs, e);
         else
             wt::step_fwd_kernel<WT_LAP_PAIRED, false><<<grd, blk, 0, st>>>(k, nx, ny, coef_batched, b, c, y1, bs1, y2, bs2, y, bs, e);
@@ -537,7 +537,7 @@ int wt_launch_step_bwd(const StepScalars& k, int batch, int nx, int ny, int coef
                        cudaStream_t st) {
     dim3 blk(wt::TY, wt::TX);
     dim3 grd((ny + wt::TY - 1) / wt::TY, (nx + wt::TX - 1) / wt::TX, 1);
-    if (k.lap_order == WT_LAP_SEQ)
+    if ((k.lap_order & 1) == WT_LAP_SEQ)
         wt::step_bwd_kernel<WT_LAP_SEQ><<<grd, blk, 0, st>>>(k, batch, nx, ny, coef_batched, b, c, y1, y2, g, gb, gcp, gy1, gy2);
     else
         wt::step_bwd_kernel<WT_LAP_PAIRED><<<grd, blk, 0, st>>>(k, batch, nx, ny, coef_batched, b, c, y1, y2, g, gb, gcp, gy1, gy2);
@@ -552,7 +552,7 @@ int wt_launch_seq_adj_step(const StepScalars& k, int batch, int nx, int ny, cons
     if (vec4_ok(ny, {b, c, lam1, lam2, hprev, lam_out, gc, e.G}, {hbs, (size_t)nx * ny})) {
         dim3 blk(32, wt::STEP4_TX);
         dim3 grd((ny + wt::STEP4_TY - 1) / wt::STEP4_TY, (nx + wt::STEP4_TX - 1) / wt::STEP4_TX, batch);
-        if (k.lap_order == WT_LAP_SEQ)
+        if ((k.lap_order & 1) == WT_LAP_SEQ)
             wt::seq_adj_step4_kernel<WT_LAP_SEQ><<<grd, blk, 0, st>>>(k, nx, ny, b, c, lam1, lam2, hprev, hbs, lam_out, gc, e);
         else
             wt::seq_adj_step4_kernel<WT_LAP_PAIRED><<<grd, blk, 0, st>>>(k, nx, ny, b, c, lam1, lam2, hprev, hbs, lam_out, gc, e);
@@ -561,7 +561,7 @@ int wt_launch_seq_adj_step(const StepScalars& k, int batch, int nx, int ny, cons
     }
     dim3 blk(wt::TY, wt::TX);
     dim3 grd((ny + wt::TY - 1) / wt::TY, (nx + wt::TX - 1) / wt::TX, batch);
-    if (k.lap_order == WT_LAP_SEQ)
+    if ((k.lap_order & 1) == WT_LAP_SEQ)
         wt::seq_adj_step_kernel<WT_LAP_SEQ><<<grd, blk, 0, st>>>(k, nx, ny, b, c, lam1, lam2, hprev, hbs, lam_out, gc, e);
     else
         wt::seq_adj_step_kernel<WT_LAP_PAIRED><<<grd, blk, 0, st>>>(k, nx, ny, b, c, lam1, lam2, hprev, hbs, lam_out, gc, e);
