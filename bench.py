@@ -21,6 +21,7 @@ from __future__ import annotations
 import argparse
 import contextlib
 import json
+import math
 import os
 import statistics
 import subprocess
@@ -251,6 +252,61 @@ def committed_traffic(kernel: str):
     return None
 
 
+def committed_count(kernel: str, name: str = "instructions.txt"):
+    """`kernel count` lines of a committed ncu summary under profiles/ (`#` comments)."""
+    p = os.path.join(HERE, "profiles", name)
+    if not os.path.exists(p):
+        return None
+    with open(p) as fh:
+        for line in fh:
+            f = line.split("#", 1)[0].split()
+            if len(f) == 2 and f[0] == kernel:
+                return float(f[1])
+    return None
+
+
+def device_peaks(dev):
+    """FP32 FFMA issue rate and shared-memory load bandwidth of the device,
+    measured by the library's wt_test_device_peaks (two kernels on every SM,
+    CUDA events): the denominators of the fused kernels' roofline."""
+    import ctypes as C
+    import torch
+    from wavetorch_gb300 import _lib
+
+    class Peaks(C.Structure):
+        _fields_ = [("ffma_per_s", C.c_double), ("warp_inst_per_s", C.c_double),
+                    ("smem_bytes_per_s", C.c_double), ("sm_mhz", C.c_double),
+                    ("sm_count", C.c_int32)]
+
+    lib = _lib.load()
+    nfn = lib.wt_test_device_peaks_scratch_floats
+    nfn.argtypes, nfn.restype = [C.POINTER(C.c_size_t)], C.c_int
+    fn = lib.wt_test_device_peaks
+    fn.argtypes = [C.POINTER(Peaks), C.c_void_p, C.c_size_t, C.c_void_p]
+    fn.restype = C.c_int
+    n = C.c_size_t(0)
+    _lib.check(nfn(C.byref(n)), "wt_test_device_peaks_scratch_floats")
+    scratch = torch.empty(n.value, dtype=torch.float32, device=dev)
+    pk = Peaks()
+    _lib.check(fn(C.byref(pk), C.c_void_p(scratch.data_ptr()), n.value,
+                  C.c_void_p(torch.cuda.current_stream(dev).cuda_stream)), "wt_test_device_peaks")
+    return {"ffma_per_s": pk.ffma_per_s, "warp_inst_per_s": pk.warp_inst_per_s,
+            "smem_bytes_per_s": pk.smem_bytes_per_s, "sm_mhz": pk.sm_mhz, "sm_count": pk.sm_count}
+
+
+# Algorithmic work of one cell-step in the fused kernels at h == 1 (the
+# reference's float32 operations, unfused, in its order): forward 4 for the
+# Laplacian + 6 for the update; adjoint 1 (c^2 g) + 4 (Laplacian) + 4 (grad_y1)
+# + 1 (grad_y2) + 1 (lambda) + 1 (dL/dc sum).  Shared-memory bytes: each step a
+# cell's new value is stored once and both horizontal neighbours loaded (12 B);
+# the adjoint also lands its tape value in shared memory by bulk copy and reads
+# it back (8 B).
+FP32_FWD, FP32_ADJ = 10, 12
+# steps of the workload the unmodified reference is timed on (its rate is flat in T)
+REFERENCE_SAMPLE_T = 350
+SMEM_FWD, SMEM_ADJ = 12, 20
+
+
 # ---------------------------------------------------------------------------
 def build_model(dev, B, T, seed, form):
     import numpy as np
@@ -314,9 +370,10 @@ def run_ours(args):
         for k in range(args.steps):
             flush.zero_()
             evs[k][0].record(stream)
-            train_step(model, x, labels)
+            loss_t = train_step(model, x, labels)
             evs[k][1].record(stream)
         torch.cuda.synchronize(dev)
+    loss_fused = float(loss_t.item())
     barrier(world, dev)
     launches = (_lib.kernel_launches() - launches0) // max(1, args.steps)
     t_step = sum(a.elapsed_time(b) for a, b in evs) / 1e3 / args.steps
@@ -414,6 +471,82 @@ def run_ours(args):
     achieved = bpc * cell_steps / t_dom / 1e9
     traffic = committed_traffic(dom)
 
+    # ---- the adjoint's two modes: the tape against sqrt(T) checkpoints ----
+    adjoint_modes = None
+    if args.form == "fused":
+        from wavetorch_gb300.functional import seq_workspace_bytes
+        seg = int(math.ceil(math.sqrt(T)))
+        modes = {}
+        for name, segment in (("tape", -1), ("checkpoint", seg)):
+            mspec = SeqSpec(B, N, N, T, src, prb, form=form_id, segment=segment)
+            tb_ = []
+            for k in range(1 + max(2, min(args.steps, 3))):
+                flush.zero_()
+                _, _, _, ws = seq_forward(mspec, sc, b, c, x)
+                e = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+                e[0].record(stream)
+                seq_backward(mspec, sc, b, c, x, gout, ws, False)
+                e[1].record(stream)
+                torch.cuda.synchronize(dev)
+                if k:
+                    tb_.append(e[0].elapsed_time(e[1]))
+                del ws
+            modes[name] = {"adjoint_ms": statistics.mean(tb_),
+                           "workspace_bytes": seq_workspace_bytes(mspec)}
+        modes["checkpoint"]["segment"] = seg
+        adjoint_modes = {**modes, "forward_ms": t_f * 1e3,
+                         "checkpoint_over_tape_step": (t_f * 1e3 + modes["checkpoint"]["adjoint_ms"]) /
+                                                      (t_f * 1e3 + modes["tape"]["adjoint_ms"]),
+                         "note": "tape: every step's Laplacian kept in HBM; checkpoint: the pair "
+                                 "(h_{t-1}, h_{t-2}) every ceil(sqrt(T)) steps, each segment "
+                                 "recomputed before its adjoint steps"}
+        torch.cuda.empty_cache()
+
+    # ---- fused form: the on-chip resources that bound it ----
+    fused_roofline = None
+    if args.form == "fused":
+        pk = device_peaks(dev)
+        ipstep = committed_count(dom)            # warp instructions per time step (ncu)
+        fp32 = (FP32_FWD * cell_steps / t_f, FP32_ADJ * cell_steps / t_b)
+        smem = (SMEM_FWD * cell_steps / t_f, SMEM_ADJ * cell_steps / t_b)
+        fused_roofline = {
+            "device_peaks": pk,
+            "fp32_fwd_frac": fp32[0] / pk["ffma_per_s"], "fp32_adj_frac": fp32[1] / pk["ffma_per_s"],
+            "smem_fwd_frac": smem[0] / pk["smem_bytes_per_s"],
+            "smem_adj_frac": smem[1] / pk["smem_bytes_per_s"],
+            "issue_inst_per_step": ipstep,
+            "note": "fp32: the reference's float32 operations per cell-step (forward 10, "
+                    "adjoint 12 at h = 1) over the FFMA rate of all SMs; smem: 12 B (forward) "
+                    "and 20 B (adjoint) of shared-memory traffic per cell-step over the "
+                    "measured load bandwidth; issue: ncu-counted warp instructions per time "
+                    "step of the launch (profiles/instructions.txt) over the FFMA loop's "
+                    "issue rate"}
+        if ipstep:
+            inst_rate = ipstep * T / t_dom
+            roofline = {"bound": "issue", "kernel": dom, "achieved": inst_rate / 1e9,
+                        "peak": pk["warp_inst_per_s"] / 1e9, "unit": "Gwarp-inst/s",
+                        "frac": inst_rate / pk["warp_inst_per_s"], "traffic": traffic,
+                        "peak_source": "wt_test_device_peaks (FFMA-only loop on all SMs, "
+                                       f"{pk['sm_mhz']:.0f} MHz), measured in this run"}
+        else:
+            roofline = {"bound": "fp32", "kernel": dom, "achieved": fp32[1] / 1e12,
+                        "peak": pk["ffma_per_s"] / 1e12, "unit": "TFFMA/s",
+                        "frac": fp32[1] / pk["ffma_per_s"], "traffic": traffic,
+                        "peak_source": "wt_test_device_peaks, measured in this run"}
+        roofline.update({"hbm_equivalent_frac": achieved / peak,
+                         "hbm_equivalent_note": "the per-step form's HBM bytes (12 B fwd / 20 B "
+                                                "adjoint per cell-step) over the fused kernel's "
+                                                f"time, against hbm_gbs of {peak_src}",
+                         "dram_frac": (traffic / t_dom / 1e9 / peak) if traffic else None,
+                         "ms_fwd_kernel": t_f * 1e3, "ms_bwd_kernels": t_b * 1e3})
+    else:
+        roofline = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak,
+                    "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
+                    "peak_source": f"hbm_gbs of {peak_src}",
+                    "algorithmic_bytes_per_cell_step": bpc,
+                    "note": "per-step kernels: algorithmic bytes = HBM bytes per step",
+                    "ms_fwd_kernel": t_f * 1e3, "ms_bwd_kernels": t_b * 1e3}
+
     # ---- plain per-step form: the metric's comparison arm ----
     plain = None
     if not args.no_plain and args.form == "fused":
@@ -476,9 +609,14 @@ def run_ours(args):
                          "CUDA graph, compared with the fused kernels' own time"}
 
     cpu = None
-    if rank == 0 and world == 1 and not args.no_cpu:
-        cpu = cpu_baseline(sample_T=WORKLOAD["steps"])
     parity = parity_vs_reference(dev) if rank == 0 else None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        full = oracle_workload(1234, B, T) if (B, T) == (WORKLOAD["batch"], WORKLOAD["steps"]) \
+            else None
+        cpu = cpu_baseline(sample_T=T, batch=B, res=full)
+        if full is not None and args.form == "fused":
+            parity["cfg1_full/fused"] = parity_full_size(dev, full, model, x, loss_fused, grad_fused)
+        del full
 
     if rank == 0:
         line = {
@@ -492,17 +630,9 @@ def run_ours(args):
             "e2e": {"value": world * cell_steps / t_e2e, "unit": "cell-steps/s",
                     "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                     "ms_per_step": t_e2e * 1e3},
-            "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak,
-                         "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
-                         "peak_source": f"hbm_gbs of {peak_src}",
-                         "algorithmic_bytes_per_cell_step": bpc,
-                         "note": "fused kernels keep the fields on chip: achieved is the "
-                                 "per-step form's HBM bytes (12 B fwd / 20 B adjoint per "
-                                 "cell-step) over the kernel's time, so it can exceed the copy "
-                                 "peak; traffic is the DRAM bytes one launch really moves "
-                                 "(the adjoint's tape reads)" if args.form == "fused" else
-                                 "per-step kernels: algorithmic bytes = HBM bytes per step",
-                         "ms_fwd_kernel": t_f * 1e3, "ms_bwd_kernels": t_b * 1e3},
+            "roofline": roofline,
+            "fused_roofline": fused_roofline,
+            "adjoint_modes": adjoint_modes,
             "cpu_baseline": cpu,
             "plain_form": plain,
             "fused_loss": fused_loss,
@@ -576,32 +706,131 @@ def parity_vs_reference(dev):
     return res
 
 
-def cpu_baseline(sample_T: int, batch: int = WORKLOAD["batch"]):
-    """The oracle port (plain C, OpenMP over all host threads) on a bounded
-    sample of the workload: the full batch and grid, the first sample_T steps."""
+def oracle_workload(seed: int, batch: int = WORKLOAD["batch"], T: int = WORKLOAD["steps"]):
+    """The oracle port (plain C, OpenMP over all host threads) on the
+    benchmark's training step with the inputs of `seed`: rho -> c, the
+    forward, the loss and its gradient (torch on the CPU), the adjoint and
+    dL/drho.  Returns the arrays and the forward + adjoint time."""
     import numpy as np
     import oracle.oracle as o
     import torch
+    import wavetorch_gb300 as wt
     from wavetorch_gb300.data import vowel_like
     from wavetorch_gb300.geom import pml_profile
-    N, T = WORKLOAD["nx"], sample_T
+    N = WORKLOAD["nx"]
     b = pml_profile((N, N), WORKLOAD["abs_N"], 3.0, 2).numpy()
-    rho = torch.rand(N, N, generator=torch.Generator().manual_seed(1234)).numpy()
+    rho = torch.rand(N, N, generator=torch.Generator().manual_seed(seed)).numpy()
     rho[b > 0] = 0
     kern = np.full((3, 3), np.float32(1.0) / np.float32(9.0), np.float32)
-    c, _ = o.rho_to_c(rho, kern, 1, 0.5, 100.0, 1.0, 0.5)
-    x, _ = vowel_like(batch, T, seed=1234)
+    c, th = o.rho_to_c(rho, kern, 1, 0.5, 100.0, 1.0, 0.5)
+    x, labels = vowel_like(batch, T, seed=seed)
     S = o.Seq(batch, N, N, T, 0.707, 1.0, [(20 * N + 60, -1)],
               [(80 * N + y, 1, i) for i, y in enumerate((35, 50, 65))])
-    g = np.ones((batch, T, 3), np.float32) * 1e-3
     t0 = time.perf_counter()
     out, hist = S.forward(b, c, x)
-    S.backward(b, c, hist, g)
-    dt = time.perf_counter() - t0
-    return {"value": batch * N * N * T / dt, "unit": "cell-steps/s", "cores": o.num_threads(),
+    t_f = time.perf_counter() - t0
+    yo = torch.from_numpy(out).requires_grad_()
+    loss = torch.nn.CrossEntropyLoss()(wt.utils.normalize_power(yo.sum(dim=1)),
+                                       torch.from_numpy(labels))
+    (g,) = torch.autograd.grad(loss, [yo])
+    g = np.ascontiguousarray(g.numpy())
+    t0 = time.perf_counter()
+    gc, _ = S.backward(b, c, hist, g)
+    t_b = time.perf_counter() - t0
+    del hist
+    grho = o.rho_to_c_bwd(th, kern, 1, 0.5, 100.0, 1.0, 0.5, gc)
+    return {"b": b, "c": c, "x": x, "labels": labels, "out": out, "loss": float(loss.item()),
+            "grad_out": g, "gc": gc, "grad_rho": grho, "seconds": t_f + t_b,
+            "threads": o.num_threads()}
+
+
+def cpu_baseline(sample_T: int, batch: int = WORKLOAD["batch"], res=None):
+    """The oracle port on a bounded sample of the workload (the full batch
+    and grid, the first sample_T steps): cell-steps/s of its forward +
+    adjoint on all host threads."""
+    N, T = WORKLOAD["nx"], sample_T
+    r = res or oracle_workload(1234, batch, T)
+    dt = r["seconds"]
+    return {"value": batch * N * N * T / dt, "unit": "cell-steps/s", "cores": r["threads"],
             "kind": "port",
             "sample": f"batch {batch}, {N}x{N}, first {T} of {WORKLOAD['steps']} steps, "
                       f"fwd + adjoint, {dt:.2f} s"}
+
+
+def parity_full_size(dev, r, model, x, loss_gpu: float, grad_rho_gpu):
+    """The timed workload (B=32, 120x120, T=3500) against the oracle on the
+    same inputs: the fused kernels on the oracle's c (probe outputs bit for
+    bit, dL/dc) and the whole training step through WaveRNN (loss, dL/drho;
+    c differs from the oracle's by ulps of tanh)."""
+    import numpy as np
+    import torch
+    from wavetorch_gb300 import _lib
+    from wavetorch_gb300.functional import SeqSpec, lap_order, scalars, seq_backward, seq_forward
+
+    def rel(a, b_):
+        a, b_ = np.asarray(a, np.float64), np.asarray(b_, np.float64)
+        return float(np.linalg.norm(a - b_) / max(np.linalg.norm(b_), 1e-300))
+
+    B, T = r["x"].shape
+    N = WORKLOAD["nx"]
+    spec = SeqSpec(B, N, N, T, model.source_table(B), model.probe_table()[0],
+                   form=_lib.WT_FORM_FUSED)
+    sc = scalars(0.707, 1.0, lap_order(B, N, N, 1.0))
+    tb, tc = (torch.from_numpy(np.ascontiguousarray(v)).to(dev) for v in (r["b"], r["c"]))
+    out, _, _, ws = seq_forward(spec, sc, tb, tc, x)
+    gc, _ = seq_backward(spec, sc, tb, tc, x, torch.from_numpy(r["grad_out"]).to(dev), ws, False)
+    torch.cuda.synchronize(dev)
+    out = out.cpu().numpy()
+    with torch.no_grad():
+        c_gpu = model.cell.geom.c.cpu().numpy()
+    return {"out_bit_exact": bool(np.array_equal(out, r["out"])), "out_rel": rel(out, r["out"]),
+            "grad_c_rel": rel(gc.cpu().numpy(), r["gc"]),
+            "c_rel": rel(c_gpu, r["c"]),
+            "loss_rel": rel(loss_gpu, r["loss"]),
+            "grad_rho_rel": rel(grad_rho_gpu.cpu().numpy(), r["grad_rho"]),
+            "workload": f"B={B}, {N}x{N}, T={T}: the timed inputs, oracle on the host"}
+
+
+def reference_cpu_path(batch: int, sample_T: int):
+    """The unmodified reference (the pip install under baseline/_ref, imported
+    through tests/golden/ref_shim.py's stand-ins for its plotting and data
+    imports) on the benchmark's model: forward and autograd backward of the
+    training loss on the CPU with all host threads, on the first sample_T
+    steps of the workload.  None when the install is absent."""
+    ref_root = os.path.join(HERE, "baseline", "_ref")
+    if not os.path.isdir(os.path.join(ref_root, "wavetorch")):
+        return None
+    os.environ["WAVETORCH_REFERENCE"] = ref_root
+    sys.path.insert(0, os.path.join(HERE, "tests", "golden"))
+    import torch
+    import ref_shim
+    from wavetorch_gb300.data import vowel_like
+    wt = ref_shim.import_reference()
+    torch.set_num_threads(os.cpu_count() or 1)
+    N = WORKLOAD["nx"]
+    geom = wt.WaveGeometryFreeForm((N, N), 1.0, c0=1.0, c1=0.5, abs_N=WORKLOAD["abs_N"],
+                                   abs_sig=3.0, abs_p=2,
+                                   rho=torch.rand(N, N, generator=torch.Generator().manual_seed(1234)))
+    model = wt.WaveRNN(wt.WaveCell(0.707, geom), [wt.WaveSource(20, 60)],
+                       [wt.WaveIntensityProbe(80, y) for y in (35, 50, 65)])
+    x, labels = vowel_like(batch, sample_T, seed=1234)
+    xt, lt = torch.from_numpy(x), torch.from_numpy(labels)
+
+    def step():
+        geom.rho.grad = None
+        y = model(xt)
+        loss = torch.nn.CrossEntropyLoss()(wt.utils.normalize_power(y.sum(dim=1)), lt)
+        loss.backward()
+
+    step()                                 # warm-up
+    t0 = time.perf_counter()
+    step()
+    dt = time.perf_counter() - t0
+    return {"value": batch * N * N * sample_T / dt, "unit": "cell-steps/s",
+            "cores": torch.get_num_threads(), "kind": "reference",
+            "sample": f"batch {batch}, {N}x{N}, first {sample_T} of {WORKLOAD['steps']} steps, "
+                      f"forward + autograd backward of the unmodified reference (torch "
+                      f"{torch.__version__}, CPU), {dt:.2f} s"}
 
 
 def run_reference(args):
@@ -626,6 +855,7 @@ def run_reference(args):
             "impl": "reference",
             "cpu_baseline": {"value": v, "unit": "cell-steps/s", "kind": "port",
                              "cores": vals[0]["cores"], "sample": vals[0]["sample"]},
+            "cpu_baseline_reference": reference_cpu_path(B, REFERENCE_SAMPLE_T),
             "e2e": {"value": v, "unit": "cell-steps/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)

@@ -22,6 +22,27 @@ int wt_test_band_missing_arrival(const wt_scalars* s, const wt_seq_desc* d, cons
                                  const float* c, const float* x, float* out, void* workspace,
                                  size_t workspace_bytes, int32_t band, wt_stream_t stream);
 
+/* Device peaks that bound the fused sequence kernels (they keep their fields
+ * on chip, so HBM does not): measured with two kernels on every SM of the
+ * current device, each timed with CUDA events after one warm-up launch.
+ *   ffma_per_s       FP32 fused multiply-adds per second (thread operations;
+ *                    independent chains, so the loop runs at the issue rate)
+ *   warp_inst_per_s  issued warp instructions per second of that loop
+ *   smem_bytes_per_s shared-memory load bandwidth (conflict-free 16-byte loads)
+ *   sm_mhz           SM clock during the FFMA loop (clock64 / global timer)
+ * `scratch` is a device buffer of at least
+ * wt_test_device_peaks_scratch_floats() floats (the kernels' outputs).      */
+typedef struct wt_device_peaks {
+    double ffma_per_s;
+    double warp_inst_per_s;
+    double smem_bytes_per_s;
+    double sm_mhz;
+    int32_t sm_count;
+} wt_device_peaks;
+int wt_test_device_peaks_scratch_floats(size_t* n);
+int wt_test_device_peaks(wt_device_peaks* out, float* scratch, size_t scratch_floats,
+                         wt_stream_t stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -13,8 +13,9 @@ project-written ``skimage.draw`` with the two functions the path calls:
 * ``line(r0, c0, r1, c1)`` -- integer Bresenham (used by
   ``wavetorch/source.py:31``).
 
-Only the golden-fixture generator imports this module, and only on a machine
-where the reference sources exist.
+The golden-fixture generator imports this module where the reference
+sources exist, and ``bench.py --impl reference`` to time the reference's own
+CPU path from its pip install (``baseline/_ref``).
 """
 import importlib.machinery
 import os
@@ -106,6 +107,14 @@ def import_reference():
         sk = _stub("skimage")
         draw = _stub("skimage.draw", circle=_circle, line=_line)
         sk.draw = draw
+    if not os.path.isdir(os.path.join(REFERENCE_ROOT, "wavetorch", "data")):
+        # the reference's setup.py packages `wavetorch` alone, so a pip install
+        # of it lacks the `wavetorch.data` subpackage (the vowel dataset
+        # loader, librosa-based, off the time-stepping path) that its
+        # __init__ imports: stand in for it as for the other data imports
+        def _no_dataset(*a, **k):
+            raise RuntimeError("the vowel dataset loader is not available")
+        _stub("wavetorch.data", load_all_vowels=_no_dataset, select_vowel_sample=_no_dataset)
     if REFERENCE_ROOT not in sys.path:
         sys.path.insert(0, REFERENCE_ROOT)
     import wavetorch  # noqa: E402

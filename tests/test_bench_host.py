@@ -42,6 +42,14 @@ def test_committed_traffic_of_the_fused_kernels():
     assert bench.committed_traffic("no_such_kernel") is None
 
 
+def test_committed_instruction_counts():
+    """Warp instructions per time step of the fused kernels' launches, read
+    from the committed ncu summary for the issue roofline."""
+    n = bench.committed_count("seq_bwd_tape_kernel")
+    assert n is None or n > 0
+    assert bench.committed_count("no_such_kernel") is None
+
+
 def test_reference_arm_prints_the_contract_line():
     """`bench.py --impl reference` (the reference's CPU path restated, on the
     host cores) prints one JSON line with the keys the benchmark contract
@@ -63,3 +71,10 @@ def test_reference_arm_prints_the_contract_line():
     assert d["cpu_baseline"]["kind"] == "port" and d["cpu_baseline"]["cores"] >= 1
     assert d["e2e"] == {"value": d["value"], "unit": "cell-steps/s", "h2d_bytes_per_step": 0,
                         "d2h_bytes_per_step": 0}
+    # the unmodified reference's own CPU path beside the port, where its
+    # install (baseline/_ref) is present
+    ref = d["cpu_baseline_reference"]
+    if os.path.isdir(os.path.join(root, "baseline", "_ref", "wavetorch")):
+        assert ref["kind"] == "reference" and ref["value"] > 0 and ref["cores"] >= 1
+    else:
+        assert ref is None

@@ -172,3 +172,4 @@ def test_missing_arrival_times_out_and_the_context_survives(cuda):
     assert seq_device_status(spec, ws) == _lib.WT_ERR_TIMEOUT
     assert 1.5 < elapsed < 60, elapsed
     check(cuda, nx, ny, B, T, src, prb, seed=7)
+
