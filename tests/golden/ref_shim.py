@@ -1,7 +1,8 @@
 """Import shim for the unmodified reference package (fancompute/wavetorch v0.2.1).
 
 The reference's ``wavetorch/__init__.py`` eagerly imports its plotting, data and
-training modules, which need librosa, pandas, seaborn, matplotlib and skimage.
+training modules, which need librosa, pandas, seaborn, matplotlib, skimage and
+(where it is not installed) scikit-learn.
 None of those are installed here and none of them is on the time-stepping path.
 This shim registers inert stand-in modules for them (each with a real
 ``__spec__`` so that ``importlib.util.find_spec`` keeps working) and a small
@@ -107,6 +108,16 @@ def import_reference():
         sk = _stub("skimage")
         draw = _stub("skimage.draw", circle=_circle, line=_line)
         sk.draw = draw
+    try:
+        import sklearn.metrics  # noqa: F401
+    except ImportError:
+        # utils.py / train.py import confusion_matrix for their accuracy
+        # reports (off the time-stepping path); machines without scikit-learn
+        # get a stand-in that raises if it is ever called
+        def _no_sklearn(*a, **k):
+            raise RuntimeError("scikit-learn is not available")
+        skl = _stub("sklearn")
+        skl.metrics = _stub("sklearn.metrics", confusion_matrix=_no_sklearn)
     if not os.path.isdir(os.path.join(REFERENCE_ROOT, "wavetorch", "data")):
         # the reference's setup.py packages `wavetorch` alone, so a pip install
         # of it lacks the `wavetorch.data` subpackage (the vowel dataset
