@@ -221,12 +221,14 @@ void or_seq_fwd(const or_desc* d, const float* b, const float* c, const float* x
     }
     float* zero = (float*)calloc(plane, sizeof(float));
     for (int t = 0; t < T; ++t) {
-#pragma omp parallel for schedule(static)
-        for (int k = 0; k < B; ++k) {
-            const float* y1 = t >= 1 ? hist + k * hb + (size_t)(t - 1) * plane : zero;
-            const float* y2 = t >= 2 ? hist + k * hb + (size_t)(t - 2) * plane : zero;
-            float* y = hist + k * hb + (size_t)t * plane;
-            for (int i = 0; i < nx; ++i)
+        /* every cell of every instance (rows in parallel too, for one large
+         * instance), then each instance's sources and probes */
+#pragma omp parallel for collapse(2) schedule(static)
+        for (int k = 0; k < B; ++k)
+            for (int i = 0; i < nx; ++i) {
+                const float* y1 = t >= 1 ? hist + k * hb + (size_t)(t - 1) * plane : zero;
+                const float* y2 = t >= 2 ? hist + k * hb + (size_t)(t - 2) * plane : zero;
+                float* y = hist + k * hb + (size_t)t * plane;
                 for (int j = 0; j < ny; ++j) {
                     size_t q = (size_t)i * ny + j;
                     float L = lap_at(y1, nx, ny, i, j, &s, d->order);
@@ -234,6 +236,9 @@ void or_seq_fwd(const or_desc* d, const float* b, const float* c, const float* x
                     v = v + C2[q] * L;
                     y[q] = A[q] * v;
                 }
+            }
+        for (int k = 0; k < B; ++k) {
+            float* y = hist + k * hb + (size_t)t * plane;
             for (int e = 0; e < d->n_src; ++e) {
                 int row = d->src_row[e] < 0 ? k : d->src_row[e];
                 y[d->src_cell[e]] = y[d->src_cell[e]] + x[(size_t)row * T + t];
@@ -280,10 +285,10 @@ void or_seq_bwd(const or_desc* d, const float* b, const float* c, const float* h
         float* L0 = lam + (size_t)(t % 3) * bp;
         const float* L1 = t + 1 < T ? lam + (size_t)((t + 1) % 3) * bp : NULL;
         const float* L2 = t + 2 < T ? lam + (size_t)((t + 2) % 3) * bp : NULL;
-#pragma omp parallel for schedule(static)
-        for (int k = 0; k < B; ++k) {
-            float* l0 = L0 + k * plane;
-            for (int i = 0; i < nx; ++i)
+#pragma omp parallel for collapse(2) schedule(static)
+        for (int k = 0; k < B; ++k)
+            for (int i = 0; i < nx; ++i) {
+                float* l0 = L0 + k * plane;
                 for (int j = 0; j < ny; ++j) {
                     size_t q = (size_t)i * ny + j;
                     float v = 0.0f;
@@ -295,6 +300,9 @@ void or_seq_bwd(const or_desc* d, const float* b, const float* c, const float* h
                     }
                     l0[q] = v;
                 }
+            }
+        for (int k = 0; k < B; ++k) {
+            float* l0 = L0 + k * plane;
             for (int a = 0; a < d->n_prb; ++a) {
                 int q = pidx[a];
                 size_t o = ((size_t)k * T + t) * d->n_prb + q;
@@ -314,8 +322,12 @@ void or_seq_bwd(const or_desc* d, const float* b, const float* c, const float* h
                 }
                 grad_x[(size_t)k * T + t] = acc;
             }
-            const float* hp = t >= 1 ? hist + k * hb + (size_t)(t - 1) * plane : NULL;
-            for (int i = 0; i < nx; ++i)
+        }
+#pragma omp parallel for collapse(2) schedule(static)
+        for (int k = 0; k < B; ++k)
+            for (int i = 0; i < nx; ++i) {
+                const float* l0 = L0 + k * plane;
+                const float* hp = t >= 1 ? hist + k * hb + (size_t)(t - 1) * plane : NULL;
                 for (int j = 0; j < ny; ++j) {
                     size_t q = (size_t)i * ny + j;
                     float L = hp ? lap_at(hp, nx, ny, i, j, &s, d->order) : 0.0f;
@@ -323,7 +335,7 @@ void or_seq_bwd(const or_desc* d, const float* b, const float* c, const float* h
                     tt = X1[q] * tt;
                     gct[k * plane + q] = tt * l0[q];
                 }
-        }
+            }
 #pragma omp parallel for schedule(static)
         for (long q = 0; q < (long)plane; ++q) {
             float sum = batch_sum(gct + q, plane, B);
