@@ -22,6 +22,28 @@ int wt_test_band_missing_arrival(const wt_scalars* s, const wt_seq_desc* d, cons
                                  const float* c, const float* x, float* out, void* workspace,
                                  size_t workspace_bytes, int32_t band, wt_stream_t stream);
 
+/* wt_seq_fwd for a sequence planned in the cluster layout (at least two
+ * CTAs per instance), with CTA `cta` of instance 0's cluster never sending
+ * its boundary rows over distributed shared memory: a host-forced missing
+ * arrival.  The neighbouring CTAs' bounded waits give up after about 2 s,
+ * each CTA leaves its loop at its next abort check, and wt_seq_device_status
+ * then reports WT_ERR_TIMEOUT; the context stays usable.  Nothing faults or
+ * hangs.  WT_ERR_UNSUPPORTED outside the cluster layout.                   */
+int wt_test_cluster_missing_arrival(const wt_scalars* s, const wt_seq_desc* d, const float* b,
+                                    const float* c, const float* x, float* out, void* workspace,
+                                    size_t workspace_bytes, int32_t cta, wt_stream_t stream);
+
+/* wt_seq_bwd for a sequence whose cluster-layout adjoint runs from the tape
+ * (after a wt_seq_fwd on the same workspace), with the tape ring's producer
+ * issuing no slice from step `step` down: the CTAs' bounded waits on that
+ * slot give up after about 2 s, the copies already in flight are drained,
+ * and wt_seq_device_status reports WT_ERR_TIMEOUT; the context stays usable.
+ * WT_ERR_UNSUPPORTED when the sequence does not run from a cluster tape.    */
+int wt_test_tape_missing_slice(const wt_scalars* s, const wt_seq_desc* d, const float* b,
+                               const float* c, const float* x, const float* grad_out,
+                               float* grad_c, void* workspace, size_t workspace_bytes,
+                               int32_t step, wt_stream_t stream);
+
 /* Device peaks that bound the fused sequence kernels (they keep their fields
  * on chip, so HBM does not): measured with two kernels on every SM of the
  * current device, each timed with CUDA events after one warm-up launch.

@@ -75,8 +75,9 @@ def test_test_hooks_are_exported(lib):
     text = open(os.path.join(ROOT, "include", "wavetorch_gb300_testing.h")).read()
     text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
     names = sorted(set(re.findall(r"\b(wt_[a-z0-9_]+)\s*\(", text)))
-    assert names == ["wt_test_band_missing_arrival", "wt_test_device_peaks",
-                     "wt_test_device_peaks_scratch_floats"]
+    assert names == ["wt_test_band_missing_arrival", "wt_test_cluster_missing_arrival",
+                     "wt_test_device_peaks", "wt_test_device_peaks_scratch_floats",
+                     "wt_test_tape_missing_slice"]
     for n in names:
         assert hasattr(lib, n), n
 

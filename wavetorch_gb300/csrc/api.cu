@@ -575,6 +575,49 @@ extern "C" int wt_test_band_missing_arrival(const wt_scalars* s, const wt_seq_de
     return wt_launch_band(true, F, P.BL, cs);
 }
 
+extern "C" int wt_test_cluster_missing_arrival(const wt_scalars* s, const wt_seq_desc* d,
+                                               const float* b, const float* c, const float* x,
+                                               float* out, void* workspace,
+                                               size_t workspace_bytes, int32_t cta,
+                                               wt_stream_t stream) {
+    if (!scalars_ok(s)) return WT_ERR_INVALID;
+    SeqPlan P;
+    int st = make_plan(d, &P);
+    if (st) return st;
+    if (P.form != WT_FORM_FUSED || P.band || P.L.C < 2) return WT_ERR_UNSUPPORTED;
+    if (cta < 0 || cta >= P.L.C) return WT_ERR_INVALID;
+    if (!b || !c || !workspace || workspace_bytes < P.total) return WT_ERR_INVALID;
+    if ((P.ns > 0 && !x) || (P.np > 0 && !out)) return WT_ERR_INVALID;
+    cudaStream_t cs = (cudaStream_t)stream;
+    if ((st = upload_tables(d, P, workspace, cs))) return st;
+    wt::FusedParams F = fused_params(s, P, b, c, x, workspace);
+    F.out = out;
+    F.mute_cta1 = cta + 1;
+    return wt_launch_fused(true, F, P.L, cs);
+}
+
+extern "C" int wt_test_tape_missing_slice(const wt_scalars* s, const wt_seq_desc* d,
+                                          const float* b, const float* c, const float* x,
+                                          const float* grad_out, float* grad_c, void* workspace,
+                                          size_t workspace_bytes, int32_t step,
+                                          wt_stream_t stream) {
+    if (!scalars_ok(s)) return WT_ERR_INVALID;
+    SeqPlan P;
+    int st = make_plan(d, &P);
+    if (st) return st;
+    if (P.form != WT_FORM_FUSED || P.band || !P.tape) return WT_ERR_UNSUPPORTED;
+    if (step < 0 || step >= P.T) return WT_ERR_INVALID;
+    if (!b || !c || !grad_c || !workspace || workspace_bytes < P.total) return WT_ERR_INVALID;
+    if (P.np > 0 && !grad_out) return WT_ERR_INVALID;
+    wt::FusedParams F = fused_params(s, P, b, c, x, workspace);
+    F.grad_out = grad_out;
+    F.skip_slice1 = step + 1;
+    cudaStream_t cs = (cudaStream_t)stream;
+    if ((st = wt_launch_fused(false, F, P.L, cs))) return st;
+    if (P.coef_batched) return WT_OK;
+    return wt_launch_seq_adj_reduce(P.B, P.plane, F.gc_part, grad_c, 1, cs);
+}
+
 // ---------------------------------------------------------------------------
 // 3. sequences of the nonlinear cell (fused form, tape mode)
 static bool nl_ok(const wt_nonlinear* nl) {

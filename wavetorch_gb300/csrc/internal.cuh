@@ -100,6 +100,10 @@ struct FusedParams {
     unsigned long long* halo;   // [batch][band][from above | from below][2][NCP] tagged words
     int* abort_g;               // launch-wide abort word (a wait gave up)
     int mute_band1;             // test hook: band index + 1 whose forward never sends; 0: none
+    int mute_cta1;              // test hook: cluster forward, CTA index + 1 of instance 0
+                                // that never sends its boundary rows; 0: none
+    int skip_slice1;            // test hook: cluster tape adjoint, step + 1 whose tape
+                                // slice is never issued; 0: none
 };
 
 // Up to INT_SCATTER_CAP int writes base[idx[i]] = val[i], passed by value as

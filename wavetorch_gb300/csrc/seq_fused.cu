@@ -222,10 +222,13 @@ WT_DEV float recv_word(const FusedParams& P, const Xchg& X, const unsigned long 
         for (uint32_t it = 1;; ++it) {
             v = ld_cluster_u64(a);
             if ((uint32_t)(v >> 32) == tag) break;
-            if ((it & 1023u) == 0 && global_ns() - t0 > WAIT_LIMIT_NS) {
-                atomicExch(P.err, WT_DEVERR_TIMEOUT);
-                *(volatile int*)X.abort = 1;
-                return 0.f;
+            if ((it & 1023u) == 0) {
+                if (*(volatile int*)X.abort) return 0.f;   // another wait gave up
+                if (global_ns() - t0 > WAIT_LIMIT_NS) {
+                    atomicExch(P.err, WT_DEVERR_TIMEOUT);
+                    *(volatile int*)X.abort = 1;
+                    return 0.f;
+                }
             }
         }
     }
@@ -251,8 +254,10 @@ WT_DEV Lane make_lane(const FusedParams& P, const Geo& g, const Xchg& X) {
     const bool top = g.strip == 0 && g.has_up, bot = g.strip == g.S - 1 && g.has_dn;
     l.rup = top ? smem_addr(X.hup + g.col) : 0u;
     l.rdn = bot ? smem_addr(X.hdn + g.col) : 0u;
-    l.sup = top ? X.up_hdn + 8u * (uint32_t)g.col : 0u;
-    l.sdn = bot ? X.dn_hup + 8u * (uint32_t)g.col : 0u;
+    // (the missing-arrival test hook: a muted CTA keeps its rows to itself)
+    const bool mute = P.mute_cta1 == g.cta + 1 && g.inst == 0;
+    l.sup = top && !mute ? X.up_hdn + 8u * (uint32_t)g.col : 0u;
+    l.sdn = bot && !mute ? X.dn_hup + 8u * (uint32_t)g.col : 0u;
     l.pstride = 8u * (uint32_t)X.NCP;
     return l;
 }
@@ -266,10 +271,13 @@ WT_DEV float recv_at(const FusedParams& P, const Xchg& X, uint32_t a, int k) {
         for (uint32_t it = 1;; ++it) {
             v = ld_cluster_u64(a);
             if ((uint32_t)(v >> 32) == tag) break;
-            if ((it & 1023u) == 0 && global_ns() - t0 > WAIT_LIMIT_NS) {
-                atomicExch(P.err, WT_DEVERR_TIMEOUT);
-                *(volatile int*)X.abort = 1;
-                return 0.f;
+            if ((it & 1023u) == 0) {
+                if (*(volatile int*)X.abort) return 0.f;   // another wait gave up
+                if (global_ns() - t0 > WAIT_LIMIT_NS) {
+                    atomicExch(P.err, WT_DEVERR_TIMEOUT);
+                    *(volatile int*)X.abort = 1;
+                    return 0.f;
+                }
             }
         }
     }
@@ -1125,20 +1133,29 @@ struct TapeRing {
     int slice;                      // floats per slice (threads * M)
 };
 
-WT_DEV void tape_issue(const FusedParams& P, const Geo& g, const TapeRing& r, int t, int s) {
+// Issue step t's slice into slot s; false when the missing-slice test hook
+// holds it back (from its step on, the producer issues nothing more, so every
+// copy in flight still has its slot's expected phase).
+WT_DEV bool tape_issue(const FusedParams& P, const Geo& g, const TapeRing& r, int t, int s) {
+    if (t + 1 <= P.skip_slice1) return false;
     const float* src = P.lap + (((size_t)t * P.batch + g.inst) * P.C + g.cta) * r.slice;
     const uint32_t mb = smem_addr(r.full + s);
     const uint32_t bytes = (uint32_t)(r.slice * sizeof(float));
     mbar_arrive_expect_tx(mb, bytes);
     bulk_g2s(smem_addr(r.buf + (size_t)s * r.slice), src, bytes, mb);
+    return true;
 }
 
-// Bounded wait for the phase of parity `par` of slot s.
-WT_DEV bool tape_wait(const FusedParams& P, const Xchg& X, const TapeRing& r, int s, uint32_t par) {
+// Bounded wait for the phase of parity `par` of slot s.  A wait that sees
+// the abort word gives up at once, unless it drains the copies in flight
+// before the kernel leaves (heed_abort false).
+WT_DEV bool tape_wait(const FusedParams& P, const Xchg& X, const TapeRing& r, int s, uint32_t par,
+                      bool heed_abort = true) {
     const uint32_t mb = smem_addr(r.full + s);
     if (mbar_try_wait_parity_cta(mb, par)) return true;
     const uint64_t t0 = global_ns();
     while (!mbar_try_wait_parity_cta(mb, par)) {
+        if (heed_abort && *(volatile int*)X.abort) return false;   // another wait gave up
         if (global_ns() - t0 > WAIT_LIMIT_NS) {
             atomicExch(P.err, WT_DEVERR_TIMEOUT);
             *(volatile int*)X.abort = 1;
@@ -1183,8 +1200,8 @@ __global__ void __launch_bounds__(bwd_max_threads(M), 1) seq_bwd_tape_kernel(Fus
     int lo = P.steps;     // lowest step issued (thread 0)
     if (threadIdx.x == 0) {
         for (int j = 0; j < P.nbuf && P.steps - 1 - j >= 0; ++j) {
-            lo = P.steps - 1 - j;
-            tape_issue(P, g, ring, lo, lo % P.nbuf);
+            const int t = P.steps - 1 - j;
+            if (tape_issue(P, g, ring, t, t % P.nbuf)) lo = t;
         }
     }
     // per-step counters kept incrementally (no division on the step path):
@@ -1226,8 +1243,8 @@ __global__ void __launch_bounds__(bwd_max_threads(M), 1) seq_bwd_tape_kernel(Fus
         // step t+1's slice was read before this barrier: refill its slot
         if (issuer && u > 0 && t + 1 - P.nbuf >= 0) {
             fence_proxy_async_smem();
-            lo = t + 1 - P.nbuf;
-            tape_issue(P, g, ring, lo, slot + 1 == P.nbuf ? 0 : slot + 1);
+            if (tape_issue(P, g, ring, t + 1 - P.nbuf, slot + 1 == P.nbuf ? 0 : slot + 1))
+                lo = t + 1 - P.nbuf;
         }
         if (g.colv) {
             Column<M> c;
@@ -1265,7 +1282,7 @@ __global__ void __launch_bounds__(bwd_max_threads(M), 1) seq_bwd_tape_kernel(Fus
         // nbuf issued steps hold one copy per slot, step s in slot s % nbuf
         // at parity ((T-1-s) / nbuf) & 1; waits are bounded)
         for (int s = lo; s < lo + P.nbuf && s < P.steps; ++s)
-            tape_wait(P, X, ring, s % P.nbuf, (uint32_t)(((P.steps - 1 - s) / P.nbuf) & 1));
+            tape_wait(P, X, ring, s % P.nbuf, (uint32_t)(((P.steps - 1 - s) / P.nbuf) & 1), false);
     }
     if (g.colv && ok) store_dc<M>(P, g, acc);
     cluster_sync_all();
@@ -1367,8 +1384,8 @@ __global__ void __launch_bounds__(bwd_max_threads(M), 1) seq_bwd_nl_kernel(Fused
     int lo = P.steps;
     if (threadIdx.x == 0) {
         for (int j = 0; j < P.nbuf && P.steps - 1 - j >= 0; ++j) {
-            lo = P.steps - 1 - j;
-            tape_issue(P, g, ring, lo, lo % P.nbuf);
+            const int t = P.steps - 1 - j;
+            if (tape_issue(P, g, ring, t, t % P.nbuf)) lo = t;
         }
     }
     const Lane ln = make_lane(P, g, X);
@@ -1409,8 +1426,8 @@ __global__ void __launch_bounds__(bwd_max_threads(M), 1) seq_bwd_nl_kernel(Fused
         if (!exchange_end(X, u)) return false;
         if (threadIdx.x == 0 && u > 0 && t + 1 - P.nbuf >= 0) {
             fence_proxy_async_smem();
-            lo = t + 1 - P.nbuf;
-            tape_issue(P, g, ring, lo, slot + 1 == P.nbuf ? 0 : slot + 1);
+            if (tape_issue(P, g, ring, t + 1 - P.nbuf, slot + 1 == P.nbuf ? 0 : slot + 1))
+                lo = t + 1 - P.nbuf;
         }
         if (g.colv) {
             // Kg*lambda of the thread's own cells and its neighbours' from
@@ -1453,7 +1470,7 @@ __global__ void __launch_bounds__(bwd_max_threads(M), 1) seq_bwd_nl_kernel(Fused
                      : step(std::integral_constant<int, 0>{}, u);
     if (!ok && threadIdx.x == 0) {
         for (int s = lo; s < lo + P.nbuf && s < P.steps; ++s)
-            tape_wait(P, X, ring, s % P.nbuf, (uint32_t)(((P.steps - 1 - s) / P.nbuf) & 1));
+            tape_wait(P, X, ring, s % P.nbuf, (uint32_t)(((P.steps - 1 - s) / P.nbuf) & 1), false);
     }
     if (g.colv && ok) {
         float* oc = P.gc_part + (size_t)g.inst * plane;
