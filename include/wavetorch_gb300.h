@@ -356,6 +356,62 @@ typedef struct wt_ragged_group {
 int wt_ragged_plan(const wt_ragged_group* groups, int32_t n_groups, int32_t n_sm,
                    int32_t* choice);
 
+/* ---- a ragged batch in one launch ------------------------------------
+ * Many single-instance models of different grids and step counts advance in
+ * ONE persistent, cooperative forward launch and ONE adjoint launch: one CTA
+ * per SM walks a list of work items, each item a band of rows of one model
+ * run for all of that model's steps (the band layout's kernels: fields in
+ * registers, boundary rows exchanged through L2 with bounded waits).  A
+ * model's bands run at once on different CTAs; every CTA takes its items in
+ * one global order (by start time in the host's schedule), so no CTA waits
+ * on a band that waits on it.  Linear cells, free-form geometries, every
+ * source driven by the model's own input.  Laplacian order per model: a
+ * batch of one (WT_LAP_PAIRED below 20,481 cells when h == 1, WT_LAP_SEQ
+ * otherwise).                                                              */
+typedef struct wt_ragged_model {
+    int32_t nx, ny, steps;
+    int32_t n_sources;
+    const wt_source_entry* sources_host;   /* host; in_row must be -1       */
+    int32_t n_probes;
+    const wt_probe_entry* probes_host;     /* host                          */
+    const float* b;                        /* device [nx][ny]               */
+    const float* c;                        /* device [nx][ny]               */
+    const float* x;                        /* device [steps]                */
+    float* out;                            /* device [steps][n_probes]      */
+    const float* grad_out;                 /* device [steps][n_probes]      */
+    float* grad_c;                         /* device [nx][ny] (dL/dc)       */
+} wt_ragged_model;
+
+/* The host-side plan of one ragged batch (filled by wt_ragged_prepare; plain
+ * data, kept by the caller and passed to the launches).                    */
+typedef struct wt_ragged_plan_t {
+    int32_t n_models, ctas, strip, n_items;
+    size_t smem_fwd, smem_bwd;
+    size_t workspace_bytes;
+    size_t off_params, off_first, off_items, off_halo, halo_bytes, off_err;
+    double est_steps_per_cta;              /* schedule length, band-steps    */
+} wt_ragged_plan_t;
+
+/* Device bytes of the workspace of a ragged batch on `sm_count` SMs (0: the
+ * current device's) with strips of `strip` cells per thread (4 or 8; 0: the
+ * tallest that every model's shared memory allows).                        */
+int wt_ragged_workspace_bytes(const wt_scalars* s, const wt_ragged_model* models,
+                              int32_t n_models, int32_t sm_count, int32_t strip, size_t* bytes);
+/* Plan the batch (band geometry per model, the schedule), and write the
+ * models' tables and launch parameters into the workspace (synchronous:
+ * do it before any stream capture; the pointers of `models` are bound
+ * here).  WT_ERR_UNSUPPORTED for a model the band layout cannot serve.     */
+int wt_ragged_prepare(const wt_scalars* s, const wt_ragged_model* models, int32_t n_models,
+                      int32_t sm_count, int32_t strip, void* workspace, size_t workspace_bytes,
+                      wt_ragged_plan_t* plan);
+/* The forward of every model (out), then the adjoint (grad_c; after the
+ * forward on the same workspace).  Launches only: capturable.              */
+int wt_ragged_fwd(const wt_ragged_plan_t* plan, void* workspace, wt_stream_t stream);
+int wt_ragged_bwd(const wt_ragged_plan_t* plan, void* workspace, wt_stream_t stream);
+/* WT_OK, or WT_ERR_TIMEOUT when a bounded wait of the last launch gave up
+ * (synchronises the stream).                                              */
+int wt_ragged_status(const wt_ragged_plan_t* plan, const void* workspace, wt_stream_t stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -409,3 +409,47 @@ def test_ragged_plan_matches_its_stated_rule(lib):
         out = (C.c_int32 * len(groups))()
         assert lib.wt_ragged_plan(grp, len(groups), n_sm, out) == _lib.WT_OK
         assert list(out) == _ragged_plan_restated(groups, n_sm)
+
+
+def _ragged_models(sizes, steps, in_row=-1):
+    from wavetorch_gb300 import _lib
+    keep, arr = [], (_lib.RaggedModel * len(sizes))()
+    for i, (N, T) in enumerate(zip(sizes, steps)):
+        src = (_lib.SourceEntry * 1)(_lib.SourceEntry(20 * N + N // 2, in_row))
+        prb = (_lib.ProbeEntry * 3)(*[_lib.ProbeEntry((N - 20) * N + N // 2 + d, 1, k)
+                                      for k, d in enumerate((-15, 0, 15))])
+        keep += [src, prb]
+        arr[i] = _lib.RaggedModel(N, N, T, 1, C.cast(src, C.POINTER(_lib.SourceEntry)), 3,
+                                  C.cast(prb, C.POINTER(_lib.ProbeEntry)),
+                                  *([C.c_void_p(256)] * 6))
+    return arr, keep
+
+
+def test_ragged_workspace_query(lib):
+    """The packed ragged plan on the host (an SM count given, so no device is
+    needed): its workspace holds every model's Laplacian tape (steps x bands
+    x 1024 threads x strip cells), so it grows with the steps; strips of 4
+    cut the larger grids into more bands than strips of 8; bad requests are
+    refused before any device work."""
+    from wavetorch_gb300 import _lib
+    sc = _lib.Scalars(0.707, 1.0, 0)
+    arr, keep = _ragged_models([64, 100, 256], [100, 200, 300])
+    n4, n8 = C.c_size_t(0), C.c_size_t(0)
+    assert lib.wt_ragged_workspace_bytes(C.byref(sc), arr, 3, 152, 4, C.byref(n4)) == _lib.WT_OK
+    assert lib.wt_ragged_workspace_bytes(C.byref(sc), arr, 3, 152, 0, C.byref(n8)) == _lib.WT_OK
+    assert n4.value > 4 * 1024 * (100 + 200 + 300) and n8.value > 0
+    longer, keep2 = _ragged_models([64, 100, 256], [200, 400, 600])
+    n = C.c_size_t(0)
+    assert lib.wt_ragged_workspace_bytes(C.byref(sc), longer, 3, 152, 4, C.byref(n)) == _lib.WT_OK
+    assert n.value > n4.value
+    bad, keep3 = _ragged_models([64], [100], in_row=0)
+    assert lib.wt_ragged_workspace_bytes(C.byref(sc), bad, 1, 152, 0, C.byref(n)) == \
+        _lib.WT_ERR_UNSUPPORTED
+    assert lib.wt_ragged_workspace_bytes(C.byref(sc), arr, 3, 152, 5, C.byref(n)) == \
+        _lib.WT_ERR_INVALID
+    assert lib.wt_ragged_workspace_bytes(C.byref(sc), arr, 0, 152, 0, C.byref(n)) == \
+        _lib.WT_ERR_INVALID
+    # a model wider than 1024 columns: no band layout serves it
+    wide, keep4 = _ragged_models([1100], [10])
+    assert lib.wt_ragged_workspace_bytes(C.byref(sc), wide, 1, 152, 0, C.byref(n)) == \
+        _lib.WT_ERR_UNSUPPORTED

@@ -1,11 +1,16 @@
-"""Ragged batches: models of different grid sizes and step counts advanced as
-one captured CUDA graph give each model the loss and dL/drho it gets when run
-alone through WaveRNN (tolerance 1e-5, the parity bar: the ragged step forms
-the loss gradient in closed form, autograd op by op)."""
+"""Ragged batches: models of different grid sizes and step counts advanced
+together (packed: one forward and one adjoint launch for all models; grouped:
+one launch per group of equal grids), as one captured CUDA graph, give each
+model the loss and dL/drho it gets when run alone through WaveRNN (tolerance
+1e-5, the parity bar: the ragged step forms the loss gradient in closed
+form, autograd op by op); the packed launch's probe outputs are bit-exact
+with the oracle and its dL/dc within FUSED_DC_TOL."""
 import numpy as np
 import pytest
 import torch
 
+from conftest import FUSED_DC_TOL
+import oracle.oracle as o
 import wavetorch_gb300 as wt
 from wavetorch_gb300 import _lib
 from wavetorch_gb300.data import vowel_like
@@ -58,11 +63,40 @@ def _check_against_alone(cuda, rb, models, inputs, labels):
         assert rel(grads[i].cpu().numpy(), m.cell.geom.rho.grad.cpu().numpy()) <= 1e-5, i
 
 
+@pytest.mark.parametrize("packed,strip", [(True, 0), (True, 4), (False, 0)])
 @pytest.mark.parametrize("graph", [False, True])
-def test_ragged_step_matches_models_run_alone(cuda, graph):
+def test_ragged_step_matches_models_run_alone(cuda, graph, packed, strip):
     models, inputs, labels = _ragged_case(cuda)
-    rb = RaggedBatch(models, inputs, labels, graph=graph)
+    rb = RaggedBatch(models, inputs, labels, graph=graph, packed=packed, strip=strip)
+    if packed and strip:
+        assert rb.strip == strip
     _check_against_alone(cuda, rb, models, inputs, labels)
+
+
+def test_packed_launch_against_the_oracle(cuda):
+    """Each model of a packed step (one forward launch for all six models,
+    one adjoint launch) against the oracle run on that model alone, on the
+    c the step computed: probe outputs bit-exact, dL/dc within
+    FUSED_DC_TOL; the models' Laplacian orders differ (a batch of one:
+    im2col order below 20,481 cells, oneDNN order above)."""
+    models, inputs, labels = _ragged_case(cuda)
+    rb = RaggedBatch(models, inputs, labels, graph=False, autotune=False)
+    launches = _lib.kernel_launches()
+    rb.step()
+    torch.cuda.synchronize()
+    assert rb.device_status() == _lib.WT_OK
+    # rho -> c (blur + projection) and its adjoint (blur + projection) per
+    # model, and the two sequence launches
+    assert _lib.kernel_launches() - launches == 4 * len(models) + 2
+    for i, m in enumerate(models):
+        N = m.cell.geom.domain_shape[0]
+        b = rb._b[i].cpu().numpy()
+        c = rb._c[i].cpu().numpy()
+        S = o.Seq(1, N, N, rb.T[i], 0.707, 1.0, m.source_table(1), m.probe_table()[0])
+        out, hist = S.forward(b, c, rb._x[i][None].cpu().numpy())
+        assert np.array_equal(rb._outs[i].cpu().numpy()[None], out), i
+        gc, _ = S.backward(b, c, hist, rb._gouts[i].cpu().numpy()[None])
+        assert rel(rb._gc[i].cpu().numpy(), gc) <= FUSED_DC_TOL, i
 
 
 @pytest.mark.parametrize("graph", [False, True])
@@ -71,7 +105,7 @@ def test_ragged_groups_in_band_layout(cuda, graph):
     per instance, cooperative launches, captured in the step's CUDA graph
     too): same losses and gradients as the models run alone."""
     models, inputs, labels = _ragged_case(cuda)
-    rb = RaggedBatch(models, inputs, labels, graph=False, autotune=False)
+    rb = RaggedBatch(models, inputs, labels, graph=False, autotune=False, packed=False)
     banded = 0
     for grp in rb.groups:
         if grp.N >= 200:

@@ -34,6 +34,8 @@ EXPORTED = [
     "wt_rho_to_c_fwd", "wt_rho_to_c_bwd", "wt_rho_to_c_work_bytes", "wt_rho_to_c_fwd_noalloc",
     "wt_holey_fwd", "wt_holey_bwd", "wt_holey_work_bytes",
     "wt_ragged_plan",
+    "wt_ragged_workspace_bytes", "wt_ragged_prepare", "wt_ragged_fwd", "wt_ragged_bwd",
+    "wt_ragged_status",
 ]
 
 
@@ -90,6 +92,23 @@ class RaggedGroup(C.Structure):
                 ("options", C.POINTER(RaggedOption))]
 
 
+class RaggedModel(C.Structure):
+    _fields_ = [("nx", C.c_int32), ("ny", C.c_int32), ("steps", C.c_int32),
+                ("n_sources", C.c_int32), ("sources_host", C.POINTER(SourceEntry)),
+                ("n_probes", C.c_int32), ("probes_host", C.POINTER(ProbeEntry)),
+                ("b", C.c_void_p), ("c", C.c_void_p), ("x", C.c_void_p), ("out", C.c_void_p),
+                ("grad_out", C.c_void_p), ("grad_c", C.c_void_p)]
+
+
+class RaggedPlan(C.Structure):
+    _fields_ = [("n_models", C.c_int32), ("ctas", C.c_int32), ("strip", C.c_int32),
+                ("n_items", C.c_int32), ("smem_fwd", C.c_size_t), ("smem_bwd", C.c_size_t),
+                ("workspace_bytes", C.c_size_t), ("off_params", C.c_size_t),
+                ("off_first", C.c_size_t), ("off_items", C.c_size_t), ("off_halo", C.c_size_t),
+                ("halo_bytes", C.c_size_t), ("off_err", C.c_size_t),
+                ("est_steps_per_cta", C.c_double)]
+
+
 _VP = C.c_void_p
 _lock = threading.Lock()
 _lib = None
@@ -129,6 +148,13 @@ def _declare(lib):
     lib.wt_holey_bwd.argtypes = [P(HoleyDesc)] + [_VP] * 10
     lib.wt_holey_work_bytes.argtypes = [P(HoleyDesc), P(C.c_size_t)]
     lib.wt_ragged_plan.argtypes = [P(RaggedGroup), C.c_int32, C.c_int32, P(C.c_int32)]
+    lib.wt_ragged_workspace_bytes.argtypes = [P(Scalars), P(RaggedModel), C.c_int32, C.c_int32,
+                                              C.c_int32, P(C.c_size_t)]
+    lib.wt_ragged_prepare.argtypes = [P(Scalars), P(RaggedModel), C.c_int32, C.c_int32,
+                                      C.c_int32, _VP, C.c_size_t, P(RaggedPlan)]
+    lib.wt_ragged_fwd.argtypes = [P(RaggedPlan), _VP, _VP]
+    lib.wt_ragged_bwd.argtypes = [P(RaggedPlan), _VP, _VP]
+    lib.wt_ragged_status.argtypes = [P(RaggedPlan), _VP, _VP]
     for name in EXPORTED:
         if name not in ("wt_version", "wt_status_string", "wt_last_error", "wt_kernel_launches"):
             getattr(lib, name).restype = C.c_int

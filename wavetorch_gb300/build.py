@@ -21,7 +21,7 @@ LIB_PATH = os.path.join(HERE, LIB_NAME)
 # (source, object name, extra flags): seq_fused.cu builds as four parts (its
 # kernels per Laplacian order) so that they compile in parallel
 SOURCES = [("api.cu", "api", []), ("step.cu", "step", []), ("seq_band.cu", "seq_band", []),
-           ("geom.cu", "geom", []), ("holey.cu", "holey", []), ("ragged.cu", "ragged", []), ("peaks.cu", "peaks", [])] + \
+           ("geom.cu", "geom", []), ("holey.cu", "holey", []), ("ragged.cu", "ragged", []), ("peaks.cu", "peaks", []), ("ragged_seq.cu", "ragged_seq", [])] + \
           [("seq_fused.cu", f"seq_fused_{k}", [f"-DWT_FUSED_PART={k}"]) for k in range(4)]
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

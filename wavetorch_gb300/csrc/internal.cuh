@@ -149,6 +149,18 @@ struct WtBandLaunch {
 };
 
 int wt_band_plan(int batch, int nx, int ny, int n_prb, int n_sm, WtBandLaunch* L);
+
+// Work list of a ragged batch's packed launch (seq_band.cu band_list_kernel):
+// one parameter block per model (batch 1, the model's pointers and band
+// plan), and per CTA a range of (model, band) items in the global order.
+struct WtBandList {
+    const wt::FusedParams* params;
+    const int* first;            // [ctas + 1]
+    const int2* items;           // (model, band)
+    int* abort_g;
+};
+int wt_launch_band_list(bool fwd, const WtBandList& L, int ctas, int M, size_t smem,
+                        cudaStream_t st);
 // Bytes of the band form's halo area (words and the abort word) for a plan.
 size_t wt_band_halo_bytes(int batch, const WtBandLaunch& L);
 int wt_launch_band(bool fwd, const wt::FusedParams& P, const WtBandLaunch& L, cudaStream_t st);

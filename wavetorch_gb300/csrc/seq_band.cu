@@ -77,14 +77,16 @@ struct Geo {
     bool colv, top, bot;
 };
 
-WT_DEV Geo make_geo(const FusedParams& P, int M) {
+// Threads past the band's R / M strips (a CTA of a work list serving a band
+// narrower than its block) hold no cells: they only join the barriers.
+WT_DEV Geo make_geo(const FusedParams& P, int M, int inst, int band) {
     Geo g;
-    g.inst = blockIdx.x / P.C;
-    g.band = blockIdx.x - g.inst * P.C;
+    g.inst = inst;
+    g.band = band;
     g.col = threadIdx.x % P.NCP;
     g.strip = threadIdx.x / P.NCP;
     g.gx0 = g.band * P.R + g.strip * M;
-    g.colv = g.col < P.ny;
+    g.colv = g.col < P.ny && g.strip < P.R / M;
     g.top = g.strip == 0 && g.band > 0;
     g.bot = g.strip == P.R / M - 1 && g.band + 1 < P.C;
     return g;
@@ -364,11 +366,11 @@ WT_DEV void fwd_step(const FusedParams& P, const Geo& g, const Lane& ln, const T
     }
 }
 
+// The forward of band g.band of instance g.inst, all T steps; true when a
+// bounded wait gave up (the whole CTA then leaves).
 template <int M, int ORDER>
-__global__ void __launch_bounds__(MAX_THREADS, 1) seq_fwd_band_kernel(FusedParams P) {
-    extern __shared__ __align__(16) float smem[];
+WT_DEV bool band_fwd_body(const FusedParams& P, const Geo& g, float* smem) {
     const int NT = blockDim.x;
-    const Geo g = make_geo(P, M);
     const int tile = (P.ny + 2) * P.LD;
     constexpr int CS = coef_stride<M, 3>();
     float* coef = smem + 2 * tile;
@@ -442,12 +444,20 @@ __global__ void __launch_bounds__(MAX_THREADS, 1) seq_fwd_band_kernel(FusedParam
             chunk0 = t + 1;
         }
     }
-    if (aborted) return;
+    if (aborted) return true;
     if (pc > 0) flush_probes(P, g, pr, pb, chunk0, pc);
     __syncthreads();
     if (P.psum)
         for (int q = threadIdx.x; q < P.n_prb; q += NT)
             if (pr.own[q]) P.psum[(size_t)g.inst * P.n_prb + q] = pr.ksum[q];
+    return false;
+}
+
+template <int M, int ORDER>
+__global__ void __launch_bounds__(MAX_THREADS, 1) seq_fwd_band_kernel(FusedParams P) {
+    extern __shared__ __align__(16) float smem[];
+    const int inst = blockIdx.x / P.C;
+    band_fwd_body<M, ORDER>(P, make_geo(P, M, inst, blockIdx.x - inst * P.C), smem);
 }
 
 // ============================================================================
@@ -458,11 +468,11 @@ __global__ void __launch_bounds__(MAX_THREADS, 1) seq_fwd_band_kernel(FusedParam
 // Each thread's M tape values of step t arrive by cp.async in its own words
 // of a shared staging area [M][threads], issued as soon as it has used the
 // previous step's (a whole step ahead of use).
+// The adjoint of band g.band of instance g.inst, all T steps (after its
+// forward filled the tape); true when a bounded wait gave up.
 template <int M, int ORDER>
-__global__ void __launch_bounds__(MAX_THREADS, 1) seq_bwd_band_kernel(FusedParams P) {
-    extern __shared__ __align__(16) float smem[];
+WT_DEV bool band_bwd_body(const FusedParams& P, const Geo& g, float* smem) {
     const int NT = blockDim.x;
-    const Geo g = make_geo(P, M);
     const int tile = (P.ny + 2) * P.LD;
     constexpr int CS = coef_stride<M, 4>();
     float* coef = smem + 2 * tile;
@@ -597,7 +607,8 @@ __global__ void __launch_bounds__(MAX_THREADS, 1) seq_bwd_band_kernel(FusedParam
     }
     cp_async_wait_all();   // no copy outlives the kernel's shared memory
     if (!aborted) aborted = __syncthreads_or(gave_up);
-    if (aborted || !g.colv) return;
+    if (aborted) return true;
+    if (!g.colv) return false;
     // dL/dc = (X1 * Kc) * sum_t Lap(h_{t-1}) * lam_t: grad_c of cell.py:36 with
     // its time-invariant factor applied once
     float* o = P.gc_part + (size_t)g.inst * P.nx * P.ny;
@@ -606,6 +617,58 @@ __global__ void __launch_bounds__(MAX_THREADS, 1) seq_bwd_band_kernel(FusedParam
         const int gx = g.gx0 + i;
         if (gx < P.nx)
             o[(size_t)gx * P.ny + g.col] = fmul(fmul(ln.coef[i], ln.coef[M + i]), acc[i]);
+    }
+    return false;
+}
+
+template <int M, int ORDER>
+__global__ void __launch_bounds__(MAX_THREADS, 1) seq_bwd_band_kernel(FusedParams P) {
+    extern __shared__ __align__(16) float smem[];
+    const int inst = blockIdx.x / P.C;
+    band_bwd_body<M, ORDER>(P, make_geo(P, M, inst, blockIdx.x - inst * P.C), smem);
+}
+
+// ============================================================================
+// A ragged batch in one launch: CTA blockIdx.x runs its items (model, band) in
+// order, each one the model's whole forward (or adjoint) of that band.  The
+// model's parameters come from its block in global memory, staged in shared
+// memory for the item.  Every CTA takes its items in one global order in
+// which all bands of a model sit at the same position, so the bands a band
+// waits on are either running or still to come on CTAs that will reach them
+// (by induction on that order: the earliest unfinished model has every band
+// running); the launch is cooperative, so every CTA is resident.  A wait that
+// gives up raises the launch-wide abort word, and each CTA stops at its next
+// item.
+template <int M>
+__global__ void __launch_bounds__(MAX_THREADS, 1) band_list_kernel(WtBandList L, int fwd) {
+    extern __shared__ __align__(16) float smem[];
+    __shared__ FusedParams Ps;
+    __shared__ int stop;
+    const int k0 = L.first[blockIdx.x], k1 = L.first[blockIdx.x + 1];
+    for (int k = k0; k < k1; ++k) {
+        __syncthreads();            // the previous item is done with Ps and the tiles
+        if (threadIdx.x == 0) {
+            Ps = L.params[L.items[k].x];
+            stop = ld_gpu_s32(L.abort_g);
+        }
+        __syncthreads();
+        if (stop) break;
+        const Geo g = make_geo(Ps, M, 0, L.items[k].y);
+        bool aborted;
+        switch (Ps.k.lap_order) {
+            case WT_LAP_SEQ | WT_LAP_UNIT:
+                aborted = fwd ? band_fwd_body<M, WT_LAP_SEQ | WT_LAP_UNIT>(Ps, g, smem)
+                              : band_bwd_body<M, WT_LAP_SEQ | WT_LAP_UNIT>(Ps, g, smem);
+                break;
+            case WT_LAP_PAIRED | WT_LAP_UNIT:
+                aborted = fwd ? band_fwd_body<M, WT_LAP_PAIRED | WT_LAP_UNIT>(Ps, g, smem)
+                              : band_bwd_body<M, WT_LAP_PAIRED | WT_LAP_UNIT>(Ps, g, smem);
+                break;
+            default:
+                aborted = fwd ? band_fwd_body<M, WT_LAP_SEQ>(Ps, g, smem)
+                              : band_bwd_body<M, WT_LAP_SEQ>(Ps, g, smem);
+        }
+        if (aborted) break;
     }
 }
 
@@ -731,4 +794,43 @@ int wt_launch_band(bool fwd, const wt::FusedParams& P0, const WtBandLaunch& L, c
         case WT_LAP_PAIRED | WT_LAP_UNIT: return launch_band_order<WT_LAP_PAIRED | WT_LAP_UNIT>(fwd, P, L, st);
     }
     return WT_ERR_INVALID;
+}
+
+// The packed launch of a ragged batch (see band_list_kernel).  The caller has
+// zeroed the models' exchange words and the abort word.
+int wt_launch_band_list(bool fwd, const WtBandList& L, int ctas, int M, size_t smem,
+                        cudaStream_t st) {
+    void (*kern)(WtBandList, int) = nullptr;
+    switch (M) {
+        case 4: kern = wt::band::band_list_kernel<4>; break;
+        case 8: kern = wt::band::band_list_kernel<8>; break;
+        default: return WT_ERR_UNSUPPORTED;
+    }
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return wt_cuda_status(e);
+    {
+        static std::mutex mu;
+        static std::map<std::pair<int, const void*>, size_t> done;
+        std::lock_guard<std::mutex> lock(mu);
+        size_t& v = done[{dev, reinterpret_cast<const void*>(kern)}];
+        if (v < smem) {
+            e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            if (e != cudaSuccess) return wt_cuda_status(e);
+            v = smem;
+        }
+    }
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(ctas, 1, 1);
+    cfg.blockDim = dim3(wt::band::MAX_THREADS, 1, 1);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;   // every CTA resident at once
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    e = cudaLaunchKernelEx(&cfg, kern, L, fwd ? 1 : 0);
+    wt_count_launches(1);
+    return wt_cuda_status(e);
 }

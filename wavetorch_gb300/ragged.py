@@ -1,23 +1,31 @@
 """Ragged batches: many single-instance wave models of different grid sizes
-and step counts, advanced together as one CUDA graph.
+and step counts, advanced together.
 
 The reference trains one ``WaveRNN`` at a time; a user with many models (a
-sweep over grid sizes, an ensemble) runs them one after another.  Here the
-instances are grouped by grid size and source/probe layout; a group runs as
-one fused sequence launch with one geometry per instance (``coef_batched``),
-its shorter inputs zero-padded to the group's longest step count and the
-loss masked to each instance's own steps, so its forward fields, losses and
-gradients are those of the instance run alone.  Every group runs on its own
-stream; one training step (rho -> c for every instance, the fused forwards,
-the losses and their gradients, the fused adjoints, c -> rho) is captured
-once into a CUDA graph and replayed.  A small autotuner times the layouts
-each group's grid admits (clusters of 1-16 CTAs per instance, or bands of
-rows) and keeps, per group, the one of least SM-time unless that group alone
-would then set the step time.
+sweep over grid sizes, an ensemble) runs them one after another.
 
-Loss per instance: ``CrossEntropy(normalize_power(sum_t I), label)``, the
-reference's training loss (wavetorch/train.py:61-62, utils.py:35-36); its
-gradient with respect to the probe series is formed in closed form.
+Packed form (the default): every model's forward runs in ONE persistent,
+cooperative launch and every adjoint in ONE more (``wt_ragged_fwd`` /
+``wt_ragged_bwd``, include/wavetorch_gb300.h section 5).  Each model is cut
+into bands of rows; one CTA per SM walks a list of (model, band) items in a
+global order the host's schedule fixes, each item that band's whole time
+loop, so a model runs its own step count with no padding.  A small
+autotuner times the strip heights the models' shared memory admits (4 or 8
+cells per thread) on a short horizon and keeps the faster.
+
+Grouped form (``packed=False``): models grouped by grid size and
+source/probe layout; a group runs as one fused sequence launch with one
+geometry per instance (``coef_batched``), its shorter inputs zero-padded to
+the group's longest step count and the loss masked to each instance's own
+steps; every group runs on its own stream, and the layout of each group
+(clusters of 1-16 CTAs per instance, or bands) is autotuned by SM-time.
+
+In both, one training step (rho -> c for every model, the forwards, the
+losses and their gradients, the adjoints, c -> rho) is captured once into a
+CUDA graph and replayed.  Loss per model: ``CrossEntropy(normalize_power(
+sum_t I), label)``, the reference's training loss (wavetorch/train.py:61-62,
+utils.py:35-36); its gradient with respect to the probe series is formed in
+closed form.
 """
 from __future__ import annotations
 
@@ -125,7 +133,8 @@ class RaggedBatch:
     """
 
     def __init__(self, models: Sequence, inputs: Sequence[torch.Tensor], labels, *,
-                 autotune: bool = True, graph: bool = True, segment: int = 0):
+                 autotune: bool = True, graph: bool = True, segment: int = 0,
+                 packed: bool = True, strip: int = 0):
         if not (len(models) == len(inputs) == len(labels)) or not models:
             raise ValueError("models, inputs and labels must be non-empty and of equal length")
         self.models = list(models)
@@ -137,6 +146,17 @@ class RaggedBatch:
             _check_model(m)
         self.T = [int(v.numel()) for v in inputs]
         self.n = len(self.models)
+        self.packed = packed
+        self.groups: List[_Group] = []
+        self.losses: Optional[torch.Tensor] = None
+        self.graph: Optional[torch.cuda.CUDAGraph] = None
+        if packed:
+            self._init_packed(inputs, labels, autotune, strip)
+            for m in self.models:
+                m.cell.geom.rho.grad = torch.zeros_like(m.cell.geom.rho)
+            if graph:
+                self._capture()
+            return
         # group by grid, physics scalars and source/probe layout
         keys = {}
         for i, m in enumerate(self.models):
@@ -149,7 +169,6 @@ class RaggedBatch:
                 raise ValueError("ragged batches take single-cell probes")
             key = (nx, dt, h, tuple(m.source_table(1)), tuple(ptab), tuple(m.cell.geom.b.shape))
             keys.setdefault(key, []).append(i)
-        self.groups: List[_Group] = []
         for key, idx in sorted(keys.items(), key=lambda kv: -kv[0][0]):
             N, dt, h, src, prb = key[0], key[1], key[2], list(key[3]), list(key[4])
             G, T = len(idx), max(self.T[i] for i in idx)
@@ -183,10 +202,145 @@ class RaggedBatch:
             m.cell.geom.rho.grad = torch.zeros_like(m.cell.geom.rho)
         if autotune:
             self._autotune()
-        self.losses: Optional[torch.Tensor] = None
-        self.graph: Optional[torch.cuda.CUDAGraph] = None
         if graph:
             self._capture()
+
+    # -- packed form ----------------------------------------------------------
+    def _packed_models(self, steps, x, out, gout, gc):
+        """The C-ABI descriptors of every model (host arrays kept alive)."""
+        keep, arr = [], (_lib.RaggedModel * self.n)()
+        for i, m in enumerate(self.models):
+            nx, ny = m.cell.geom.domain_shape
+            src = m.source_table(1)
+            prb, _ = m.probe_table()
+            sa = (_lib.SourceEntry * max(1, len(src)))(*[_lib.SourceEntry(c, r) for c, r in src])
+            pa = (_lib.ProbeEntry * max(1, len(prb)))(*[_lib.ProbeEntry(c, k, o) for c, k, o in prb])
+            keep += [sa, pa]
+            arr[i] = _lib.RaggedModel(nx, ny, steps[i], len(src), C.cast(sa, C.POINTER(_lib.SourceEntry)),
+                                      len(prb), C.cast(pa, C.POINTER(_lib.ProbeEntry)),
+                                      _ptr(self._b[i]), _ptr(self._c[i]), _ptr(x[i]), _ptr(out[i]),
+                                      _ptr(gout[i]), _ptr(gc[i]))
+        return arr, keep
+
+    def _prepare(self, steps, x, out, gout, gc, strip):
+        """Workspace and plan of a packed run over the given buffers."""
+        lib = _lib.load()
+        arr, keep = self._packed_models(steps, x, out, gout, gc)
+        n = C.c_size_t(0)
+        _lib.check(lib.wt_ragged_workspace_bytes(C.byref(self._sc), arr, self.n, 0, strip,
+                                                 C.byref(n)), "wt_ragged_workspace_bytes")
+        ws = torch.empty(n.value, dtype=torch.uint8, device=self.device)
+        plan = _lib.RaggedPlan()
+        _lib.check(lib.wt_ragged_prepare(C.byref(self._sc), arr, self.n, 0, strip, _ptr(ws),
+                                         n.value, C.byref(plan)), "wt_ragged_prepare")
+        return ws, plan
+
+    def _init_packed(self, inputs, labels, autotune: bool, strip: int) -> None:
+        dev = self.device
+        scal = {m.cell.scalars()[:2] for m in self.models}
+        if len(scal) != 1:
+            raise ValueError("a packed ragged batch needs one dt and one h for all models")
+        dt, h = scal.pop()
+        self._sc = scalars(dt, h, _lib.WT_LAP_SEQ)     # each model's order is planned per model
+        nprb = set()
+        for m in self.models:
+            ptab, L = m.probe_table()
+            if L != 1:
+                raise ValueError("ragged batches take single-cell probes")
+            nprb.add(len(ptab))
+            if any(r != -1 for _, r in m.source_table(1)):
+                raise ValueError("ragged batches take sources driven by the model's own input")
+        if len(nprb) != 1 or 0 in nprb:
+            raise ValueError("a packed ragged batch needs the same number of probes in every model")
+        P = nprb.pop()
+        self._P = P
+        self._b = [m.cell.geom.b.contiguous() for m in self.models]
+        self._c = [torch.empty_like(b) for b in self._b]
+        self._x = [inputs[i].to(dev, torch.float32).reshape(-1).contiguous() for i in range(self.n)]
+        rows = sum(self.T)
+        self._out = torch.empty(rows, P, device=dev)
+        self._gout = torch.empty(rows, P, device=dev)
+        offs = [0]
+        for t in self.T:
+            offs.append(offs[-1] + t)
+        self._outs = [self._out[offs[i]:offs[i + 1]] for i in range(self.n)]
+        self._gouts = [self._gout[offs[i]:offs[i + 1]] for i in range(self.n)]
+        self._gc = [torch.empty_like(b) for b in self._b]
+        self._seg = torch.repeat_interleave(torch.arange(self.n, device=dev),
+                                            torch.as_tensor(self.T, device=dev))
+        self._labels = torch.as_tensor([int(v) for v in labels], device=dev)
+        self._onehot = torch.nn.functional.one_hot(self._labels, P).to(torch.float32)
+        nwork = C.c_size_t(0)
+        self._work = []
+        for m in self.models:
+            gd = m.cell.geom.geom_desc()
+            _lib.check(_lib.load().wt_rho_to_c_work_bytes(C.byref(gd), C.byref(nwork)),
+                       "wt_rho_to_c_work_bytes")
+            self._work.append(torch.empty(nwork.value // 4, device=dev))
+        self.strip = strip or (self._tune_strip() if autotune else 0)
+        self._ws, self._plan = self._prepare(self.T, self._x, self._outs, self._gouts, self._gc,
+                                             self.strip)
+        self.strip = self._plan.strip
+
+    def _tune_strip(self, steps: int = 64) -> int:
+        """The strip height (4 or 8 cells per thread) of the faster forward +
+        adjoint on the first `steps` steps of every model; 0 when only one
+        height fits."""
+        dev = self.device
+        T = [min(t, steps) for t in self.T]
+        x = [v[:t].contiguous() for v, t in zip(self._x, T)]
+        out = [torch.zeros(t, self._P, device=dev) for t in T]
+        gout = [torch.ones(t, self._P, device=dev) for t in T]
+        gc = [torch.empty_like(b) for b in self._b]
+        for i in range(self.n):
+            self._c[i].fill_(0.75)
+        best, best_t = 0, None
+        for strip in (8, 4):
+            try:
+                ws, plan = self._prepare(T, x, out, gout, gc, strip)
+            except _lib.WaveKernelError:
+                continue
+            st = _stream(dev)
+            ts = []
+            for r in range(3):
+                torch.cuda.synchronize(dev)
+                t0 = time.perf_counter()
+                _lib.check(_lib.load().wt_ragged_fwd(C.byref(plan), _ptr(ws), st), "wt_ragged_fwd")
+                _lib.check(_lib.load().wt_ragged_bwd(C.byref(plan), _ptr(ws), st), "wt_ragged_bwd")
+                torch.cuda.synchronize(dev)
+                if r:
+                    ts.append(time.perf_counter() - t0)
+            del ws
+            if best_t is None or min(ts) < best_t:
+                best, best_t = strip, min(ts)
+        self.tuned = {"strip": best, "seconds": best_t, "steps": steps}
+        return best
+
+    def _run_packed(self) -> torch.Tensor:
+        lib = _lib.load()
+        st = _stream(self.device)
+        for i, m in enumerate(self.models):                     # rho -> c
+            geom = m.cell.geom
+            _lib.check(lib.wt_rho_to_c_fwd(C.byref(geom.geom_desc()), _ptr(geom.rho),
+                                           _ptr(geom.blur_kernel[0, 0]), _ptr(self._c[i]),
+                                           _ptr(self._work[i]), st), "wt_rho_to_c_fwd")
+        _lib.check(lib.wt_ragged_fwd(C.byref(self._plan), _ptr(self._ws), st), "wt_ragged_fwd")
+        # loss = CE(normalize_power(sum over each model's own steps))
+        I = torch.zeros(self.n, self._P, device=self.device).index_add_(0, self._seg, self._out)
+        S = I.sum(dim=1, keepdim=True)
+        p = I / S
+        loss = -torch.log_softmax(p, dim=1).gather(1, self._labels[:, None])[:, 0]
+        dp = torch.softmax(p, dim=1) - self._onehot
+        dI = (dp - (dp * p).sum(dim=1, keepdim=True)) / S          # dloss/dI per model
+        self._gout.copy_(dI.index_select(0, self._seg))
+        _lib.check(lib.wt_ragged_bwd(C.byref(self._plan), _ptr(self._ws), st), "wt_ragged_bwd")
+        for i, m in enumerate(self.models):                     # c -> rho
+            geom = m.cell.geom
+            _lib.check(lib.wt_rho_to_c_bwd(C.byref(geom.geom_desc()), _ptr(geom.rho),
+                                           _ptr(geom.blur_kernel[0, 0]), _ptr(self._gc[i]),
+                                           _ptr(geom.rho.grad), _ptr(self._work[i]), st),
+                       "wt_rho_to_c_bwd")
+        return loss
 
     def _fit_memory(self, share: float = 0.6) -> None:
         """Groups whose tapes would take the workspaces past `share` of the
@@ -206,6 +360,8 @@ class RaggedBatch:
 
     def workspace_bytes(self) -> int:
         """Device bytes the sequence workspaces of one step take."""
+        if self.packed:
+            return int(self._plan.workspace_bytes)
         return sum(seq_workspace_bytes(g.spec) for g in self.groups)
 
     # -- one step, eagerly ------------------------------------------------
@@ -253,22 +409,26 @@ class RaggedBatch:
         return torch.cat(parts)
 
     def _capture(self) -> None:
+        run = self._run_packed if self.packed else self._run
         side = torch.cuda.Stream(device=self.device)
         side.wait_stream(torch.cuda.current_stream(self.device))
         with torch.cuda.stream(side):
             for _ in range(2):
-                self._run()
+                run()
         torch.cuda.current_stream(self.device).wait_stream(side)
         torch.cuda.synchronize(self.device)
         torch.cuda.empty_cache()   # the warm-up's workspaces: the graph gets its own pool
         self.graph = torch.cuda.CUDAGraph()
         with torch.cuda.graph(self.graph):
-            self.losses = self._run()
+            self.losses = run()
 
     def device_status(self) -> int:
         """The sequence kernels' status words of the last step (synchronises):
         WT_OK, or WT_ERR_TIMEOUT when a bounded wait gave up."""
         from .functional import seq_device_status
+        if self.packed:
+            return int(_lib.load().wt_ragged_status(C.byref(self._plan), _ptr(self._ws),
+                                                    _stream(self.device)))
         worst = _lib.WT_OK
         for grp in self.groups:
             if grp.ws is not None:
@@ -281,7 +441,7 @@ class RaggedBatch:
         if self.graph is not None:
             self.graph.replay()
             return self.losses
-        return self._run()
+        return self._run_packed() if self.packed else self._run()
 
     # -- autotuner ----------------------------------------------------------
     def _autotune(self, steps: int = 96) -> None:
