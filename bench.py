@@ -912,7 +912,8 @@ def run_ragged(args):
     """Ragged workload: `instances` single-instance models, grid side
     U{64..256} (PML 20), step count U{500..4000}, the vowel-like generator
     with independent seeds, source (20, N/2), intensity probes (N-20,
-    N/2 + {-15, 0, 15}); one training step of all models as one CUDA graph.
+    N/2 + {-15, 0, 15}); one training step of all models as one CUDA graph
+    holding one forward and one adjoint launch for all models (packed form).
     Compared with the per-model loops a user of the reference would run:
     each model alone through WaveRNN, plain form and fused form, timed on a
     16-model subsample and scaled by cell-steps."""
@@ -988,8 +989,16 @@ def run_ragged(args):
         "data": "synthetic (seeded vowel-like waveforms, random-init rho)",
         "config": {"workload": f"ragged: {n} models, N ~ U{{64..256}} (PML 20), T ~ U{{500..4000}}, "
                                "fwd + adjoint to dL/drho per model",
-                   "instances": n, "groups": len(rb.groups), "cell_steps": cell_steps,
-                   "layouts": layout_counts(rb),
+                   "instances": n, "cell_steps": cell_steps,
+                   "launch": ({"form": "packed: one cooperative forward launch and one adjoint "
+                                       "launch over (model, band) work items",
+                               "ctas": rb._plan.ctas, "strip": rb._plan.strip,
+                               "work_items": rb._plan.n_items,
+                               "autotune": getattr(rb, "tuned", None),
+                               "workspace_GB": rb._plan.workspace_bytes / 1e9}
+                              if rb.packed else
+                              {"form": "grouped", "groups": len(rb.groups),
+                               "layouts": layout_counts(rb)}),
                    "l2": "flushed (512 MiB write) before every timed step",
                    "setup_s": t_setup},
         "per_model_loop": {"plain_cell_steps_per_s": loops["plain"],

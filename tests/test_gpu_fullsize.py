@@ -1,8 +1,8 @@
 """GPU checks at the benchmark configurations' full sizes: agreement with
 the oracle on the batched training configuration (B=32, 120x120, T=3500),
 the nonlinear configuration (B=64, 120x120, T=5000) and the large lens grid
-(1024x1024, T=2000 of its 8000 steps: the oracle's field history at 8000
-steps would take 34 GB of host memory), plain/fused agreement, and
+(1024x1024, T=8000; the oracle keeps its 34 GB field history in host
+memory), plain/fused agreement, and
 size-independent properties (exact linearity under power-of-two input
 scaling, silence for zero input)."""
 import numpy as np
@@ -289,12 +289,12 @@ def test_cfg2_nonlinear_full_size_against_oracle(cuda):
 def test_cfg3_lens_against_oracle(cuda):
     """The large-grid lens configuration: 1024x1024 (PML 40), line source at
     x=60 over y=200..824 driven by sin(2 pi 0.02 t), intensity probe at
-    (900, 512), first 2000 of its 8000 steps (the wave reaches the focal
-    point after about 1200).  The fused form runs it in the band layout; its
-    probe outputs are bit-exact with the oracle and dL/dc (objective
-    -sum_t I) is within FUSED_DC_TOL."""
+    (900, 512), all 8000 steps (the wave reaches the focal point after about
+    1200).  The fused form runs it in the band layout; its probe outputs are
+    bit-exact with the oracle and dL/dc (objective -sum_t I) is within
+    FUSED_DC_TOL."""
     from wavetorch_gb300.data import sinusoid
-    N, T = 1024, 2000
+    N, T = 1024, 8000
     geom = wt.WaveGeometryFreeForm((N, N), 1.0, c0=1.0, c1=0.5, abs_N=40, abs_sig=3.0, abs_p=2,
                                    rho=torch.rand(N, N, generator=torch.Generator().manual_seed(3)))
     geom = geom.to(cuda)
