@@ -173,3 +173,65 @@ def test_missing_arrival_times_out_and_the_context_survives(cuda):
     assert 1.5 < elapsed < 60, elapsed
     check(cuda, nx, ny, B, T, src, prb, seed=7)
 
+
+
+@pytest.mark.parametrize("B", [2, 3])
+def test_band_rounds_against_oracle(cuda, B):
+    """A batch whose bands outnumber the SMs it may use (300 x 400 grid, 16
+    SMs): the band layout runs in rounds, a work list of (instance, band)
+    items per CTA; probe outputs bit-exact with the oracle, dL/dc within
+    FUSED_DC_TOL, the status word clean."""
+    nx, ny, T = 300, 400, 60
+    src = [(100 * ny + 200, -1)]
+    prb = [(110 * ny + 200, 1, 0), (150 * ny + 101, 0, 1)]
+    b, c, x = problem(nx, ny, B, T, 9)
+    g = np.random.default_rng(10).standard_normal((B, T, 2)).astype(np.float32)
+    spec = SeqSpec(B, nx, ny, T, src, prb, form=_lib.WT_FORM_FUSED, sm_count=16)
+    assert fused_supported(spec)
+    sc = scalars(0.707, 1.0, lap_order(B, nx, ny, 1.0))
+    tb, tc, tx = (torch.from_numpy(v).to(cuda) for v in (b, c, x))
+    out, _, _, ws = seq_forward(spec, sc, tb, tc, tx)
+    gc, _ = seq_backward(spec, sc, tb, tc, tx, torch.from_numpy(g).to(cuda), ws, False)
+    torch.cuda.synchronize()
+    assert seq_device_status(spec, ws) == _lib.WT_OK
+    S = o.Seq(B, nx, ny, T, 0.707, 1.0, src, prb)
+    oout, hist = S.forward(b, c, x)
+    ogc, _ = S.backward(b, c, hist, g)
+    assert np.array_equal(out.cpu().numpy(), oout)
+    assert rel(gc.cpu().numpy(), ogc) <= FUSED_DC_TOL
+
+
+def test_lens_grid_batch_of_two_runs_fused(cuda):
+    """The lens grid (1024x1024, PML 40) with a batch of two: 2 x 147 bands
+    outnumber the 152 SMs, so the fused form runs the bands in rounds
+    instead of falling back to the plain form.  A point source per instance
+    (the reference's line source broadcasts a batch only when it equals the
+    line's length, wavetorch/source.py:19-20); T=200; outputs bit-exact with
+    the oracle, dL/dc within FUSED_DC_TOL."""
+    import wavetorch_gb300 as wt
+    N, B, T = 1024, 2, 200
+    geom = wt.WaveGeometryFreeForm((N, N), 1.0, c0=1.0, c1=0.5, abs_N=40, abs_sig=3.0, abs_p=2,
+                                   rho=torch.rand(N, N, generator=torch.Generator().manual_seed(3)))
+    geom = geom.to(cuda)
+    with torch.no_grad():
+        c = geom.c.detach().contiguous()
+    b = geom.b.contiguous()
+    src = [(60 * N + 512, -1)]
+    prb = [(160 * N + 512, 1, 0)]
+    t = np.arange(T, dtype=np.float32)
+    x = np.stack([np.sin(2 * np.pi * 0.02 * t), np.sin(2 * np.pi * 0.03 * t)]).astype(np.float32)
+    g = np.random.default_rng(4).standard_normal((B, T, 1)).astype(np.float32)
+    spec = SeqSpec(B, N, N, T, src, prb, form=_lib.WT_FORM_FUSED)
+    assert fused_supported(spec)
+    sc = scalars(0.707, 1.0, lap_order(B, N, N, 1.0))
+    tx = torch.from_numpy(x).to(cuda)
+    out, _, _, ws = seq_forward(spec, sc, b, c, tx)
+    gc, _ = seq_backward(spec, sc, b, c, tx, torch.from_numpy(g).to(cuda), ws, False)
+    torch.cuda.synchronize()
+    assert seq_device_status(spec, ws) == _lib.WT_OK
+    S = o.Seq(B, N, N, T, 0.707, 1.0, src, prb)
+    oout, hist = S.forward(b.cpu().numpy(), c.cpu().numpy(), x)
+    ogc, _ = S.backward(b.cpu().numpy(), c.cpu().numpy(), hist, g)
+    assert np.abs(oout).max() > 0
+    assert np.array_equal(out.cpu().numpy(), oout)
+    assert rel(gc.cpu().numpy(), ogc) <= FUSED_DC_TOL

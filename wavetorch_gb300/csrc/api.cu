@@ -117,6 +117,9 @@ struct SeqPlan {
     size_t o_hist, o_zero, o_lam, o_gc;             // plain
     size_t o_ckpt, o_stash, o_gcpart, o_lap, o_grho; // fused
     size_t o_halo;                                  // fused, band layout
+    size_t o_rfirst, o_ritems;                      // band layout in rounds: the work list
+    int rctas;                                      // CTAs of the rounds (0: one launch of
+                                                    // batch x bands CTAs)
     size_t total;
     int seg, nseg;
     bool tape;                                      // fused: tape mode
@@ -164,6 +167,56 @@ int plan_band(const wt_seq_desc* d, SeqPlan& P, size_t o) {
         if (++cnt[key(d->probes_host[i].cell)] > 2) return WT_ERR_UNSUPPORTED;
     P.total = o;
     return WT_OK;
+}
+
+// The band layout in rounds: instance i's band p is work item (i, p) on CTA
+// (i * PR + p) % ctas, each CTA taking its items in instance order, so the
+// bands of one instance run at once and the instances follow one another
+// (the kernels' band bodies as a work list; see band_list_kernel).  The
+// lists go into the int tables, which upload_tables writes.
+int plan_rounds(const wt_seq_desc* d, SeqPlan& P, size_t o, int sms) {
+    int st = plan_band(d, P, o);
+    if (st) return st;
+    P.rctas = std::min(sms, P.B * P.BL.PR);
+    P.o_rfirst = up(P.total);
+    P.o_ritems = up(P.o_rfirst + (size_t)(P.rctas + 1) * sizeof(int));
+    P.total = up(P.o_ritems + (size_t)2 * P.B * P.BL.PR * sizeof(int));
+    return WT_OK;
+}
+
+// Write the rounds' work list (first[ctas + 1], items (instance, band)) into
+// the workspace with the scatter kernel (no host wait; capturable).
+int upload_rounds(const SeqPlan& P, void* ws, cudaStream_t st) {
+    const int PR = P.BL.PR, C = P.rctas, n = P.B * PR;
+    std::vector<int> first(C + 1, 0), items(2 * (size_t)n);
+    for (int k = 0; k < n; ++k) ++first[k % C + 1];
+    for (int c = 0; c < C; ++c) first[c + 1] += first[c];
+    std::vector<int> fill(first.begin(), first.end() - 1);
+    for (int k = 0; k < n; ++k) {          // item k = (k / PR, k % PR), in instance order
+        const int at_ = fill[k % C]++;
+        items[2 * (size_t)at_] = k / PR;
+        items[2 * (size_t)at_ + 1] = k % PR;
+    }
+    static thread_local wt::IntScatter sc;
+    int* base = reinterpret_cast<int*>(static_cast<char*>(ws));
+    auto flush = [&]() -> int {
+        int rc = sc.n ? wt_launch_scatter_ints(base, sc, st) : WT_OK;
+        sc.n = 0;
+        return rc;
+    };
+    sc.n = 0;
+    auto put = [&](size_t off_bytes, const std::vector<int>& v) -> int {
+        for (size_t i = 0; i < v.size(); ++i) {
+            if (sc.n == wt::INT_SCATTER_CAP) { int rc = flush(); if (rc) return rc; }
+            sc.idx[sc.n] = (int)(off_bytes / sizeof(int) + i);
+            sc.val[sc.n++] = v[i];
+        }
+        return WT_OK;
+    };
+    int rc = put(P.o_rfirst, first);
+    if (!rc) rc = put(P.o_ritems, items);
+    if (!rc) rc = flush();
+    return rc;
 }
 
 int make_plan(const wt_seq_desc* d, SeqPlan* p, bool nl = false) {
@@ -227,6 +280,10 @@ int make_plan(const wt_seq_desc* d, SeqPlan* p, bool nl = false) {
             const int sms = band_sms(d);
             if (sms > 0 && wt_band_plan(P.B, P.nx, P.ny, P.np, sms, &P.BL) == WT_OK)
                 return plan_band(d, P, o);
+            // more bands than SMs for the whole batch: one instance's bands on
+            // the SMs, the instances in rounds (a work list, see plan_rounds)
+            if (sms > 0 && P.B > 1 && wt_band_plan(1, P.nx, P.ny, P.np, sms, &P.BL) == WT_OK)
+                return plan_rounds(d, P, o, sms);
         }
         if (st) return st;
         const size_t tape_bytes = (size_t)(nl ? 2 : 1) * P.T * P.B * P.L.C * P.L.threads * P.L.M * F;
@@ -466,6 +523,11 @@ extern "C" int wt_seq_fwd(const wt_scalars* s, const wt_seq_desc* d, const float
         F.out = out;
         F.fields = d->output_fields ? fields : nullptr;
         F.psum = P.np > 0 ? probe_sum : nullptr;   // summed in the probe flushes
+        if (P.rctas) {
+            if ((st = upload_rounds(P, workspace, cs))) return st;
+            return wt_launch_band_rounds(true, F, P.BL, P.rctas, at<int>(workspace, P.o_rfirst),
+                                         at<int>(workspace, P.o_ritems), cs);
+        }
         return P.band ? wt_launch_band(true, F, P.BL, cs) : wt_launch_fused(true, F, P.L, cs);
     }
     if (probe_sum && P.np > 0)
@@ -533,7 +595,13 @@ extern "C" int wt_seq_bwd(const wt_scalars* s, const wt_seq_desc* d, const float
     F.grad_out = grad_out;
     F.grad_x = grad_x;
     if (P.coef_batched) F.gc_part = grad_c;   // per-instance dL/dc is the result
-    st = P.band ? wt_launch_band(false, F, P.BL, cs) : wt_launch_fused(false, F, P.L, cs);
+    if (P.rctas) {
+        if ((st = upload_rounds(P, workspace, cs))) return st;
+        st = wt_launch_band_rounds(false, F, P.BL, P.rctas, at<int>(workspace, P.o_rfirst),
+                                   at<int>(workspace, P.o_ritems), cs);
+    } else {
+        st = P.band ? wt_launch_band(false, F, P.BL, cs) : wt_launch_fused(false, F, P.L, cs);
+    }
     if (st) return st;
     if (P.coef_batched) return WT_OK;
     return wt_launch_seq_adj_reduce(P.B, plane, F.gc_part, grad_c, 1, cs);

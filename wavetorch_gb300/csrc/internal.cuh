@@ -164,6 +164,11 @@ int wt_launch_band_list(bool fwd, const WtBandList& L, int ctas, int M, size_t s
 // Bytes of the band form's halo area (words and the abort word) for a plan.
 size_t wt_band_halo_bytes(int batch, const WtBandLaunch& L);
 int wt_launch_band(bool fwd, const wt::FusedParams& P, const WtBandLaunch& L, cudaStream_t st);
+// The band layout in rounds (more bands than SMs for the batch): `ctas` CTAs,
+// CTA c running items first[c] .. first[c+1]-1 of `items` ((instance, band)
+// int pairs, in instance order).
+int wt_launch_band_rounds(bool fwd, const wt::FusedParams& P, const WtBandLaunch& L, int ctas,
+                          const int* first, const int* items, cudaStream_t st);
 
 int wt_launch_step_fwd(const StepScalars& k, int batch, int nx, int ny, int coef_batched,
                        const float* b, const float* c, const float* y1, size_t bs1,

@@ -629,6 +629,31 @@ __global__ void __launch_bounds__(MAX_THREADS, 1) seq_bwd_band_kernel(FusedParam
 }
 
 // ============================================================================
+// The band layout in rounds: a batch whose bands outnumber the SMs.  CTA
+// blockIdx.x runs its items (instance, band) one after another, in instance
+// order, with the batch's parameter block; an instance's bands sit on
+// distinct CTAs, so the earliest unfinished instance always has all its
+// bands running (the work-list argument of band_list_kernel below).
+template <int M, int ORDER>
+__global__ void __launch_bounds__(MAX_THREADS, 1) band_rounds_kernel(FusedParams P,
+                                                                    const int* first,
+                                                                    const int* items, int fwd) {
+    extern __shared__ __align__(16) float smem[];
+    __shared__ int stop;
+    const int k0 = first[blockIdx.x], k1 = first[blockIdx.x + 1];
+    for (int k = k0; k < k1; ++k) {
+        __syncthreads();            // the previous item is done with the tiles
+        if (threadIdx.x == 0) stop = ld_gpu_s32(P.abort_g);
+        __syncthreads();
+        if (stop) break;
+        const Geo g = make_geo(P, M, items[2 * k], items[2 * k + 1]);
+        const bool aborted = fwd ? band_fwd_body<M, ORDER>(P, g, smem)
+                                 : band_bwd_body<M, ORDER>(P, g, smem);
+        if (aborted) break;
+    }
+}
+
+// ============================================================================
 // A ragged batch in one launch: CTA blockIdx.x runs its items (model, band) in
 // order, each one the model's whole forward (or adjoint) of that band.  The
 // model's parameters come from its block in global memory, staged in shared
@@ -833,4 +858,73 @@ int wt_launch_band_list(bool fwd, const WtBandList& L, int ctas, int M, size_t s
     e = cudaLaunchKernelEx(&cfg, kern, L, fwd ? 1 : 0);
     wt_count_launches(1);
     return wt_cuda_status(e);
+}
+
+template <int M, int ORDER>
+static int launch_rounds_m(bool fwd, const wt::FusedParams& P, const WtBandLaunch& L, int ctas,
+                           const int* first, const int* items, cudaStream_t st) {
+    void (*kern)(wt::FusedParams, const int*, const int*, int) =
+        wt::band::band_rounds_kernel<M, ORDER>;
+    const size_t smem = std::max(L.smem_fwd, L.smem_bwd);
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return wt_cuda_status(e);
+    {
+        static std::mutex mu;
+        static std::map<std::pair<int, const void*>, size_t> done;
+        std::lock_guard<std::mutex> lock(mu);
+        size_t& v = done[{dev, reinterpret_cast<const void*>(kern)}];
+        if (v < smem) {
+            e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            if (e != cudaSuccess) return wt_cuda_status(e);
+            v = smem;
+        }
+    }
+    // fresh exchange words (tag 0: nothing sent yet) and abort word
+    e = cudaMemsetAsync(P.halo, 0, wt_band_halo_bytes(P.batch, L), st);
+    if (e != cudaSuccess) return wt_cuda_status(e);
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(ctas, 1, 1);
+    cfg.blockDim = dim3(L.threads, 1, 1);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;   // every CTA resident at once
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    e = cudaLaunchKernelEx(&cfg, kern, P, first, items, fwd ? 1 : 0);
+    wt_count_launches(1);
+    return wt_cuda_status(e);
+}
+
+template <int ORDER>
+static int launch_rounds_order(bool fwd, const wt::FusedParams& P, const WtBandLaunch& L,
+                               int ctas, const int* first, const int* items, cudaStream_t st) {
+    switch (L.M) {
+        case 2: return launch_rounds_m<2, ORDER>(fwd, P, L, ctas, first, items, st);
+        case 3: return launch_rounds_m<3, ORDER>(fwd, P, L, ctas, first, items, st);
+        case 4: return launch_rounds_m<4, ORDER>(fwd, P, L, ctas, first, items, st);
+        case 5: return launch_rounds_m<5, ORDER>(fwd, P, L, ctas, first, items, st);
+        case 6: return launch_rounds_m<6, ORDER>(fwd, P, L, ctas, first, items, st);
+        case 7: return launch_rounds_m<7, ORDER>(fwd, P, L, ctas, first, items, st);
+        case 8: return launch_rounds_m<8, ORDER>(fwd, P, L, ctas, first, items, st);
+        default: return WT_ERR_UNSUPPORTED;
+    }
+}
+
+int wt_launch_band_rounds(bool fwd, const wt::FusedParams& P0, const WtBandLaunch& L, int ctas,
+                          const int* first, const int* items, cudaStream_t st) {
+    if (!P0.lap || !P0.halo || ctas <= 0) return WT_ERR_INVALID;
+    wt::FusedParams P = P0;
+    P.C = L.PR; P.R = L.R; P.NCP = L.NCP; P.LD = L.LD; P.PB = L.PB;
+    P.abort_g = reinterpret_cast<int*>(P.halo + (size_t)P.batch * L.PR * 4 * L.NCP);
+    switch (P.k.lap_order) {
+        case WT_LAP_SEQ: return launch_rounds_order<WT_LAP_SEQ>(fwd, P, L, ctas, first, items, st);
+        case WT_LAP_SEQ | WT_LAP_UNIT:
+            return launch_rounds_order<WT_LAP_SEQ | WT_LAP_UNIT>(fwd, P, L, ctas, first, items, st);
+        case WT_LAP_PAIRED | WT_LAP_UNIT:
+            return launch_rounds_order<WT_LAP_PAIRED | WT_LAP_UNIT>(fwd, P, L, ctas, first, items, st);
+    }
+    return WT_ERR_INVALID;
 }
