@@ -193,8 +193,9 @@ def test_band_layout_plan(lib):
     """Grids no cluster holds run in bands of rows, one CTA per band and SM:
     1024x1024 on 152 SMs takes 147 bands of 7 rows (1024 threads), and its
     workspace is the tape (T x 147 x 1024 x 7 floats), the exchange words,
-    dL/dc and the tables.  Refused (the caller uses the plain form): more
-    bands than SMs, more than 1024 columns, field outputs, checkpoint modes,
+    dL/dc and the tables; a batch whose bands outnumber the SMs runs in
+    rounds.  Refused (the caller uses the plain form): more than 1024 columns,
+    field outputs, checkpoint modes,
     an explicit cluster size, more than two sources on one thread's cells."""
     from wavetorch_gb300 import _lib
     from wavetorch_gb300.functional import SeqSpec, fused_supported, seq_workspace_bytes
@@ -217,7 +218,11 @@ def test_band_layout_plan(lib):
         return lib.wt_seq_workspace_bytes(C.byref(d), C.byref(n))
 
     U = _lib.WT_ERR_UNSUPPORTED
-    assert status(batch=2) == U                      # 2 x 147 bands > 152 SMs
+    # 2 x 147 bands > 152 SMs: the bands run in rounds (a work list), with
+    # both instances' tapes and a list of 2 x 147 items
+    assert status(batch=2) == _lib.WT_OK
+    ws2 = seq_workspace_bytes(SeqSpec(2, N, N, T, src, prb, sm_count=152))
+    assert 2 * tape + 2 * halo < ws2 < 2 * ws + 16 * 2**20
     assert status(ny=1056, sources=[(61, -1)], probes=[(70, 1, 0)]) == U   # > 1024 columns
     assert status(output_fields=True, probes=[]) == U
     assert status(segment=50) == U

@@ -154,8 +154,9 @@ def seq_workspace_bytes(spec: SeqSpec) -> int:
 def fused_supported(spec: SeqSpec) -> bool:
     """Whether the fused form can plan this sequence: on one thread-block
     cluster per instance (grids up to 256x256 cells), or in bands of rows, one
-    CTA per band and SM (up to 1024 columns, batch x bands within the SM
-    count).  Any other error is left for the real call to report."""
+    CTA per band and SM (up to 1024 columns; a batch whose bands outnumber the
+    SMs runs its instances in rounds).  Any other error is left for the real
+    call to report."""
     d, keep = dataclasses.replace(spec, form=_lib.WT_FORM_FUSED).desc()
     n = C.c_size_t(0)
     return _lib.load().wt_seq_workspace_bytes(C.byref(d), C.byref(n)) != _lib.WT_ERR_UNSUPPORTED
