@@ -177,11 +177,11 @@ def test_missing_arrival_times_out_and_the_context_survives(cuda):
 
 @pytest.mark.parametrize("B", [2, 3])
 def test_band_rounds_against_oracle(cuda, B):
-    """A batch whose bands outnumber the SMs it may use (300 x 400 grid, 16
-    SMs): the band layout runs in rounds, a work list of (instance, band)
-    items per CTA; probe outputs bit-exact with the oracle, dL/dc within
-    FUSED_DC_TOL, the status word clean."""
-    nx, ny, T = 300, 400, 60
+    """A batch whose bands outnumber the SMs it may use (300 x 300 grid: 13
+    bands per instance on 16 SMs): the band layout runs in rounds, a work
+    list of (instance, band) items per CTA; probe outputs bit-exact with the
+    oracle, dL/dc within FUSED_DC_TOL, the status word clean."""
+    nx, ny, T = 300, 300, 60
     src = [(100 * ny + 200, -1)]
     prb = [(110 * ny + 200, 1, 0), (150 * ny + 101, 0, 1)]
     b, c, x = problem(nx, ny, B, T, 9)
