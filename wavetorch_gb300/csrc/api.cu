@@ -114,7 +114,7 @@ struct SeqPlan {
     size_t tables_end;
     // float areas
     size_t o_amp;
-    size_t o_hist, o_zero, o_lam, o_gc;             // plain
+    size_t o_hist, o_zero, o_lam, o_gc, o_kco;      // plain
     size_t o_ckpt, o_stash, o_gcpart, o_lap, o_grho; // fused
     size_t o_halo;                                  // fused, band layout
     size_t o_rfirst, o_ritems;                      // band layout in rounds: the work list
@@ -268,6 +268,7 @@ int make_plan(const wt_seq_desc* d, SeqPlan* p, bool nl = false) {
         P.o_zero = o; o = up(o + P.plane * F);
         P.o_lam = o; o = up(o + 3 * bp * F);
         P.o_gc = o; o = up(o + bp * F);
+        P.o_kco = o; o = up(o + 4 * P.plane * F);
     } else {
         if (d->segment < -2 || d->cluster < -1) return WT_ERR_INVALID;
         // cluster -1 asks for the band layout; 0 takes a cluster when one
@@ -559,6 +560,8 @@ extern "C" int wt_seq_bwd(const wt_scalars* s, const wt_seq_desc* d, const float
         float* hist = at<float>(workspace, P.o_hist);
         float* lam = at<float>(workspace, P.o_lam);
         float* gc = at<float>(workspace, P.o_gc);
+        float* kco = at<float>(workspace, P.o_kco);
+        if ((st = wt_launch_adj_coef(k, plane, b, c, kco, cs))) return st;
         wt::AdjEpilogue e{};
         e.probemap = at<int>(workspace, P.o_prbmap);
         e.probe_next = at<int>(workspace, P.o_prbnext);
@@ -583,7 +586,7 @@ extern "C" int wt_seq_bwd(const wt_scalars* s, const wt_seq_desc* d, const float
                 e.G = grad_c;
                 e.first = t == P.T - 1;
             }
-            st = wt_launch_seq_adj_step(k, P.B, P.nx, P.ny, b, c, l1, l2, hp, hbs,
+            st = wt_launch_seq_adj_step(k, P.B, P.nx, P.ny, b, c, kco, l1, l2, hp, hbs,
                                         lam + (size_t)(t % 3) * bp, gc, e, cs);
             if (st) return st;
             if (P.B > 1 && (st = wt_launch_seq_adj_reduce(P.B, plane, gc, grad_c, t == P.T - 1, cs)))

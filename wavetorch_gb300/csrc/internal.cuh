@@ -178,8 +178,11 @@ int wt_launch_step_bwd(const StepScalars& k, int batch, int nx, int ny, int coef
                        const float* b, const float* c, const float* y1, const float* y2,
                        const float* g, float* gb, float* gcp, float* gy1, float* gy2,
                        cudaStream_t st);
+// The adjoint's coefficient planes [X1 | Kc | Kg | Ky2] of b and c (4 x plane).
+int wt_launch_adj_coef(const StepScalars& k, size_t plane, const float* b, const float* c,
+                       float* kco, cudaStream_t st);
 int wt_launch_seq_adj_step(const StepScalars& k, int batch, int nx, int ny, const float* b,
-                           const float* c, const float* lam1, const float* lam2,
+                           const float* c, const float* kco, const float* lam1, const float* lam2,
                            const float* hprev, size_t hbs, float* lam_out, float* gc,
                            const wt::AdjEpilogue& epi, cudaStream_t st);
 int wt_launch_seq_adj_reduce(int batch, size_t plane, const float* gc, float* G, int first,

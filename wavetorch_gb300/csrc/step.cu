@@ -310,17 +310,22 @@ step_fwd4_kernel(StepScalars k, int nx, int ny, int coef_batched, const float* _
     const int inst = blockIdx.z;
     const int x0 = blockIdx.y * STEP4_TX, y0 = blockIdx.x * STEP4_TY;
     const size_t plane = (size_t)nx * ny;
+    const int gx = x0 + threadIdx.y, gy = y0 + 4 * threadIdx.x;
+    const bool mine = gx < nx && gy < ny;
+    const size_t cell = mine ? (size_t)gx * ny + gy : 0;
+    const size_t ci = coef_batched ? inst * plane + cell : cell;
+    // the thread's own operands first, in flight while the tile is staged
+    float4 b4 = make_float4(0.f, 0.f, 0.f, 0.f), c4 = b4, p4 = b4;
+    if (mine) {
+        b4 = __ldg(reinterpret_cast<const float4*>(b + ci));
+        c4 = __ldg(reinterpret_cast<const float4*>(c + ci));
+        p4 = __ldg(reinterpret_cast<const float4*>(y2 + inst * bs2 + cell));
+    }
     stage_tile4(s, y1 + inst * bs1, nx, ny, x0, y0);
     __syncthreads();
-    const int gx = x0 + threadIdx.y, gy = y0 + 4 * threadIdx.x;
     Quad Q;
     load_quad(Q, s, threadIdx.y + 1, 4 + 4 * threadIdx.x);   // all lanes: the shuffles need them
-    if (gx >= nx || gy >= ny) return;
-    const size_t cell = (size_t)gx * ny + gy;
-    const size_t ci = coef_batched ? inst * plane + cell : cell;
-    const float4 b4 = __ldg(reinterpret_cast<const float4*>(b + ci));
-    const float4 c4 = __ldg(reinterpret_cast<const float4*>(c + ci));
-    const float4 p4 = __ldg(reinterpret_cast<const float4*>(y2 + inst * bs2 + cell));
+    if (!mine) return;
     const float bb[4] = {b4.x, b4.y, b4.z, b4.w}, cc[4] = {c4.x, c4.y, c4.z, c4.w};
     const float pp[4] = {p4.x, p4.y, p4.z, p4.w};
     float v[4];
@@ -348,34 +353,43 @@ step_fwd4_kernel(StepScalars k, int nx, int ny, int coef_batched, const float* _
     *reinterpret_cast<float4*>(y + inst * bs + cell) = make_float4(v[0], v[1], v[2], v[3]);
 }
 
-// The adjoint's staged field Kg * lam_{t+1} (coefficients of the cell).
-WT_DEV void stage_c2g4(float (*s)[S4W], const float* __restrict__ lam, const float* __restrict__ b,
-                       const float* __restrict__ c, const StepScalars& k, int nx, int ny, int x0,
-                       int y0) {
+// The adjoint's time-invariant coefficients as four planes [X1 | Kc | Kg |
+// Ky2] (wavetorch/cell.py:33-42, bwd_coef's arithmetic), formed once per
+// sequence instead of once per cell and step (each holds a division).
+__global__ void adj_coef_kernel(StepScalars k, size_t plane, const float* __restrict__ b,
+                                const float* __restrict__ c, float* __restrict__ kco) {
+    const size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= plane) return;
+    const BwdCoef kb = bwd_coef(__ldg(b + q), __ldg(c + q), k);
+    kco[q] = kb.X1;
+    kco[plane + q] = kb.Kc;
+    kco[2 * plane + q] = kb.Kg;
+    kco[3 * plane + q] = kb.Ky2;
+}
+
+// The adjoint's staged field Kg * lam_{t+1} (Kg: the coefficient plane).
+WT_DEV void stage_c2g4(float (*s)[S4W], const float* __restrict__ lam, const float* __restrict__ Kg,
+                       int nx, int ny, int x0, int y0) {
     const int tid = threadIdx.y * 32 + threadIdx.x;
     constexpr int CH = S4W / 4;
     for (int i = tid; i < (STEP4_TX + 2) * CH; i += STEP4_TX * 32) {
         const int rr = i / CH, j = i - rr * CH;
         const int gx = x0 - 1 + rr, gy = y0 - 4 + 4 * j;
-        float o[4] = {0.f, 0.f, 0.f, 0.f};
+        float4 o = make_float4(0.f, 0.f, 0.f, 0.f);
         if (lam && gx >= 0 && gx < nx && gy >= 0 && gy < ny) {
             const size_t hc = (size_t)gx * ny + gy;
             const float4 l4 = __ldg(reinterpret_cast<const float4*>(lam + hc));
-            const float4 b4 = __ldg(reinterpret_cast<const float4*>(b + hc));
-            const float4 c4 = __ldg(reinterpret_cast<const float4*>(c + hc));
-            const float ll[4] = {l4.x, l4.y, l4.z, l4.w}, bb[4] = {b4.x, b4.y, b4.z, b4.w};
-            const float cv[4] = {c4.x, c4.y, c4.z, c4.w};
-#pragma unroll
-            for (int m = 0; m < 4; ++m) o[m] = fmul(bwd_coef(bb[m], cv[m], k).Kg, ll[m]);
+            const float4 g4 = __ldg(reinterpret_cast<const float4*>(Kg + hc));
+            o = make_float4(fmul(g4.x, l4.x), fmul(g4.y, l4.y), fmul(g4.z, l4.z), fmul(g4.w, l4.w));
         }
-        *reinterpret_cast<float4*>(&s[rr][4 * j]) = make_float4(o[0], o[1], o[2], o[3]);
+        *reinterpret_cast<float4*>(&s[rr][4 * j]) = o;
     }
 }
 
 template <int ORDER>
 __global__ void __launch_bounds__(STEP4_TX * 32)
-seq_adj_step4_kernel(StepScalars k, int nx, int ny, const float* __restrict__ b,
-                     const float* __restrict__ c, const float* __restrict__ lam1,
+seq_adj_step4_kernel(StepScalars k, int nx, int ny, const float* __restrict__ kco,
+                     const float* __restrict__ lam1,
                      const float* __restrict__ lam2, const float* __restrict__ hprev, size_t hbs,
                      float* __restrict__ lam_out, float* __restrict__ gc, AdjEpilogue e) {
     __shared__ __align__(16) float sg[STEP4_TX + 2][S4W];
@@ -383,34 +397,37 @@ seq_adj_step4_kernel(StepScalars k, int nx, int ny, const float* __restrict__ b,
     const int inst = blockIdx.z;
     const int x0 = blockIdx.y * STEP4_TX, y0 = blockIdx.x * STEP4_TY;
     const size_t plane = (size_t)nx * ny;
-    stage_c2g4(sg, lam1 ? lam1 + inst * plane : nullptr, b, c, k, nx, ny, x0, y0);
+    const int gx = x0 + threadIdx.y, gy = y0 + 4 * threadIdx.x;
+    const bool mine = gx < nx && gy < ny;
+    const size_t cell = mine ? (size_t)gx * ny + gy : 0;
+    const size_t ic = inst * plane + cell;
+    // the thread's own operands first, so that their loads are in flight
+    // while the tiles are staged
+    float4 l1v = make_float4(0.f, 0.f, 0.f, 0.f), l2v = l1v, x1v = l1v, kcv = l1v, ky2v = l1v;
+    if (mine) {
+        if (lam1) l1v = __ldg(reinterpret_cast<const float4*>(lam1 + ic));
+        if (lam2) l2v = __ldg(reinterpret_cast<const float4*>(lam2 + ic));
+        x1v = __ldg(reinterpret_cast<const float4*>(kco + cell));
+        kcv = __ldg(reinterpret_cast<const float4*>(kco + plane + cell));
+        ky2v = __ldg(reinterpret_cast<const float4*>(kco + 3 * plane + cell));
+    }
+    stage_c2g4(sg, lam1 ? lam1 + inst * plane : nullptr, kco + 2 * plane, nx, ny, x0, y0);
     if (hprev) stage_tile4(sy, hprev + inst * hbs, nx, ny, x0, y0);
     __syncthreads();
-    const int gx = x0 + threadIdx.y, gy = y0 + 4 * threadIdx.x;
     const int r = threadIdx.y + 1, q0 = 4 + 4 * threadIdx.x;
     Quad G, Y;
     load_quad(G, sg, r, q0);
     if (hprev) load_quad(Y, sy, r, q0);
-    if (gx >= nx || gy >= ny) return;
-    const size_t cell = (size_t)gx * ny + gy;
-    const size_t ic = inst * plane + cell;
-    const float4 b4 = __ldg(reinterpret_cast<const float4*>(b + cell));
-    const float4 c4 = __ldg(reinterpret_cast<const float4*>(c + cell));
-    const float bb[4] = {b4.x, b4.y, b4.z, b4.w}, cv[4] = {c4.x, c4.y, c4.z, c4.w};
-    float l1[4] = {0.f, 0.f, 0.f, 0.f}, l2[4] = {0.f, 0.f, 0.f, 0.f};
-    if (lam1) {
-        const float4 v = __ldg(reinterpret_cast<const float4*>(lam1 + ic));
-        l1[0] = v.x; l1[1] = v.y; l1[2] = v.z; l1[3] = v.w;
-    }
-    if (lam2) {
-        const float4 v = __ldg(reinterpret_cast<const float4*>(lam2 + ic));
-        l2[0] = v.x; l2[1] = v.y; l2[2] = v.z; l2[3] = v.w;
-    }
+    if (!mine) return;
+    const float l1[4] = {l1v.x, l1v.y, l1v.z, l1v.w}, l2[4] = {l2v.x, l2v.y, l2v.z, l2v.w};
+    const float X1s[4] = {x1v.x, x1v.y, x1v.z, x1v.w}, Kcs[4] = {kcv.x, kcv.y, kcv.z, kcv.w};
+    const float Ky2s[4] = {ky2v.x, ky2v.y, ky2v.z, ky2v.w};
     const bool taps = !e.tileflag || __ldg(e.tileflag + blockIdx.y * e.tiles_y + blockIdx.x);
     float lam[4], g4[4];
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
-        const BwdCoef kb = bwd_coef(bb[j], cv[j], k);
+        BwdCoef kb;
+        kb.X1 = X1s[j]; kb.Kc = Kcs[j]; kb.Ky2 = Ky2s[j];
         // gradient arriving at h_t: first gy2 from step t+2, then gy1 from t+1
         float lv = 0.f;
         if (lam2) lv = fmul(kb.Ky2, l2[j]);
@@ -545,17 +562,24 @@ int wt_launch_step_bwd(const StepScalars& k, int batch, int nx, int ny, int coef
     return wt_cuda_status(cudaGetLastError());
 }
 
+int wt_launch_adj_coef(const StepScalars& k, size_t plane, const float* b, const float* c,
+                       float* kco, cudaStream_t st) {
+    wt::adj_coef_kernel<<<(unsigned)((plane + 255) / 256), 256, 0, st>>>(k, plane, b, c, kco);
+    wt_count_launches(1);
+    return wt_cuda_status(cudaGetLastError());
+}
+
 int wt_launch_seq_adj_step(const StepScalars& k, int batch, int nx, int ny, const float* b,
-                           const float* c, const float* lam1, const float* lam2,
+                           const float* c, const float* kco, const float* lam1, const float* lam2,
                            const float* hprev, size_t hbs, float* lam_out, float* gc,
                            const wt::AdjEpilogue& e, cudaStream_t st) {
-    if (vec4_ok(ny, {b, c, lam1, lam2, hprev, lam_out, gc, e.G}, {hbs, (size_t)nx * ny})) {
+    if (vec4_ok(ny, {b, c, kco, lam1, lam2, hprev, lam_out, gc, e.G}, {hbs, (size_t)nx * ny})) {
         dim3 blk(32, wt::STEP4_TX);
         dim3 grd((ny + wt::STEP4_TY - 1) / wt::STEP4_TY, (nx + wt::STEP4_TX - 1) / wt::STEP4_TX, batch);
         if ((k.lap_order & 1) == WT_LAP_SEQ)
-            wt::seq_adj_step4_kernel<WT_LAP_SEQ><<<grd, blk, 0, st>>>(k, nx, ny, b, c, lam1, lam2, hprev, hbs, lam_out, gc, e);
+            wt::seq_adj_step4_kernel<WT_LAP_SEQ><<<grd, blk, 0, st>>>(k, nx, ny, kco, lam1, lam2, hprev, hbs, lam_out, gc, e);
         else
-            wt::seq_adj_step4_kernel<WT_LAP_PAIRED><<<grd, blk, 0, st>>>(k, nx, ny, b, c, lam1, lam2, hprev, hbs, lam_out, gc, e);
+            wt::seq_adj_step4_kernel<WT_LAP_PAIRED><<<grd, blk, 0, st>>>(k, nx, ny, kco, lam1, lam2, hprev, hbs, lam_out, gc, e);
         wt_count_launches(1);
         return wt_cuda_status(cudaGetLastError());
     }
