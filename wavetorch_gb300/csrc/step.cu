@@ -488,6 +488,31 @@ __global__ void seq_adj_reduce_kernel(int batch, size_t plane, const float* __re
     G[cell] = first ? acc : fadd(G[cell], acc);
 }
 
+// The same sums with the blocks of 16 instances in parallel: thread (x, y)
+// forms the block sums j = y, y + blockDim.y, ... of cell x of its 32 cells
+// (warps read 32 consecutive cells of one instance), then row 0 adds the
+// blocks in order -- seq_adj_reduce_kernel's arithmetic, operand for operand.
+constexpr int RED_CELLS = 32;
+__global__ void seq_adj_reduce_blocks_kernel(int batch, size_t plane, const float* __restrict__ gc,
+                                             float* __restrict__ G, int first) {
+    extern __shared__ float part[];   // [blocks of 16][RED_CELLS]
+    const int nb = (batch + 15) / 16;
+    const size_t cell = (size_t)blockIdx.x * RED_CELLS + threadIdx.x;
+    for (int j = threadIdx.y; j < nb; j += blockDim.y) {
+        float blk = 0.f;
+        if (cell < plane) {
+            const int i1 = min(batch, 16 * j + 16);
+            for (int i = 16 * j; i < i1; ++i) blk = fadd(blk, __ldg(gc + (size_t)i * plane + cell));
+        }
+        part[j * RED_CELLS + threadIdx.x] = blk;
+    }
+    __syncthreads();
+    if (threadIdx.y != 0 || cell >= plane) return;
+    float acc = part[threadIdx.x];
+    for (int j = 1; j < nb; ++j) acc = fadd(acc, part[j * RED_CELLS + threadIdx.x]);
+    G[cell] = first ? acc : fadd(G[cell], acc);
+}
+
 __global__ void fill_zero_kernel(float* p, size_t n) {
     size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) p[i] = 0.f;
@@ -595,6 +620,15 @@ int wt_launch_seq_adj_step(const StepScalars& k, int batch, int nx, int ny, cons
 
 int wt_launch_seq_adj_reduce(int batch, size_t plane, const float* gc, float* G, int first,
                              cudaStream_t st) {
+    const int nb = (batch + 15) / 16;
+    const size_t smem = (size_t)nb * wt::RED_CELLS * sizeof(float);
+    if (batch > 16 && smem <= 48 * 1024) {   // blocks of 16 in parallel
+        dim3 blk(wt::RED_CELLS, 8);
+        wt::seq_adj_reduce_blocks_kernel<<<(unsigned)((plane + wt::RED_CELLS - 1) / wt::RED_CELLS),
+                                           blk, smem, st>>>(batch, plane, gc, G, first);
+        wt_count_launches(1);
+        return wt_cuda_status(cudaGetLastError());
+    }
     int thr = 256;
     wt::seq_adj_reduce_kernel<<<(unsigned)((plane + thr - 1) / thr), thr, 0, st>>>(batch, plane, gc, G, first);
     wt_count_launches(1);
