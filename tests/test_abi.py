@@ -265,6 +265,18 @@ def test_fused_adjoint_modes(lib):
     assert lib.wt_seq_workspace_bytes(C.byref(d), C.byref(n)) == _lib.WT_ERR_INVALID
 
 
+def test_checkpoint_workspace_is_a_small_fraction_of_the_tape(lib):
+    """At the benchmark size (B=32, 120x120, T=3500) the checkpoints at
+    sqrt(T) intervals and the two-segment recompute stash take hundreds of
+    MB, against the tape's 6.9 GB."""
+    from wavetorch_gb300.functional import SeqSpec, seq_workspace_bytes
+    prb = [(80 * 120 + y, 1, i) for i, y in enumerate((35, 50, 65))]
+    sz = lambda seg: seq_workspace_bytes(SeqSpec(32, 120, 120, 3500, [(2460, -1)], prb, segment=seg))
+    assert sz(-1) > 6e9
+    assert sz(60) < 6e8
+    assert sz(-2) == sz(60)              # the automatic interval: ceil(sqrt(3500))
+
+
 def test_per_instance_geometry_flag(lib):
     """coef_batched: fused form only; anything but 0/1 is invalid."""
     from wavetorch_gb300 import _lib

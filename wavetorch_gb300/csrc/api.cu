@@ -314,10 +314,24 @@ int make_plan(const wt_seq_desc* d, SeqPlan* p, bool nl = false) {
             P.o_lap = o; o = up(o + tape_bytes);
         } else {
             const size_t per_step = (size_t)P.B * P.L.C * P.L.M * P.L.threads * F;
+            // the recompute beside the adjoint where its kernel fits (a
+            // sqrt(T) interval unless asked; the stash holds two segments in
+            // global memory), else the recompute before each segment's
+            // adjoint steps
+            WtFusedLaunch W = P.L;
+            W.seg = d->segment > 0 ? std::min(d->segment, P.T)
+                                   : std::max(1, (int)std::ceil(std::sqrt((double)P.T)));
+            if (wt_ws_plan(P.B, P.ny, P.np, &W) == WT_OK) {
+                P.L = W;
+                P.L.ws = 1;
+                P.L.stash_smem = 0;
+            }
             P.seg = P.L.seg;
             P.nseg = (P.T + P.seg - 1) / P.seg;
             P.o_ckpt = o; o = up(o + (size_t)P.nseg * 2 * bp * F);
-            P.o_stash = o; o = up(o + (P.L.stash_smem ? 0 : (size_t)P.seg * per_step));
+            P.o_stash = o;
+            o = up(o + (P.L.ws ? 2 * (size_t)P.seg * per_step
+                               : P.L.stash_smem ? 0 : (size_t)P.seg * per_step));
         }
         P.o_gcpart = o; o = up(o + bp * F);
         if (nl) { P.o_grho = o; o = up(o + bp * F); }

@@ -135,7 +135,46 @@ struct WtFusedLaunch {
     size_t smem_bwd_base;   // adjoint shared memory before the tape ring
     int nbuf_nl;            // ring slices of the nonlinear adjoint (two-part slices)
     size_t smem_nl_coef;    // the nonlinear adjoint's per-thread coefficient words
+    // checkpoint mode with the segment recompute beside the adjoint
+    // (seq_bwd_ws_kernel: 2 x threads, a stash of two segments in global
+    // memory): ring slices, shared memory, and whether the plan uses it
+    int nbuf_ws;
+    size_t smem_ws;
+    int ws;
 };
+
+namespace wt {
+// seq_bwd_ws_kernel (checkpoint adjoint with the segment recompute beside
+// it): per-thread coefficient words (3 per cell, stride rounded up to odd),
+// threads (two groups of the adjoint's strips), and its shared-memory layout
+// in float offsets: both groups' tile slots, their halo words [4][NCP],
+// their coefficients, the adjoint seeds of two segments [2][seg][n_prb],
+// dL/dx of two segments [2][seg], the ring of stash slices (16-byte
+// aligned) and its mbarriers (byte offset).
+__host__ __device__ constexpr int ws_coef_stride(int M) { return (3 * M) | 1; }
+__host__ __device__ constexpr int ws_max_threads(int M) { return M >= 10 ? 768 : 1024; }
+struct WsLayout {
+    int tile, haloR, haloA, coefR, coefA, seeds, gx, ring, mbar;
+    __host__ __device__ WsLayout(int ny, int LD, int NCP, int NG, int M, int n_prb, int seg,
+                                 int nbuf) {
+        tile = (ny + 2) * LD;
+        haloR = 4 * tile;
+        haloA = haloR + 8 * NCP;
+        coefR = haloA + 8 * NCP;
+        coefA = coefR + NG * ws_coef_stride(M);
+        seeds = coefA + NG * ws_coef_stride(M);
+        gx = seeds + ((2 * seg * n_prb + 3) & ~3);
+        ring = gx + ((2 * seg + 3) & ~3);
+        mbar = 4 * (ring + nbuf * NG * M);
+    }
+    __host__ __device__ size_t bytes(int nbuf) const { return (size_t)mbar + 8 * (size_t)nbuf; }
+};
+}  // namespace wt
+
+// Size the ring of seq_bwd_ws_kernel for a fused plan whose checkpoint
+// interval L->seg is set (2 to 4 slices in shared memory): sets L->nbuf_ws
+// and L->smem_ws; WT_ERR_UNSUPPORTED where the kernel does not apply.
+int wt_ws_plan(int batch, int ny, int n_prb, WtFusedLaunch* L);
 
 // Launch shape of the band kernels (see seq_band.cu).
 struct WtBandLaunch {

@@ -1289,6 +1289,473 @@ __global__ void __launch_bounds__(bwd_max_threads(M), 1) seq_bwd_tape_kernel(Fus
 }
 
 // ============================================================================
+// Checkpoint adjoint with the segment recompute running beside the adjoint.
+// The CTA's threads form two groups of NG = blockDim.x / 2 with the same
+// strip layout: group R (threads [0, NG)) recomputes the forward of segment
+// s - 1 from its checkpoint while group A (threads [NG, 2 NG)) runs the
+// adjoint steps of segment s, from the Laplacians R stored in the phase
+// before.  Phase p pairs R on segment nseg-1-p with A on segment nseg-p, and
+// the CTA meets at one barrier per phase.  Each group is a step chain whose
+// pace is set by its exchanges with the neighbouring CTAs rather than by
+// issue, so each group's instructions fill the other's idle issue slots.
+//
+// R writes the Laplacians of segment s into half (s & 1) of this CTA's stash
+// [2][seg][slice] in global memory (a slice: NG x M floats in the tape's
+// chunk-major layout), and A streams them back through the tape kernel's
+// ring of bulk copies.  Each group has its own tile slots, halo words and
+// exchange sequence and synchronises on its own named barrier; the per-cell
+// coefficients of both live in shared memory (the groups share the register
+// file).  The arithmetic is the tape kernels', operand for operand.
+constexpr int WS_BAR_R = 1, WS_BAR_A = 2;
+
+WT_DEV void ws_bar(int id, int n) { asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(n) : "memory"); }
+
+// Group barrier closing an exchange; false when the CTA must leave its loop
+// (the abort word, read every 32nd barrier by the whole group).
+WT_DEV bool ws_exchange_end(const Xchg& X, int id, int n, int k) {
+    ws_bar(id, n);
+    return (k & 31) != 0 || *(volatile int*)X.abort == 0;
+}
+
+WT_DEV Geo ws_geo(const FusedParams& P, int M, int ltid) {
+    Geo g;
+    g.cta = (int)cluster_ctarank();
+    g.inst = blockIdx.x / P.C;
+    g.col = ltid % P.NCP;
+    g.strip = ltid / P.NCP;
+    g.xl0 = g.strip * M;
+    g.gx0 = g.cta * P.R + g.xl0;
+    g.S = P.R / M;
+    g.colv = g.col < P.ny;
+    g.has_up = g.cta > 0;
+    g.has_dn = g.cta + 1 < P.C;
+    return g;
+}
+
+WT_DEV void ws_xchg(Xchg& X, const FusedParams& P, const Geo& g, float* tiles, int tile,
+                    unsigned long long* words, int* abort) {
+    X.tiles = tiles;
+    X.tile = tile;
+    X.NCP = P.NCP;
+    X.hup = words;
+    X.hdn = words + 2 * P.NCP;
+    X.abort = abort;
+    X.up_hdn = g.has_up ? map_shared_rank(X.hdn, g.cta - 1) : 0u;
+    X.dn_hup = g.has_dn ? map_shared_rank(X.hup, g.cta + 1) : 0u;
+}
+
+// Taps of seq_bwd_ws_kernel, two 16-bit entries per word (the entries'
+// fields fit 16 bits: input rows < 2048, probe columns < 1024, cells < 32,
+// which the host checks before it plans this kernel).
+struct PTaps {
+    int meta;                 // ns | np << 3 | src_edge << 6
+    int s01, s23, p01, p23;
+    WT_DEV int ns() const { return meta & 7; }
+    WT_DEV int np() const { return (meta >> 3) & 7; }
+    WT_DEV bool src_edge() const { return (meta >> 6) & 1; }
+    WT_DEV int s(int e) const { return ((e < 2 ? s01 : s23) >> (16 * (e & 1))) & 0xffff; }
+    WT_DEV int p(int e) const { return ((e < 2 ? p01 : p23) >> (16 * (e & 1))) & 0xffff; }
+    WT_DEV int src_i(int e) const { return s(e) & 31; }
+    WT_DEV int src_row(int e) const { return s(e) >> 5; }
+    WT_DEV int prb_i(int e) const { return p(e) & 31; }
+    WT_DEV int prb_col(int e) const { return p(e) >> 6; }
+};
+
+WT_DEV PTaps pack_taps(const Taps& t) {
+    PTaps q;
+    q.meta = t.ns | (t.np << 3) | ((t.src_edge ? 1 : 0) << 6);
+    q.s01 = (t.s0 & 0xffff) | (t.s1 << 16);
+    q.s23 = (t.s2 & 0xffff) | (t.s3 << 16);
+    q.p01 = (t.p0 & 0xffff) | (t.p1 << 16);
+    q.p23 = (t.p2 & 0xffff) | (t.p3 << 16);
+    return q;
+}
+
+// apply_sources and seed_and_read on packed taps.
+template <int M>
+WT_DEV void apply_sources_p(const FusedParams& P, const PTaps& tp, float (&y)[M],
+                            float (&xv)[SRCMAX], int tnext) {
+#pragma unroll
+    for (int e = 0; e < SRCMAX; ++e)
+        if (e < tp.ns()) add_at<M>(y, tp.src_i(e), xv[e]);
+    if (tnext >= 0 && tnext < P.steps) {
+#pragma unroll
+        for (int e = 0; e < SRCMAX; ++e)
+            if (e < tp.ns()) xv[e] = __ldg(P.x + (size_t)tp.src_row(e) * P.steps + tnext);
+    }
+}
+template <int M>
+WT_DEV void seed_and_read_p(const FusedParams& P, const Geo& g, const PTaps& tp, int t,
+                            float (&lam)[M], const float* sr) {
+#pragma unroll
+    for (int e = 0; e < PRBMAX; ++e)
+        if (e < tp.np()) add_at<M>(lam, tp.prb_i(e), sr[tp.prb_col(e) * P.PB]);
+    if (P.grad_x && tp.ns()) {
+#pragma unroll
+        for (int e = 0; e < SRCMAX; ++e)
+            if (e < tp.ns() && tp.src_row(e) == g.inst)
+                P.grad_x[(size_t)g.inst * P.steps + t] = value_at<M>(lam, tp.src_i(e));
+    }
+}
+
+// One recompute step of group R.  Exchange kx (tile slot RS = kx & 1, halo
+// parity RS) holds h_{t-1}; h_t overwrites inout (h_{t-2}), goes to slot
+// RS ^ 1 and, when `send`, out as exchange kx + 1.  L receives Lap(h_{t-1}).
+// Coefficients cf: [A | Bc | c^2] of the thread's M cells.
+template <int M, int ORDER, int RS>
+WT_DEV void ws_rec_step(const FusedParams& P, const Geo& g, const Xchg& X, const Lane& ln,
+                        const PTaps& tp, int kx, bool send, float (&xv)[SRCMAX], int tnext,
+                        const float* cf, const float (&cur)[M], float (&inout)[M],
+                        float (&L)[M]) {
+    const float* rcol = ln.col0 + RS * ln.tile;
+    float* wcol = ln.col0 + (RS ^ 1) * ln.tile;
+    const int LD = P.LD;
+    float up = rcol[-1], dn = rcol[M];
+    if (ln.rup) up = recv_at(P, X, ln.rup + RS * ln.pstride, kx);
+    if (ln.rdn) dn = recv_at(P, X, ln.rdn + RS * ln.pstride, kx);
+    auto update = [&](int i, float u, float d) {
+        L[i] = lap5<ORDER>(u, rcol[i - LD], cur[i], rcol[i + LD], d, P.k.lap_w, P.k.lap_w4);
+        inout[i] = leapfrog(cf[i], cf[M + i], cf[2 * M + i], P.k.two_over, cur[i], inout[i], L[i]);
+    };
+    update(0, up, cur[1]);
+    update(M - 1, cur[M - 2], dn);
+    const unsigned long long tag = (unsigned long long)(uint32_t)(kx + 2) << 32;
+    if (send && !tp.src_edge()) {
+        if (ln.sup) st_cluster_u64(ln.sup + (RS ^ 1) * ln.pstride, tag | __float_as_uint(inout[0]));
+        if (ln.sdn) st_cluster_u64(ln.sdn + (RS ^ 1) * ln.pstride, tag | __float_as_uint(inout[M - 1]));
+    }
+#pragma unroll
+    for (int i = 1; i < M - 1; ++i) update(i, cur[i - 1], cur[i + 1]);
+    if (tp.ns()) {
+        apply_sources_p<M>(P, tp, inout, xv, tnext);
+        if (send && tp.src_edge()) {
+            if (ln.sup) st_cluster_u64(ln.sup + (RS ^ 1) * ln.pstride, tag | __float_as_uint(inout[0]));
+            if (ln.sdn) st_cluster_u64(ln.sdn + (RS ^ 1) * ln.pstride, tag | __float_as_uint(inout[M - 1]));
+        }
+    }
+#pragma unroll
+    for (int i = 0; i < M; ++i) wcol[i] = inout[i];
+}
+
+// The adjoint group's ring of stash slices: copies are issued and consumed
+// in the same order (descending steps within a segment, segments descending),
+// so the k-th copy sits in slot k % nbuf at mbarrier phase parity
+// (k / nbuf) & 1.
+struct WsRing {
+    uint32_t buf, full;     // shared addresses of slot 0 and of its mbarrier
+    int slice, nbuf;        // floats per slice, slots
+};
+
+// Issue the copy of one stash slice into slot `slot`.
+WT_DEV void ws_issue(const WsRing& r, const float* src, int slot) {
+    const uint32_t mb = r.full + 8u * (uint32_t)slot;
+    const uint32_t bytes = (uint32_t)(r.slice * sizeof(float));
+    mbar_arrive_expect_tx(mb, bytes);
+    bulk_g2s(r.buf + (uint32_t)(slot * r.slice) * 4u, src, bytes, mb);
+}
+
+// Bounded wait for the phase of parity `par` of slot s (tape_wait's rule).
+WT_DEV bool ws_wait(const FusedParams& P, const Xchg& X, const WsRing& r, int s, uint32_t par,
+                    bool heed_abort = true) {
+    const uint32_t mb = r.full + 8u * (uint32_t)s;
+    if (mbar_try_wait_parity_cta(mb, par)) return true;
+    const uint64_t t0 = global_ns();
+    while (!mbar_try_wait_parity_cta(mb, par)) {
+        if (heed_abort && *(volatile int*)X.abort) return false;
+        if (global_ns() - t0 > WAIT_LIMIT_NS) {
+            atomicExch(P.err, WT_DEVERR_TIMEOUT);
+            *(volatile int*)X.abort = 1;
+            return false;
+        }
+    }
+    return true;
+}
+
+// 4-byte load from a shared address.
+WT_DEV float lds_f32(uint32_t a) {
+    float v;
+    asm volatile("ld.shared.f32 %0, [%1];" : "=f"(v) : "r"(a));
+    return v;
+}
+
+// Group R of seq_bwd_ws_kernel: phase p recomputes segment nseg-1-p into
+// stash half (segment & 1); one phase barrier per phase.
+template <int M, int ORDER>
+WT_DEV void ws_recompute_group(const FusedParams& P, const Geo& g, const Xchg& X, const Lane& ln,
+                               const PTaps& tp, const float* cf, float* seeds, const float* gxs,
+                               int slice, int nseg, int ltid, int NG) {
+    constexpr int V = chunk_width<M>();
+    const int cstride = NG * V;
+    const size_t cta_stash = ((size_t)g.inst * P.C + g.cta) * 2 * P.seg * (size_t)slice;
+    int kx = 0;           // exchange index (tile slot and halo parity kx & 1)
+    // dL/dx of the segment group A finished in phase q (staged in gxs)
+    // (dL/dx is served for one point source: the CTA whose rows hold it)
+    auto copy_gx = [&](int q) {
+        const int s = nseg - q;
+        if (!P.grad_x || s >= nseg || g.cta != (__ldg(P.src_cell) / P.ny) / P.R) return;
+        const int t0 = s * P.seg, n = min(P.steps, t0 + P.seg) - t0;
+        for (int k = ltid; k < n; k += NG)
+            P.grad_x[(size_t)g.inst * P.steps + t0 + k] = gxs[(s & 1) * P.seg + k];
+    };
+    bool ok = true;
+    for (int p = 0; p <= nseg && ok; ++p) {
+        if (p > 0) copy_gx(p - 1);
+        const int sR = nseg - 1 - p;
+        if (sR >= 0) {
+            const int t0 = sR * P.seg, t1 = min(P.steps, t0 + P.seg);
+            float ya[M], yb[M];   // h_{t0-1}, h_{t0-2}
+#pragma unroll
+            for (int i = 0; i < M; ++i) ya[i] = yb[i] = 0.f;
+            if (sR > 0 && g.colv) {
+                const size_t plane = (size_t)P.nx * P.ny, bplane = (size_t)P.batch * plane;
+                const float* cp = P.ckpt + (size_t)sR * 2 * bplane + (size_t)g.inst * plane;
+#pragma unroll
+                for (int i = 0; i < M; ++i) {
+                    const int gx = g.gx0 + i;
+                    if (gx < P.nx) {
+                        const size_t cell = (size_t)gx * P.ny + g.col;
+                        ya[i] = __ldcg(cp + cell);
+                        yb[i] = __ldcg(cp + bplane + cell);
+                    }
+                }
+            }
+            if (g.colv) publish<M>(P, g, X, kx & 1, kx, ya);
+            ok = ws_exchange_end(X, WS_BAR_R, NG, 0);
+            float xv[SRCMAX];
+#pragma unroll
+            for (int e = 0; e < SRCMAX; ++e)
+                xv[e] = (e < tp.ns()) ? __ldg(P.x + (size_t)tp.src_row(e) * P.steps + t0) : 0.f;
+            float* out = P.stash + cta_stash + (size_t)(sR & 1) * P.seg * slice + (size_t)ltid * V;
+            for (int t = t0; t < t1 && ok; ++t) {
+                float L[M];
+                const bool send = t + 1 < t1;
+                const int tn = t + 1 < t1 ? t + 1 : -1;
+                if (g.colv) {
+                    if (kx & 1) {
+                        if ((t - t0) & 1) ws_rec_step<M, ORDER, 1>(P, g, X, ln, tp, kx, send, xv, tn, cf, yb, ya, L);
+                        else              ws_rec_step<M, ORDER, 1>(P, g, X, ln, tp, kx, send, xv, tn, cf, ya, yb, L);
+                    } else {
+                        if ((t - t0) & 1) ws_rec_step<M, ORDER, 0>(P, g, X, ln, tp, kx, send, xv, tn, cf, yb, ya, L);
+                        else              ws_rec_step<M, ORDER, 0>(P, g, X, ln, tp, kx, send, xv, tn, cf, ya, yb, L);
+                    }
+                    st_chunks_at<M>(out + (size_t)(t - t0) * slice, cstride, L);
+                }
+                ++kx;
+                if (t + 1 < t1) ok = ws_exchange_end(X, WS_BAR_R, NG, t - t0 + 1);
+            }
+            // the adjoint seeds of the segment's steps, for group A in the
+            // next phase: seeds[sR & 1][t - t0][q], intensity g * (2 y)
+            // (autograd's PowBackward), amplitude g
+            float* sd = seeds + (size_t)(sR & 1) * P.seg * P.n_prb;
+            const int tot = (t1 - t0) * P.n_prb;
+            for (int idx = ltid; idx < tot; idx += NG) {
+                const int k = idx / P.n_prb, q = idx - k * P.n_prb;
+                const size_t oi = ((size_t)g.inst * P.steps + t0 + k) * P.n_prb + q;
+                const float gv = P.grad_w ? __ldg(P.grad_w + (size_t)g.inst * P.n_prb + q)
+                                          : __ldg(P.grad_out + oi);
+                sd[idx] = __ldg(P.prb_kind_col + q) ? fmul(gv, fmul(2.0f, __ldg(P.amp + oi))) : gv;
+            }
+            // the stash's generic writes before the adjoint group's bulk
+            // copies read them (after the phase barrier)
+            asm volatile("fence.proxy.async;" ::: "memory");
+        }
+        __syncthreads();   // phase barrier
+        ok = ok && *(volatile int*)X.abort == 0;
+    }
+    if (ok) copy_gx(nseg);
+}
+
+// Group A of seq_bwd_ws_kernel: phase p runs the adjoint steps of segment
+// nseg-p (t descending) from stash half (segment & 1), then writes dL/dc.
+template <int M, int ORDER>
+WT_DEV void ws_adjoint_group(const FusedParams& P, const Geo& g, const Xchg& X, const Lane& ln,
+                             const PTaps& tp, const float* cf, const float* seeds, float* gxs,
+                             const WsRing& ring, int nseg, int ltid, int NG) {
+    constexpr int V = chunk_width<M>();
+    const int cstride = NG * V;
+    float lam[M], pend[M], acc[M];
+#pragma unroll
+    for (int i = 0; i < M; ++i) lam[i] = pend[i] = acc[i] = 0.f;
+    int u = 0;                        // adjoint steps done (and stash slices consumed)
+    int cslot = 0, islot = 0;         // ring slots of the next wait / issue
+    uint32_t phase = 0;               // per slot: parity of its next wait
+    int niss = 0;                     // copies issued (the issuer's count)
+    const bool issuer = ltid == 0;
+    const bool taps_here = tp.np() || (P.grad_x && tp.ns());
+    bool ok = true;
+    for (int p = 0; p <= nseg && ok; ++p) {
+        const int sA = nseg - p;
+        if (sA < nseg) {
+            const int t0 = sA * P.seg, t1 = min(P.steps, t0 + P.seg);
+            // this CTA's stash half of the segment: step t at (t - t0) slices
+            auto stash_at = [&](int t) {
+                return P.stash + ((((size_t)g.inst * P.C + g.cta) * 2 + (sA & 1)) * P.seg +
+                                  (t - t0)) * (size_t)ring.slice;
+            };
+            if (issuer) {
+                fence_proxy_async_smem();   // the slots' last readers passed the phase barrier
+                for (int j = 0; j < ring.nbuf && t1 - 1 - j >= t0; ++j) {
+                    ws_issue(ring, stash_at(t1 - 1 - j), islot);
+                    islot = islot + 1 == ring.nbuf ? 0 : islot + 1;
+                    ++niss;
+                }
+            }
+            for (int t = t1 - 1; t >= t0 && ok; --t) {
+                const int par = u & 1;
+                float* col = ln.col0 + par * ln.tile;
+                if (g.colv) {
+                    if (taps_here) {
+                        // seeds at their cells (descending reference order)
+                        // and dL/dx at the source, through the thread's column
+                        // of the slot it is about to publish into
+#pragma unroll
+                        for (int i = 0; i < M; ++i) col[i] = lam[i];
+                        const float* sr = seeds + ((size_t)(sA & 1) * P.seg + (t - t0)) * P.n_prb;
+#pragma unroll
+                        for (int e = 0; e < PRBMAX; ++e)
+                            if (e < tp.np()) col[tp.prb_i(e)] = fadd(col[tp.prb_i(e)], sr[tp.prb_col(e)]);
+                        if (P.grad_x) {   // one such cell per instance (a point source)
+#pragma unroll
+                            for (int e = 0; e < SRCMAX; ++e)
+                                if (e < tp.ns() && tp.src_row(e) == g.inst)
+                                    gxs[(sA & 1) * P.seg + (t - t0)] = col[tp.src_i(e)];
+                        }
+#pragma unroll
+                        for (int i = 0; i < M; ++i) lam[i] = col[i];
+                    }
+                    // Kg * lambda: sent for the end cells, stored into the tile
+                    // column (read back after the barrier, by this thread too)
+                    const unsigned long long tag = (unsigned long long)(uint32_t)(u + 1) << 32;
+                    if (ln.sup) st_cluster_u64(ln.sup + par * ln.pstride, tag | __float_as_uint(fmul(cf[M], lam[0])));
+                    if (ln.sdn) st_cluster_u64(ln.sdn + par * ln.pstride, tag | __float_as_uint(fmul(cf[2 * M - 1], lam[M - 1])));
+#pragma unroll
+                    for (int i = 0; i < M; ++i) col[i] = fmul(cf[M + i], lam[i]);
+                }
+                if (!(ok = ws_exchange_end(X, WS_BAR_A, NG, u))) break;
+                // step t+1's slice was read before this barrier: refill its slot
+                if (issuer && t < t1 - 1 && t + 1 - ring.nbuf >= t0) {
+                    fence_proxy_async_smem();
+                    ws_issue(ring, stash_at(t + 1 - ring.nbuf), islot);
+                    islot = islot + 1 == ring.nbuf ? 0 : islot + 1;
+                    ++niss;
+                }
+                if (g.colv) {
+                    const int LD = P.LD;
+                    const float w = P.k.lap_w, w4 = P.k.lap_w4, dt2 = P.k.dt2;
+                    ws_wait(P, X, ring, cslot, (phase >> cslot) & 1u);
+                    const uint32_t ly = ring.buf + 4u * (uint32_t)(cslot * ring.slice + ltid * V);
+                    auto update = [&](int i, float up, float dn) {
+                        const float lg = lap5<ORDER>(up, col[i - LD], col[i], col[i + LD], dn, w, w4);
+                        const float Ly = lds_f32(ly + 4u * (uint32_t)((i / V) * cstride + (i % V)));
+                        adj_cell_lp(lg, lam[i], Ly, cf[i], cf[2 * M + i], dt2, acc[i], pend[i]);
+                    };
+#pragma unroll
+                    for (int i = 1; i < M - 1; ++i) update(i, col[i - 1], col[i + 1]);
+                    float up = col[-1], dn = col[M];
+                    if (ln.rup) up = recv_at(P, X, ln.rup + par * ln.pstride, u);
+                    if (ln.rdn) dn = recv_at(P, X, ln.rdn + par * ln.pstride, u);
+                    update(0, up, col[1]);
+                    update(M - 1, col[M - 2], dn);
+                }
+                phase ^= 1u << cslot;
+                cslot = cslot + 1 == ring.nbuf ? 0 : cslot + 1;
+                ++u;
+            }
+        }
+        __syncthreads();   // phase barrier: the stash half group R filled is complete
+        ok = ok && *(volatile int*)X.abort == 0;
+    }
+    if (issuer && u < niss) {
+        // leaving early: let the copies still in flight land first (bounded waits)
+        for (int k = u; k < niss; ++k) {
+            ws_wait(P, X, ring, cslot, (phase >> cslot) & 1u, false);
+            phase ^= 1u << cslot;
+            cslot = cslot + 1 == ring.nbuf ? 0 : cslot + 1;
+        }
+    }
+    if (g.colv && ok) {
+        // dL/dc = (X1 * Kc) * sum_t Lap * lam (store_dc's arithmetic, X1 from
+        // the coefficient words)
+        float* o = P.gc_part + (size_t)g.inst * P.nx * P.ny;
+#pragma unroll
+        for (int i = 0; i < M; ++i) {
+            const int gx = g.gx0 + i;
+            if (gx < P.nx) {
+                const size_t cell = (size_t)gx * P.ny + g.col;
+                const float Kc = fmul(fmul(2.0f, __ldg(P.c + P.coef_stride * g.inst + cell)), P.k.dt2);
+                o[cell] = fmul(fmul(cf[i], Kc), acc[i]);
+            }
+        }
+    }
+}
+
+template <int M, int ORDER>
+__global__ void __launch_bounds__(ws_max_threads(M), 1) seq_bwd_ws_kernel(FusedParams P) {
+    extern __shared__ __align__(16) float smem[];
+    __shared__ int abort_flag;
+    const int NG = blockDim.x >> 1;
+    const bool grpA = (int)threadIdx.x >= NG;
+    const int ltid = grpA ? (int)threadIdx.x - NG : (int)threadIdx.x;
+    const Geo g = ws_geo(P, M, ltid);
+    const WsLayout lay(P.ny, P.LD, P.NCP, NG, M, P.n_prb, P.seg, P.nbuf);
+    constexpr int CS = ws_coef_stride(M);
+    // zero both groups' tiles and halo words
+    for (int i = threadIdx.x; i < lay.coefR; i += blockDim.x) smem[i] = 0.f;
+    if (threadIdx.x == 0) abort_flag = 0;
+    Xchg X;
+    ws_xchg(X, P, g, smem + (grpA ? 2 * lay.tile : 0), lay.tile,
+            reinterpret_cast<unsigned long long*>(smem + (grpA ? lay.haloA : lay.haloR)),
+            &abort_flag);
+    float* cf = smem + (grpA ? lay.coefA : lay.coefR) + ltid * CS;
+    // per-cell coefficients: R [A | Bc | c^2], A [X1 | Kg | Ky2]
+#pragma unroll
+    for (int i = 0; i < M; ++i) {
+        float k0 = 0.f, k1 = 0.f, k2 = 0.f;
+        const int gx = g.gx0 + i;
+        if (g.colv && gx < P.nx) {
+            const size_t cell = P.coef_stride * g.inst + (size_t)gx * P.ny + g.col;
+            const float bv = __ldg(P.b + cell), cv = __ldg(P.c + cell);
+            if (grpA) {
+                const BwdCoef k = bwd_coef(bv, cv, P.k);
+                k0 = k.X1; k1 = k.Kg; k2 = k.Ky2;
+            } else {
+                const FwdCoef f = fwd_coef(bv, cv, P.k);
+                k0 = f.A; k1 = f.Bc; k2 = f.c2;
+            }
+        }
+        cf[i] = k0;
+        cf[M + i] = k1;
+        cf[2 * M + i] = k2;
+    }
+    PTaps tp;
+    {
+        Taps t;
+        build_taps<M>(P, g, t);
+        tp = pack_taps(t);
+    }
+    float* seeds = smem + lay.seeds;
+    WsRing ring;
+    ring.buf = smem_addr(smem + lay.ring);
+    ring.full = smem_addr(smem) + (uint32_t)lay.mbar;
+    ring.slice = NG * M;
+    ring.nbuf = P.nbuf;
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < P.nbuf; ++s) mbar_init(ring.full + 8u * (uint32_t)s, 1);
+        fence_mbarrier_init_cluster();
+    }
+    const Lane ln = make_lane(P, g, X);
+    cluster_sync_all();   // zeroed tiles and halo words, coefficients, barriers
+
+    const int nseg = (P.steps + P.seg - 1) / P.seg;
+    // each group runs its own loop over the nseg + 1 phases (its state lives
+    // only on its own path); both meet at the same phase barriers
+    float* gxs = smem + lay.gx;
+    if (grpA) ws_adjoint_group<M, ORDER>(P, g, X, ln, tp, cf, seeds, gxs, ring, nseg, ltid, NG);
+    else      ws_recompute_group<M, ORDER>(P, g, X, ln, tp, cf, seeds, gxs, ring.slice, nseg, ltid, NG);
+    cluster_sync_all();
+}
+
+// ============================================================================
 // Nonlinear cell, adjoint (tape mode).  Per step s, with g = lam_s and the
 // tape's Lap(h1), h1 = h_{s-1} (slot s) and h2 = h_{s-2} (part 1 of slot
 // s-1), TimeStep's backward (wavetorch/cell.py:33-42) at the step's own b, c,
@@ -1591,7 +2058,32 @@ int wt_fused_plan(int nx, int ny, int steps, int n_prb, int cluster_req, int seg
                              ? (int)((nl_room - L->smem_nl_coef) / (2 * slice + 8)) : 0;
         L->nbuf_nl = std::min(8, nfit);
         if (L->smem_fwd_tape > SMEM_MAX || L->threads > wt::fwd_max_threads(M)) L->nbuf = 0;
+        // checkpoints with the recompute beside the adjoint: 10-cell strips
+        // (two groups of at most 384 threads share the register file); its
+        // ring and shared memory are sized once the interval is known
+        // (wt_ws_plan)
+        L->nbuf_ws = 0;
+        L->smem_ws = 0;
+        L->ws = 0;
         return 0;
+    }
+    return WT_ERR_UNSUPPORTED;
+}
+
+int wt_ws_plan(int batch, int ny, int n_prb, WtFusedLaunch* L) {
+    const size_t SMEM_MAX = 227 * 1024 - 64;
+    const size_t slice = (size_t)L->M * L->threads * sizeof(float);
+    // packed taps (PTaps): input rows < 2048, probe columns < 1024
+    if (L->M != 10 || 2 * L->threads > wt::ws_max_threads(L->M) || slice >= (1u << 20) ||
+        batch >= 2048 || n_prb >= 1024 || L->seg < 1)
+        return WT_ERR_UNSUPPORTED;
+    for (int nb = 4; nb >= 2; --nb) {
+        const wt::WsLayout lay(ny, L->LD, L->NCP, L->threads, L->M, n_prb, L->seg, nb);
+        if (lay.bytes(nb) <= SMEM_MAX) {
+            L->nbuf_ws = nb;
+            L->smem_ws = lay.bytes(nb);
+            return WT_OK;
+        }
     }
     return WT_ERR_UNSUPPORTED;
 }
@@ -1738,6 +2230,12 @@ static int launch_bwd(const wt::FusedParams& P0, const WtFusedLaunch& L, cudaStr
     P.LD = L.LD;
     if (P.lap)
         return launch_kernel(wt::seq_bwd_tape_kernel<M, ORDER>, P, L.C, L.threads, L.smem_tape, st);
+    if constexpr (M == 10) {
+        if (L.ws) {
+            P.nbuf = L.nbuf_ws;
+            return launch_kernel(wt::seq_bwd_ws_kernel<M, ORDER>, P, L.C, 2 * L.threads, L.smem_ws, st);
+        }
+    }
     return launch_kernel(wt::seq_bwd_fused_kernel<M, ORDER>, P, L.C, L.threads, L.smem_bwd, st);
 }
 
