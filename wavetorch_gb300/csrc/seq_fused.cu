@@ -1409,12 +1409,16 @@ WT_DEV void ws_rec_step(const FusedParams& P, const Geo& g, const Xchg& X, const
                         float (&L)[M]) {
     const float* rcol = ln.col0 + RS * ln.tile;
     float* wcol = ln.col0 + (RS ^ 1) * ln.tile;
-    const int LD = P.LD;
+    // the neighbour columns by 8-byte loads (conflict-free: the tile stride
+    // is an odd number of 8-byte words)
+    float lf[M], rt[M];
+    lds_col<M>(lf, rcol - P.LD);
+    lds_col<M>(rt, rcol + P.LD);
     float up = rcol[-1], dn = rcol[M];
     if (ln.rup) up = recv_at(P, X, ln.rup + RS * ln.pstride, kx);
     if (ln.rdn) dn = recv_at(P, X, ln.rdn + RS * ln.pstride, kx);
     auto update = [&](int i, float u, float d) {
-        L[i] = lap5<ORDER>(u, rcol[i - LD], cur[i], rcol[i + LD], d, P.k.lap_w, P.k.lap_w4);
+        L[i] = lap5<ORDER>(u, lf[i], cur[i], rt[i], d, P.k.lap_w, P.k.lap_w4);
         inout[i] = leapfrog(cf[i], cf[M + i], cf[2 * M + i], P.k.two_over, cur[i], inout[i], L[i]);
     };
     update(0, up, cur[1]);
@@ -1433,8 +1437,7 @@ WT_DEV void ws_rec_step(const FusedParams& P, const Geo& g, const Xchg& X, const
             if (ln.sdn) st_cluster_u64(ln.sdn + (RS ^ 1) * ln.pstride, tag | __float_as_uint(inout[M - 1]));
         }
     }
-#pragma unroll
-    for (int i = 0; i < M; ++i) wcol[i] = inout[i];
+    sts_col<M>(wcol, inout);
 }
 
 // The adjoint group's ring of stash slices: copies are issued and consumed
@@ -1471,10 +1474,10 @@ WT_DEV bool ws_wait(const FusedParams& P, const Xchg& X, const WsRing& r, int s,
     return true;
 }
 
-// 4-byte load from a shared address.
-WT_DEV float lds_f32(uint32_t a) {
-    float v;
-    asm volatile("ld.shared.f32 %0, [%1];" : "=f"(v) : "r"(a));
+// 8-byte load from a shared address (8-byte aligned).
+WT_DEV float2 lds_f32x2(uint32_t a) {
+    float2 v;
+    asm volatile("ld.shared.v2.f32 {%0, %1}, [%2];" : "=f"(v.x), "=f"(v.y) : "r"(a));
     return v;
 }
 
@@ -1625,11 +1628,13 @@ WT_DEV void ws_adjoint_group(const FusedParams& P, const Geo& g, const Xchg& X, 
                     }
                     // Kg * lambda: sent for the end cells, stored into the tile
                     // column (read back after the barrier, by this thread too)
-                    const unsigned long long tag = (unsigned long long)(uint32_t)(u + 1) << 32;
-                    if (ln.sup) st_cluster_u64(ln.sup + par * ln.pstride, tag | __float_as_uint(fmul(cf[M], lam[0])));
-                    if (ln.sdn) st_cluster_u64(ln.sdn + par * ln.pstride, tag | __float_as_uint(fmul(cf[2 * M - 1], lam[M - 1])));
+                    float c2g[M];
 #pragma unroll
-                    for (int i = 0; i < M; ++i) col[i] = fmul(cf[M + i], lam[i]);
+                    for (int i = 0; i < M; ++i) c2g[i] = fmul(cf[M + i], lam[i]);
+                    const unsigned long long tag = (unsigned long long)(uint32_t)(u + 1) << 32;
+                    if (ln.sup) st_cluster_u64(ln.sup + par * ln.pstride, tag | __float_as_uint(c2g[0]));
+                    if (ln.sdn) st_cluster_u64(ln.sdn + par * ln.pstride, tag | __float_as_uint(c2g[M - 1]));
+                    sts_col<M>(col, c2g);
                 }
                 if (!(ok = ws_exchange_end(X, WS_BAR_A, NG, u))) break;
                 // step t+1's slice was read before this barrier: refill its slot
@@ -1643,19 +1648,38 @@ WT_DEV void ws_adjoint_group(const FusedParams& P, const Geo& g, const Xchg& X, 
                     const int LD = P.LD;
                     const float w = P.k.lap_w, w4 = P.k.lap_w4, dt2 = P.k.dt2;
                     ws_wait(P, X, ring, cslot, (phase >> cslot) & 1u);
+                    // this thread's chunk 0 of the slice (chunk j of 2 cells
+                    // at + j * cstride floats)
                     const uint32_t ly = ring.buf + 4u * (uint32_t)(cslot * ring.slice + ltid * V);
-                    auto update = [&](int i, float up, float dn) {
-                        const float lg = lap5<ORDER>(up, col[i - LD], col[i], col[i + LD], dn, w, w4);
-                        const float Ly = lds_f32(ly + 4u * (uint32_t)((i / V) * cstride + (i % V)));
+                    float own[M];
+                    lds_col<M>(own, col);
+                    auto update = [&](int i, float up, float dn, float lf, float rt, float Ly) {
+                        const float lg = lap5<ORDER>(up, lf, own[i], rt, dn, w, w4);
                         adj_cell_lp(lg, lam[i], Ly, cf[i], cf[2 * M + i], dt2, acc[i], pend[i]);
                     };
+                    // cells in pairs (8-byte accesses); the end cells last,
+                    // after the halo words
+                    const float2 l0 = *reinterpret_cast<const float2*>(col - LD);
+                    const float2 r0 = *reinterpret_cast<const float2*>(col + LD);
+                    const float2 y0 = lds_f32x2(ly);
+                    update(1, own[0], own[2], l0.y, r0.y, y0.y);
 #pragma unroll
-                    for (int i = 1; i < M - 1; ++i) update(i, col[i - 1], col[i + 1]);
+                    for (int j = 1; j < M / 2 - 1; ++j) {
+                        const float2 l = *reinterpret_cast<const float2*>(col - LD + 2 * j);
+                        const float2 r = *reinterpret_cast<const float2*>(col + LD + 2 * j);
+                        const float2 y = lds_f32x2(ly + 4u * (uint32_t)(j * cstride));
+                        update(2 * j, own[2 * j - 1], own[2 * j + 1], l.x, r.x, y.x);
+                        update(2 * j + 1, own[2 * j], own[2 * j + 2], l.y, r.y, y.y);
+                    }
+                    const float2 l9 = *reinterpret_cast<const float2*>(col - LD + M - 2);
+                    const float2 r9 = *reinterpret_cast<const float2*>(col + LD + M - 2);
+                    const float2 y9 = lds_f32x2(ly + 4u * (uint32_t)((M / 2 - 1) * cstride));
+                    update(M - 2, own[M - 3], own[M - 1], l9.x, r9.x, y9.x);
                     float up = col[-1], dn = col[M];
                     if (ln.rup) up = recv_at(P, X, ln.rup + par * ln.pstride, u);
                     if (ln.rdn) dn = recv_at(P, X, ln.rdn + par * ln.pstride, u);
-                    update(0, up, col[1]);
-                    update(M - 1, col[M - 2], dn);
+                    update(0, up, own[1], l0.x, r0.x, y0.x);
+                    update(M - 1, own[M - 2], dn, l9.y, r9.y, y9.y);
                 }
                 phase ^= 1u << cslot;
                 cslot = cslot + 1 == ring.nbuf ? 0 : cslot + 1;
