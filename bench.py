@@ -498,8 +498,9 @@ def run_ours(args):
                          "checkpoint_over_tape_step": (t_f * 1e3 + modes["checkpoint"]["adjoint_ms"]) /
                                                       (t_f * 1e3 + modes["tape"]["adjoint_ms"]),
                          "note": "tape: every step's Laplacian kept in HBM; checkpoint: the pair "
-                                 "(h_{t-1}, h_{t-2}) every ceil(sqrt(T)) steps, each segment "
-                                 "recomputed before its adjoint steps"}
+                                 "(h_{t-1}, h_{t-2}) every ceil(sqrt(T)) steps, one thread group "
+                                 "recomputing segment s-1 while a second runs the adjoint steps "
+                                 "of segment s (two segments' Laplacians staged in HBM)"}
         torch.cuda.empty_cache()
 
     # ---- fused form: the on-chip resources that bound it ----

@@ -152,10 +152,18 @@ typedef struct wt_seq_desc {
  *       of the kernels' strips) and the adjoint streams it back; no
  *       recompute.
  *   >0  checkpoints every `segment` steps; the adjoint recomputes each
- *       segment's forward (workspace ~ 2 fields per segment).
+ *       segment's forward (workspace ~ 2 fields per segment).  Where the
+ *       cluster layout runs 10-cell strips (120 x 120 grids among them) one
+ *       group of threads per CTA recomputes the next segment while a second
+ *       runs the adjoint steps of the current one, and two segments'
+ *       Laplacians (2 x segment x batch x nx x ny floats, plus strip
+ *       padding) are staged in the workspace; elsewhere each segment is
+ *       recomputed in shared memory or a one-segment stash before its
+ *       adjoint steps.
  *    0  automatic: the tape when it takes at most 16 GiB and output_fields
- *       is 0, else checkpoints at the largest interval whose recompute stash
- *       fits in shared memory.
+ *       is 0, else checkpoints: every ceil(sqrt(steps)) steps where the
+ *       two-group recompute applies, else at the largest interval whose
+ *       recompute stash fits in shared memory.
  *   -2  checkpoints at that automatic interval (never the tape).
  * Both modes give identical results.  The plain form ignores it.            */
 
