@@ -194,8 +194,10 @@ def test_band_layout_plan(lib):
     1024x1024 on 152 SMs takes 147 bands of 7 rows (1024 threads), and its
     workspace is the tape (T x 147 x 1024 x 7 floats), the exchange words,
     dL/dc and the tables; a batch whose bands outnumber the SMs runs in
-    rounds.  Refused (the caller uses the plain form): more than 1024 columns,
-    field outputs, checkpoint modes,
+    rounds.  From checkpoints (segment > 0 or -2, or automatically past a
+    64 GiB tape) it keeps the pairs of fields every `segment` steps, one
+    segment's stash of Laplacians and the adjoint's per-cell state.  Refused
+    (the caller uses the plain form): more than 1024 columns, field outputs,
     an explicit cluster size, more than two sources on one thread's cells."""
     from wavetorch_gb300 import _lib
     from wavetorch_gb300.functional import SeqSpec, fused_supported, seq_workspace_bytes
@@ -225,8 +227,17 @@ def test_band_layout_plan(lib):
     assert 2 * tape + 2 * halo < ws2 < 2 * ws + 16 * 2**20
     assert status(ny=1056, sources=[(61, -1)], probes=[(70, 1, 0)]) == U   # > 1024 columns
     assert status(output_fields=True, probes=[]) == U
-    assert status(segment=50) == U
-    assert status(segment=-2) == U
+    assert status(segment=50) == _lib.WT_OK
+    assert status(segment=-2) == _lib.WT_OK
+    slice_ = 147 * 1024 * 7 * 4                      # one step of tape
+    ckpt = lambda seg: -(-T // seg) * 2 * N * N * 4 + seg * slice_ + 3 * slice_
+    ws50 = seq_workspace_bytes(SeqSpec(1, N, N, T, src, prb, sm_count=152, segment=50))
+    assert ckpt(50) + halo < ws50 < ckpt(50) + halo + N * N * 4 + 16 * 2**20
+    ws_auto = seq_workspace_bytes(SeqSpec(1, N, N, T, src, prb, sm_count=152, segment=-2))
+    assert ckpt(10) + halo < ws_auto < ckpt(10) + halo + N * N * 4 + 16 * 2**20   # ceil(sqrt(100))
+    # a tape past 64 GiB: checkpoints in the automatic mode
+    long_T = 20000
+    assert seq_workspace_bytes(SeqSpec(1, N, N, long_T, src, prb, sm_count=152)) < 8 * 2**30
     assert status(cluster=4) == U
     assert status(sources=[(60 * N + 5, -1), (61 * N + 5, -1), (62 * N + 5, -1)]) == U
     assert status(sources=[(60 * N + 5, -1), (61 * N + 5, -1)]) == _lib.WT_OK
@@ -238,7 +249,7 @@ def test_band_layout_plan(lib):
     # cluster -1 asks for bands where a cluster would hold the grid; below -1 invalid
     small = dict(nx=120, ny=120, sources=[(20 * 120 + 60, -1)], probes=[(80 * 120 + 50, 1, 0)])
     assert status(cluster=-1, sm_count=16, **small) == _lib.WT_OK
-    assert status(cluster=-1, sm_count=16, segment=-2, **small) == U
+    assert status(cluster=-1, sm_count=16, segment=-2, **small) == _lib.WT_OK
     assert status(cluster=-2, **small) == _lib.WT_ERR_INVALID
     sz = lambda **kw: seq_workspace_bytes(SeqSpec(1, 120, 120, T, [(20 * 120 + 60, -1)],
                                                   [(80 * 120 + 50, 1, 0)], **kw))

@@ -235,3 +235,59 @@ def test_lens_grid_batch_of_two_runs_fused(cuda):
     assert np.abs(oout).max() > 0
     assert np.array_equal(out.cpu().numpy(), oout)
     assert rel(gc.cpu().numpy(), ogc) <= FUSED_DC_TOL
+
+
+def _band_modes(cuda, nx, ny, B, T, src, prb, segments, sm_count, seed):
+    """Outputs, probe sums, dL/dc and dL/dx of the band layout from the tape
+    and from checkpoints every `segment` steps (each segment recomputed by
+    one launch, its adjoint steps run by the next)."""
+    b, c, x = problem(nx, ny, B, T, seed)
+    g = np.random.default_rng(seed + 1).standard_normal((B, T, len(prb))).astype(np.float32)
+    sc = scalars(0.707, 1.0, lap_order(B, nx, ny, 1.0))
+    tb, tc, tx = (torch.from_numpy(v).to(cuda) for v in (b, c, x))
+    tg = torch.from_numpy(g).to(cuda)
+    res = {}
+    for seg in (-1,) + tuple(segments):
+        spec = SeqSpec(B, nx, ny, T, src, prb, form=_lib.WT_FORM_FUSED, sm_count=sm_count,
+                       segment=seg, cluster=-1)
+        out, _, psum, ws = seq_forward(spec, sc, tb, tc, tx, want_sum=True)
+        gc, gx = seq_backward(spec, sc, tb, tc, tx, tg, ws, len(src) == 1)
+        torch.cuda.synchronize()
+        assert seq_device_status(spec, ws) == _lib.WT_OK
+        res[seg] = (out, psum, gc) + ((gx,) if gx is not None else ())
+    return res
+
+
+@pytest.mark.parametrize("segments", [(1, 7, 50), (120, 500)])
+def test_band_checkpoints_equal_the_tape(cuda, segments):
+    """300 x 300 in bands on 16 SMs, T=120: from checkpoints (one-step
+    segments, intervals that do not divide T, a single segment) the outputs,
+    probe sums, dL/dc and dL/dx equal the tape mode's bit for bit."""
+    N = 300
+    src = [(40 * N + 150, -1)]
+    prb = [(260 * N + 150, 1, 0), (131 * N + 20, 0, 1)]
+    res = _band_modes(cuda, N, N, 1, 120, src, prb, segments, 16, 41)
+    for seg in segments:
+        for a, t_ in zip(res[seg], res[-1]):
+            assert torch.equal(a, t_), seg
+
+
+def test_band_checkpoints_in_rounds_equal_the_tape(cuda):
+    """Three instances whose bands outnumber 16 SMs run in rounds; from
+    checkpoints every 13 steps they agree with the tape bit for bit."""
+    N = 300
+    src = [(40 * N + 150, -1)]
+    prb = [(260 * N + 150, 1, 0)]
+    res = _band_modes(cuda, N, N, 3, 90, src, prb, (13,), 16, 42)
+    for a, t_ in zip(res[13], res[-1]):
+        assert torch.equal(a, t_)
+
+
+def test_lens_grid_checkpoints_equal_the_tape(cuda):
+    """The lens grid (1024 x 1024, 147 bands), T=300, sqrt(T) segments."""
+    N = 1024
+    src = [(60 * N + y, -1) for y in range(200, 825)]
+    prb = [(900 * N + 512, 1, 0)]
+    res = _band_modes(cuda, N, N, 1, 300, src, prb, (18,), 0, 43)
+    for a, t_ in zip(res[18], res[-1]):
+        assert torch.equal(a, t_)

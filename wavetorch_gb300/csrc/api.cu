@@ -99,6 +99,9 @@ constexpr size_t ALIGN = 256;
 // Laplacian, T x batch x nx x pitch floats) when it takes at most this many
 // bytes, else checkpoints with segment recompute.
 constexpr size_t WT_TAPE_AUTO_MAX_BYTES = (size_t)16 << 30;
+// The same choice in the band layout (grids larger than a cluster holds,
+// whose tapes are large: 31 GiB at 1024 x 1024, T=8000).
+constexpr size_t WT_BAND_TAPE_AUTO_MAX_BYTES = (size_t)64 << 30;
 size_t up(size_t v) { return (v + ALIGN - 1) / ALIGN * ALIGN; }
 
 struct SeqPlan {
@@ -117,6 +120,8 @@ struct SeqPlan {
     size_t o_hist, o_zero, o_lam, o_gc, o_kco;      // plain
     size_t o_ckpt, o_stash, o_gcpart, o_lap, o_grho; // fused
     size_t o_halo;                                  // fused, band layout
+    size_t o_bstate;                                // band layout from checkpoints:
+                                                    // the adjoint's saved state
     size_t o_rfirst, o_ritems;                      // band layout in rounds: the work list
     int rctas;                                      // CTAs of the rounds (0: one launch of
                                                     // batch x bands CTAs)
@@ -142,17 +147,31 @@ int band_sms(const wt_seq_desc* d) {
 }
 
 // Workspace of the band layout after the shared tables (offset o): the tape
-// (every step's Laplacian, [step][batch][band][M][threads]), the exchange
-// words, the per-instance dL/dc.  Sources and probes: at most two of each per
-// thread.
+// (every step's Laplacian, [step][batch][band][M][threads]) or, from
+// checkpoints, the pairs (h_{t-1}, h_{t-2}) every `seg` steps
+// ([nseg][2][batch][nx][ny]), one segment's stash of Laplacians (the tape's
+// layout, seg steps deep) and the adjoint's state between its segment
+// launches ([batch][band][3][M][threads]); then the exchange words and the
+// per-instance dL/dc.  Sources and probes: at most two of each per thread.
 int plan_band(const wt_seq_desc* d, SeqPlan& P, size_t o) {
     const WtBandLaunch& B = P.BL;
     const size_t F = sizeof(float);
+    const size_t slice = (size_t)P.B * B.PR * B.threads * B.M * F;   // one step of tape
     P.band = true;
-    P.tape = true;
-    P.seg = P.T;
-    P.nseg = 1;
-    P.o_lap = o; o = up(o + (size_t)P.T * P.B * B.PR * B.threads * B.M * F);
+    P.tape = d->segment == -1 ||
+             (d->segment == 0 && (size_t)P.T * slice <= WT_BAND_TAPE_AUTO_MAX_BYTES);
+    if (P.tape) {
+        P.seg = P.T;
+        P.nseg = 1;
+        P.o_lap = o; o = up(o + (size_t)P.T * slice);
+    } else {
+        P.seg = d->segment > 0 ? std::min(d->segment, P.T)
+                               : std::max(1, (int)std::ceil(std::sqrt((double)P.T)));
+        P.nseg = (P.T + P.seg - 1) / P.seg;
+        P.o_ckpt = o; o = up(o + (size_t)P.nseg * 2 * P.B * P.plane * F);
+        P.o_stash = o; o = up(o + (size_t)P.seg * slice);
+        P.o_bstate = o; o = up(o + 3 * slice);
+    }
     P.o_halo = o; o = up(o + wt_band_halo_bytes(P.B, B));
     P.o_gcpart = o; o = up(o + (size_t)P.B * P.plane * F);
     std::vector<int> cnt((size_t)B.PR * B.S * B.NCP, 0);
@@ -275,8 +294,7 @@ int make_plan(const wt_seq_desc* d, SeqPlan* p, bool nl = false) {
         // holds the instance, else bands
         int st = d->cluster == -1 ? (int)WT_ERR_UNSUPPORTED
                                   : wt_fused_plan(P.nx, P.ny, P.T, P.np, d->cluster, d->segment, &P.L);
-        if (st == WT_ERR_UNSUPPORTED && !nl && d->cluster <= 0 && !d->output_fields &&
-            (d->segment == 0 || d->segment == -1)) {
+        if (st == WT_ERR_UNSUPPORTED && !nl && d->cluster <= 0 && !d->output_fields) {
             // too large for one cluster: bands of rows, one CTA per band
             const int sms = band_sms(d);
             if (sms > 0 && wt_band_plan(P.B, P.nx, P.ny, P.np, sms, &P.BL) == WT_OK)
@@ -471,6 +489,7 @@ wt::FusedParams fused_params(const wt_scalars* s, const SeqPlan& P, const float*
     F.gc_part = at<float>(ws, P.o_gcpart);
     F.err = at<int>(ws, P.o_err);
     F.halo = P.band ? at<unsigned long long>(ws, P.o_halo) : nullptr;
+    F.bstate = P.band && !P.tape ? at<float>(ws, P.o_bstate) : nullptr;
     return F;
 }
 
@@ -612,12 +631,32 @@ extern "C" int wt_seq_bwd(const wt_scalars* s, const wt_seq_desc* d, const float
     F.grad_out = grad_out;
     F.grad_x = grad_x;
     if (P.coef_batched) F.gc_part = grad_c;   // per-instance dL/dc is the result
-    if (P.rctas) {
-        if ((st = upload_rounds(P, workspace, cs))) return st;
-        st = wt_launch_band_rounds(false, F, P.BL, P.rctas, at<int>(workspace, P.o_rfirst),
-                                   at<int>(workspace, P.o_ritems), cs);
+    if (P.rctas && (st = upload_rounds(P, workspace, cs))) return st;
+    auto band_launch = [&](bool fwd, const wt::FusedParams& G) {
+        return P.rctas ? wt_launch_band_rounds(fwd, G, P.BL, P.rctas, at<int>(workspace, P.o_rfirst),
+                                               at<int>(workspace, P.o_ritems), cs)
+                       : wt_launch_band(fwd, G, P.BL, cs);
+    };
+    if (P.band && !P.tape) {
+        // from checkpoints, one segment at a time, last first: a launch of the
+        // forward rebuilds the segment's Laplacians into the stash, a launch
+        // of the adjoint runs the segment's steps from it (its state carried
+        // from the previous segment's launch)
+        for (int sg = P.nseg - 1; sg >= 0 && !st; --sg) {
+            wt::FusedParams G = F;
+            G.t_lo = sg * P.seg;
+            G.t_hi = std::min(P.T, G.t_lo + P.seg);
+            G.lap = G.stash;
+            G.recompute = 1;
+            st = band_launch(true, G);
+            if (st) break;
+            G.recompute = 0;
+            st = band_launch(false, G);
+        }
+    } else if (P.band) {
+        st = band_launch(false, F);
     } else {
-        st = P.band ? wt_launch_band(false, F, P.BL, cs) : wt_launch_fused(false, F, P.L, cs);
+        st = wt_launch_fused(false, F, P.L, cs);
     }
     if (st) return st;
     if (P.coef_batched) return WT_OK;

@@ -104,6 +104,14 @@ struct FusedParams {
                                 // that never sends its boundary rows; 0: none
     int skip_slice1;            // test hook: cluster tape adjoint, step + 1 whose tape
                                 // slice is never issued; 0: none
+    // band layout from checkpoints: a launch runs the steps [t_lo, t_hi) only
+    // (t_hi 0: the whole sequence), its tape is the segment's stash (step t
+    // at t - t_lo), `recompute` 1 in the forward launches that rebuild a
+    // segment (no outputs), and the adjoint keeps its per-cell state between
+    // its segment launches in bstate [batch][band][3][M][threads]
+    int t_lo, t_hi;
+    int recompute;
+    float* bstate;
 };
 
 // Up to INT_SCATTER_CAP int writes base[idx[i]] = val[i], passed by value as

@@ -296,6 +296,24 @@ WT_DEV void stage_seeds(const FusedParams& P, const Geo& g, float* seeds, int c)
     }
 }
 
+// The checkpoint before step t, (h_{t-1}, h_{t-2}), of band g.band from the
+// tile slots t & 1 and its other slot, by the whole CTA (row-major runs).
+WT_DEV void store_band_ckpt(const FusedParams& P, const Geo& g, const float* tiles, int t) {
+    const size_t plane = (size_t)P.nx * P.ny, bplane = (size_t)P.batch * plane;
+    const int tile = (P.ny + 2) * P.LD;
+    const int rows = min(P.R, P.nx - g.band * P.R);
+    float* cp = P.ckpt + (size_t)(t / P.seg) * 2 * bplane + (size_t)g.inst * plane +
+                (size_t)g.band * P.R * P.ny;
+    const float* s1 = tiles + (t & 1) * tile;
+    const float* s2 = tiles + ((t & 1) ^ 1) * tile;
+    for (int idx = threadIdx.x; idx < rows * P.ny; idx += blockDim.x) {
+        const int r = idx / P.ny, y = idx - r * P.ny;
+        const int o = (y + 1) * P.LD + OFF + r;
+        __stcg(cp + idx, s1[o]);
+        __stcg(cp + bplane + idx, s2[o]);
+    }
+}
+
 // ============================================================================
 // Forward.  Step t computes h_t from h_{t-1} (cur) and h_{t-2} (inout, which
 // it overwrites); tile slot RS = t & 1 holds h_{t-1}, slot RS ^ 1 receives
@@ -303,7 +321,7 @@ WT_DEV void stage_seeds(const FusedParams& P, const Geo& g, float* seeds, int c)
 // INNER: every cell of the thread has b = 0, where the reference's
 // coefficients are A = (dt^-2)^-1 and Bc = dt^-2 for every cell (only c^2
 // is read from shared memory).
-template <int M, int ORDER, int RS, bool INNER>
+template <int M, int ORDER, int RS, bool INNER, bool SEG>
 WT_DEV void fwd_step(const FusedParams& P, const Geo& g, const Lane& ln, const Taps& tp,
                      const ProbeRing& pr, int t, int pb, int pc, float* tape, float (&xv)[SRCMAX],
                      const float (&cur)[M], float (&inout)[M], unsigned long long& hu,
@@ -317,7 +335,7 @@ WT_DEV void fwd_step(const FusedParams& P, const Geo& g, const Lane& ln, const T
         const float A = INNER ? ln.a0 : ln.coef[i];
         const float Bc = INNER ? P.k.inv_dt2 : ln.coef[M + i];
         inout[i] = leapfrog(A, Bc, ln.coef[2 * M + i], P.k.two_over, cur[i], inout[i], L);
-        __stcs(tape + (size_t)i * NT, L);
+        if (!SEG || tape) __stcs(tape + (size_t)i * NT, L);
     };
     // the end cells first: their halo values were sent early in the
     // neighbours' previous step, and this step's go out while the interior
@@ -368,7 +386,7 @@ WT_DEV void fwd_step(const FusedParams& P, const Geo& g, const Lane& ln, const T
 
 // The forward of band g.band of instance g.inst, all T steps; true when a
 // bounded wait gave up (the whole CTA then leaves).
-template <int M, int ORDER>
+template <int M, int ORDER, bool SEG = false>
 WT_DEV bool band_fwd_body(const FusedParams& P, const Geo& g, float* smem) {
     const int NT = blockDim.x;
     const int tile = (P.ny + 2) * P.LD;
@@ -405,37 +423,87 @@ WT_DEV bool band_fwd_body(const FusedParams& P, const Geo& g, float* smem) {
     const Lane ln = make_lane(P, g, smem, coef + threadIdx.x * CS);
     Taps tp;
     build_taps<M>(P, g, tp);
+    if (SEG && P.recompute) tp.meta &= ~(3 << 2);   // a recomputed segment records no probes
+    // the steps this launch runs (SEG: a segment when recomputing from
+    // checkpoints)
+    const int tl = SEG && P.t_hi > 0 ? P.t_lo : 0, th = SEG && P.t_hi > 0 ? P.t_hi : P.steps;
     float xv[SRCMAX];
 #pragma unroll
     for (int e = 0; e < SRCMAX; ++e)
-        xv[e] = e < tp.ns() ? __ldg(P.x + (size_t)tp.src_row(e) * P.steps) : 0.f;
+        xv[e] = e < tp.ns() ? __ldg(P.x + (size_t)tp.src_row(e) * P.steps + tl) : 0.f;
     __syncthreads();      // ownership flags cleared before the owners mark theirs
     if (g.colv) {
 #pragma unroll
         for (int e = 0; e < PRBMAX; ++e)
             if (e < tp.np()) pr.own[tp.prb_col(e)] = tp.prb_intensity(e) ? 2 : 1;
     }
-    __syncthreads();      // tiles, coefficients and flags in place
 
     float ya[M], yb[M];   // ya: h_{t-1} at even t, yb at odd t
 #pragma unroll
     for (int i = 0; i < M; ++i) ya[i] = yb[i] = 0.f;
-    float* tape = P.lap + ((size_t)g.inst * P.C + g.band) * NT * M + threadIdx.x;
+    if (SEG && tl > 0) {
+        const size_t plane = (size_t)P.nx * P.ny, bplane = (size_t)P.batch * plane;
+        // start from the checkpoint before step tl, (h_{tl-1}, h_{tl-2}), and
+        // publish h_{tl-1} as exchange tl - 1: tile slot tl & 1, halo words of
+        // parity (tl - 1) & 1 with tag tl
+        float h1[M], h2[M];
+#pragma unroll
+        for (int i = 0; i < M; ++i) h1[i] = h2[i] = 0.f;
+        if (g.colv) {
+            const float* cp = P.ckpt + (size_t)(tl / P.seg) * 2 * bplane + (size_t)g.inst * plane;
+#pragma unroll
+            for (int i = 0; i < M; ++i) {
+                const int gx = g.gx0 + i;
+                if (gx < P.nx) {
+                    const size_t cell = (size_t)gx * P.ny + g.col;
+                    h1[i] = __ldcg(cp + cell);
+                    h2[i] = __ldcg(cp + bplane + cell);
+                }
+            }
+            float* col = ln.col0 + (tl & 1) * ln.tile;
+#pragma unroll
+            for (int i = 0; i < M; ++i) col[i] = h1[i];
+            const int q = (tl - 1) & 1;
+            if (g.top) send(ln.me + (q - 2) * P.NCP, (uint32_t)tl, h1[0]);
+            if (g.bot) send(ln.me + (4 + q) * P.NCP, (uint32_t)tl, h1[M - 1]);
+        }
+#pragma unroll
+        for (int i = 0; i < M; ++i) {
+            ya[i] = (tl & 1) ? h2[i] : h1[i];
+            yb[i] = (tl & 1) ? h1[i] : h2[i];
+        }
+    }
+    __syncthreads();      // tiles, coefficients and flags in place
+
+    // the tape (or the segment's stash): step t at t - tl steps; none in the
+    // forward that keeps checkpoints instead
+    float* tape = !SEG || P.lap ? P.lap + ((size_t)g.inst * P.C + g.band) * NT * M + threadIdx.x
+                                : nullptr;
     const size_t tape_step = (size_t)P.batch * P.C * NT * M;
-    int pb = 0, pc = 0, chunk0 = 0;
+    // checkpoints of the forward that keeps no tape: (h_{t-1}, h_{t-2}) before
+    // every step t that starts a segment, copied by the whole CTA from the
+    // two tile slots (slot t & 1 holds h_{t-1}, the other h_{t-2}), then a
+    // barrier before step t overwrites h_{t-2}
+    int next_ck = SEG && !P.lap && P.ckpt && !P.recompute ? P.seg : P.steps;
+    int pb = 0, pc = 0, chunk0 = tl;
     bool gave_up = false, aborted = false;
     unsigned long long hu = 0, hd = 0;
-    for (int t = 0; t < P.steps; ++t) {
+    for (int t = tl; t < th; ++t) {
+        if (SEG && t == next_ck) {
+            store_band_ckpt(P, g, smem, t);
+            next_ck += P.seg;
+            __syncthreads();
+        }
         if (g.colv) {
             if (inner) {
-                if (t & 1) fwd_step<M, ORDER, 1, true>(P, g, ln, tp, pr, t, pb, pc, tape, xv, yb, ya, hu, hd, gave_up);
-                else       fwd_step<M, ORDER, 0, true>(P, g, ln, tp, pr, t, pb, pc, tape, xv, ya, yb, hu, hd, gave_up);
+                if (t & 1) fwd_step<M, ORDER, 1, true, SEG>(P, g, ln, tp, pr, t, pb, pc, tape, xv, yb, ya, hu, hd, gave_up);
+                else       fwd_step<M, ORDER, 0, true, SEG>(P, g, ln, tp, pr, t, pb, pc, tape, xv, ya, yb, hu, hd, gave_up);
             } else {
-                if (t & 1) fwd_step<M, ORDER, 1, false>(P, g, ln, tp, pr, t, pb, pc, tape, xv, yb, ya, hu, hd, gave_up);
-                else       fwd_step<M, ORDER, 0, false>(P, g, ln, tp, pr, t, pb, pc, tape, xv, ya, yb, hu, hd, gave_up);
+                if (t & 1) fwd_step<M, ORDER, 1, false, SEG>(P, g, ln, tp, pr, t, pb, pc, tape, xv, yb, ya, hu, hd, gave_up);
+                else       fwd_step<M, ORDER, 0, false, SEG>(P, g, ln, tp, pr, t, pb, pc, tape, xv, ya, yb, hu, hd, gave_up);
             }
         }
-        tape += tape_step;
+        if (!SEG || tape) tape += tape_step;
         if ((aborted = __syncthreads_or(gave_up))) break;
         if (++pc == P.PB) {
             flush_probes(P, g, pr, pb, chunk0, P.PB);
@@ -453,11 +521,11 @@ WT_DEV bool band_fwd_body(const FusedParams& P, const Geo& g, float* smem) {
     return false;
 }
 
-template <int M, int ORDER>
+template <int M, int ORDER, bool SEG>
 __global__ void __launch_bounds__(MAX_THREADS, 1) seq_fwd_band_kernel(FusedParams P) {
     extern __shared__ __align__(16) float smem[];
     const int inst = blockIdx.x / P.C;
-    band_fwd_body<M, ORDER>(P, make_geo(P, M, inst, blockIdx.x - inst * P.C), smem);
+    band_fwd_body<M, ORDER, SEG>(P, make_geo(P, M, inst, blockIdx.x - inst * P.C), smem);
 }
 
 // ============================================================================
@@ -470,7 +538,7 @@ __global__ void __launch_bounds__(MAX_THREADS, 1) seq_fwd_band_kernel(FusedParam
 // previous step's (a whole step ahead of use).
 // The adjoint of band g.band of instance g.inst, all T steps (after its
 // forward filled the tape); true when a bounded wait gave up.
-template <int M, int ORDER>
+template <int M, int ORDER, bool SEG = false>
 WT_DEV bool band_bwd_body(const FusedParams& P, const Geo& g, float* smem) {
     const int NT = blockDim.x;
     const int tile = (P.ny + 2) * P.LD;
@@ -505,14 +573,31 @@ WT_DEV bool band_bwd_body(const FusedParams& P, const Geo& g, float* smem) {
     // threads without a probe cell send their end cells' exchange at the end
     // of the previous step (no seed can change them in between)
     const bool early = tp.np() == 0;
-    stage_seeds(P, g, seeds, 0);
+    // the adjoint steps this launch runs: u in [u_lo, u_hi) (t = T-1-u in
+    // [tl, th)); a launch of one checkpoint segment starts from the state the
+    // previous one saved
+    const int tl = SEG && P.t_hi > 0 ? P.t_lo : 0, th = SEG && P.t_hi > 0 ? P.t_hi : P.steps;
+    const int u_lo = P.steps - th, u_hi = P.steps - tl;
+    int pk = u_lo % P.PB, pcn = u_lo / P.PB;
+    stage_seeds(P, g, seeds, pcn);
+    if (pk != 0 && (pcn + 1) * P.PB < P.steps) stage_seeds(P, g, seeds, pcn + 1);
     __syncthreads();
 
     float lam[M], pend[M], acc[M];
 #pragma unroll
     for (int i = 0; i < M; ++i) lam[i] = pend[i] = acc[i] = 0.f;
+    float* state = SEG && P.bstate ? P.bstate + ((size_t)g.inst * P.C + g.band) * 3 * M * NT + threadIdx.x
+                                   : nullptr;
+    if (SEG && th < P.steps && state) {
+#pragma unroll
+        for (int i = 0; i < M; ++i) {
+            lam[i] = state[(size_t)i * NT];
+            pend[i] = state[(size_t)(M + i) * NT];
+            acc[i] = state[(size_t)(2 * M + i) * NT];
+        }
+    }
     const size_t tape_step = (size_t)P.batch * P.C * NT * M;
-    const float* tape = P.lap + (size_t)(P.steps - 1) * tape_step +
+    const float* tape = P.lap + (size_t)(th - 1 - tl) * tape_step +
                         ((size_t)g.inst * P.C + g.band) * NT * M + threadIdx.x;
     if (g.colv) {
 #pragma unroll
@@ -521,10 +606,9 @@ WT_DEV bool band_bwd_body(const FusedParams& P, const Geo& g, float* smem) {
     }
     const int LD = P.LD;
     const float w = P.k.lap_w, w4 = P.k.lap_w4, dt2 = P.k.dt2;
-    int pk = 0, pcn = 0;
     bool gave_up = false, aborted = false;
     unsigned long long hu = 0, hd = 0;
-    for (int u = 0; u < P.steps; ++u) {
+    for (int u = u_lo; u < u_hi; ++u) {
         const int t = P.steps - 1 - u;
         float* col = ln.col0 + (u & 1) * ln.tile;
         if (pk == 0 && u + P.PB < P.steps)   // next chunk, a barrier ahead of use
@@ -554,7 +638,7 @@ WT_DEV bool band_bwd_body(const FusedParams& P, const Geo& g, float* smem) {
             // this thread for its own cells and by its neighbours)
 #pragma unroll
             for (int i = 0; i < M; ++i) col[i] = fmul(ln.coef[2 * M + i], lam[i]);
-            if (!early || u == 0) {
+            if (!early || u == u_lo) {
                 if (g.top) send(ln.me + ((u & 1) - 2) * P.NCP, (uint32_t)(u + 1), col[0]);
                 if (g.bot) send(ln.me + (4 + (u & 1)) * P.NCP, (uint32_t)(u + 1), col[M - 1]);
             }
@@ -583,7 +667,7 @@ WT_DEV bool band_bwd_body(const FusedParams& P, const Geo& g, float* smem) {
             if (g.bot) dn = recv_pre(P, hd, ln.me + (2 + (u & 1)) * P.NCP, (uint32_t)(u + 1), gave_up);
             update(0, up, col[1]);
             update(M - 1, col[M - 2], dn);
-            if (early && u + 1 < P.steps) {
+            if (early && u + 1 < u_hi) {
                 // the end cells' next lambda is final (no seed on this thread)
                 const int q = (u + 1) & 1;
                 if (g.top) send(ln.me + (q - 2) * P.NCP, (uint32_t)(u + 2), fmul(ln.coef[2 * M], lam[0]));
@@ -598,7 +682,7 @@ WT_DEV bool band_bwd_body(const FusedParams& P, const Geo& g, float* smem) {
             else       phase2(std::false_type{});
         }
         tape -= tape_step;
-        if (g.colv && u + 1 < P.steps) {   // the staged words were all read above
+        if (g.colv && u + 1 < u_hi) {   // the staged words were all read above
 #pragma unroll
             for (int i = 0; i < M; ++i) cp_async4(lys + i * NT, tape + (size_t)i * NT);
             cp_async_commit();
@@ -609,6 +693,15 @@ WT_DEV bool band_bwd_body(const FusedParams& P, const Geo& g, float* smem) {
     if (!aborted) aborted = __syncthreads_or(gave_up);
     if (aborted) return true;
     if (!g.colv) return false;
+    if (SEG && tl > 0) {   // a later segment launch goes on from here
+#pragma unroll
+        for (int i = 0; i < M; ++i) {
+            state[(size_t)i * NT] = lam[i];
+            state[(size_t)(M + i) * NT] = pend[i];
+            state[(size_t)(2 * M + i) * NT] = acc[i];
+        }
+        return false;
+    }
     // dL/dc = (X1 * Kc) * sum_t Lap(h_{t-1}) * lam_t: grad_c of cell.py:36 with
     // its time-invariant factor applied once
     float* o = P.gc_part + (size_t)g.inst * P.nx * P.ny;
@@ -621,11 +714,11 @@ WT_DEV bool band_bwd_body(const FusedParams& P, const Geo& g, float* smem) {
     return false;
 }
 
-template <int M, int ORDER>
+template <int M, int ORDER, bool SEG>
 __global__ void __launch_bounds__(MAX_THREADS, 1) seq_bwd_band_kernel(FusedParams P) {
     extern __shared__ __align__(16) float smem[];
     const int inst = blockIdx.x / P.C;
-    band_bwd_body<M, ORDER>(P, make_geo(P, M, inst, blockIdx.x - inst * P.C), smem);
+    band_bwd_body<M, ORDER, SEG>(P, make_geo(P, M, inst, blockIdx.x - inst * P.C), smem);
 }
 
 // ============================================================================
@@ -634,7 +727,7 @@ __global__ void __launch_bounds__(MAX_THREADS, 1) seq_bwd_band_kernel(FusedParam
 // order, with the batch's parameter block; an instance's bands sit on
 // distinct CTAs, so the earliest unfinished instance always has all its
 // bands running (the work-list argument of band_list_kernel below).
-template <int M, int ORDER>
+template <int M, int ORDER, bool SEG>
 __global__ void __launch_bounds__(MAX_THREADS, 1) band_rounds_kernel(FusedParams P,
                                                                     const int* first,
                                                                     const int* items, int fwd) {
@@ -647,8 +740,8 @@ __global__ void __launch_bounds__(MAX_THREADS, 1) band_rounds_kernel(FusedParams
         __syncthreads();
         if (stop) break;
         const Geo g = make_geo(P, M, items[2 * k], items[2 * k + 1]);
-        const bool aborted = fwd ? band_fwd_body<M, ORDER>(P, g, smem)
-                                 : band_bwd_body<M, ORDER>(P, g, smem);
+        const bool aborted = fwd ? band_fwd_body<M, ORDER, SEG>(P, g, smem)
+                                 : band_bwd_body<M, ORDER, SEG>(P, g, smem);
         if (aborted) break;
     }
 }
@@ -770,8 +863,11 @@ static int band_attributes(void (*kern)(wt::FusedParams), size_t smem) {
 template <int M, int ORDER>
 static int launch_band_m(bool fwd, const wt::FusedParams& P, const WtBandLaunch& L,
                          cudaStream_t st) {
-    void (*kern)(wt::FusedParams) = fwd ? wt::band::seq_fwd_band_kernel<M, ORDER>
-                                        : wt::band::seq_bwd_band_kernel<M, ORDER>;
+    // checkpoint mode (a workspace with checkpoints): the kernels' segment form
+    const bool seg = P.ckpt != nullptr;
+    void (*kern)(wt::FusedParams) =
+        fwd ? (seg ? wt::band::seq_fwd_band_kernel<M, ORDER, true> : wt::band::seq_fwd_band_kernel<M, ORDER, false>)
+            : (seg ? wt::band::seq_bwd_band_kernel<M, ORDER, true> : wt::band::seq_bwd_band_kernel<M, ORDER, false>);
     const size_t smem = fwd ? L.smem_fwd : L.smem_bwd;
     int rc = band_attributes(kern, smem);
     if (rc) return rc;
@@ -809,7 +905,7 @@ static int launch_band_order(bool fwd, const wt::FusedParams& P, const WtBandLau
 }
 
 int wt_launch_band(bool fwd, const wt::FusedParams& P0, const WtBandLaunch& L, cudaStream_t st) {
-    if (!P0.lap || !P0.halo) return WT_ERR_INVALID;
+    if ((!P0.lap && !(fwd && P0.ckpt)) || !P0.halo) return WT_ERR_INVALID;
     wt::FusedParams P = P0;
     P.C = L.PR; P.R = L.R; P.NCP = L.NCP; P.LD = L.LD; P.PB = L.PB;
     P.abort_g = reinterpret_cast<int*>(P.halo + (size_t)P.batch * L.PR * 4 * L.NCP);
@@ -864,7 +960,7 @@ template <int M, int ORDER>
 static int launch_rounds_m(bool fwd, const wt::FusedParams& P, const WtBandLaunch& L, int ctas,
                            const int* first, const int* items, cudaStream_t st) {
     void (*kern)(wt::FusedParams, const int*, const int*, int) =
-        wt::band::band_rounds_kernel<M, ORDER>;
+        P.ckpt ? wt::band::band_rounds_kernel<M, ORDER, true> : wt::band::band_rounds_kernel<M, ORDER, false>;
     const size_t smem = std::max(L.smem_fwd, L.smem_bwd);
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
@@ -915,7 +1011,7 @@ static int launch_rounds_order(bool fwd, const wt::FusedParams& P, const WtBandL
 
 int wt_launch_band_rounds(bool fwd, const wt::FusedParams& P0, const WtBandLaunch& L, int ctas,
                           const int* first, const int* items, cudaStream_t st) {
-    if (!P0.lap || !P0.halo || ctas <= 0) return WT_ERR_INVALID;
+    if ((!P0.lap && !(fwd && P0.ckpt)) || !P0.halo || ctas <= 0) return WT_ERR_INVALID;
     wt::FusedParams P = P0;
     P.C = L.PR; P.R = L.R; P.NCP = L.NCP; P.LD = L.LD; P.PB = L.PB;
     P.abort_g = reinterpret_cast<int*>(P.halo + (size_t)P.batch * L.PR * 4 * L.NCP);
