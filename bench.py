@@ -1101,12 +1101,12 @@ def run_lens(args):
     N, T = 1024, args.T if args.T != WORKLOAD["steps"] else 8000
     x = torch.from_numpy(sinusoid(T, 0.02)).to(dev)          # [1, T]
 
-    def make(form):
+    def make(form, segment=0):
         geom = wt.WaveGeometryFreeForm((N, N), 1.0, c0=1.0, c1=0.5, abs_N=40, abs_sig=3.0,
                                        abs_p=2,
                                        rho=torch.rand(N, N, generator=torch.Generator().manual_seed(3)))
         return wt.WaveRNN(wt.WaveCell(0.707, geom), wt.WaveLineSource(60, 200, 60, 824),
-                          [wt.WaveIntensityProbe(900, 512)], form=form).to(dev)
+                          [wt.WaveIntensityProbe(900, 512)], form=form, segment=segment).to(dev)
 
     def timed(model, steps, warmup, clk=None):
         def step():
@@ -1133,6 +1133,15 @@ def run_lens(args):
     t, g_fused = timed(fused, args.steps, args.warmup, clk)
     del fused
     torch.cuda.empty_cache()
+    # the same step from sqrt(T) checkpoints (segment -2): each segment
+    # recomputed by one launch, its adjoint steps run by the next
+    from wavetorch_gb300.functional import SeqSpec, seq_workspace_bytes
+    ck = make("fused", segment=-2)
+    t_ck, g_ck = timed(ck, 1, 1)
+    del ck
+    torch.cuda.empty_cache()
+    ws_spec = lambda seg: SeqSpec(1, N, N, T, [(60 * N + y, -1) for y in range(200, 825)],
+                                  [(900 * N + 512, 1, 0)], segment=seg)
     t_plain, g_plain = timed(make("plain"), 1, 1) if not args.no_plain else (None, None)
     alg_bytes = (12 + 20) * N * N * T   # per-step form's algorithmic HBM bytes, fwd + adjoint
     line = {
@@ -1148,6 +1157,13 @@ def run_lens(args):
                    "l2": "inputs (tape 31 GiB) larger than L2"},
         "algorithmic_GBps": alg_bytes / t / 1e9,
         "tape_GBps": 8 * N * N * T / t / 1e9,
+        "adjoint_modes": {"tape": {"ms_per_step": t * 1e3,
+                                   "workspace_bytes": seq_workspace_bytes(ws_spec(-1))},
+                          "checkpoint": {"ms_per_step": t_ck * 1e3,
+                                         "workspace_bytes": seq_workspace_bytes(ws_spec(-2)),
+                                         "segment": int(math.ceil(math.sqrt(T))),
+                                         "grad_rel_diff_vs_tape":
+                                             float((g_ck - g_fused).norm() / g_fused.norm())}},
         "clocks": clk.summary(),
     }
     if t_plain is not None:

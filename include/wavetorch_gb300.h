@@ -140,8 +140,12 @@ typedef struct wt_seq_desc {
  * cluster per instance with the band boundaries exchanged over distributed
  * shared memory.  Larger grids (up to 1024 columns) run in bands of rows, one
  * CTA per band and SM in a cooperative launch, the band boundaries exchanged
- * through global memory; that layout needs batch x bands <= sm_count, no
- * output_fields, and runs its adjoint from the tape only (segment 0 or -1).
+ * through global memory (a batch whose bands outnumber sm_count runs its
+ * instances in rounds); that layout needs no output_fields.  From
+ * checkpoints (segment > 0 or -2, or automatically past a 64 GiB tape) its
+ * adjoint runs one segment at a time, last first: a launch recomputes the
+ * segment's Laplacians into a one-segment stash and the next runs the
+ * segment's adjoint steps from it.
  * `cluster` > 0 fixes the cluster size; -1 asks for the band layout even
  * where a cluster would hold the instance (its CTAs need not share a GPC,
  * as a cluster's must).                                                     */
