@@ -316,3 +316,24 @@ def test_cfg3_lens_against_oracle(cuda):
     ogc, _ = S.backward(b.cpu().numpy(), c.cpu().numpy(), hist, g.cpu().numpy())
     del hist
     assert rel(gc.cpu().numpy(), ogc) <= FUSED_DC_TOL
+
+
+@pytest.mark.parametrize("B,N,steps", [(560, 120, 12), (128, 256, 10)])
+def test_plain_large_batches_against_oracle(cuda, B, N, steps):
+    """Large batches in the plain form (the batch reduction over 35 and 8
+    blocks of 16 instances, probes on the vector kernels' tile edges):
+    outputs and dL/dc bit-exact with the oracle, i.e. with the reference's
+    batch reduction order; the forward reads its coefficients from planes
+    formed once per sequence."""
+    b, c, x, _, _, _ = cfg1_problem(cuda, B=B, N=N, steps=steps, seed=17)
+    src = [(20 * N + N // 2, -1)]
+    # probes on tile edges: rows 7/8 (tiles of 8 rows), column 127/128
+    prb = [(7 * N + N // 2, 1, 0), (8 * N + min(N - 1, 127), 1, 1), ((N - 20) * N + N // 2, 0, 2)]
+    g = torch.randn(B, steps, 3, generator=torch.Generator().manual_seed(18)).to(cuda)
+    sc = scalars(0.707, 1.0, lap_order(B, N, N, 1.0))
+    S = o.Seq(B, N, N, steps, 0.707, 1.0, src, prb)
+    oout, hist = S.forward(b.cpu().numpy(), c.cpu().numpy(), x.cpu().numpy())
+    ogc, _ = S.backward(b.cpu().numpy(), c.cpu().numpy(), hist, g.cpu().numpy())
+    out, gc = run(SeqSpec(B, N, N, steps, src, prb, form=_lib.WT_FORM_PLAIN), sc, b, c, x, g)
+    assert np.array_equal(out.cpu().numpy(), oout)
+    assert np.array_equal(gc.cpu().numpy(), ogc)

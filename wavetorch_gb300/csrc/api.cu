@@ -118,6 +118,7 @@ struct SeqPlan {
     // float areas
     size_t o_amp;
     size_t o_hist, o_zero, o_lam, o_gc, o_kco;      // plain
+    size_t o_fco;                                   // plain: the forward's coefficient planes
     size_t o_ckpt, o_stash, o_gcpart, o_lap, o_grho; // fused
     size_t o_halo;                                  // fused, band layout
     size_t o_bstate;                                // band layout from checkpoints:
@@ -288,6 +289,7 @@ int make_plan(const wt_seq_desc* d, SeqPlan* p, bool nl = false) {
         P.o_lam = o; o = up(o + 3 * bp * F);
         P.o_gc = o; o = up(o + bp * F);
         P.o_kco = o; o = up(o + 4 * P.plane * F);
+        P.o_fco = o; o = up(o + 3 * P.plane * F);
     } else {
         if (d->segment < -2 || d->cluster < -1) return WT_ERR_INVALID;
         // cluster -1 asks for the band layout; 0 takes a cluster when one
@@ -539,12 +541,15 @@ extern "C" int wt_seq_fwd(const wt_scalars* s, const wt_seq_desc* d, const float
         e.tileflag = at<int>(workspace, P.o_tileflag);
         e.tiles_y = P.tiles_y;
         const size_t hbs = (size_t)P.T * plane;   // history is [B][T][nx][ny]
+        // the update coefficients once per sequence (each A holds a division)
+        float* fco = at<float>(workspace, P.o_fco);
+        if ((st = wt_launch_fwd_coef(k, plane, b, c, fco, cs))) return st;
         for (int t = 0; t < P.T; ++t) {
             e.t = t;
             const float* y1 = t >= 1 ? hist + (size_t)(t - 1) * plane : zero;
             const float* y2 = t >= 2 ? hist + (size_t)(t - 2) * plane : zero;
             st = wt_launch_step_fwd(k, P.B, P.nx, P.ny, 0, b, c, y1, t >= 1 ? hbs : 0, y2,
-                                    t >= 2 ? hbs : 0, hist + (size_t)t * plane, hbs, &e, cs);
+                                    t >= 2 ? hbs : 0, hist + (size_t)t * plane, hbs, &e, cs, fco);
             if (st) return st;
         }
         if (d->output_fields) {
@@ -615,12 +620,12 @@ extern "C" int wt_seq_bwd(const wt_scalars* s, const wt_seq_desc* d, const float
             const float* l1 = t + 1 < P.T ? lam + (size_t)((t + 1) % 3) * bp : nullptr;
             const float* l2 = t + 2 < P.T ? lam + (size_t)((t + 2) % 3) * bp : nullptr;
             const float* hp = t >= 1 ? hist + (size_t)(t - 1) * plane : nullptr;
+            float* lo = lam + (size_t)(t % 3) * bp;
             if (P.B == 1) {       // one instance: the step accumulates dL/dc itself
                 e.G = grad_c;
                 e.first = t == P.T - 1;
             }
-            st = wt_launch_seq_adj_step(k, P.B, P.nx, P.ny, b, c, kco, l1, l2, hp, hbs,
-                                        lam + (size_t)(t % 3) * bp, gc, e, cs);
+            st = wt_launch_seq_adj_step(k, P.B, P.nx, P.ny, b, c, kco, l1, l2, hp, hbs, lo, gc, e, cs);
             if (st) return st;
             if (P.B > 1 && (st = wt_launch_seq_adj_reduce(P.B, plane, gc, grad_c, t == P.T - 1, cs)))
                 return st;

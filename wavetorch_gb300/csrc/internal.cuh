@@ -217,10 +217,14 @@ int wt_launch_band(bool fwd, const wt::FusedParams& P, const WtBandLaunch& L, cu
 int wt_launch_band_rounds(bool fwd, const wt::FusedParams& P, const WtBandLaunch& L, int ctas,
                           const int* first, const int* items, cudaStream_t st);
 
+// fco (nullable): the forward's coefficient planes [A | Bc | c^2] of b, c
+// (wt_launch_fwd_coef), read instead of forming them per cell and step.
 int wt_launch_step_fwd(const StepScalars& k, int batch, int nx, int ny, int coef_batched,
                        const float* b, const float* c, const float* y1, size_t bs1,
                        const float* y2, size_t bs2, float* y, size_t bs,
-                       const wt::SeqEpilogue* epi, cudaStream_t st);
+                       const wt::SeqEpilogue* epi, cudaStream_t st, const float* fco = nullptr);
+int wt_launch_fwd_coef(const StepScalars& k, size_t plane, const float* b, const float* c,
+                       float* fco, cudaStream_t st);
 int wt_launch_step_bwd(const StepScalars& k, int batch, int nx, int ny, int coef_batched,
                        const float* b, const float* c, const float* y1, const float* y2,
                        const float* g, float* gb, float* gcp, float* gy1, float* gy2,

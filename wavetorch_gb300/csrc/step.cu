@@ -303,7 +303,8 @@ WT_DEV void load_quad(Quad& Q, float (*s)[S4W], int r, int q0) {
 template <int ORDER, bool EPI>
 __global__ void __launch_bounds__(STEP4_TX * 32)
 step_fwd4_kernel(StepScalars k, int nx, int ny, int coef_batched, const float* __restrict__ b,
-                 const float* __restrict__ c, const float* __restrict__ y1, size_t bs1,
+                 const float* __restrict__ c, const float* __restrict__ fco,
+                 const float* __restrict__ y1, size_t bs1,
                  const float* __restrict__ y2, size_t bs2, float* __restrict__ y, size_t bs,
                  SeqEpilogue e) {
     __shared__ __align__(16) float s[STEP4_TX + 2][S4W];
@@ -314,11 +315,19 @@ step_fwd4_kernel(StepScalars k, int nx, int ny, int coef_batched, const float* _
     const bool mine = gx < nx && gy < ny;
     const size_t cell = mine ? (size_t)gx * ny + gy : 0;
     const size_t ci = coef_batched ? inst * plane + cell : cell;
-    // the thread's own operands first, in flight while the tile is staged
-    float4 b4 = make_float4(0.f, 0.f, 0.f, 0.f), c4 = b4, p4 = b4;
+    // the thread's own operands first, in flight while the tile is staged;
+    // with coefficient planes (fco: [A | Bc | c^2], formed once per sequence)
+    // b4, c4, a4 carry A, Bc, c^2 instead of b, c
+    float4 b4 = make_float4(0.f, 0.f, 0.f, 0.f), c4 = b4, a4 = b4, p4 = b4;
     if (mine) {
-        b4 = __ldg(reinterpret_cast<const float4*>(b + ci));
-        c4 = __ldg(reinterpret_cast<const float4*>(c + ci));
+        if (fco) {
+            a4 = __ldg(reinterpret_cast<const float4*>(fco + cell));
+            b4 = __ldg(reinterpret_cast<const float4*>(fco + plane + cell));
+            c4 = __ldg(reinterpret_cast<const float4*>(fco + 2 * plane + cell));
+        } else {
+            b4 = __ldg(reinterpret_cast<const float4*>(b + ci));
+            c4 = __ldg(reinterpret_cast<const float4*>(c + ci));
+        }
         p4 = __ldg(reinterpret_cast<const float4*>(y2 + inst * bs2 + cell));
     }
     stage_tile4(s, y1 + inst * bs1, nx, ny, x0, y0);
@@ -327,11 +336,14 @@ step_fwd4_kernel(StepScalars k, int nx, int ny, int coef_batched, const float* _
     load_quad(Q, s, threadIdx.y + 1, 4 + 4 * threadIdx.x);   // all lanes: the shuffles need them
     if (!mine) return;
     const float bb[4] = {b4.x, b4.y, b4.z, b4.w}, cc[4] = {c4.x, c4.y, c4.z, c4.w};
+    const float aa[4] = {a4.x, a4.y, a4.z, a4.w};
     const float pp[4] = {p4.x, p4.y, p4.z, p4.w};
     float v[4];
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
-        const FwdCoef f = fwd_coef(bb[j], cc[j], k);
+        FwdCoef f;
+        if (fco) { f.A = aa[j]; f.Bc = bb[j]; f.c2 = cc[j]; }
+        else     f = fwd_coef(bb[j], cc[j], k);
         const float L = lap5<ORDER>(Q.u[j], Q.l[j], Q.c[j], Q.r[j], Q.d[j], k.lap_w, k.lap_w4);
         v[j] = leapfrog(f.A, f.Bc, f.c2, k.two_over, Q.c[j], pp[j], L);
     }
@@ -351,6 +363,19 @@ step_fwd4_kernel(StepScalars k, int nx, int ny, int coef_batched, const float* _
         }
     }
     *reinterpret_cast<float4*>(y + inst * bs + cell) = make_float4(v[0], v[1], v[2], v[3]);
+}
+
+// The forward's time-invariant coefficients as three planes [A | Bc | c^2]
+// (wavetorch/cell.py:13-16, fwd_coef's arithmetic: A holds a division),
+// formed once per sequence.
+__global__ void fwd_coef_kernel(StepScalars k, size_t plane, const float* __restrict__ b,
+                                const float* __restrict__ c, float* __restrict__ fco) {
+    const size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= plane) return;
+    const FwdCoef f = fwd_coef(__ldg(b + q), __ldg(c + q), k);
+    fco[q] = f.A;
+    fco[plane + q] = f.Bc;
+    fco[2 * plane + q] = f.c2;
 }
 
 // The adjoint's time-invariant coefficients as four planes [X1 | Kc | Kg |
@@ -537,19 +562,19 @@ static bool vec4_ok(int ny, std::initializer_list<const void*> ptrs,
 int wt_launch_step_fwd(const StepScalars& k, int batch, int nx, int ny, int coef_batched,
                        const float* b, const float* c, const float* y1, size_t bs1,
                        const float* y2, size_t bs2, float* y, size_t bs,
-                       const wt::SeqEpilogue* epi, cudaStream_t st) {
-    if (vec4_ok(ny, {b, c, y1, y2, y}, {bs1, bs2, bs})) {
+                       const wt::SeqEpilogue* epi, cudaStream_t st, const float* fco) {
+    if (vec4_ok(ny, {b, c, fco, y1, y2, y}, {bs1, bs2, bs, (size_t)nx * ny})) {
         dim3 blk(32, wt::STEP4_TX);
         dim3 grd((ny + wt::STEP4_TY - 1) / wt::STEP4_TY, (nx + wt::STEP4_TX - 1) / wt::STEP4_TX, batch);
         wt::SeqEpilogue e{};
         if (epi) e = *epi;
         const bool ep = epi != nullptr;
         if ((k.lap_order & 1) == WT_LAP_SEQ) {
-            if (ep) wt::step_fwd4_kernel<WT_LAP_SEQ, true><<<grd, blk, 0, st>>>(k, nx, ny, coef_batched, b, c, y1, bs1, y2, bs2, y, bs, e);
-            else    wt::step_fwd4_kernel<WT_LAP_SEQ, false><<<grd, blk, 0, st>>>(k, nx, ny, coef_batched, b, c, y1, bs1, y2, bs2, y, bs, e);
+            if (ep) wt::step_fwd4_kernel<WT_LAP_SEQ, true><<<grd, blk, 0, st>>>(k, nx, ny, coef_batched, b, c, fco, y1, bs1, y2, bs2, y, bs, e);
+            else    wt::step_fwd4_kernel<WT_LAP_SEQ, false><<<grd, blk, 0, st>>>(k, nx, ny, coef_batched, b, c, fco, y1, bs1, y2, bs2, y, bs, e);
         } else {
-            if (ep) wt::step_fwd4_kernel<WT_LAP_PAIRED, true><<<grd, blk, 0, st>>>(k, nx, ny, coef_batched, b, c, y1, bs1, y2, bs2, y, bs, e);
-            else    wt::step_fwd4_kernel<WT_LAP_PAIRED, false><<<grd, blk, 0, st>>>(k, nx, ny, coef_batched, b, c, y1, bs1, y2, bs2, y, bs, e);
+            if (ep) wt::step_fwd4_kernel<WT_LAP_PAIRED, true><<<grd, blk, 0, st>>>(k, nx, ny, coef_batched, b, c, fco, y1, bs1, y2, bs2, y, bs, e);
+            else    wt::step_fwd4_kernel<WT_LAP_PAIRED, false><<<grd, blk, 0, st>>>(k, nx, ny, coef_batched, b, c, fco, y1, bs1, y2, bs2, y, bs, e);
         }
         wt_count_launches(1);
         return wt_cuda_status(cudaGetLastError());
@@ -587,6 +612,12 @@ int wt_launch_step_bwd(const StepScalars& k, int batch, int nx, int ny, int coef
     return wt_cuda_status(cudaGetLastError());
 }
 
+int wt_launch_fwd_coef(const StepScalars& k, size_t plane, const float* b, const float* c,
+                       float* fco, cudaStream_t st) {
+    wt::fwd_coef_kernel<<<(unsigned)((plane + 255) / 256), 256, 0, st>>>(k, plane, b, c, fco);
+    wt_count_launches(1);
+    return wt_cuda_status(cudaGetLastError());
+}
 int wt_launch_adj_coef(const StepScalars& k, size_t plane, const float* b, const float* c,
                        float* kco, cudaStream_t st) {
     wt::adj_coef_kernel<<<(unsigned)((plane + 255) / 256), 256, 0, st>>>(k, plane, b, c, kco);
