@@ -50,6 +50,8 @@ def parse():
     p.add_argument("--form", choices=["fused", "plain"], default="fused")
     p.add_argument("--no-plain", action="store_true", help="skip the plain-form comparison")
     p.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
+    p.add_argument("--no-workloads", action="store_true",
+                   help="skip the compact pass over the other workloads after the headline")
     p.add_argument("--batch", type=int, default=WORKLOAD["batch"])
     p.add_argument("--T", type=int, default=WORKLOAD["steps"])
     p.add_argument("--kernels-only", action="store_true",
@@ -641,9 +643,46 @@ def run_ours(args):
             "clocks": clk.summary(),
             "gpu_launches": int(launches),
         }
+        if world == 1 and args.form == "fused" and not args.no_workloads and \
+                (B, T) == (WORKLOAD["batch"], WORKLOAD["steps"]):
+            del model
+            torch.cuda.empty_cache()
+            line["workloads"] = other_workloads(args)
         print(json.dumps(line), flush=True)
     if world > 1:
         dist.destroy_process_group()
+
+
+def other_workloads(args):
+    """The other workloads of this benchmark, each run once in compact form
+    after the headline (3 warm-up and 2 timed steps each) so that their
+    numbers come from the same run: the lens grid (band layout, tape and
+    sqrt(T) checkpoints), the nonlinear cell, the ragged batch in one packed
+    launch, field streaming and the hole geometry.  Each one's JSON line
+    (what `--workload NAME` prints) goes under its name; a workload that fails
+    records its error instead and the others still run."""
+    import copy
+    import io
+    import torch
+    out = {}
+    for name, fn in (("lens", run_lens), ("nonlinear", run_nonlinear), ("ragged", run_ragged),
+                     ("fields", run_fields), ("holey", run_holey)):
+        a = copy.copy(args)
+        a.workload, a.steps, a.warmup = name, 2, 3
+        buf = io.StringIO()
+        t0 = time.time()
+        try:
+            with contextlib.redirect_stdout(buf):
+                fn(a)
+            lines = [ln for ln in buf.getvalue().splitlines() if ln.startswith("{")]
+            out[name] = json.loads(lines[-1]) if lines else {"error": "no result line"}
+        except Exception as e:   # keep the headline and the other workloads
+            out[name] = {"error": f"{type(e).__name__}: {e}"[:400]}
+        out[name]["wall_s"] = round(time.time() - t0, 2)
+        if torch.cuda.is_available():
+            torch.cuda.synchronize()
+            torch.cuda.empty_cache()
+    return out
 
 
 # ---------------------------------------------------------------------------

@@ -78,3 +78,32 @@ def test_reference_arm_prints_the_contract_line():
         assert ref["kind"] == "reference" and ref["value"] > 0 and ref["cores"] >= 1
     else:
         assert ref is None
+
+
+def test_other_workloads_keep_going_after_a_failure(monkeypatch):
+    """The compact pass over the other workloads records each one's result
+    line under its name, and a workload that raises records its error while
+    the rest still run (and print nothing of their own)."""
+    import argparse
+    import json
+
+    def ok(name):
+        def run(a):
+            print("some log line")
+            print(json.dumps({"metric": name, "value": 1.0, "steps": a.steps, "warmup": a.warmup}))
+        return run
+
+    def boom(a):
+        raise RuntimeError("out of memory")
+
+    monkeypatch.setattr(bench, "run_lens", ok("lens"))
+    monkeypatch.setattr(bench, "run_nonlinear", boom)
+    monkeypatch.setattr(bench, "run_ragged", ok("ragged"))
+    monkeypatch.setattr(bench, "run_fields", ok("fields"))
+    monkeypatch.setattr(bench, "run_holey", ok("holey"))
+    out = bench.other_workloads(argparse.Namespace(steps=5, warmup=3, workload="batched"))
+    assert list(out) == ["lens", "nonlinear", "ragged", "fields", "holey"]
+    assert out["lens"]["metric"] == "lens" and out["lens"]["steps"] == 2
+    assert out["lens"]["warmup"] == 3 and out["lens"]["wall_s"] >= 0
+    assert out["nonlinear"]["error"].startswith("RuntimeError: out of memory")
+    assert out["holey"]["value"] == 1.0
