@@ -33,12 +33,13 @@ int wt_test_cluster_missing_arrival(const wt_scalars* s, const wt_seq_desc* d, c
                                     const float* c, const float* x, float* out, void* workspace,
                                     size_t workspace_bytes, int32_t cta, wt_stream_t stream);
 
-/* wt_seq_bwd for a sequence whose cluster-layout adjoint runs from the tape
- * (after a wt_seq_fwd on the same workspace), with the tape ring's producer
- * issuing no slice from step `step` down: the CTAs' bounded waits on that
- * slot give up after about 2 s, the copies already in flight are drained,
- * and wt_seq_device_status reports WT_ERR_TIMEOUT; the context stays usable.
- * WT_ERR_UNSUPPORTED when the sequence does not run from a cluster tape.    */
+/* wt_seq_bwd for a sequence whose cluster-layout adjoint runs from the tape,
+ * or from checkpoints with the recompute beside the adjoint (after a
+ * wt_seq_fwd on the same workspace), with the ring's producer issuing no
+ * slice from step `step` down: the CTAs' bounded waits on that slot give up
+ * after about 2 s, the copies already in flight are drained, and
+ * wt_seq_device_status reports WT_ERR_TIMEOUT; the context stays usable.
+ * WT_ERR_UNSUPPORTED when the sequence runs neither way.                    */
 int wt_test_tape_missing_slice(const wt_scalars* s, const wt_seq_desc* d, const float* b,
                                const float* c, const float* x, const float* grad_out,
                                float* grad_c, void* workspace, size_t workspace_bytes,

@@ -78,10 +78,14 @@ def test_cluster_missing_arrival_times_out_and_the_context_survives(cuda):
     assert rel(fgc, pgc) <= 5e-6
 
 
-def test_tape_missing_slice_times_out_and_the_context_survives(cuda):
+@pytest.mark.parametrize("segment", [-1, 7])
+def test_tape_missing_slice_times_out_and_the_context_survives(cuda, segment):
+    """The adjoint's ring of Laplacian slices (from the tape, or from the
+    checkpoint mode's two-segment stash, segment 7) loses every slice from
+    the middle step down: the waits give up after 2 s, nothing faults."""
     b, c, x, g = problem(cuda)
     sc = scalars(0.707, 1.0, lap_order(B, N, N, 1.0))
-    spec = SeqSpec(B, N, N, T, SRC, PRB, form=_lib.WT_FORM_FUSED, segment=-1)
+    spec = SeqSpec(B, N, N, T, SRC, PRB, form=_lib.WT_FORM_FUSED, segment=segment)
     d, keep = spec.desc()
     n = seq_workspace_bytes(spec)
     out, _, _, ws = seq_forward(spec, sc, b, c, x)

@@ -734,7 +734,7 @@ extern "C" int wt_test_tape_missing_slice(const wt_scalars* s, const wt_seq_desc
     SeqPlan P;
     int st = make_plan(d, &P);
     if (st) return st;
-    if (P.form != WT_FORM_FUSED || P.band || !P.tape) return WT_ERR_UNSUPPORTED;
+    if (P.form != WT_FORM_FUSED || P.band || !(P.tape || P.L.ws)) return WT_ERR_UNSUPPORTED;
     if (step < 0 || step >= P.T) return WT_ERR_INVALID;
     if (!b || !c || !grad_c || !workspace || workspace_bytes < P.total) return WT_ERR_INVALID;
     if (P.np > 0 && !grad_out) return WT_ERR_INVALID;

@@ -1582,8 +1582,28 @@ WT_DEV void ws_adjoint_group(const FusedParams& P, const Geo& g, const Xchg& X, 
     int u = 0;                        // adjoint steps done (and stash slices consumed)
     int cslot = 0, islot = 0;         // ring slots of the next wait / issue
     uint32_t phase = 0;               // per slot: parity of its next wait
-    int niss = 0;                     // copies issued (the issuer's count)
+    // the issuer's record per slot: a copy in flight that its own wait has
+    // not seen land (inflight), that copy's phase parity (ppar), the parity of
+    // the slot's next copy (ipar); it refills a slot only after its own wait
+    // saw the slot's copy land, and issues nothing once a wait gave up (or
+    // from the missing-slice test hook's step down), so every slot holds at
+    // most one copy it has not seen land, and it waits for those before the
+    // kernel leaves
+    uint32_t inflight = 0, ppar = 0, ipar = 0;
+    bool halted = false;
     const bool issuer = ltid == 0;
+    auto issue = [&](const float* src, int t) {
+        if (halted || t + 1 <= P.skip_slice1 || *(volatile int*)X.abort) {
+            halted = true;
+            return;
+        }
+        const uint32_t bit = 1u << islot;
+        ws_issue(ring, src, islot);
+        inflight |= bit;
+        ppar = (ppar & ~bit) | (ipar & bit);
+        ipar ^= bit;
+        islot = islot + 1 == ring.nbuf ? 0 : islot + 1;
+    };
     const bool taps_here = tp.np() || (P.grad_x && tp.ns());
     bool ok = true;
     for (int p = 0; p <= nseg && ok; ++p) {
@@ -1597,11 +1617,8 @@ WT_DEV void ws_adjoint_group(const FusedParams& P, const Geo& g, const Xchg& X, 
             };
             if (issuer) {
                 fence_proxy_async_smem();   // the slots' last readers passed the phase barrier
-                for (int j = 0; j < ring.nbuf && t1 - 1 - j >= t0; ++j) {
-                    ws_issue(ring, stash_at(t1 - 1 - j), islot);
-                    islot = islot + 1 == ring.nbuf ? 0 : islot + 1;
-                    ++niss;
-                }
+                for (int j = 0; j < ring.nbuf && t1 - 1 - j >= t0; ++j)
+                    issue(stash_at(t1 - 1 - j), t1 - 1 - j);
             }
             for (int t = t1 - 1; t >= t0 && ok; --t) {
                 const int par = u & 1;
@@ -1640,14 +1657,13 @@ WT_DEV void ws_adjoint_group(const FusedParams& P, const Geo& g, const Xchg& X, 
                 // step t+1's slice was read before this barrier: refill its slot
                 if (issuer && t < t1 - 1 && t + 1 - ring.nbuf >= t0) {
                     fence_proxy_async_smem();
-                    ws_issue(ring, stash_at(t + 1 - ring.nbuf), islot);
-                    islot = islot + 1 == ring.nbuf ? 0 : islot + 1;
-                    ++niss;
+                    issue(stash_at(t + 1 - ring.nbuf), t + 1 - ring.nbuf);
                 }
                 if (g.colv) {
                     const int LD = P.LD;
                     const float w = P.k.lap_w, w4 = P.k.lap_w4, dt2 = P.k.dt2;
-                    ws_wait(P, X, ring, cslot, (phase >> cslot) & 1u);
+                    if (ws_wait(P, X, ring, cslot, (phase >> cslot) & 1u) && issuer)
+                        inflight &= ~(1u << cslot);
                     // this thread's chunk 0 of the slice (chunk j of 2 cells
                     // at + j * cstride floats)
                     const uint32_t ly = ring.buf + 4u * (uint32_t)(cslot * ring.slice + ltid * V);
@@ -1689,13 +1705,10 @@ WT_DEV void ws_adjoint_group(const FusedParams& P, const Geo& g, const Xchg& X, 
         __syncthreads();   // phase barrier: the stash half group R filled is complete
         ok = ok && *(volatile int*)X.abort == 0;
     }
-    if (issuer && u < niss) {
+    if (issuer && inflight) {
         // leaving early: let the copies still in flight land first (bounded waits)
-        for (int k = u; k < niss; ++k) {
-            ws_wait(P, X, ring, cslot, (phase >> cslot) & 1u, false);
-            phase ^= 1u << cslot;
-            cslot = cslot + 1 == ring.nbuf ? 0 : cslot + 1;
-        }
+        for (int sl = 0; sl < ring.nbuf; ++sl)
+            if ((inflight >> sl) & 1u) ws_wait(P, X, ring, sl, (ppar >> sl) & 1u, false);
     }
     if (g.colv && ok) {
         // dL/dc = (X1 * Kc) * sum_t Lap * lam (store_dc's arithmetic, X1 from
