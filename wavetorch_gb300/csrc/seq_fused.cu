@@ -1241,7 +1241,9 @@ __global__ void __launch_bounds__(bwd_max_threads(M), 1) seq_bwd_tape_kernel(Fus
         }
         if (!exchange_end(X, u)) return false;
         // step t+1's slice was read before this barrier: refill its slot
-        if (issuer && u > 0 && t + 1 - P.nbuf >= 0) {
+        // (not once a wait gave up: a wait that saw the abort word may have
+        // left its slot's copy in flight, which the drain below then covers)
+        if (issuer && u > 0 && t + 1 - P.nbuf >= 0 && *(volatile int*)X.abort == 0) {
             fence_proxy_async_smem();
             if (tape_issue(P, g, ring, t + 1 - P.nbuf, slot + 1 == P.nbuf ? 0 : slot + 1))
                 lo = t + 1 - P.nbuf;
@@ -1928,7 +1930,8 @@ __global__ void __launch_bounds__(bwd_max_threads(M), 1) seq_bwd_nl_kernel(Fused
             sts_col<M>(col, c2g);
         }
         if (!exchange_end(X, u)) return false;
-        if (threadIdx.x == 0 && u > 0 && t + 1 - P.nbuf >= 0) {
+        // (no refill once a wait gave up, as in the linear tape adjoint)
+        if (threadIdx.x == 0 && u > 0 && t + 1 - P.nbuf >= 0 && *(volatile int*)X.abort == 0) {
             fence_proxy_async_smem();
             if (tape_issue(P, g, ring, t + 1 - P.nbuf, slot + 1 == P.nbuf ? 0 : slot + 1))
                 lo = t + 1 - P.nbuf;
