@@ -282,12 +282,15 @@ class RaggedBatch:
                                              self.strip)
         self.strip = self._plan.strip
 
-    def _tune_strip(self, steps: int = 64) -> int:
+    def _tune_strip(self, steps: int = 256) -> int:
         """The strip height (4 or 8 cells per thread) of the faster forward +
-        adjoint on the first `steps` steps of every model; 0 when only one
-        height fits."""
+        adjoint on the first steps of every model, each model's count scaled
+        by one factor so that the longest runs `steps` (the schedule keeps
+        its shape: equal counts would balance the CTAs differently); 0 when
+        only one height fits."""
         dev = self.device
-        T = [min(t, steps) for t in self.T]
+        top = max(self.T)
+        T = [max(1, min(t, -(-t * steps // top))) for t in self.T]
         x = [v[:t].contiguous() for v, t in zip(self._x, T)]
         out = [torch.zeros(t, self._P, device=dev) for t in T]
         gout = [torch.ones(t, self._P, device=dev) for t in T]
