@@ -61,7 +61,7 @@ def check(cuda, nx, ny, B, T, src, prb, seed=0):
         assert np.array_equal(fields.cpu().numpy(), hist), form
 
 
-@pytest.mark.parametrize("nx,ny", [(72, 100), (100, 72), (37, 53), (64, 33)])
+@pytest.mark.parametrize("nx,ny", [(72, 100), (100, 72), (37, 53), (64, 33), (45, 260), (130, 136)])
 def test_rectangular_grids(cuda, nx, ny):
     src = [((nx // 4) * ny + ny // 2, -1)]
     prb = [((3 * nx // 4) * ny + ny // 3, 1, 0), ((3 * nx // 4) * ny + 2 * ny // 3, 0, 1)]
@@ -109,3 +109,14 @@ def test_fixed_input_rows(cuda):
     src = [((10 + l) * N + 20, l) for l in range(B)]
     prb = [(30 * N + 20, 1, 0)]
     check(cuda, N, N, B, 60, src, prb)
+
+
+def test_taps_on_column_chunk_edges(cuda):
+    """45 x 260: the plain form's vector kernels cut rows into 128-column
+    chunks (lanes of 4 cells) and groups of 4 rows, so sources and probes sit
+    on chunk edges (columns 127, 128, 255, 256, 259) and on the ragged last
+    row group (rows 44)."""
+    nx, ny = 45, 260
+    src = [(10 * ny + 127, -1), (11 * ny + 128, -1), (44 * ny + 259, -1)]
+    prb = [(30 * ny + 255, 1, 0), (30 * ny + 256, 0, 1), (44 * ny + 128, 1, 2), (3 * ny + 127, 1, 3)]
+    check(cuda, nx, ny, 2, 80, src, prb)

@@ -318,10 +318,11 @@ def test_cfg3_lens_against_oracle(cuda):
     assert rel(gc.cpu().numpy(), ogc) <= FUSED_DC_TOL
 
 
-@pytest.mark.parametrize("B,N,steps", [(560, 120, 12), (128, 256, 10)])
+@pytest.mark.parametrize("B,N,steps", [(560, 120, 12), (128, 256, 10), (37, 132, 20)])
 def test_plain_large_batches_against_oracle(cuda, B, N, steps):
-    """Large batches in the plain form (the batch reduction over 35 and 8
-    blocks of 16 instances, probes on the vector kernels' tile edges):
+    """Large batches in the plain form (the batch reduction over 35, 8 and
+    three blocks of 16 instances, the last one short, formed in the adjoint
+    step's kernel; probes on the vector kernels' tile edges):
     outputs and dL/dc bit-exact with the oracle, i.e. with the reference's
     batch reduction order; the forward reads its coefficients from planes
     formed once per sequence."""

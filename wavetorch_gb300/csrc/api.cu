@@ -625,10 +625,11 @@ extern "C" int wt_seq_bwd(const wt_scalars* s, const wt_seq_desc* d, const float
                 e.G = grad_c;
                 e.first = t == P.T - 1;
             }
-            st = wt_launch_seq_adj_step(k, P.B, P.nx, P.ny, b, c, kco, l1, l2, hp, hbs, lo, gc, e, cs);
+            // the step's dL/dc terms summed over the batch into grad_c (by the
+            // step itself for one instance)
+            st = wt_launch_seq_adj_step(k, P.B, P.nx, P.ny, b, c, kco, l1, l2, hp, hbs, lo, gc,
+                                        grad_c, t == P.T - 1, e, cs);
             if (st) return st;
-            if (P.B > 1 && (st = wt_launch_seq_adj_reduce(P.B, plane, gc, grad_c, t == P.T - 1, cs)))
-                return st;
         }
         return WT_OK;
     }

@@ -234,8 +234,8 @@ int wt_launch_adj_coef(const StepScalars& k, size_t plane, const float* b, const
                        float* kco, cudaStream_t st);
 int wt_launch_seq_adj_step(const StepScalars& k, int batch, int nx, int ny, const float* b,
                            const float* c, const float* kco, const float* lam1, const float* lam2,
-                           const float* hprev, size_t hbs, float* lam_out, float* gc,
-                           const wt::AdjEpilogue& epi, cudaStream_t st);
+                           const float* hprev, size_t hbs, float* lam_out, float* gc, float* G,
+                           int first, const wt::AdjEpilogue& epi, cudaStream_t st);
 int wt_launch_seq_adj_reduce(int batch, size_t plane, const float* gc, float* G, int first,
                              cudaStream_t st);
 int wt_launch_fill_zero(float* p, size_t n, cudaStream_t st);

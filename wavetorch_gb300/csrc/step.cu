@@ -365,6 +365,108 @@ step_fwd4_kernel(StepScalars k, int nx, int ny, int coef_batched, const float* _
     *reinterpret_cast<float4*>(y + inst * bs + cell) = make_float4(v[0], v[1], v[2], v[3]);
 }
 
+// The same step with the coefficient planes, streamed by rows: a warp runs
+// STEP4R_ROWS consecutive rows of one 128-column chunk (lane: 4 cells of
+// each row), with every field and coefficient word it needs loaded before
+// any is used -- the rows above and below from registers, the left / right
+// neighbours from the adjacent lanes and, at a chunk's edges, from memory.
+// No shared memory and no barrier: each warp keeps 22 16-byte loads in
+// flight instead of a tile's staging round.  Warps of a CTA take
+// consecutive row groups of one instance; all rows of a warp lie in one
+// STEP4_TX-row tile.  The arithmetic per cell is step_fwd4_kernel's.
+constexpr int STEP4R_ROWS = 4;
+constexpr int STEP4R_WARPS = 4;
+constexpr int ADJ4R_ROWS = 1;     // the adjoint's rows per warp (more operands per row)
+// The row-streaming kernels serve sequences of at least this many cells per
+// step (batch x grid); below it the tile kernels' shorter chains per warp win.
+// Forward / adjoint us per step at 120x120, tiles against rows (CUDA graph):
+// B=32 3.3 / 8.0 vs 4.5 / 9.1; B=128 7.1 / 17.3 vs 7.6 / 20.9; B=256 (3.7 M
+// cells) 11.2 / 29.2 vs 11.3 / 29.9; B=512 21.3 / 60.3 vs 20.2 / 51.0; B=1024
+// 45.4 / 118.6 vs 40.8 / 88.3.
+constexpr size_t STREAM_MIN_CELLS = size_t(4) << 20;
+static_assert(STEP4_TX % STEP4R_ROWS == 0, "row groups inside one tile");
+
+template <int ORDER, bool EPI>
+__global__ void __launch_bounds__(STEP4R_WARPS * 32, 4)
+step_fwd4r_kernel(StepScalars k, int nx, int ny, const float* __restrict__ fco,
+                  const float* __restrict__ y1, size_t bs1, const float* __restrict__ y2,
+                  size_t bs2, float* __restrict__ y, size_t bs, SeqEpilogue e) {
+    constexpr int R = STEP4R_ROWS;
+    const int inst = blockIdx.z;
+    const int x0 = (blockIdx.y * STEP4R_WARPS + threadIdx.y) * R;
+    if (x0 >= nx) return;                       // whole warps only
+    const int lane = threadIdx.x, y0 = blockIdx.x * STEP4_TY, gy = y0 + 4 * lane;
+    const bool colv = gy < ny;
+    const size_t plane = (size_t)nx * ny;
+    const float* f1 = y1 + inst * bs1;
+    const float* f2 = y2 + inst * bs2;
+    const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
+    float4 Y[R + 2], P[R], A[R], B[R], C2[R];
+    float le[R], re[R];
+#pragma unroll
+    for (int i = 0; i < R + 2; ++i) {
+        const int gx = x0 - 1 + i;
+        Y[i] = colv && gx >= 0 && gx < nx ? __ldg(reinterpret_cast<const float4*>(f1 + (size_t)gx * ny + gy))
+                                          : z4;
+    }
+#pragma unroll
+    for (int i = 0; i < R; ++i) {
+        const int gx = x0 + i;
+        const bool v = colv && gx < nx;
+        const size_t cell = (size_t)gx * ny + gy;
+        P[i] = v ? __ldg(reinterpret_cast<const float4*>(f2 + cell)) : z4;
+        A[i] = v ? __ldg(reinterpret_cast<const float4*>(fco + cell)) : z4;
+        B[i] = v ? __ldg(reinterpret_cast<const float4*>(fco + plane + cell)) : z4;
+        C2[i] = v ? __ldg(reinterpret_cast<const float4*>(fco + 2 * plane + cell)) : z4;
+        le[i] = lane == 0 && y0 > 0 && gx < nx ? __ldg(f1 + (size_t)gx * ny + y0 - 1) : 0.f;
+        re[i] = lane == 31 && y0 + STEP4_TY < ny && gx < nx
+                    ? __ldg(f1 + (size_t)gx * ny + y0 + STEP4_TY) : 0.f;
+    }
+    const bool taps = EPI && (!e.tileflag ||
+                              __ldg(e.tileflag + (x0 / STEP4_TX) * e.tiles_y + blockIdx.x));
+#pragma unroll
+    for (int i = 0; i < R; ++i) {
+        const int gx = x0 + i;
+        if (gx >= nx) break;                    // uniform over the warp
+        const float4 C = Y[i + 1], U = Y[i], D = Y[i + 2];
+        float left = __shfl_up_sync(0xffffffffu, C.w, 1);
+        float right = __shfl_down_sync(0xffffffffu, C.x, 1);
+        if (lane == 0) left = le[i];
+        if (lane == 31) right = re[i];
+        const float c[4] = {C.x, C.y, C.z, C.w}, u[4] = {U.x, U.y, U.z, U.w};
+        const float d[4] = {D.x, D.y, D.z, D.w};
+        const float l[4] = {left, C.x, C.y, C.z}, r[4] = {C.y, C.z, C.w, right};
+        const float aa[4] = {A[i].x, A[i].y, A[i].z, A[i].w};
+        const float bb[4] = {B[i].x, B[i].y, B[i].z, B[i].w};
+        const float cc[4] = {C2[i].x, C2[i].y, C2[i].z, C2[i].w};
+        const float pp[4] = {P[i].x, P[i].y, P[i].z, P[i].w};
+        if (!colv) continue;
+        const size_t cell = (size_t)gx * ny + gy;
+        float v[4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const float L = lap5<ORDER>(u[j], l[j], c[j], r[j], d[j], k.lap_w, k.lap_w4);
+            v[j] = leapfrog(aa[j], bb[j], cc[j], k.two_over, c[j], pp[j], L);
+        }
+        if (taps) {
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                for (int en = __ldg(e.srcmap + cell + j); en >= 0; en = __ldg(e.src_next + en)) {
+                    int row = __ldg(e.src_row + en);
+                    row = row < 0 ? inst : row;
+                    v[j] = fadd(v[j], __ldg(e.x + (size_t)row * e.steps + e.t));
+                }
+                for (int en = __ldg(e.probemap + cell + j); en >= 0; en = __ldg(e.probe_next + en)) {
+                    size_t o = ((size_t)inst * e.steps + e.t) * e.n_probe + en;
+                    e.out[o] = __ldg(e.probe_kind + en) ? fmul(v[j], v[j]) : v[j];
+                    if (e.amp) e.amp[o] = v[j];
+                }
+            }
+        }
+        *reinterpret_cast<float4*>(y + inst * bs + cell) = make_float4(v[0], v[1], v[2], v[3]);
+    }
+}
+
 // The forward's time-invariant coefficients as three planes [A | Bc | c^2]
 // (wavetorch/cell.py:13-16, fwd_coef's arithmetic: A holds a division),
 // formed once per sequence.
@@ -496,6 +598,199 @@ seq_adj_step4_kernel(StepScalars k, int nx, int ny, const float* __restrict__ kc
     }
 }
 
+// The same adjoint step streamed by rows, as step_fwd4r_kernel: a warp runs
+// R consecutive rows of one 128-column chunk with every operand loaded
+// before any is used (Kg * lam_{t+1} and h_{t-1} for rows x0-1 .. x0+R, the
+// rest for its own rows), the neighbours above and below from registers,
+// left and right from the adjacent lanes or, at a chunk's edges, from
+// memory.  The arithmetic per cell is seq_adj_step_kernel's.
+//
+// A CTA of W warps serves one row group for one block of 16 instances
+// (blockIdx.z): the time-invariant coefficients of its rows are loaded once,
+// then its warps take one instance each per round (instance base + w).
+// After each round the
+// warps' dL/dc terms go through shared memory to the threads that own the
+// cells, which add them in instance order.  So the block's sum of the
+// step's terms -- the first stage of the batch reduction, seq_adj_reduce_
+// kernel's blocks of 16 summed from 0 in instance order -- is formed here
+// and one plane per block goes to gsum instead of one term plane per
+// instance; with one instance the owners accumulate into e.G.
+constexpr int ADJ_BLOCK = 16;
+template <int ORDER, int R, int W, int MINB>
+__global__ void __launch_bounds__(W * 32, MINB)
+seq_adj_step4r_kernel(StepScalars k, int batch, int nx, int ny, const float* __restrict__ kco,
+                      const float* __restrict__ lam1, const float* __restrict__ lam2,
+                      const float* __restrict__ hprev, size_t hbs, float* __restrict__ lam_out,
+                      float* __restrict__ gsum, AdjEpilogue e) {
+    static_assert(STEP4_TX % R == 0, "row groups inside one tile");
+    static_assert(R <= W, "one owner thread per 4-cell slot");
+    __shared__ float4 part[W][R * 32];
+    const int w = threadIdx.y, lane = threadIdx.x;
+    const int x0 = blockIdx.y * R;              // < nx: the grid has one CTA per row group
+    const int y0 = blockIdx.x * STEP4_TY, gy = y0 + 4 * lane;
+    const bool colv = gy < ny;
+    const size_t plane = (size_t)nx * ny;
+    const float* Kg = kco + 2 * plane;
+    const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
+    const bool taps = !e.tileflag || __ldg(e.tileflag + (x0 / STEP4_TX) * e.tiles_y + blockIdx.x);
+    auto g4 = [](float4 kg, float4 l) {
+        return make_float4(fmul(kg.x, l.x), fmul(kg.y, l.y), fmul(kg.z, l.z), fmul(kg.w, l.w));
+    };
+    // the time-invariant words of the rows (Kg with the halo rows)
+    float4 KG[R + 2], X1[R], KC[R], KY[R];
+    float kgl[R], kgr[R];
+#pragma unroll
+    for (int i = 0; i < R + 2; ++i) {
+        const int gx = x0 - 1 + i;
+        KG[i] = colv && gx >= 0 && gx < nx && lam1 ? __ldg(reinterpret_cast<const float4*>(Kg + (size_t)gx * ny + gy))
+                                                   : z4;
+    }
+    const bool le = lane == 0 && y0 > 0, re = lane == 31 && y0 + STEP4_TY < ny;
+#pragma unroll
+    for (int i = 0; i < R; ++i) {
+        const int gx = x0 + i;
+        const bool v = colv && gx < nx;
+        const size_t cell = (size_t)gx * ny + gy;
+        X1[i] = v ? __ldg(reinterpret_cast<const float4*>(kco + cell)) : z4;
+        KC[i] = v ? __ldg(reinterpret_cast<const float4*>(kco + plane + cell)) : z4;
+        KY[i] = v ? __ldg(reinterpret_cast<const float4*>(kco + 3 * plane + cell)) : z4;
+        kgl[i] = le && gx < nx ? __ldg(Kg + (size_t)gx * ny + y0 - 1) : 0.f;
+        kgr[i] = re && gx < nx ? __ldg(Kg + (size_t)gx * ny + y0 + STEP4_TY) : 0.f;
+    }
+    // the 4-cell slot this thread owns in the sums: row x0 + orow, lanes' chunk oln
+    const int slot = w * 32 + lane, orow = slot / 32, oln = slot % 32;
+    const bool owner = slot < R * 32 && x0 + orow < nx && y0 + 4 * oln < ny;
+    float4 blk = z4;
+    const int i0 = blockIdx.z * ADJ_BLOCK, i1 = min(batch, i0 + ADJ_BLOCK);
+    for (int base = i0; base < i1; base += W) {
+        const int inst = base + w;
+        if (inst < i1) {                        // uniform over the warp
+            // every load first
+            const float* l1p = lam1 ? lam1 + inst * plane : nullptr;
+            const float* hp = hprev ? hprev + inst * hbs : nullptr;
+            const float* l2p = lam2 ? lam2 + inst * plane : nullptr;
+            float4 L1[R + 2], H[R + 2], L2[R];
+            float l1l[R], l1r[R], hl_[R], hr_[R];
+#pragma unroll
+            for (int i = 0; i < R + 2; ++i) {
+                const int gx = x0 - 1 + i;
+                const bool v = colv && gx >= 0 && gx < nx;
+                const size_t cell = (size_t)gx * ny + gy;
+                L1[i] = v && l1p ? __ldg(reinterpret_cast<const float4*>(l1p + cell)) : z4;
+                H[i] = v && hp ? __ldg(reinterpret_cast<const float4*>(hp + cell)) : z4;
+            }
+#pragma unroll
+            for (int i = 0; i < R; ++i) {
+                const int gx = x0 + i;
+                const bool v = colv && gx < nx;
+                const size_t cell = (size_t)gx * ny + gy;
+                L2[i] = v && l2p ? __ldg(reinterpret_cast<const float4*>(l2p + cell)) : z4;
+                const size_t lc = (size_t)gx * ny + y0 - 1, rc = (size_t)gx * ny + y0 + STEP4_TY;
+                l1l[i] = le && gx < nx && l1p ? __ldg(l1p + lc) : 0.f;
+                l1r[i] = re && gx < nx && l1p ? __ldg(l1p + rc) : 0.f;
+                hl_[i] = le && gx < nx && hp ? __ldg(hp + lc) : 0.f;
+                hr_[i] = re && gx < nx && hp ? __ldg(hp + rc) : 0.f;
+            }
+#pragma unroll
+            for (int i = 0; i < R; ++i) {
+                const int gx = x0 + i;
+                if (gx >= nx) break;            // uniform over the warp
+                const float4 GU = g4(KG[i], L1[i]), GC = g4(KG[i + 1], L1[i + 1]);
+                const float4 GD = g4(KG[i + 2], L1[i + 2]);
+                const float4 HU = H[i], HC = H[i + 1], HD = H[i + 2];
+                float gl = __shfl_up_sync(0xffffffffu, GC.w, 1), gr = __shfl_down_sync(0xffffffffu, GC.x, 1);
+                float hl = __shfl_up_sync(0xffffffffu, HC.w, 1), hr = __shfl_down_sync(0xffffffffu, HC.x, 1);
+                if (lane == 0) { gl = fmul(kgl[i], l1l[i]); hl = hl_[i]; }
+                if (lane == 31) { gr = fmul(kgr[i], l1r[i]); hr = hr_[i]; }
+                if (!colv) continue;
+                const float Gc[4] = {GC.x, GC.y, GC.z, GC.w}, Gu[4] = {GU.x, GU.y, GU.z, GU.w};
+                const float Gd[4] = {GD.x, GD.y, GD.z, GD.w};
+                const float Gl[4] = {gl, GC.x, GC.y, GC.z}, Gr[4] = {GC.y, GC.z, GC.w, gr};
+                const float Hc[4] = {HC.x, HC.y, HC.z, HC.w}, Hu[4] = {HU.x, HU.y, HU.z, HU.w};
+                const float Hd[4] = {HD.x, HD.y, HD.z, HD.w};
+                const float Hl[4] = {hl, HC.x, HC.y, HC.z}, Hr[4] = {HC.y, HC.z, HC.w, hr};
+                const float l1[4] = {L1[i + 1].x, L1[i + 1].y, L1[i + 1].z, L1[i + 1].w};
+                const float l2[4] = {L2[i].x, L2[i].y, L2[i].z, L2[i].w};
+                const float x1[4] = {X1[i].x, X1[i].y, X1[i].z, X1[i].w};
+                const float kc[4] = {KC[i].x, KC[i].y, KC[i].z, KC[i].w};
+                const float ky[4] = {KY[i].x, KY[i].y, KY[i].z, KY[i].w};
+                const size_t cell = (size_t)gx * ny + gy;
+                float lam[4], gt[4];
+#pragma unroll
+                for (int j = 0; j < 4; ++j) {
+                    // gradient arriving at h_t: first gy2 from step t+2, then gy1 from t+1
+                    float lv = 0.f;
+                    if (lam2) lv = fmul(ky[j], l2[j]);
+                    if (lam1) {
+                        const float lg = lap5<ORDER>(Gu[j], Gl[j], Gc[j], Gr[j], Gd[j], k.lap_w, k.lap_w4);
+                        const float gy1 = fadd(fmul(k.dt2, lg), fmul(fmul(2.0f, l1[j]), x1[j]));
+                        lv = lam2 ? fadd(lv, gy1) : gy1;
+                    }
+                    if (taps) {
+                        for (int en = __ldg(e.probemap + cell + j); en >= 0; en = __ldg(e.probe_next + en)) {
+                            size_t o = ((size_t)inst * e.steps + e.t) * e.n_probe + en;
+                            float gv = __ldg(e.grad_out + o);
+                            float sd = __ldg(e.probe_kind + en) ? fmul(gv, fmul(2.0f, __ldg(e.amp + o))) : gv;
+                            lv = fadd(lv, sd);
+                        }
+                    }
+                    lam[j] = lv;
+                    const float L = hp ? lap5<ORDER>(Hu[j], Hl[j], Hc[j], Hr[j], Hd[j], k.lap_w, k.lap_w4)
+                                       : 0.0f;
+                    gt[j] = fmul(fmul(x1[j], fmul(kc[j], L)), lv);
+                    if (e.grad_x && taps) {
+                        for (int en = __ldg(e.srcmap + cell + j); en >= 0; en = __ldg(e.src_next + en))
+                            if (__ldg(e.src_row + en) < 0) e.grad_x[(size_t)inst * e.steps + e.t] = lv;
+                    }
+                }
+                *reinterpret_cast<float4*>(lam_out + inst * plane + cell) =
+                    make_float4(lam[0], lam[1], lam[2], lam[3]);
+                part[w][i * 32 + lane] = make_float4(gt[0], gt[1], gt[2], gt[3]);
+            }
+        }
+        __syncthreads();
+        if (owner) {
+            const int n = min(W, i1 - base);
+            for (int q = 0; q < n; ++q) {       // instance order
+                const float4 v = part[q][slot];
+                blk = make_float4(fadd(blk.x, v.x), fadd(blk.y, v.y), fadd(blk.z, v.z), fadd(blk.w, v.w));
+            }
+        }
+        __syncthreads();
+    }
+    if (!owner) return;
+    const size_t cell = (size_t)(x0 + orow) * ny + y0 + 4 * oln;
+    if (e.G) {          // one instance: blk holds fadd(0, term), as the reduction's
+        float4* gp = reinterpret_cast<float4*>(e.G + cell);
+        float4 acc = blk;
+        if (!e.first) {
+            const float4 o = *gp;
+            acc = make_float4(fadd(o.x, acc.x), fadd(o.y, acc.y), fadd(o.z, acc.z), fadd(o.w, acc.w));
+        }
+        *gp = acc;
+    } else if (gsum) {
+        *reinterpret_cast<float4*>(gsum + blockIdx.z * plane + cell) = blk;
+    }
+}
+
+// Second stage of the batch reduction after seq_adj_step4r_kernel: G (+)= the
+// block sums in block order (seq_adj_reduce_kernel's acc).
+__global__ void seq_adj_sum_blocks_kernel(int nb, size_t plane, const float* __restrict__ gsum,
+                                          float* __restrict__ G, int first) {
+    const size_t cell = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (cell >= plane) return;
+    float acc = 0.f;
+    for (int j0 = 0; j0 < nb; j0 += 64) {       // 64 loads in flight, then the sums in order
+        float v[64];
+#pragma unroll
+        for (int u = 0; u < 64; ++u) v[u] = j0 + u < nb ? __ldg(gsum + (size_t)(j0 + u) * plane + cell) : 0.f;
+#pragma unroll
+        for (int u = 0; u < 64; ++u)
+            if (j0 + u < nb) acc = j0 + u == 0 ? v[u] : fadd(acc, v[u]);
+    }
+    G[cell] = first ? acc : fadd(G[cell], acc);
+}
+
 // Phase 2: G_c += chunked batch sum of gc (wavetorch autograd: sum-to-shape of
 // each step's [batch,nx,ny] grad_c, then accumulation over steps).
 __global__ void seq_adj_reduce_kernel(int batch, size_t plane, const float* __restrict__ gc,
@@ -563,6 +858,25 @@ int wt_launch_step_fwd(const StepScalars& k, int batch, int nx, int ny, int coef
                        const float* b, const float* c, const float* y1, size_t bs1,
                        const float* y2, size_t bs2, float* y, size_t bs,
                        const wt::SeqEpilogue* epi, cudaStream_t st, const float* fco) {
+    if (fco && !coef_batched && (size_t)batch * nx * ny >= wt::STREAM_MIN_CELLS &&
+        vec4_ok(ny, {fco, y1, y2, y}, {bs1, bs2, bs, (size_t)nx * ny})) {
+        const int groups = (nx + wt::STEP4R_ROWS - 1) / wt::STEP4R_ROWS;
+        dim3 blk(32, wt::STEP4R_WARPS);
+        dim3 grd((ny + wt::STEP4_TY - 1) / wt::STEP4_TY, (groups + wt::STEP4R_WARPS - 1) / wt::STEP4R_WARPS,
+                 batch);
+        wt::SeqEpilogue e{};
+        if (epi) e = *epi;
+        const bool ep = epi != nullptr;
+        if ((k.lap_order & 1) == WT_LAP_SEQ) {
+            if (ep) wt::step_fwd4r_kernel<WT_LAP_SEQ, true><<<grd, blk, 0, st>>>(k, nx, ny, fco, y1, bs1, y2, bs2, y, bs, e);
+            else    wt::step_fwd4r_kernel<WT_LAP_SEQ, false><<<grd, blk, 0, st>>>(k, nx, ny, fco, y1, bs1, y2, bs2, y, bs, e);
+        } else {
+            if (ep) wt::step_fwd4r_kernel<WT_LAP_PAIRED, true><<<grd, blk, 0, st>>>(k, nx, ny, fco, y1, bs1, y2, bs2, y, bs, e);
+            else    wt::step_fwd4r_kernel<WT_LAP_PAIRED, false><<<grd, blk, 0, st>>>(k, nx, ny, fco, y1, bs1, y2, bs2, y, bs, e);
+        }
+        wt_count_launches(1);
+        return wt_cuda_status(cudaGetLastError());
+    }
     if (vec4_ok(ny, {b, c, fco, y1, y2, y}, {bs1, bs2, bs, (size_t)nx * ny})) {
         dim3 blk(32, wt::STEP4_TX);
         dim3 grd((ny + wt::STEP4_TY - 1) / wt::STEP4_TY, (nx + wt::STEP4_TX - 1) / wt::STEP4_TX, batch);
@@ -627,17 +941,36 @@ int wt_launch_adj_coef(const StepScalars& k, size_t plane, const float* b, const
 
 int wt_launch_seq_adj_step(const StepScalars& k, int batch, int nx, int ny, const float* b,
                            const float* c, const float* kco, const float* lam1, const float* lam2,
-                           const float* hprev, size_t hbs, float* lam_out, float* gc,
-                           const wt::AdjEpilogue& e, cudaStream_t st) {
-    if (vec4_ok(ny, {b, c, kco, lam1, lam2, hprev, lam_out, gc, e.G}, {hbs, (size_t)nx * ny})) {
-        dim3 blk(32, wt::STEP4_TX);
+                           const float* hprev, size_t hbs, float* lam_out, float* gc, float* G,
+                           int first, const wt::AdjEpilogue& e, cudaStream_t st) {
+    const size_t plane = (size_t)nx * ny;
+    if (kco && vec4_ok(ny, {kco, lam1, lam2, hprev, lam_out, gc, e.G}, {hbs, plane})) {
+        if ((size_t)batch * plane >= wt::STREAM_MIN_CELLS) {   // row-streaming, block sums
+            constexpr int R = wt::ADJ4R_ROWS;
+            const int nb = (batch + wt::ADJ_BLOCK - 1) / wt::ADJ_BLOCK;
+            dim3 grd((ny + wt::STEP4_TY - 1) / wt::STEP4_TY, (nx + R - 1) / R, nb);
+            dim3 blk(32, 4);
+            if ((k.lap_order & 1) == WT_LAP_SEQ)
+                wt::seq_adj_step4r_kernel<WT_LAP_SEQ, R, 4, 6><<<grd, blk, 0, st>>>(k, batch, nx, ny, kco, lam1, lam2, hprev, hbs, lam_out, gc, e);
+            else
+                wt::seq_adj_step4r_kernel<WT_LAP_PAIRED, R, 4, 6><<<grd, blk, 0, st>>>(k, batch, nx, ny, kco, lam1, lam2, hprev, hbs, lam_out, gc, e);
+            wt_count_launches(1);
+            cudaError_t ce = cudaGetLastError();
+            if (ce != cudaSuccess || e.G || !G) return wt_cuda_status(ce);
+            wt::seq_adj_sum_blocks_kernel<<<(unsigned)((plane + 255) / 256), 256, 0, st>>>(nb, plane, gc, G, first);
+            wt_count_launches(1);
+            return wt_cuda_status(cudaGetLastError());
+        }
+        dim3 blk(32, wt::STEP4_TX);           // tiles, one term plane per instance
         dim3 grd((ny + wt::STEP4_TY - 1) / wt::STEP4_TY, (nx + wt::STEP4_TX - 1) / wt::STEP4_TX, batch);
         if ((k.lap_order & 1) == WT_LAP_SEQ)
             wt::seq_adj_step4_kernel<WT_LAP_SEQ><<<grd, blk, 0, st>>>(k, nx, ny, kco, lam1, lam2, hprev, hbs, lam_out, gc, e);
         else
             wt::seq_adj_step4_kernel<WT_LAP_PAIRED><<<grd, blk, 0, st>>>(k, nx, ny, kco, lam1, lam2, hprev, hbs, lam_out, gc, e);
         wt_count_launches(1);
-        return wt_cuda_status(cudaGetLastError());
+        cudaError_t ce = cudaGetLastError();
+        if (ce != cudaSuccess || e.G || !G) return wt_cuda_status(ce);
+        return wt_launch_seq_adj_reduce(batch, plane, gc, G, first, st);
     }
     dim3 blk(wt::TY, wt::TX);
     dim3 grd((ny + wt::TY - 1) / wt::TY, (nx + wt::TX - 1) / wt::TX, batch);
@@ -646,7 +979,9 @@ int wt_launch_seq_adj_step(const StepScalars& k, int batch, int nx, int ny, cons
     else
         wt::seq_adj_step_kernel<WT_LAP_PAIRED><<<grd, blk, 0, st>>>(k, nx, ny, b, c, lam1, lam2, hprev, hbs, lam_out, gc, e);
     wt_count_launches(1);
-    return wt_cuda_status(cudaGetLastError());
+    cudaError_t ce = cudaGetLastError();
+    if (ce != cudaSuccess || e.G || !G) return wt_cuda_status(ce);
+    return wt_launch_seq_adj_reduce(batch, plane, gc, G, first, st);
 }
 
 int wt_launch_seq_adj_reduce(int batch, size_t plane, const float* gc, float* G, int first,
