@@ -120,3 +120,33 @@ def test_taps_on_column_chunk_edges(cuda):
     src = [(10 * ny + 127, -1), (11 * ny + 128, -1), (44 * ny + 259, -1)]
     prb = [(30 * ny + 255, 1, 0), (30 * ny + 256, 0, 1), (44 * ny + 128, 1, 2), (3 * ny + 127, 1, 3)]
     check(cuda, nx, ny, 2, 80, src, prb)
+
+
+@pytest.mark.parametrize("B,nx,ny", [(400, 45, 260), (700, 61, 100)])
+def test_row_streaming_kernels_on_ragged_rows_and_chunk_edges(cuda, B, nx, ny):
+    """Batches past the row-streaming kernels' threshold (4 M cells per step)
+    on grids whose rows do not fill the last group of 4 (forward) and whose
+    columns span several 128-column chunks, taps on chunk edges and on the
+    last rows, and a batch that ends in a short block of 16 (the adjoint's
+    block sums): outputs, fields and dL/dc bit-exact with the oracle."""
+    assert B * nx * ny >= 4 << 20
+    src = [(10 * ny + min(127, ny - 1), -1), ((nx - 1) * ny + ny - 1, -1)]
+    prb = [(30 * ny + min(128, ny - 2), 1, 0), ((nx - 1) * ny + ny // 2, 0, 1), (3 * ny + 127 % ny, 1, 2)]
+    T = 10
+    b, c, x = problem(nx, ny, B, T, 5)
+    g = np.random.default_rng(6).standard_normal((B, T, len(prb))).astype(np.float32)
+    S = o.Seq(B, nx, ny, T, 0.707, 1.0, src, prb)
+    oout, hist = S.forward(b, c, x)
+    ogc = S.backward(b, c, hist, g)[0]
+    sc = scalars(0.707, 1.0, lap_order(B, nx, ny, 1.0))
+    tb, tc, tx = (torch.from_numpy(v).to(cuda) for v in (b, c, x))
+    spec = SeqSpec(B, nx, ny, T, src, prb, form=_lib.WT_FORM_PLAIN)
+    out, _, _, ws = seq_forward(spec, sc, tb, tc, tx)
+    gc, _ = seq_backward(spec, sc, tb, tc, tx, torch.from_numpy(g).to(cuda), ws, False)
+    torch.cuda.synchronize()
+    assert seq_device_status(spec, ws) == _lib.WT_OK
+    assert np.array_equal(out.cpu().numpy(), oout)
+    assert np.array_equal(gc.cpu().numpy(), ogc)
+    spec_f = SeqSpec(B, nx, ny, T, src, [], form=_lib.WT_FORM_PLAIN, output_fields=True)
+    _, fields, _, _ = seq_forward(spec_f, sc, tb, tc, tx)
+    assert np.array_equal(fields.cpu().numpy(), hist)
