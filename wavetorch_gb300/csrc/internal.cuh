@@ -143,6 +143,7 @@ struct WtFusedLaunch {
     size_t smem_bwd_base;   // adjoint shared memory before the tape ring
     int nbuf_nl;            // ring slices of the nonlinear adjoint (two-part slices)
     size_t smem_nl_coef;    // the nonlinear adjoint's per-thread coefficient words
+    int nl_cache;           // ... with the step's X1, q, sat kept between its halves
     // checkpoint mode with the segment recompute beside the adjoint
     // (seq_bwd_ws_kernel: 2 x threads, a stash of two segments in global
     // memory): ring slices, shared memory, and whether the plan uses it

@@ -721,7 +721,10 @@ constexpr int fwd_max_threads(int M) {
 }
 constexpr int bwd_max_threads(int M) { return M >= 10 ? 384 : 512; }
 // Per-thread coefficient words of the nonlinear adjoint (b_pml, c_lin, rho).
-__host__ __device__ constexpr int nl_coef_stride(int M) { return (3 * M) | 1; }
+// Per-thread shared words of the nonlinear adjoint: b_pml, c_lin, rho of its
+// cells, and with CACHE also the step's X1, q and sat from the first half of
+// the step (the exchange of Kg * lambda) for the second (odd: conflict-free)
+__host__ __device__ constexpr int nl_coef_stride(int M, bool cache) { return ((cache ? 6 : 3) * M) | 1; }
 
 // ============================================================================
 // Forward
@@ -1804,12 +1807,12 @@ __global__ void __launch_bounds__(ws_max_threads(M), 1) seq_bwd_ws_kernel(FusedP
 //   dL/dh1  += grad_b * rho * dsat/dh1 + grad_c * (rho c_nl) * 2 h1
 //   dL/drho += grad_b * sat + grad_c * h1^2 * c_nl      (direct; accr)
 //   dL/dc_lin += grad_c                                  (accc)
+// n and X1 = 1 / (b*dt + 1) are the step's coefficients at h1 (formed by the
+// caller, or kept from the first half of the step).
 WT_DEV void adj_cell_nl(const FusedParams& P, float lg, float& lam, float Ly, float h1, float h2,
-                        float bp, float cl, float rh, float& accc, float& accr, float& pend) {
-    const NLCoef n = nl_coef(P, bp, cl, rh, h1);
+                        const NLCoef& n, float X1, float rh, float& accc, float& accr, float& pend) {
     const float dt = P.k.dt, dt2 = P.k.dt2;
     const float v = fadd(fmul(n.b, dt), 1.0f);                          // b*dt + 1
-    const float X1 = fdiv(1.0f, v);
     const float gc = fmul(fmul(X1, fmul(fmul(fmul(2.0f, n.c), dt2), Ly)), lam);
     float gh = fadd(fmul(dt2, lg), fmul(fmul(2.0f, lam), X1));            // grad_y1
     const float g2 = fmul(fmul(fsub(fmul(n.b, dt), 1.0f), X1), lam);      // grad_y2
@@ -1841,7 +1844,7 @@ WT_DEV void adj_cell_nl(const FusedParams& P, float lg, float& lam, float Ly, fl
     pend = g2;
 }
 
-template <int M, int ORDER>
+template <int M, int ORDER, bool CACHE>
 __global__ void __launch_bounds__(bwd_max_threads(M), 1) seq_bwd_nl_kernel(FusedParams P) {
     extern __shared__ __align__(16) float smem[];
     __shared__ int abort_flag;
@@ -1858,7 +1861,7 @@ __global__ void __launch_bounds__(bwd_max_threads(M), 1) seq_bwd_nl_kernel(Fused
     // b_pml, c_lin and rho of the thread's cells: per-thread shared words at
     // constant offsets (stride 3M rounded up to odd: conflict-free), then the
     // tape ring (16-byte aligned)
-    constexpr int CS = nl_coef_stride(M);
+    constexpr int CS = nl_coef_stride(M, CACHE);
     float* coefs = seeds + ((2 * P.n_prb * P.PB + 3) & ~3);
     float* cw = coefs + threadIdx.x * CS;
     TapeRing ring;
@@ -1923,6 +1926,11 @@ __global__ void __launch_bounds__(bwd_max_threads(M), 1) seq_bwd_nl_kernel(Fused
                 const NLCoef n = nl_coef(P, cw[i], cw[M + i], cw[2 * M + i], h1[i]);
                 const float X1 = fdiv(1.0f, fadd(fmul(n.b, P.k.dt), 1.0f));
                 c2g[i] = fmul(fmul(X1, fmul(n.c, n.c)), lam[i]);   // (b*dt+1)^-1 * c^2 * g
+                if constexpr (CACHE) {      // the divisions' results for the second half
+                    cw[3 * M + i] = X1;
+                    cw[4 * M + i] = n.q;
+                    cw[5 * M + i] = n.sat;
+                }
             }
             const unsigned long long tag = (unsigned long long)(uint32_t)(u + 1) << 32;
             if (ln.sup) st_cluster_u64(ln.sup + PAR * ln.pstride, tag | __float_as_uint(c2g[0]));
@@ -1956,17 +1964,31 @@ __global__ void __launch_bounds__(bwd_max_threads(M), 1) seq_bwd_nl_kernel(Fused
                 for (int i = 0; i < M; ++i) h2[i] = 0.f;
             }
             phase ^= 1u << slot;
+            // the step's coefficients at h1, as in the first half (kept from it
+            // with CACHE: the same operations on the same values)
+            auto cell = [&](int i, float lg) {
+                NLCoef n;
+                float X1;
+                if constexpr (CACHE) {
+                    X1 = cw[3 * M + i];
+                    n.q = cw[4 * M + i];
+                    n.sat = cw[5 * M + i];
+                    n.b = P.b0 > 0.f ? fadd(cw[i], fmul(cw[2 * M + i], n.sat)) : cw[i];
+                    n.c = P.cnl != 0.f ? fadd(cw[M + i], fmul(fmul(cw[2 * M + i], P.cnl), fmul(h1[i], h1[i])))
+                                       : cw[M + i];
+                } else {
+                    n = nl_coef(P, cw[i], cw[M + i], cw[2 * M + i], h1[i]);
+                    X1 = fdiv(1.0f, fadd(fmul(n.b, P.k.dt), 1.0f));
+                }
+                adj_cell_nl(P, lg, lam[i], Ly[i], h1[i], h2[i], n, X1, cw[2 * M + i], accc[i], accr[i],
+                            pend[i]);
+            };
 #pragma unroll
-            for (int i = 1; i < M - 1; ++i)
-                adj_cell_nl(P, lap_cell<M, ORDER>(P, c, c2g, i), lam[i], Ly[i], h1[i], h2[i], cw[i],
-                            cw[M + i], cw[2 * M + i], accc[i], accr[i], pend[i]);
+            for (int i = 1; i < M - 1; ++i) cell(i, lap_cell<M, ORDER>(P, c, c2g, i));
             if (ln.rup) c.up = recv_at(P, X, ln.rup + PAR * ln.pstride, u);
             if (ln.rdn) c.dn = recv_at(P, X, ln.rdn + PAR * ln.pstride, u);
-            adj_cell_nl(P, lap_cell<M, ORDER>(P, c, c2g, 0), lam[0], Ly[0], h1[0], h2[0], cw[0],
-                        cw[M], cw[2 * M], accc[0], accr[0], pend[0]);
-            adj_cell_nl(P, lap_cell<M, ORDER>(P, c, c2g, M - 1), lam[M - 1], Ly[M - 1], h1[M - 1],
-                        h2[M - 1], cw[M - 1], cw[2 * M - 1], cw[3 * M - 1], accc[M - 1],
-                        accr[M - 1], pend[M - 1]);
+            cell(0, lap_cell<M, ORDER>(P, c, c2g, 0));
+            cell(M - 1, lap_cell<M, ORDER>(P, c, c2g, M - 1));
         }
         slot = prev;
         if (++pk == P.PB) { pk = 0; ++pc; }
@@ -2091,12 +2113,17 @@ int wt_fused_plan(int nx, int ny, int steps, int n_prb, int cluster_req, int seg
         L->smem_fwd_tape = tiles + aux_fwd;
         L->smem_bwd_base = tiles + aux_bwd;
         // the nonlinear adjoint keeps its cells' b_pml, c_lin, rho in shared
-        // memory before the ring
-        L->smem_nl_coef = r16((size_t)wt::nl_coef_stride(M) * L->threads * sizeof(float));
+        // memory before the ring, and the step's X1, q, sat between the two
+        // halves of a step where that leaves the ring 3 slots
         const size_t nl_room = SMEM_MAX - tiles - aux_bwd;
-        const int nfit = 2 * slice < (1u << 20) && nl_room > L->smem_nl_coef
-                             ? (int)((nl_room - L->smem_nl_coef) / (2 * slice + 8)) : 0;
-        L->nbuf_nl = std::min(8, nfit);
+        auto nl_fit = [&](bool cache, size_t& words) {
+            words = r16((size_t)wt::nl_coef_stride(M, cache) * L->threads * sizeof(float));
+            const int n = 2 * slice < (1u << 20) && nl_room > words
+                              ? (int)((nl_room - words) / (2 * slice + 8)) : 0;
+            return std::min(8, n);
+        };
+        L->nl_cache = nl_fit(true, L->smem_nl_coef) >= 3;
+        L->nbuf_nl = nl_fit(L->nl_cache != 0, L->smem_nl_coef);
         if (L->smem_fwd_tape > SMEM_MAX || L->threads > wt::fwd_max_threads(M)) L->nbuf = 0;
         // checkpoints with the recompute beside the adjoint: 10-cell strips
         // (two groups of at most 384 threads share the register file); its
@@ -2309,7 +2336,8 @@ static int launch_nl(bool fwd, const wt::FusedParams& P0, const WtFusedLaunch& L
     if (fwd) return launch_kernel(wt::seq_fwd_nl_kernel<M, ORDER>, P, L.C, L.threads, L.smem_fwd_tape, st);
     const size_t smem = L.smem_bwd_base + L.smem_nl_coef +
                         (size_t)P.nbuf * (2 * (size_t)L.threads * M * sizeof(float) + 8);
-    return launch_kernel(wt::seq_bwd_nl_kernel<M, ORDER>, P, L.C, L.threads, smem, st);
+    if (L.nl_cache) return launch_kernel(wt::seq_bwd_nl_kernel<M, ORDER, true>, P, L.C, L.threads, smem, st);
+    return launch_kernel(wt::seq_bwd_nl_kernel<M, ORDER, false>, P, L.C, L.threads, smem, st);
 }
 
 template <int ORDER>

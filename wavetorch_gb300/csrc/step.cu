@@ -608,9 +608,9 @@ seq_adj_step4_kernel(StepScalars k, int nx, int ny, const float* __restrict__ kc
 // A CTA of W warps serves one row group for one block of 16 instances
 // (blockIdx.z): the time-invariant coefficients of its rows are loaded once,
 // then its warps take one instance each per round (instance base + w).
-// After each round the
-// warps' dL/dc terms go through shared memory to the threads that own the
-// cells, which add them in instance order.  So the block's sum of the
+// After each round the warps' dL/dc terms go through shared memory to the
+// threads that own the cells, which add them in instance order.  So the
+// block's sum of the
 // step's terms -- the first stage of the batch reduction, seq_adj_reduce_
 // kernel's blocks of 16 summed from 0 in instance order -- is formed here
 // and one plane per block goes to gsum instead of one term plane per
