@@ -150,3 +150,28 @@ def test_row_streaming_kernels_on_ragged_rows_and_chunk_edges(cuda, B, nx, ny):
     spec_f = SeqSpec(B, nx, ny, T, src, [], form=_lib.WT_FORM_PLAIN, output_fields=True)
     _, fields, _, _ = seq_forward(spec_f, sc, tb, tc, tx)
     assert np.array_equal(fields.cpu().numpy(), hist)
+
+
+def test_row_streaming_kernels_on_one_large_instance(cuda):
+    """One instance of 2052 x 2052 (past the row-streaming threshold on its
+    own): the adjoint accumulates dL/dc into the result itself (a block of
+    one instance), 17 column chunks with taps on chunk edges; outputs and
+    dL/dc bit-exact with the oracle."""
+    B, nx, ny, T = 1, 2052, 2052, 6
+    assert B * nx * ny >= 4 << 20
+    src = [(1000 * ny + 1023, -1)]
+    prb = [(1001 * ny + 1024, 1, 0), (1003 * ny + 2047, 0, 1), (999 * ny + 1151, 1, 2)]
+    b, c, x = problem(nx, ny, B, T, 8)
+    g = np.random.default_rng(9).standard_normal((B, T, len(prb))).astype(np.float32)
+    S = o.Seq(B, nx, ny, T, 0.707, 1.0, src, prb)
+    oout, hist = S.forward(b, c, x)
+    ogc = S.backward(b, c, hist, g)[0]
+    sc = scalars(0.707, 1.0, lap_order(B, nx, ny, 1.0))
+    tb, tc, tx = (torch.from_numpy(v).to(cuda) for v in (b, c, x))
+    spec = SeqSpec(B, nx, ny, T, src, prb, form=_lib.WT_FORM_PLAIN)
+    out, _, _, ws = seq_forward(spec, sc, tb, tc, tx)
+    gc, _ = seq_backward(spec, sc, tb, tc, tx, torch.from_numpy(g).to(cuda), ws, False)
+    torch.cuda.synchronize()
+    assert seq_device_status(spec, ws) == _lib.WT_OK
+    assert np.array_equal(out.cpu().numpy(), oout)
+    assert np.array_equal(gc.cpu().numpy(), ogc)
