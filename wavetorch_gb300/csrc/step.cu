@@ -553,33 +553,39 @@ seq_adj_step4_kernel(StepScalars k, int nx, int ny, const float* __restrict__ kc
     float lam[4], g4[4];
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
-        BwdCoef kb;
-        kb.X1 = X1s[j]; kb.Kc = Kcs[j]; kb.Ky2 = Ky2s[j];
         // gradient arriving at h_t: first gy2 from step t+2, then gy1 from t+1
         float lv = 0.f;
-        if (lam2) lv = fmul(kb.Ky2, l2[j]);
+        if (lam2) lv = fmul(Ky2s[j], l2[j]);
         if (lam1) {
             const float lg = lap5<ORDER>(G.u[j], G.l[j], G.c[j], G.r[j], G.d[j], k.lap_w, k.lap_w4);
-            const float gy1 = fadd(fmul(k.dt2, lg), fmul(fmul(2.0f, l1[j]), kb.X1));
+            const float gy1 = fadd(fmul(k.dt2, lg), fmul(fmul(2.0f, l1[j]), X1s[j]));
             lv = lam2 ? fadd(lv, gy1) : gy1;
         }
-        if (taps) {
-            // probe seeds, highest probe index first (descending chains)
+        lam[j] = lv;
+    }
+    // probe seeds, highest probe index first (descending chains), and dL/dx:
+    // a block of its own, entered only in tiles that hold taps
+    if (taps) {
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
             for (int en = __ldg(e.probemap + cell + j); en >= 0; en = __ldg(e.probe_next + en)) {
                 size_t o = ((size_t)inst * e.steps + e.t) * e.n_probe + en;
                 float gv = __ldg(e.grad_out + o);
                 float sd = __ldg(e.probe_kind + en) ? fmul(gv, fmul(2.0f, __ldg(e.amp + o))) : gv;
-                lv = fadd(lv, sd);
+                lam[j] = fadd(lam[j], sd);
             }
+        if (e.grad_x) {
+#pragma unroll
+            for (int j = 0; j < 4; ++j)
+                for (int en = __ldg(e.srcmap + cell + j); en >= 0; en = __ldg(e.src_next + en))
+                    if (__ldg(e.src_row + en) < 0) e.grad_x[(size_t)inst * e.steps + e.t] = lam[j];
         }
-        lam[j] = lv;
+    }
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
         const float L = hprev ? lap5<ORDER>(Y.u[j], Y.l[j], Y.c[j], Y.r[j], Y.d[j], k.lap_w, k.lap_w4)
                               : 0.0f;
-        g4[j] = fmul(fmul(kb.X1, fmul(kb.Kc, L)), lv);
-        if (e.grad_x && taps) {
-            for (int en = __ldg(e.srcmap + cell + j); en >= 0; en = __ldg(e.src_next + en))
-                if (__ldg(e.src_row + en) < 0) e.grad_x[(size_t)inst * e.steps + e.t] = lv;
-        }
+        g4[j] = fmul(fmul(X1s[j], fmul(Kcs[j], L)), lam[j]);
     }
     *reinterpret_cast<float4*>(lam_out + ic) = make_float4(lam[0], lam[1], lam[2], lam[3]);
     if (e.G) {
@@ -645,6 +651,7 @@ seq_adj_step4r_kernel(StepScalars k, int batch, int nx, int ny, const float* __r
         KG[i] = colv && gx >= 0 && gx < nx && lam1 ? __ldg(reinterpret_cast<const float4*>(Kg + (size_t)gx * ny + gy))
                                                    : z4;
     }
+    const bool edges = y0 > 0 || y0 + STEP4_TY < ny;
     const bool le = lane == 0 && y0 > 0, re = lane == 31 && y0 + STEP4_TY < ny;
 #pragma unroll
     for (int i = 0; i < R; ++i) {
@@ -685,11 +692,14 @@ seq_adj_step4r_kernel(StepScalars k, int batch, int nx, int ny, const float* __r
                 const bool v = colv && gx < nx;
                 const size_t cell = (size_t)gx * ny + gy;
                 L2[i] = v && l2p ? __ldg(reinterpret_cast<const float4*>(l2p + cell)) : z4;
-                const size_t lc = (size_t)gx * ny + y0 - 1, rc = (size_t)gx * ny + y0 + STEP4_TY;
-                l1l[i] = le && gx < nx && l1p ? __ldg(l1p + lc) : 0.f;
-                l1r[i] = re && gx < nx && l1p ? __ldg(l1p + rc) : 0.f;
-                hl_[i] = le && gx < nx && hp ? __ldg(hp + lc) : 0.f;
-                hr_[i] = re && gx < nx && hp ? __ldg(hp + rc) : 0.f;
+                l1l[i] = l1r[i] = hl_[i] = hr_[i] = 0.f;
+                if (edges) {                    // uniform: a chunk with a neighbour chunk
+                    const size_t lc = (size_t)gx * ny + y0 - 1, rc = (size_t)gx * ny + y0 + STEP4_TY;
+                    l1l[i] = le && gx < nx && l1p ? __ldg(l1p + lc) : 0.f;
+                    l1r[i] = re && gx < nx && l1p ? __ldg(l1p + rc) : 0.f;
+                    hl_[i] = le && gx < nx && hp ? __ldg(hp + lc) : 0.f;
+                    hr_[i] = re && gx < nx && hp ? __ldg(hp + rc) : 0.f;
+                }
             }
 #pragma unroll
             for (int i = 0; i < R; ++i) {
@@ -726,22 +736,32 @@ seq_adj_step4r_kernel(StepScalars k, int batch, int nx, int ny, const float* __r
                         const float gy1 = fadd(fmul(k.dt2, lg), fmul(fmul(2.0f, l1[j]), x1[j]));
                         lv = lam2 ? fadd(lv, gy1) : gy1;
                     }
-                    if (taps) {
+                    lam[j] = lv;
+                }
+                // probe seeds (descending chains) in their own block, entered
+                // by the warps of tiles that hold taps only: inside the loop
+                // above, their chains cost every warp ~20 % of its instructions
+                if (taps) {
+#pragma unroll
+                    for (int j = 0; j < 4; ++j)
                         for (int en = __ldg(e.probemap + cell + j); en >= 0; en = __ldg(e.probe_next + en)) {
                             size_t o = ((size_t)inst * e.steps + e.t) * e.n_probe + en;
                             float gv = __ldg(e.grad_out + o);
                             float sd = __ldg(e.probe_kind + en) ? fmul(gv, fmul(2.0f, __ldg(e.amp + o))) : gv;
-                            lv = fadd(lv, sd);
+                            lam[j] = fadd(lam[j], sd);
                         }
+                    if (e.grad_x) {
+#pragma unroll
+                        for (int j = 0; j < 4; ++j)
+                            for (int en = __ldg(e.srcmap + cell + j); en >= 0; en = __ldg(e.src_next + en))
+                                if (__ldg(e.src_row + en) < 0) e.grad_x[(size_t)inst * e.steps + e.t] = lam[j];
                     }
-                    lam[j] = lv;
+                }
+#pragma unroll
+                for (int j = 0; j < 4; ++j) {
                     const float L = hp ? lap5<ORDER>(Hu[j], Hl[j], Hc[j], Hr[j], Hd[j], k.lap_w, k.lap_w4)
                                        : 0.0f;
-                    gt[j] = fmul(fmul(x1[j], fmul(kc[j], L)), lv);
-                    if (e.grad_x && taps) {
-                        for (int en = __ldg(e.srcmap + cell + j); en >= 0; en = __ldg(e.src_next + en))
-                            if (__ldg(e.src_row + en) < 0) e.grad_x[(size_t)inst * e.steps + e.t] = lv;
-                    }
+                    gt[j] = fmul(fmul(x1[j], fmul(kc[j], L)), lam[j]);
                 }
                 *reinterpret_cast<float4*>(lam_out + inst * plane + cell) =
                     make_float4(lam[0], lam[1], lam[2], lam[3]);
@@ -951,9 +971,9 @@ int wt_launch_seq_adj_step(const StepScalars& k, int batch, int nx, int ny, cons
             dim3 grd((ny + wt::STEP4_TY - 1) / wt::STEP4_TY, (nx + R - 1) / R, nb);
             dim3 blk(32, 4);
             if ((k.lap_order & 1) == WT_LAP_SEQ)
-                wt::seq_adj_step4r_kernel<WT_LAP_SEQ, R, 4, 6><<<grd, blk, 0, st>>>(k, batch, nx, ny, kco, lam1, lam2, hprev, hbs, lam_out, gc, e);
+                wt::seq_adj_step4r_kernel<WT_LAP_SEQ, R, 4, 5><<<grd, blk, 0, st>>>(k, batch, nx, ny, kco, lam1, lam2, hprev, hbs, lam_out, gc, e);
             else
-                wt::seq_adj_step4r_kernel<WT_LAP_PAIRED, R, 4, 6><<<grd, blk, 0, st>>>(k, batch, nx, ny, kco, lam1, lam2, hprev, hbs, lam_out, gc, e);
+                wt::seq_adj_step4r_kernel<WT_LAP_PAIRED, R, 4, 5><<<grd, blk, 0, st>>>(k, batch, nx, ny, kco, lam1, lam2, hprev, hbs, lam_out, gc, e);
             wt_count_launches(1);
             cudaError_t ce = cudaGetLastError();
             if (ce != cudaSuccess || e.G || !G) return wt_cuda_status(ce);
