@@ -878,7 +878,10 @@ int wt_launch_step_fwd(const StepScalars& k, int batch, int nx, int ny, int coef
                        const float* b, const float* c, const float* y1, size_t bs1,
                        const float* y2, size_t bs2, float* y, size_t bs,
                        const wt::SeqEpilogue* epi, cudaStream_t st, const float* fco) {
+    // (grid rows: one per CTA of STEP4R_WARPS row groups, at most 65535)
+    constexpr int RPC = wt::STEP4R_ROWS * wt::STEP4R_WARPS;
     if (fco && !coef_batched && (size_t)batch * nx * ny >= wt::STREAM_MIN_CELLS &&
+        (nx + RPC - 1) / RPC <= 65535 &&
         vec4_ok(ny, {fco, y1, y2, y}, {bs1, bs2, bs, (size_t)nx * ny})) {
         const int groups = (nx + wt::STEP4R_ROWS - 1) / wt::STEP4R_ROWS;
         dim3 blk(32, wt::STEP4R_WARPS);
@@ -965,7 +968,8 @@ int wt_launch_seq_adj_step(const StepScalars& k, int batch, int nx, int ny, cons
                            int first, const wt::AdjEpilogue& e, cudaStream_t st) {
     const size_t plane = (size_t)nx * ny;
     if (kco && vec4_ok(ny, {kco, lam1, lam2, hprev, lam_out, gc, e.G}, {hbs, plane})) {
-        if ((size_t)batch * plane >= wt::STREAM_MIN_CELLS) {   // row-streaming, block sums
+        // row-streaming with block sums (grid rows: one per row, at most 65535)
+        if ((size_t)batch * plane >= wt::STREAM_MIN_CELLS && nx <= 65535 * wt::ADJ4R_ROWS) {
             constexpr int R = wt::ADJ4R_ROWS;
             const int nb = (batch + wt::ADJ_BLOCK - 1) / wt::ADJ_BLOCK;
             dim3 grd((ny + wt::STEP4_TY - 1) / wt::STEP4_TY, (nx + R - 1) / R, nb);
