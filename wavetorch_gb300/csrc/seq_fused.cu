@@ -341,6 +341,10 @@ WT_DEV void zero_smem(float* s, int n) {
 struct Taps {
     int ns, np;
     bool src_edge;        // a source sits on a cell this thread sends as a halo
+    // some thread of the warp holds a source / a probe (warp-uniform): the
+    // per-step tap work sits behind these, so that warps without taps --
+    // all but a few -- branch over it instead of running it predicated off
+    bool wsrc, wprb;
     int s0, s1, s2, s3;
     int p0, p1, p2, p3;
     WT_DEV int s(int e) const { return e == 0 ? s0 : e == 1 ? s1 : e == 2 ? s2 : s3; }
@@ -392,6 +396,8 @@ WT_DEV void build_taps(const FusedParams& P, const Geo& g, Taps& tp) {
                           (i == M - 1 && g.strip == g.S - 1 && g.has_dn)))
             tp.src_edge = true;
     }
+    tp.wsrc = __any_sync(0xffffffffu, tp.ns > 0);   // every thread of the CTA gets here
+    tp.wprb = __any_sync(0xffffffffu, tp.np > 0);
 }
 
 // Per-cell coefficients of one phase, re-formed from b and c.
@@ -469,7 +475,7 @@ WT_DEV void apply_sources(const FusedParams& P, const Taps& tp, float (&y)[M], f
                           int tnext) {
 #pragma unroll
     for (int e = 0; e < SRCMAX; ++e)
-        if (e < tp.ns) add_at<M>(y, tp.src_i(e), xv[e]);
+        if (e < tp.ns) add_at<M>(y, tp.src_i(e), xv[e]);   // xv: a register per entry
     if (tnext >= 0 && tnext < P.steps) {
 #pragma unroll
         for (int e = 0; e < SRCMAX; ++e)
@@ -503,7 +509,7 @@ WT_DEV void fwd_update(const FusedParams& P, const Geo& g, const Xchg& X, const 
         L[i] = lap_cell<M, ORDER>(P, c, cur, i);
         inout[i] = leapfrog(A[i], Bc[i], C2[i], P.k.two_over, cur[i], inout[i], L[i]);
     }
-    if (tp.ns) {
+    if (tp.wsrc && tp.ns) {
         apply_sources<M>(P, tp, inout, xv, tnext);
         if (ks >= 0 && tp.src_edge) send_halo(g, X, ks, inout[0], inout[M - 1]);
     }
@@ -578,7 +584,7 @@ WT_DEV void fwd_update_lane(const FusedParams& P, const Geo& g, const Xchg& X, c
     }
 #pragma unroll
     for (int i = 1; i < M - 1; ++i) update(i);
-    if (tp.ns) {
+    if (tp.wsrc && tp.ns) {
         apply_sources<M>(P, tp, inout, xv, t + 1);
         if (send && tp.src_edge) {
             if (ln.sup) st_cluster_u64(ln.sup + RS * ln.pstride, tag | __float_as_uint(inout[0]));
@@ -688,7 +694,7 @@ WT_DEV void fwd_step(const FusedParams& P, const Geo& g, const Xchg& X, const La
                 *p = L[j];
         }
     }
-    if (tp.np) {          // probe values from the column just stored (no register indexing)
+    if (tp.wprb && tp.np) {   // probe values from the column just stored (no register indexing)
         const float* colp = ln.col0 + (RS ^ 1) * ln.tile;
         float* row = pr.buf + (size_t)st.pb * P.n_prb * P.PB + st.pc;
 #pragma unroll
@@ -832,7 +838,7 @@ WT_DEV void fwd_step_nl(const FusedParams& P, const Geo& g, const Xchg& X, const
     const int stride = (int)blockDim.x * chunk_width<M>();
     st_chunks_at<M>(tape, stride, L);
     st_chunks_at<M>(tape + (size_t)blockDim.x * M, stride, cur);
-    if (tp.np) {
+    if (tp.wprb && tp.np) {
         const float* colp = ln.col0 + (RS ^ 1) * ln.tile;
         float* row = pr.buf + (size_t)st.pb * P.n_prb * P.PB + st.pc;
 #pragma unroll
@@ -954,9 +960,11 @@ WT_DEV void stage_seeds(const FusedParams& P, const Geo& g, float* seeds, int c)
 template <int M>
 WT_DEV void seed_and_read(const FusedParams& P, const Geo& g, const Taps& tp, int t,
                           float (&lam)[M], const float* sr) {
-#pragma unroll
-    for (int e = 0; e < PRBMAX; ++e)
-        if (e < tp.np) add_at<M>(lam, tp.prb_i(e), sr[tp.prb_col(e) * P.PB]);
+    // a loop on the thread's own count, not unrolled: threads without probes
+    // (whole warps, nearly always) branch over it rather than run it
+    // predicated off on every step
+#pragma unroll 1
+    for (int e = 0; e < tp.np; ++e) add_at<M>(lam, tp.prb_i(e), sr[tp.prb_col(e) * P.PB]);
     if (P.grad_x && tp.ns) {
 #pragma unroll
         for (int e = 0; e < SRCMAX; ++e)
@@ -1085,7 +1093,7 @@ __global__ void __launch_bounds__(bwd_max_threads(M), 1) seq_bwd_fused_kernel(Fu
             if (u % P.PB == 0 && u + P.PB < P.steps)   // next chunk, a barrier ahead of use
                 stage_seeds(P, g, seeds, u / P.PB + 1);
             if (g.colv) {
-                if (tp.np || (P.grad_x && tp.ns))
+                if ((tp.wprb || tp.wsrc) && (tp.np || (P.grad_x && tp.ns)))
                     seed_and_read<M>(P, g, tp, t, lam,
                                      seeds + (size_t)((u / P.PB) & 1) * P.n_prb * P.PB + u % P.PB);
 #pragma unroll
@@ -1217,6 +1225,7 @@ __global__ void __launch_bounds__(bwd_max_threads(M), 1) seq_bwd_tape_kernel(Fus
     const Lane ln = make_lane(P, g, X);
     const bool issuer = threadIdx.x == 0;
     const bool taps_here = tp.np || (P.grad_x && tp.ns);   // seeds to add / dL/dx to read
+    const bool taps_warp = tp.wprb || (P.grad_x && tp.wsrc);
     // this thread's chunk 0 in the slot of the current step (kept
     // incrementally), and the chunk stride of a slice
     constexpr int V = chunk_width<M>();
@@ -1233,7 +1242,7 @@ __global__ void __launch_bounds__(bwd_max_threads(M), 1) seq_bwd_tape_kernel(Fus
         if (pk == 0 && u + P.PB < P.steps)   // next chunk, a barrier ahead of use
             stage_seeds(P, g, seeds, pc + 1);
         if (g.colv) {
-            if (taps_here)
+            if (taps_warp && taps_here)
                 seed_and_read<M>(P, g, tp, t, lam, seeds + (size_t)(pc & 1) * P.n_prb * P.PB + pk);
 #pragma unroll
             for (int i = 0; i < M; ++i) c2g[i] = fmul(Kg[i], lam[i]);
@@ -1392,9 +1401,9 @@ WT_DEV void apply_sources_p(const FusedParams& P, const PTaps& tp, float (&y)[M]
 template <int M>
 WT_DEV void seed_and_read_p(const FusedParams& P, const Geo& g, const PTaps& tp, int t,
                             float (&lam)[M], const float* sr) {
-#pragma unroll
-    for (int e = 0; e < PRBMAX; ++e)
-        if (e < tp.np()) add_at<M>(lam, tp.prb_i(e), sr[tp.prb_col(e) * P.PB]);
+    // a loop on the thread's own count (see seed_and_read)
+#pragma unroll 1
+    for (int e = 0; e < tp.np(); ++e) add_at<M>(lam, tp.prb_i(e), sr[tp.prb_col(e) * P.PB]);
     if (P.grad_x && tp.ns()) {
 #pragma unroll
         for (int e = 0; e < SRCMAX; ++e)
@@ -1918,7 +1927,7 @@ __global__ void __launch_bounds__(bwd_max_threads(M), 1) seq_bwd_nl_kernel(Fused
             tape_wait(P, X, ring, slot, (phase >> slot) & 1u);
             float h1[M];
             ld_chunks_at<M>(h1, sl + part + lane_off, stride);
-            if (tp.np || (P.grad_x && tp.ns))
+            if ((tp.wprb || tp.wsrc) && (tp.np || (P.grad_x && tp.ns)))
                 seed_and_read<M>(P, g, tp, t, lam, seeds + (size_t)(pc & 1) * P.n_prb * P.PB + pk);
             float c2g[M];
 #pragma unroll
