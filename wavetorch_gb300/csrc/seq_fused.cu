@@ -341,9 +341,11 @@ WT_DEV void zero_smem(float* s, int n) {
 struct Taps {
     int ns, np;
     bool src_edge;        // a source sits on a cell this thread sends as a halo
-    // some thread of the warp holds a source / a probe (warp-uniform): the
-    // per-step tap work sits behind these, so that warps without taps --
-    // all but a few -- branch over it instead of running it predicated off
+    // some thread of the warp holds a source / a probe (warp-uniform), tested
+    // before the per-step tap work.  On their own these guards did not change
+    // the compiled step (same instruction count); what lets warps without
+    // probes skip the seeds is the loop on the thread's own count in
+    // seed_and_read.
     bool wsrc, wprb;
     int s0, s1, s2, s3;
     int p0, p1, p2, p3;
