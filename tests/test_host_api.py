@@ -216,6 +216,20 @@ def test_ragged_layout_choice_with_band_options():
     assert _option_spec((-1, 8), 3) == (-1, 24) and _option_spec((4, 0), 3) == (4, 0)
 
 
+def test_ragged_strip_trial_keeps_the_step_ratios():
+    """The packed batch's strip-height trial runs every model on one scaled
+    step count: the longest gets exactly `steps`, the others keep their
+    ratio to it (rounded up, at least one step, never more than their own)."""
+    from wavetorch_gb300.ragged import trial_steps
+    T = [4000, 2000, 500, 3999, 7]
+    got = trial_steps(T, 256)
+    assert got[0] == 256 and got[1] == 128 and got[2] == 32 and got[3] == 256
+    assert got[4] == 1
+    assert trial_steps([100, 50], 256) == [100, 50]          # short runs: their own counts
+    ratios = [g / t for g, t in zip(trial_steps(T[:4], 256), T[:4])]
+    assert max(ratios) - min(ratios) < 1e-3 * 5
+
+
 def test_save_load_roundtrip_hole_geometry(tmp_path):
     """A model on a hole geometry round-trips through the model file: the
     geometry class is rebuilt by name from its reconstruction arguments

@@ -119,6 +119,14 @@ def _check_model(m) -> None:
         raise TypeError("ragged batches need point sources and probes")
 
 
+def trial_steps(T, steps: int):
+    """Step counts of the strip-height trial: every model's count scaled by
+    one factor (rounded up, at least 1, at most its own) so that the longest
+    runs `steps`; the models keep their ratios and so the schedule its shape."""
+    top = max(T)
+    return [max(1, min(t, -(-t * steps // top))) for t in T]
+
+
 class RaggedBatch:
     """One training step over many models.
 
@@ -289,8 +297,7 @@ class RaggedBatch:
         its shape: equal counts would balance the CTAs differently); 0 when
         only one height fits."""
         dev = self.device
-        top = max(self.T)
-        T = [max(1, min(t, -(-t * steps // top))) for t in self.T]
+        T = trial_steps(self.T, steps)
         x = [v[:t].contiguous() for v, t in zip(self._x, T)]
         out = [torch.zeros(t, self._P, device=dev) for t in T]
         gout = [torch.ones(t, self._P, device=dev) for t in T]
