@@ -294,8 +294,8 @@ class RaggedBatch:
         """The strip height (4 or 8 cells per thread) of the faster forward +
         adjoint on the first steps of every model, each model's count scaled
         by one factor so that the longest runs `steps` (the schedule keeps
-        its shape: equal counts would balance the CTAs differently); 0 when
-        only one height fits."""
+        its shape: equal counts would balance the CTAs differently); the one
+        that fits when only one does, 0 when neither does."""
         dev = self.device
         T = trial_steps(self.T, steps)
         x = [v[:t].contiguous() for v, t in zip(self._x, T)]
